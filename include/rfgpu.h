@@ -1,0 +1,179 @@
+/*
+ * rfgpu.h - C ABI of the GB300 residual engine for RocfluMP.
+ *
+ * The engine replaces the per-region body of the Runge-Kutta stage loop and
+ * the time-step computation of the Fortran solver.  Each entry point names
+ * the reference routine(s) it stands in for.  Arrays are passed exactly as the
+ * Fortran host holds them (column-major, 1-based cell indices, C_LOC of
+ * contiguous arrays); the engine converts them once to 0-based
+ * structure-of-arrays device copies and keeps the state resident on the GPU.
+ *
+ * Error convention: every entry returns an int, RFGPU_OK (0) on success.  The
+ * Fortran shim maps non-zero codes onto ModError codes and calls ErrorStop
+ * (modfloflu/ModError.F90:486).  Device-detected invalid states (NaN,
+ * non-positive density or pressure) are latched in a device status word and
+ * reported by rfgpu_status, replacing the host checks of AfterUpdateMP
+ * (libfloflu/AfterUpdateMP.F90:134-136).
+ *
+ * Threading: a handle is used by one host thread at a time.  Calls are
+ * stream-ordered and asynchronous; rfgpu_dt, rfgpu_download, rfgpu_status,
+ * rfgpu_residual (with a host output) and rfgpu_sync synchronise.
+ */
+#ifndef RFGPU_H
+#define RFGPU_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rfgpu_region_s *rfgpu_region_t;
+typedef struct rfgpu_batch_s *rfgpu_batch_t;
+
+enum {
+  RFGPU_OK = 0,
+  RFGPU_ERR_ARG = 1,          /* bad pointer / size / index */
+  RFGPU_ERR_UNSUPPORTED = 2,  /* option outside the supported envelope */
+  RFGPU_ERR_CUDA = 3,         /* CUDA runtime error */
+  RFGPU_ERR_NOMEM = 4,        /* device allocation failed */
+  RFGPU_ERR_STATE = 5,        /* invalid flow state detected on the device */
+  RFGPU_ERR_TIMEOUT = 6       /* a bounded device wait expired */
+};
+
+/* status bits returned by rfgpu_status */
+enum {
+  RFGPU_ST_NAN = 1,     /* RFLU_CheckValidity would stop (NaN rho,u,v,w,p,T) */
+  RFGPU_ST_NEGPOS = 2,  /* RFLU_CheckPositivity would stop (rho<=0 or p<=0) */
+  RFGPU_ST_PFLOOR = 4,  /* CheckPositivity energy floor applied */
+  RFGPU_ST_PCLAMP = 8   /* EnforceBounds clamped a tiny negative pressure */
+};
+
+/* values of the keys below (modfloflu/ModParameters.F90) */
+enum {
+  RFGPU_DISCR_UPW_ROE = 1, RFGPU_DISCR_UPW_HLLC = 3, RFGPU_DISCR_UPW_AUSMPLUS = 4,
+  RFGPU_RECONST_NONE = 0, RFGPU_RECONST_LIM_VENKAT = 11,
+  RFGPU_RK_SCHEME_4_CLASSICAL = 1, RFGPU_RK_SCHEME_3_WRAY = 2, RFGPU_RK_SCHEME_1_EULER = 3,
+  RFGPU_BC_OUTFLOW = 20, RFGPU_BC_SLIPWALL = 60,
+  RFGPU_BCOPT_SUPERSONIC = 0, RFGPU_BCOPT_SUBSONIC = 1, RFGPU_BCOPT_MIXED = 2,
+  RFGPU_GAS_MODEL_TCPERF = 1, RFGPU_FLOW_EULER = 0,
+  RFGPU_PREC_FP64 = 0,   /* everything FP64; bit-identical to the reference order */
+  RFGPU_PREC_MIXED = 1   /* FP32 prim/gradients/limiter/flux; FP64 geometry,
+                            residual accumulation, RK update and EOS */
+};
+
+/* One boundary patch (modfloflu/ModBndPatch.F90:112-162). */
+typedef struct {
+  int bcType;            /* RFGPU_BC_SLIPWALL or RFGPU_BC_OUTFLOW */
+  int spaceOrder;        /* .bc ORDER: 1 or 2 */
+  int bcOptType;         /* outflow TYPE: BCOPT_* */
+  int nBFaces;
+  const int *bf2c;       /* bf2c(nBFaces), 1-based */
+  const double *fn;      /* fn(4,nBFaces): unit normal, area */
+  const double *fc;      /* fc(3,nBFaces) */
+  const double *vals;    /* outflow static pressure: vals(nBFaces) if distrib, else vals(1) */
+  int distrib;
+} rfgpu_patch_t;
+
+/* Everything RFLU_InitFlowSolver has built for one region, plus the numerics
+ * keys.  Mirrors t_region / t_grid / t_mixt_input fields
+ * (modfloflu/ModDataStruct.F90:100-167, ModGrid.F90:84-317,
+ * ModMixture.F90:76-195). */
+typedef struct {
+  int nCells;            /* nCells == nCellsTot: one region, no virtual cells */
+  int nFaces;            /* interior faces (nFaces); f2c may have a larger leading dim */
+  int f2cLd;             /* leading dimension of f2c (>= 2) */
+  const int *f2c;        /* f2c(f2cLd,nFaces), 1-based */
+  const double *fn;      /* fn(4,nFaces) */
+  const double *fc;      /* fc(3,nFaces) */
+  const double *cofg;    /* cofg(3,nCells) */
+  const double *vol;     /* vol(nCells) */
+  const int *c2csOffsets;/* (nCells+1) 0-based offsets into c2csMembers */
+  const int *c2csMembers;/* flattened c2cs(icg)%cellMembs, 1-based */
+  const double *xyzMoms; /* xyzMoms(10,nCells) (XYZ_MOM_11..44) */
+  int nPatches;
+  const rfgpu_patch_t *patches;
+  const double *cv;      /* cv(5,nCells) conserved state */
+  const double *dv;      /* dv(3,nCells) p, T, a; NULL: computed from cv */
+  /* numerics */
+  int gasModel, flowModel;
+  int spaceDiscr, spaceOrder, reconst, rkScheme;
+  double refCp, refGamma;  /* global%refCp, global%refGamma (flux kernels) */
+  double gvCp, gvMol;      /* gv(GV_MIXT_CP), gv(GV_MIXT_MOL) (EOS, conversions) */
+  double epsentr, dissFact;
+  int precision;           /* RFGPU_PREC_* */
+  int venkatGuard;         /* 0: limiter term exactly as the reference;
+                              1: guard added with the sign of the denominator */
+} rfgpu_region_desc_t;
+
+/* Register a region: copies and reorders the arrays to device-resident SoA.
+ * Replaces nothing in the reference (one-time setup after
+ * rocflu/RFLU_InitFlowSolver.F90:1071); refuses options outside the
+ * supported envelope with RFGPU_ERR_UNSUPPORTED. */
+int rfgpu_region_create(const rfgpu_region_desc_t *desc, rfgpu_region_t *out);
+int rfgpu_region_destroy(rfgpu_region_t h);
+
+/* One RK stage for the region (libfloflu/RungeKuttaMP.F90:219-260 and
+ * :280-370): RKInitMP, CellGradientsMP, ConvectiveFluxesMP, ZeroResidualsMP,
+ * SourceTermsMP, ZeroDummyCellsMP, RKUpdateMP, RFLU_SetVarsContWrapper,
+ * AfterUpdateMP.  istage in 1..nrkSteps; dtMin = global%dtMin. */
+int rfgpu_stage(rfgpu_region_t h, int istage, double dtMin);
+
+/* RFLU_TimeStepInviscid + RFLU_MinimumTimeStep
+ * (rocflu/RFLU_TimeStepping.F90:458,473): returns global%dtMin.  Synchronous. */
+int rfgpu_dt(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
+             double currentTime, double *dtMin);
+
+/* One full time step on the device without host round trips: dt as above
+ * using the device-resident current time, clipped so time does not pass
+ * endTime (rocflu/RFLU_TimeStepping.F90:490-493; endTime <= 0 disables the
+ * clip), then nrkSteps stages, then time += dtMin. */
+int rfgpu_step(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
+               double endTime);
+
+/* Capture rfgpu_step in a CUDA graph and replay it nSteps times. */
+int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed,
+                      double dtMinLimit, double endTime);
+
+/* Residual only: CellGradientsMP + ConvectiveFluxesMP (libfloflu/RungeKuttaMP.F90:223-233)
+ * on the resident state, which it does not modify.  rhs (5,nCells) host
+ * output or NULL (result stays on the device). */
+int rfgpu_residual(rfgpu_region_t h, double *rhs);
+
+/* Host copies: cv(5,nCells), dv(3,nCells); either may be NULL. */
+int rfgpu_download(rfgpu_region_t h, double *cv, double *dv);
+/* Restart / host edits: cv(5,nCells); dv NULL recomputes dv from cv. */
+int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv);
+
+/* Limited gradients of the last residual/stage: grad(3,5,nCells). */
+int rfgpu_download_grad(rfgpu_region_t h, double *grad);
+
+/* Time state: current time and last dtMin. */
+int rfgpu_time(rfgpu_region_t h, double *currentTime, double *dtMin);
+int rfgpu_set_time(rfgpu_region_t h, double currentTime);
+
+/* Latched status bits since the last call (clears them).  Synchronous. */
+int rfgpu_status(rfgpu_region_t h, int *flags);
+int rfgpu_sync(rfgpu_region_t h);
+/* The cudaStream_t the handle launches on. */
+void *rfgpu_stream(rfgpu_region_t h);
+/* Device bytes held by the handle. */
+long long rfgpu_device_bytes(rfgpu_region_t h);
+/* Kernel launches issued by the handle since creation. */
+long long rfgpu_launch_count(rfgpu_region_t h);
+/* Launch configuration used by the kernels (block size); 0 = default. */
+int rfgpu_set_tuning(rfgpu_region_t h, int blockCells, int blockFaces);
+
+/* Batches: many independent regions advanced together, one launch per pass
+ * over all regions (a persistent grid walking a tile work list). */
+int rfgpu_batch_create(rfgpu_region_t *regions, int nRegions, rfgpu_batch_t *out);
+int rfgpu_batch_destroy(rfgpu_batch_t b);
+int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMinLimit,
+                     double endTime);
+int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtImposed,
+                            double dtMinLimit, double endTime);
+int rfgpu_batch_sync(rfgpu_batch_t b);
+void *rfgpu_batch_stream(rfgpu_batch_t b);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,92 @@
+/*
+ * rfmesh.h - host-side mesh builder that produces the region arrays the
+ * residual engine (rfgpu.h) registers.
+ *
+ * In RocfluMP these arrays come from the Fortran initialisation chain
+ * (rocflu/RFLU_InitFlowSolver.F90:604-1071): face list, geometry,
+ * vertex-to-cell lists, cell-to-cell stencils and WLSQ moments.  This library
+ * restates that chain for synthetic box meshes so the engine and the CPU oracle
+ * can be fed identical, reference-shaped inputs without the Fortran host:
+ *
+ *   - cell numbering by type: tets, hexes, prisms, pyramids
+ *       (modflu/RFLU_ModCellMapping.F90:330-432)
+ *   - face vectors / centroids (libfloflu/FaceVector.F90:79-136,
+ *       libfloflu/FaceCentroid.F90:77-122), volumes and centroids by the
+ *       divergence theorem (modflu/RFLU_ModGeometry.F90:307-672), approximate
+ *       centroids = vertex averages (RFLU_ModGeometry.F90:1277-1460)
+ *   - c2c stencils: vertex neighbours ranked by shared-vertex fraction with the
+ *       reference's quicksort, truncated to 10x the minimum size and re-sorted
+ *       (modflu/RFLU_ModStencilsCells.F90:750-1416,2816-2909,
+ *        modflu/RFLU_ModStencilsUtils.F90:696-979,1093-1137,
+ *        modfloflu/ModSortSearch.F90:898-990), layer growth decided by the
+ *       singular-value ratio test of libflu/RFLU_InvertMatrixSVD.F90:150-190
+ *   - WLSQ moments (modflu/RFLU_ModWeights.F90:1770-1894)
+ *
+ * Face order is this library's own (first encounter while sweeping cells in
+ * global order); the engine and the oracle consume it as given, exactly as the
+ * engine consumes whatever face list the Fortran host passes.
+ *
+ * All arrays are returned in Fortran layout (column-major, first index fastest)
+ * with 1-based cell indices, i.e. exactly what the Fortran host would pass
+ * through ISO_C_BINDING.  Pointers stay valid until rfmesh_destroy.
+ */
+#ifndef RFMESH_H
+#define RFMESH_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct rfmesh_s *rfmesh_t;
+
+enum {
+  RFMESH_HEX = 0,   /* nx*ny*nz hexahedra */
+  RFMESH_TET = 1,   /* every hex split into 6 Kuhn (Freudenthal) tets */
+  RFMESH_MIXED = 2  /* hexes; x>mid -> 2 prisms; z>mid -> 6 tets (prism
+                       precedence); pyramid/tet transition cubes where a tet
+                       cube meets a quad face, so the mesh is conforming */
+};
+
+/* patch order of box meshes */
+enum { RFMESH_XLO = 0, RFMESH_XHI, RFMESH_YLO, RFMESH_YHI, RFMESH_ZLO, RFMESH_ZHI,
+       RFMESH_NPATCH };
+
+/* size slots of rfmesh_sizes */
+enum {
+  RFMESH_NVERT = 0, RFMESH_NCELLS, RFMESH_NFACES, RFMESH_NPATCHES, RFMESH_NMEMBS,
+  RFMESH_NTETS, RFMESH_NHEXS, RFMESH_NPRIS, RFMESH_NPYRS, RFMESH_NBFACES,
+  RFMESH_MAXMEMBS, RFMESH_NSIZES
+};
+
+/* Return codes */
+enum { RFMESH_OK = 0, RFMESH_ERR_ARG = 1, RFMESH_ERR_GEOM = 2, RFMESH_ERR_NOMEM = 3 };
+
+/* Build a box mesh over [lo,hi] with nx*ny*nz base hexes.  Interior vertices
+ * are displaced by U(-jitter,+jitter)*h per coordinate from a 64-bit Mersenne
+ * twister seeded with `seed`.  nThreads <= 0 uses all host threads. */
+int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3],
+                      const double hi[3], double jitter, unsigned long long seed,
+                      int nThreads, rfmesh_t *out);
+int rfmesh_destroy(rfmesh_t m);
+int rfmesh_sizes(rfmesh_t m, long long sizes[RFMESH_NSIZES]);
+int rfmesh_patch_nbfaces(rfmesh_t m, int iPatch);
+
+/* Fortran-layout views */
+const double *rfmesh_xyz(rfmesh_t m);      /* (3,nVert) */
+const double *rfmesh_vol(rfmesh_t m);      /* (nCells) */
+const double *rfmesh_cofg(rfmesh_t m);     /* (3,nCells) */
+const int *rfmesh_f2c(rfmesh_t m);         /* (2,nFaces), 1-based */
+const double *rfmesh_fn(rfmesh_t m);       /* (4,nFaces): unit normal + area */
+const double *rfmesh_fc(rfmesh_t m);       /* (3,nFaces) */
+const int *rfmesh_c2cs_offsets(rfmesh_t m);/* (nCells+1), 0-based CSR offsets */
+const int *rfmesh_c2cs_members(rfmesh_t m);/* (nMembs), 1-based cell ids */
+const double *rfmesh_xyzmoms(rfmesh_t m);  /* (10,nCells) XYZ_MOM_11..44 */
+const int *rfmesh_cell_type(rfmesh_t m);   /* (nCells) 0 tet 1 hex 2 pri 3 pyr */
+const int *rfmesh_bf2c(rfmesh_t m, int iPatch);   /* (nBFaces), 1-based */
+const double *rfmesh_bfn(rfmesh_t m, int iPatch); /* (4,nBFaces) */
+const double *rfmesh_bfc(rfmesh_t m, int iPatch); /* (3,nBFaces) */
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,228 @@
+"""Run configuration mirroring the RocfluMP input keys the engine honours, and
+builders for the synthetic workloads (shock tubes, perturbed tet boxes,
+mixed-element boxes, batched tubes).
+
+Keyword meanings follow libfloflu/ReadNumericsSection.F90:110-130 and
+libflu/RFLU_InitInputValues.F90:151-200; defaults follow the latter and
+libflu/RFLU_InitGlobal.F90:353-354 (refCp = 1004.5, refGamma = 1.4).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field, replace
+from typing import List, Optional
+
+import numpy as np
+
+from . import mesh as _mesh
+
+# modfloflu/ModParameters.F90
+DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS = 1, 3, 4
+RECONST_NONE, RECONST_LIM_VENKAT = 0, 11
+RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
+BC_OUTFLOW, BC_SLIPWALL = 20, 60
+BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
+PREC_FP64, PREC_MIXED = 0, 1
+
+SCHEME_NAMES = {DISCR_UPW_ROE: "roe", DISCR_UPW_HLLC: "hllc", DISCR_UPW_AUSMPLUS: "ausm+"}
+
+
+@dataclass
+class Numerics:
+    """The NUMERICS / TIMESTEP keys the engine supports (others are refused)."""
+    spaceDiscr: int = DISCR_UPW_AUSMPLUS  # DISCR
+    spaceOrder: int = 2                  # ORDER
+    reconst: int = RECONST_LIM_VENKAT    # RECONST
+    rkScheme: int = RK_SCHEME_3_WRAY     # RKSCHEME
+    refCp: float = 1004.5
+    refGamma: float = 1.4
+    epsentr: float = 0.05                # ENTROPY
+    dissFact: float = 1.0                # DISSFACT
+    cfl: float = 0.5                     # CFL
+    precision: int = PREC_FP64
+    # 0: Venkatakrishnan term numer/(denom+1e-12) exactly as the reference;
+    # 1: labelled extension adding 1e-12 with the sign of denom (d2 < 0 case)
+    venkatGuard: int = 0
+
+    @property
+    def gv(self):
+        """(cp, M) as RFLU_SetGasVars stores them for TCPERF
+        (libflu/RFLU_SetGasVars.F90:173-179): M = 8314.3 / (cp - cp/g)."""
+        gc = self.refCp - self.refCp / self.refGamma
+        return self.refCp, 8314.3 / gc
+
+    @property
+    def gamma_gv(self) -> float:
+        """gamma as the EOS recovers it from gv (RFLU_SetDependentVars.F90:257-258)."""
+        cp, mol = self.gv
+        gc = 8314.3 / mol
+        return cp / (cp - gc)
+
+
+@dataclass
+class PatchBC:
+    bcType: int = BC_SLIPWALL
+    spaceOrder: int = 1          # .bc ORDER; defaults to spaceOrderBFaces = 1
+    bcOptType: int = BCOPT_SUPERSONIC
+    pout: Optional[np.ndarray] = None  # outflow static pressure (1,) or (nBFaces,)
+
+
+@dataclass
+class Case:
+    name: str
+    mesh: _mesh.BoxMesh
+    numerics: Numerics
+    bcs: List[PatchBC]
+    cv: np.ndarray               # (nCells,5) == Fortran cv(5,nCells)
+    dv: np.ndarray               # (nCells,3)
+    t_end: float = 0.0
+    n_steps: int = 0
+    meta: dict = field(default_factory=dict)
+
+    def with_numerics(self, **kw) -> "Case":
+        return replace(self, numerics=replace(self.numerics, **kw), cv=self.cv.copy(),
+                       dv=self.dv.copy())
+
+
+def eos_dv(num: Numerics, cv: np.ndarray) -> np.ndarray:
+    """RFLU_SetDependentVars for TCPERF (libflu/RFLU_SetDependentVars.F90:256-287),
+    element by element in the same operation order (NumPy ufuncs are single
+    IEEE operations)."""
+    cp, mol = num.gv
+    gc = 8314.3 / mol
+    g = cp / (cp - gc)
+    r = cv[:, 0]
+    ir = 1.0 / r
+    Eo = ir * cv[:, 4]
+    Vm2 = (ir * ir) * ((cv[:, 1] * cv[:, 1] + cv[:, 2] * cv[:, 2]) + cv[:, 3] * cv[:, 3])
+    p = ((g - 1.0) * r) * ((Eo - 0.5 * Vm2) - 0.0)
+    T = p / (r * gc)
+    a = np.sqrt((g * gc) * T)
+    return np.stack([p, T, a], axis=1)
+
+
+def prim_to_cv(num: Numerics, r, u, v, w, p) -> np.ndarray:
+    """Conserved state from (rho,u,v,w,p) with E = rho*Eo(rho,g,p,u,v,w)."""
+    g = num.gamma_gv
+    Eo = p / (r * (g - 1.0)) + 0.5 * ((u * u + v * v) + w * w) + 0.0
+    return np.stack([r, r * u, r * v, r * w, r * Eo], axis=1).astype(np.float64)
+
+
+def tube_bcs(order: int = 2) -> List[PatchBC]:
+    """Supersonic outflow (extrapolation) at both x ends, slip walls elsewhere."""
+    b = [PatchBC(BC_OUTFLOW, order, BCOPT_SUPERSONIC), PatchBC(BC_OUTFLOW, order, BCOPT_SUPERSONIC)]
+    b += [PatchBC(BC_SLIPWALL, order) for _ in range(4)]
+    return b
+
+
+def shock_tube(n: int = 1000, ny: int = 2, nz: int = 2, length=(1.0, 0.01, 0.01),
+               left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1), x0: float = 0.5,
+               numerics: Optional[Numerics] = None, bc_order: int = 2, t_end: float = 0.2,
+               threads: int = 0) -> Case:
+    """Sod-type tube of n*ny*nz hexes: (rho,u,p) = left for x < x0, right otherwise."""
+    num = numerics or Numerics()
+    m = _mesh.box(_mesh.HEX, n, ny, nz, hi=length, threads=threads)
+    x = m.cofg[:, 0]
+    L = x < x0 * length[0]
+    r = np.where(L, left[0], right[0])
+    u = np.where(L, left[1], right[1])
+    p = np.where(L, left[2], right[2])
+    z = np.zeros_like(r)
+    cv = prim_to_cv(num, r, u, z, z, p)
+    return Case("shock_tube", m, num, tube_bcs(bc_order), cv, eos_dv(num, cv), t_end=t_end,
+                meta={"n": n, "left": left, "right": right, "x0": x0})
+
+
+def rankine_hugoniot(Ms: float, gamma: float, rho1: float, p1: float):
+    """Post-shock state of a normal shock of Mach Ms moving into gas at rest
+    (standard normal-shock relations)."""
+    g = gamma
+    rho_ratio = (g + 1.0) * Ms * Ms / ((g - 1.0) * Ms * Ms + 2.0)
+    p_ratio = 1.0 + 2.0 * g / (g + 1.0) * (Ms * Ms - 1.0)
+    a1 = np.sqrt(g * p1 / rho1)
+    rho2 = rho1 * rho_ratio
+    u2 = Ms * a1 * (1.0 - rho1 / rho2)
+    return rho2, u2, p1 * p_ratio
+
+
+def tet_shock_box(n: int = 128, seed: int = 2024, jitter: float = 0.1, Ms: float = 2.0,
+                  sigma: float = 0.1, x_shock: float = 0.2, numerics: Optional[Numerics] = None,
+                  n_steps: int = 100, threads: int = 0) -> Case:
+    """Planar Ms shock over a perturbed tetrahedral box: n^3 hexes x 6 Kuhn tets,
+    interior vertices jittered by U(+-jitter*h); quiescent air rho=1.2, p=1e5
+    times a per-cell lognormal density factor exp(sigma*Z); Rankine-Hugoniot
+    post-shock state for x < x_shock.  Slip walls on y/z, supersonic outflow
+    (extrapolation) on the x ends."""
+    num = numerics or Numerics(spaceDiscr=DISCR_UPW_ROE)
+    m = _mesh.box(_mesh.TET, n, n, n, jitter=jitter, seed=seed, threads=threads)
+    rng = np.random.default_rng(seed)
+    rho1, p1 = 1.2, 1.0e5
+    r = rho1 * np.exp(sigma * rng.standard_normal(m.nCells))
+    p = np.full(m.nCells, p1)
+    u = np.zeros(m.nCells)
+    rho2, u2, p2 = rankine_hugoniot(Ms, num.refGamma, rho1, p1)
+    post = m.cofg[:, 0] < x_shock
+    r = np.where(post, rho2, r)
+    u = np.where(post, u2, u)
+    p = np.where(post, p2, p)
+    z = np.zeros_like(r)
+    cv = prim_to_cv(num, r, u, z, z, p)
+    return Case("tet_shock_box", m, num, tube_bcs(2), cv, eos_dv(num, cv), n_steps=n_steps,
+                meta={"n": n, "seed": seed, "Ms": Ms, "sigma": sigma})
+
+
+def fourier_state(xyz: np.ndarray, seed: int, n_modes: int = 8):
+    """Smooth random field: sum of n_modes seeded Fourier modes per variable,
+    affinely rescaled to rho in [0.5,2], p in [0.5e5,2e5], |u_i| <= 300/sqrt(3)."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(5):
+        k = rng.uniform(1.0, 4.0, size=(n_modes, 3)) * 2.0 * np.pi * rng.choice([-1, 1], size=(n_modes, 3))
+        ph = rng.uniform(0.0, 2.0 * np.pi, size=n_modes)
+        amp = rng.uniform(0.5, 1.0, size=n_modes)
+        f = np.zeros(xyz.shape[0])
+        for j in range(n_modes):
+            f += amp[j] * np.sin(xyz @ k[j] + ph[j])
+        f = (f - f.min()) / max(f.max() - f.min(), 1e-300)  # [0,1]
+        out.append(f)
+    r = 0.5 + 1.5 * out[0]
+    p = 0.5e5 + 1.5e5 * out[4]
+    umax = 300.0 / np.sqrt(3.0)
+    u, v, w = [(2.0 * o - 1.0) * umax for o in out[1:4]]
+    return r, u, v, w, p
+
+
+def mixed_box(n: int = 96, seed: int = 7, numerics: Optional[Numerics] = None,
+              threads: int = 0) -> Case:
+    """n^3 box: hexes with x > 0.5 split into 2 prisms, hexes with z > 0.5 into 6
+    tets (prism precedence), pyramid transition cubes where tets meet quad faces;
+    smooth seeded Fourier state.  Slip walls everywhere (residual benchmark)."""
+    num = numerics or Numerics()
+    m = _mesh.box(_mesh.MIXED, n, n, n, threads=threads)
+    r, u, v, w, p = fourier_state(m.cofg, seed)
+    cv = prim_to_cv(num, r, u, v, w, p)
+    bcs = [PatchBC(BC_SLIPWALL, 2) for _ in range(6)]
+    return Case("mixed_box", m, num, bcs, cv, eos_dv(num, cv), meta={"n": n, "seed": seed})
+
+
+def tube_ensemble(count: int = 256, seed: int = 11, n_min: int = 500, n_max: int = 125000,
+                  cross: int = 2, numerics: Optional[Numerics] = None, n_steps: int = 300,
+                  threads: int = 0, scale: float = 1.0) -> List[Case]:
+    """Independent 3-D shock tubes n x cross x cross hexes, n log-uniform in
+    [n_min, n_max] (times `scale` for reduced tests); left/right rho and p
+    log-uniform in [0.1,10], u uniform in [-1,1], diaphragm in [0.3,0.7]."""
+    num = numerics or Numerics(precision=PREC_MIXED)
+    rng = np.random.default_rng(seed)
+    cases = []
+    for i in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(n_min), np.log(n_max))) * scale))
+        n = max(n, 4)
+        rl, rr, pl, pr = np.exp(rng.uniform(np.log(0.1), np.log(10.0), size=4))
+        ul, ur = rng.uniform(-1.0, 1.0, size=2)
+        x0 = rng.uniform(0.3, 0.7)
+        c = shock_tube(n, cross, cross, length=(1.0, 1.0 / n * cross, 1.0 / n * cross),
+                       left=(rl, ul, pl), right=(rr, ur, pr), x0=x0, numerics=num,
+                       threads=threads)
+        c.name = f"tube{i}"
+        c.n_steps = n_steps
+        cases.append(c)
+    return cases

@@ -1,0 +1,767 @@
+// rfgpu_host.cu - C ABI of the residual engine (include/rfgpu.h): region
+// registration (Fortran image -> 0-based SoA + SELL-32 lists on the device),
+// stage / step / residual / time-step drivers, CUDA-graph replay and batches.
+#include "rfgpu.h"
+#include "rfgpu_internal.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+using namespace rfgpu;
+
+namespace {
+
+struct DevAlloc {
+  std::vector<void *> ptrs;
+  long long bytes = 0;
+  template <typename T>
+  T *alloc(size_t n) {
+    if (n == 0) n = 1;
+    void *p = nullptr;
+    if (cudaMalloc(&p, n * sizeof(T)) != cudaSuccess) throw std::bad_alloc();
+    ptrs.push_back(p);
+    bytes += (long long)(n * sizeof(T));
+    return (T *)p;
+  }
+  template <typename T>
+  T *upload(const std::vector<T> &v, cudaStream_t s) {
+    T *d = alloc<T>(v.size());
+    if (!v.empty() &&
+        cudaMemcpyAsync(d, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s) != cudaSuccess)
+      throw std::bad_alloc();
+    return d;
+  }
+  void free_all() {
+    for (void *p : ptrs) cudaFree(p);
+    ptrs.clear();
+  }
+};
+
+struct Sell {
+  std::vector<long long> off;  // per slice
+  std::vector<int> cnt;        // per cell
+  long long total = 0;
+  void build(const std::vector<int> &counts) {
+    int N = (int)counts.size();
+    int nSl = (N + kSlice - 1) / kSlice;
+    off.assign(nSl + 1, 0);
+    cnt = counts;
+    for (int s = 0; s < nSl; ++s) {
+      int w = 0;
+      for (int l = 0; l < kSlice && s * kSlice + l < N; ++l) w = std::max(w, counts[s * kSlice + l]);
+      off[s + 1] = off[s] + (long long)w * kSlice;
+    }
+    total = off[nSl];
+  }
+  long long at(int c, int k) const { return off[c / kSlice] + (long long)k * kSlice + c % kSlice; }
+};
+
+}  // namespace
+
+struct rfgpu_region_s {
+  int prec = 0;
+  int nCells = 0, nFaces = 0, nBFaces = 0;
+  int rkScheme = 2, nSteps = 3, spaceOrder = 2, reconst = 11;
+  cudaStream_t stream = nullptr;
+  DevAlloc mem;
+  RegionDev<double> rd64{};
+  RegionDev<float> rd32{};
+  void *regsDev = nullptr;  // RegionDev<R>[1]
+  Tile *cellTiles = nullptr, *faceTiles = nullptr, *bfaceTiles = nullptr;
+  Work work{};
+  double *stage = nullptr;  // staging for AoS transfers, 5*N doubles
+  long long launches = 0;
+  // graph cache
+  cudaGraphExec_t graph = nullptr;
+  double gkey[4] = {0, 0, 0, 0};
+  long long perStep = 0;
+};
+
+struct rfgpu_batch_s {
+  int prec = 0;
+  std::vector<rfgpu_region_t> regs;
+  cudaStream_t stream = nullptr;
+  DevAlloc mem;
+  void *regsDev = nullptr;
+  Work work{};
+  int spaceOrder = 1, reconst = 0, nSteps = 3;
+  long long launches = 0;
+  cudaGraphExec_t graph = nullptr;
+  double gkey[4] = {0, 0, 0, 0};
+  long long perStep = 0;
+};
+
+namespace {
+
+int cuda_rc(cudaError_t e) { return e == cudaSuccess ? RFGPU_OK : RFGPU_ERR_CUDA; }
+
+void rk_coeffs(int scheme, Phys &ph) {
+  for (int i = 0; i < 5; ++i) ph.ark[i] = ph.grk[i] = 0.0;
+  if (scheme == RFGPU_RK_SCHEME_4_CLASSICAL) {
+    ph.ark[0] = 0.5; ph.ark[1] = 0.5; ph.ark[2] = 1.0; ph.ark[3] = 1.0 / 6.0;
+    ph.grk[0] = 1.0; ph.grk[1] = 2.0; ph.grk[2] = 2.0; ph.grk[3] = 1.0;
+    ph.nSteps = 4;
+  } else if (scheme == RFGPU_RK_SCHEME_3_WRAY) {  // libflu/RFLU_DerivedInputValues.F90:374-389
+    ph.ark[0] = 8.0 / 15.0; ph.ark[1] = 5.0 / 12.0; ph.ark[2] = 0.75;
+    ph.grk[0] = 0.0; ph.grk[1] = 17.0 / 25.0; ph.grk[2] = 5.0 / 9.0;
+    ph.nSteps = 3;
+  } else {
+    ph.ark[0] = 1.0; ph.grk[0] = 1.0;
+    ph.nSteps = 1;
+  }
+}
+
+std::vector<Tile> make_tiles(int region, int n, int block) {
+  std::vector<Tile> t;
+  for (int i = 0; i < n; i += block) t.push_back(Tile{region, i});
+  return t;
+}
+
+int check_desc(const rfgpu_region_desc_t *d) {
+  if (!d || d->nCells <= 0 || d->nFaces < 0 || d->nPatches < 0 || !d->cv || !d->vol ||
+      !d->cofg || (d->nFaces > 0 && (!d->f2c || !d->fn || !d->fc)) || d->f2cLd < 2 ||
+      !d->c2csOffsets || !d->c2csMembers || !d->xyzMoms || (d->nPatches > 0 && !d->patches))
+    return RFGPU_ERR_ARG;
+  if (d->gasModel != RFGPU_GAS_MODEL_TCPERF || d->flowModel != RFGPU_FLOW_EULER)
+    return RFGPU_ERR_UNSUPPORTED;
+  if (d->spaceDiscr != RFGPU_DISCR_UPW_ROE && d->spaceDiscr != RFGPU_DISCR_UPW_HLLC &&
+      d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUS)
+    return RFGPU_ERR_UNSUPPORTED;
+  if (d->spaceOrder != 1 && d->spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
+  if (d->reconst != RFGPU_RECONST_NONE && d->reconst != RFGPU_RECONST_LIM_VENKAT)
+    return RFGPU_ERR_UNSUPPORTED;
+  if (d->rkScheme < 1 || d->rkScheme > 3) return RFGPU_ERR_UNSUPPORTED;
+  if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED) return RFGPU_ERR_UNSUPPORTED;
+  for (int ip = 0; ip < d->nPatches; ++ip) {
+    const rfgpu_patch_t &p = d->patches[ip];
+    if (p.nBFaces < 0 || (p.nBFaces > 0 && (!p.bf2c || !p.fn || !p.fc))) return RFGPU_ERR_ARG;
+    if (p.bcType != RFGPU_BC_SLIPWALL && p.bcType != RFGPU_BC_OUTFLOW) return RFGPU_ERR_UNSUPPORTED;
+    if (p.spaceOrder != 1 && p.spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
+    if (p.bcType == RFGPU_BC_OUTFLOW) {
+      if (p.bcOptType < 0 || p.bcOptType > 2) return RFGPU_ERR_UNSUPPORTED;
+      if (p.bcOptType != RFGPU_BCOPT_SUPERSONIC && !p.vals) return RFGPU_ERR_ARG;
+    }
+  }
+  const long long N = d->nCells;
+  for (int f = 0; f < d->nFaces; ++f)
+    for (int k = 0; k < 2; ++k) {
+      int c = d->f2c[(long long)f * d->f2cLd + k];
+      if (c < 1 || c > N) return RFGPU_ERR_ARG;
+    }
+  if (d->c2csOffsets[0] != 0) return RFGPU_ERR_ARG;
+  for (long long c = 0; c < N; ++c)
+    if (d->c2csOffsets[c + 1] < d->c2csOffsets[c]) return RFGPU_ERR_ARG;
+  for (long long e = 0; e < d->c2csOffsets[N]; ++e)
+    if (d->c2csMembers[e] < 1 || d->c2csMembers[e] > N) return RFGPU_ERR_ARG;
+  for (int ip = 0; ip < d->nPatches; ++ip)
+    for (int b = 0; b < d->patches[ip].nBFaces; ++b)
+      if (d->patches[ip].bf2c[b] < 1 || d->patches[ip].bf2c[b] > N) return RFGPU_ERR_ARG;
+  return RFGPU_OK;
+}
+
+template <typename R>
+std::vector<R> cast(const std::vector<double> &v) {
+  return std::vector<R>(v.begin(), v.end());
+}
+
+template <typename R>
+RegionDev<R> &rd(rfgpu_region_s *h);
+template <>
+RegionDev<double> &rd<double>(rfgpu_region_s *h) { return h->rd64; }
+template <>
+RegionDev<float> &rd<float>(rfgpu_region_s *h) { return h->rd32; }
+
+// Fill device arrays of precision R.
+template <typename R>
+void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &ph) {
+  cudaStream_t s = h->stream;
+  DevAlloc &M = h->mem;
+  const int N = d->nCells, F = d->nFaces;
+  RegionDev<R> g{};
+  g.nCells = N;
+  g.nFaces = F;
+  g.ph = ph;
+  // ---- cells
+  std::vector<double> cofg(3 * (size_t)N), vol(N), epsq(N), moms(6 * (size_t)N);
+  for (int c = 0; c < N; ++c) {
+    for (int k = 0; k < 3; ++k) cofg[(size_t)k * N + c] = d->cofg[3 * (size_t)c + k];
+    vol[c] = d->vol[c];
+    // eps^2 = (K*vol^(1/3))^3, K = 1 (modflu/RFLU_ModLimiters.F90:386,459-462)
+    double ds = std::pow(d->vol[c], 1.0 / 3.0);
+    epsq[c] = ds * ds * ds;
+    for (int k = 0; k < 6; ++k) moms[(size_t)k * N + c] = d->xyzMoms[10 * (size_t)c + k];
+  }
+  g.vol = M.upload(vol, s);
+  g.epsq = M.upload(cast<R>(epsq), s);
+  // ---- stencil SELL
+  {
+    std::vector<int> cnt(N);
+    for (int c = 0; c < N; ++c) cnt[c] = d->c2csOffsets[c + 1] - d->c2csOffsets[c];
+    Sell sl;
+    sl.build(cnt);
+    std::vector<int> idx(sl.total, 0);
+    for (int c = 0; c < N; ++c)
+      for (int k = 0; k < cnt[c]; ++k) idx[sl.at(c, k)] = d->c2csMembers[d->c2csOffsets[c] + k] - 1;
+    g.stOff = M.upload(sl.off, s);
+    g.stCnt = M.upload(sl.cnt, s);
+    g.stIdx = M.upload(idx, s);
+    g.stTotal = sl.total;
+    // weights on the device with the reference arithmetic (FP64 unit)
+    double *dcofg = M.alloc<double>(cofg.size());
+    double *dmoms = M.alloc<double>(moms.size());
+    cudaMemcpyAsync(dcofg, cofg.data(), cofg.size() * 8, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(dmoms, moms.data(), moms.size() * 8, cudaMemcpyHostToDevice, s);
+    double *w64 = M.alloc<double>(3 * (size_t)sl.total);
+    launch_weights64(g.stOff, g.stCnt, g.stIdx, N, dcofg, dmoms, w64, s, sl.total);
+    if (sizeof(R) == 8) {
+      g.stW = (const R *)w64;
+    } else {
+      float *w32 = M.alloc<float>(3 * (size_t)sl.total);
+      launch_to_f32(w64, w32, 3 * sl.total, s);
+      g.stW = (const R *)w32;
+    }
+  }
+  // ---- faces
+  std::vector<int> f2c(2 * (size_t)F);
+  std::vector<double> fn(4 * (size_t)F), fdl(3 * (size_t)F), fdr(3 * (size_t)F);
+  for (int f = 0; f < F; ++f) {
+    int c1 = d->f2c[(long long)f * d->f2cLd] - 1, c2 = d->f2c[(long long)f * d->f2cLd + 1] - 1;
+    f2c[f] = c1;
+    f2c[(size_t)F + f] = c2;
+    for (int k = 0; k < 4; ++k) fn[(size_t)k * F + f] = d->fn[4 * (size_t)f + k];
+    for (int k = 0; k < 3; ++k) {
+      double xc = d->fc[3 * (size_t)f + k];
+      fdl[(size_t)k * F + f] = xc - d->cofg[3 * (size_t)c1 + k];
+      fdr[(size_t)k * F + f] = xc - d->cofg[3 * (size_t)c2 + k];
+    }
+  }
+  g.f2c = M.upload(f2c, s);
+  g.fn64 = M.upload(fn, s);
+  g.fn = sizeof(R) == 8 ? (const R *)g.fn64 : M.upload(cast<R>(fn), s);
+  g.fdl = M.upload(cast<R>(fdl), s);
+  g.fdr = M.upload(cast<R>(fdr), s);
+  g.flux = M.alloc<R>(5 * (size_t)F);
+  g.srad = M.alloc<double>(F);
+  // ---- boundary faces, patches in order
+  std::vector<int> bf2c, bkind;
+  std::vector<double> bfnA, bfdA, bpout;
+  for (int ip = 0; ip < d->nPatches; ++ip) {
+    const rfgpu_patch_t &p = d->patches[ip];
+    int type = p.bcType == RFGPU_BC_SLIPWALL ? BK_SLIP : BK_OUTFLOW;
+    for (int b = 0; b < p.nBFaces; ++b) {
+      int c = p.bf2c[b] - 1;
+      bf2c.push_back(c);
+      bkind.push_back(bk_pack(type, p.spaceOrder, type == BK_OUTFLOW ? p.bcOptType : 0));
+      double pout = 0.0;
+      if (type == BK_OUTFLOW && p.bcOptType != RFGPU_BCOPT_SUPERSONIC) pout = p.vals[p.distrib ? b : 0];
+      bpout.push_back(pout);
+      for (int k = 0; k < 4; ++k) bfnA.push_back(p.fn[4 * (size_t)b + k]);
+      for (int k = 0; k < 3; ++k) bfdA.push_back(p.fc[3 * (size_t)b + k] - d->cofg[3 * (size_t)c + k]);
+    }
+  }
+  const int B = (int)bf2c.size();
+  g.nBFaces = B;
+  std::vector<double> bfn(4 * (size_t)B), bfd(3 * (size_t)B);
+  for (int b = 0; b < B; ++b) {
+    for (int k = 0; k < 4; ++k) bfn[(size_t)k * B + b] = bfnA[4 * (size_t)b + k];
+    for (int k = 0; k < 3; ++k) bfd[(size_t)k * B + b] = bfdA[3 * (size_t)b + k];
+  }
+  g.bf2c = M.upload(bf2c, s);
+  g.bkind = M.upload(bkind, s);
+  g.bpout = M.upload(bpout, s);
+  g.bfn64 = M.upload(bfn, s);
+  g.bfn = sizeof(R) == 8 ? (const R *)g.bfn64 : M.upload(cast<R>(bfn), s);
+  g.bfd = M.upload(cast<R>(bfd), s);
+  g.bflux = M.alloc<R>(5 * (size_t)B);
+  g.sradb = M.alloc<double>(B);
+  // ---- cell -> face lists in the reference accumulation order
+  {
+    std::vector<int> cnt(N, 0);
+    for (int f = 0; f < F; ++f) {
+      cnt[f2c[f]]++;
+      cnt[f2c[(size_t)F + f]]++;
+    }
+    for (int b = 0; b < B; ++b) cnt[bf2c[b]]++;
+    Sell sl;
+    sl.build(cnt);
+    std::vector<int> code(sl.total, 0), nb(sl.total, -1);
+    std::vector<double> cd(3 * (size_t)sl.total, 0.0);
+    std::vector<int> fill(N, 0);
+    for (int f = 0; f < F; ++f) {
+      for (int side = 0; side < 2; ++side) {
+        int c = f2c[(size_t)side * F + f];
+        long long e = sl.at(c, fill[c]++);
+        code[e] = 2 * f + side;
+        nb[e] = f2c[(size_t)(1 - side) * F + f];
+        const std::vector<double> &fd = side == 0 ? fdl : fdr;
+        for (int k = 0; k < 3; ++k) cd[(size_t)k * sl.total + e] = -fd[(size_t)k * F + f];
+      }
+    }
+    for (int b = 0; b < B; ++b) {
+      int c = bf2c[b];
+      long long e = sl.at(c, fill[c]++);
+      code[e] = -(b + 1);
+    }
+    g.cfOff = M.upload(sl.off, s);
+    g.cfCnt = M.upload(sl.cnt, s);
+    g.cfCode = M.upload(code, s);
+    g.cfNb = M.upload(nb, s);
+    g.cfD = M.upload(cast<R>(cd), s);
+    g.cfTotal = sl.total;
+  }
+  // ---- state
+  g.cv = M.alloc<double>(5 * (size_t)N);
+  g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
+  g.rhsSum = M.alloc<double>(5 * (size_t)N);
+  g.dv = M.alloc<double>(3 * (size_t)N);
+  g.rhs = M.alloc<double>(5 * (size_t)N);
+  g.prim = M.alloc<R>(5 * (size_t)N);
+  g.grad = M.alloc<R>(15 * (size_t)N);
+  cudaMemsetAsync(g.grad, 0, 15 * (size_t)N * sizeof(R), s);
+  cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
+  g.dtBits = M.alloc<unsigned long long>(1);
+  unsigned long long inf = 0x7FF0000000000000ull;
+  cudaMemcpyAsync(g.dtBits, &inf, 8, cudaMemcpyHostToDevice, s);
+  g.scal = M.alloc<double>(4);
+  cudaMemsetAsync(g.scal, 0, 4 * sizeof(double), s);
+  g.status = M.alloc<unsigned>(1);
+  cudaMemsetAsync(g.status, 0, sizeof(unsigned), s);
+  h->nBFaces = B;
+  rd<R>(h) = g;
+  RegionDev<R> *dregs = M.alloc<RegionDev<R>>(1);
+  cudaMemcpyAsync(dregs, &rd<R>(h), sizeof(RegionDev<R>), cudaMemcpyHostToDevice, s);
+  h->regsDev = dregs;
+  cudaStreamSynchronize(s);  // host vectors above go out of scope
+}
+
+template <typename R>
+const RegionDev<R> *regs_of(rfgpu_region_s *h) {
+  return (const RegionDev<R> *)h->regsDev;
+}
+
+int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
+  cudaStream_t s = h->stream;
+  const int N = h->nCells;
+  double *dcv = h->prec ? h->rd32.cv : h->rd64.cv;
+  double *ddv = h->prec ? h->rd32.dv : h->rd64.dv;
+  if (cudaMemcpyAsync(h->stage, cv, 5 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  launch_aos_to_soa(h->stage, dcv, N, 5, s);
+  if (dv) {
+    if (cudaMemcpyAsync(h->stage, dv, 3 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    launch_aos_to_soa(h->stage, ddv, N, 3, s);
+  }
+  if (h->prec)
+    launch_prim<float>(regs_of<float>(h), h->work, dv ? 0 : 1, s);
+  else
+    launch_prim<double>(regs_of<double>(h), h->work, dv ? 0 : 1, s);
+  h->launches += dv ? 3 : 2;
+  return cuda_rc(cudaGetLastError());
+}
+
+void stage_launch(rfgpu_region_s *h, const StepArgs &a) {
+  if (h->prec)
+    launch_stage<float>(regs_of<float>(h), h->work, a, h->stream, &h->launches, h->spaceOrder,
+                        h->reconst);
+  else
+    launch_stage<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches, h->spaceOrder,
+                         h->reconst);
+}
+
+void dt_launch(rfgpu_region_s *h, const DtArgs &a) {
+  if (h->prec)
+    launch_dt<float>(regs_of<float>(h), h->work, a, h->stream, &h->launches);
+  else
+    launch_dt<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches);
+}
+
+void step_launch(rfgpu_region_s *h, double cfl, double dtImposed, double dtMinLimit,
+                 double endTime) {
+  DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
+  dt_launch(h, da);
+  for (int is = 1; is <= h->nSteps; ++is) {
+    StepArgs sa{is, 1, 0.0, 0, 1};
+    stage_launch(h, sa);
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
+  if (!out) return RFGPU_ERR_ARG;
+  *out = nullptr;
+  int rc = check_desc(d);
+  if (rc != RFGPU_OK) return rc;
+  rfgpu_region_s *h = new (std::nothrow) rfgpu_region_s();
+  if (!h) return RFGPU_ERR_NOMEM;
+  h->prec = d->precision;
+  h->nCells = d->nCells;
+  h->nFaces = d->nFaces;
+  h->rkScheme = d->rkScheme;
+  h->spaceOrder = d->spaceOrder;
+  h->reconst = d->spaceOrder > 1 ? d->reconst : 0;
+  if (cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete h;
+    return RFGPU_ERR_CUDA;
+  }
+  Phys ph{};
+  ph.refCp = d->refCp;
+  ph.refGamma = d->refGamma;
+  ph.gcRef = d->refCp - d->refCp / d->refGamma;   // MixtPerf_R_CpG
+  ph.gvCp = d->gvCp;
+  ph.gvMol = d->gvMol;
+  ph.gvR = 8314.3 / d->gvMol;                     // MixtPerf_R_M
+  ph.gvG = d->gvCp / (d->gvCp - ph.gvR);          // MixtPerf_G_CpR
+  ph.epsentr = d->epsentr;
+  ph.dissFact = d->dissFact;
+  rk_coeffs(d->rkScheme, ph);
+  ph.rkScheme = d->rkScheme;
+  ph.spaceDiscr = d->spaceDiscr;
+  ph.spaceOrder = d->spaceOrder;
+  ph.reconst = h->reconst;
+  ph.venkatGuard = d->venkatGuard;
+  h->nSteps = ph.nSteps;
+  try {
+    if (h->prec)
+      build_region<float>(h, d, ph);
+    else
+      build_region<double>(h, d, ph);
+    const int block = 128;
+    auto ct = make_tiles(0, h->nCells, block);
+    auto ft = make_tiles(0, h->nFaces, block);
+    auto bt = make_tiles(0, h->nBFaces, block);
+    h->cellTiles = h->mem.upload(ct, h->stream);
+    h->faceTiles = h->mem.upload(ft, h->stream);
+    h->bfaceTiles = h->mem.upload(bt, h->stream);
+    h->work = Work{h->cellTiles, h->faceTiles, h->bfaceTiles, (int)ct.size(), (int)ft.size(),
+                   (int)bt.size(), 0, block, 1};
+    h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
+    cudaStreamSynchronize(h->stream);
+  } catch (const std::bad_alloc &) {
+    h->mem.free_all();
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return RFGPU_ERR_NOMEM;
+  }
+  rc = upload_state(h, d->cv, d->dv);
+  if (rc == RFGPU_OK) rc = cuda_rc(cudaStreamSynchronize(h->stream));
+  if (rc != RFGPU_OK) {
+    h->mem.free_all();
+    cudaStreamDestroy(h->stream);
+    delete h;
+    return rc;
+  }
+  *out = h;
+  return RFGPU_OK;
+}
+
+int rfgpu_region_destroy(rfgpu_region_t h) {
+  if (!h) return RFGPU_ERR_ARG;
+  cudaStreamSynchronize(h->stream);
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  h->mem.free_all();
+  cudaStreamDestroy(h->stream);
+  delete h;
+  return RFGPU_OK;
+}
+
+int rfgpu_stage(rfgpu_region_t h, int istage, double dtMin) {
+  if (!h || istage < 1 || istage > h->nSteps) return RFGPU_ERR_ARG;
+  StepArgs a{istage, 0, dtMin, 0, 1};
+  stage_launch(h, a);
+  return cuda_rc(cudaGetLastError());
+}
+
+int rfgpu_dt(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
+             double currentTime, double *dtMin) {
+  if (!h || !dtMin) return RFGPU_ERR_ARG;
+  DtArgs a{cfl, dtImposed, dtMinLimit, 0.0, 0, currentTime};
+  dt_launch(h, a);
+  double *scal = h->prec ? h->rd32.scal : h->rd64.scal;
+  if (cudaMemcpyAsync(dtMin, scal, 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_step(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit, double endTime) {
+  if (!h) return RFGPU_ERR_ARG;
+  step_launch(h, cfl, dtImposed, dtMinLimit, endTime);
+  return cuda_rc(cudaGetLastError());
+}
+
+int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed,
+                      double dtMinLimit, double endTime) {
+  if (!h || nSteps < 0) return RFGPU_ERR_ARG;
+  double key[4] = {cfl, dtImposed, dtMinLimit, endTime};
+  if (!h->graph || std::memcmp(key, h->gkey, sizeof(key)) != 0) {
+    if (h->graph) {
+      cudaGraphExecDestroy(h->graph);
+      h->graph = nullptr;
+    }
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    long long before = h->launches;
+    step_launch(h, cfl, dtImposed, dtMinLimit, endTime);
+    h->perStep = h->launches - before;  // counted at replay
+    h->launches = before;
+    if (cudaStreamEndCapture(h->stream, &g) != cudaSuccess) return RFGPU_ERR_CUDA;
+    cudaError_t e = cudaGraphInstantiate(&h->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return RFGPU_ERR_CUDA;
+    std::memcpy(h->gkey, key, sizeof(key));
+  }
+  for (int i = 0; i < nSteps; ++i)
+    if (cudaGraphLaunch(h->graph, h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  h->launches += h->perStep * nSteps;
+  return RFGPU_OK;
+}
+
+int rfgpu_residual(rfgpu_region_t h, double *rhs) {
+  if (!h) return RFGPU_ERR_ARG;
+  StepArgs a{1, 0, 0.0, 1, 0};
+  stage_launch(h, a);
+  if (!rhs) return cuda_rc(cudaGetLastError());
+  const int N = h->nCells;
+  double *drhs = h->prec ? h->rd32.rhs : h->rd64.rhs;
+  launch_soa_to_aos(drhs, h->stage, N, 5, h->stream);
+  h->launches++;
+  if (cudaMemcpyAsync(rhs, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
+  if (!h) return RFGPU_ERR_ARG;
+  const int N = h->nCells;
+  if (cv) {
+    launch_soa_to_aos(h->prec ? h->rd32.cv : h->rd64.cv, h->stage, N, 5, h->stream);
+    h->launches++;
+    if (cudaMemcpyAsync(cv, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+  }
+  if (dv) {
+    // stage is reused: wait for the cv copy first
+    if (cv && cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+    launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->stream);
+    h->launches++;
+    if (cudaMemcpyAsync(dv, h->stage, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+  }
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv) {
+  if (!h || !cv) return RFGPU_ERR_ARG;
+  int rc = upload_state(h, cv, dv);
+  if (rc != RFGPU_OK) return rc;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_download_grad(rfgpu_region_t h, double *grad) {
+  if (!h || !grad) return RFGPU_ERR_ARG;
+  const int N = h->nCells;
+  double *tmp = nullptr;
+  if (cudaMalloc(&tmp, 15 * (size_t)N * 8) != cudaSuccess) return RFGPU_ERR_NOMEM;
+  if (h->prec)
+    launch_soa_to_aos_f32(h->rd32.grad, tmp, N, 15, h->stream);
+  else
+    launch_soa_to_aos(h->rd64.grad, tmp, N, 15, h->stream);
+  h->launches++;
+  cudaError_t e = cudaMemcpyAsync(grad, tmp, 15 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);
+  cudaFree(tmp);
+  return cuda_rc(e);
+}
+
+int rfgpu_time(rfgpu_region_t h, double *currentTime, double *dtMin) {
+  if (!h) return RFGPU_ERR_ARG;
+  double sc[4];
+  double *scal = h->prec ? h->rd32.scal : h->rd64.scal;
+  if (cudaMemcpyAsync(sc, scal, sizeof(sc), cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (currentTime) *currentTime = sc[1];
+  if (dtMin) *dtMin = sc[2];
+  return RFGPU_OK;
+}
+
+int rfgpu_set_time(rfgpu_region_t h, double currentTime) {
+  if (!h) return RFGPU_ERR_ARG;
+  double *scal = h->prec ? h->rd32.scal : h->rd64.scal;
+  if (cudaMemcpyAsync(scal + 1, &currentTime, 8, cudaMemcpyHostToDevice, h->stream) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_status(rfgpu_region_t h, int *flags) {
+  if (!h || !flags) return RFGPU_ERR_ARG;
+  unsigned *st = h->prec ? h->rd32.status : h->rd64.status;
+  unsigned v = 0;
+  if (cudaMemcpyAsync(&v, st, 4, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (cudaMemsetAsync(st, 0, 4, h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  *flags = (int)v;
+  return (v & (RFGPU_ST_NAN | RFGPU_ST_NEGPOS)) ? RFGPU_ERR_STATE : RFGPU_OK;
+}
+
+int rfgpu_sync(rfgpu_region_t h) {
+  if (!h) return RFGPU_ERR_ARG;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+void *rfgpu_stream(rfgpu_region_t h) { return h ? (void *)h->stream : nullptr; }
+long long rfgpu_device_bytes(rfgpu_region_t h) { return h ? h->mem.bytes : -1; }
+long long rfgpu_launch_count(rfgpu_region_t h) { return h ? h->launches : -1; }
+
+int rfgpu_set_tuning(rfgpu_region_t h, int gridCap, int unused) {
+  (void)unused;
+  if (!h || gridCap < 0) return RFGPU_ERR_ARG;
+  h->work.grid = gridCap;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  return RFGPU_OK;
+}
+
+// ---- batches ------------------------------------------------------------------
+
+int rfgpu_batch_create(rfgpu_region_t *regions, int n, rfgpu_batch_t *out) {
+  if (!regions || n <= 0 || !out) return RFGPU_ERR_ARG;
+  *out = nullptr;
+  int prec = regions[0] ? regions[0]->prec : -1;
+  for (int i = 0; i < n; ++i)
+    if (!regions[i] || regions[i]->prec != prec) return RFGPU_ERR_ARG;
+  rfgpu_batch_s *b = new (std::nothrow) rfgpu_batch_s();
+  if (!b) return RFGPU_ERR_NOMEM;
+  b->prec = prec;
+  b->regs.assign(regions, regions + n);
+  if (cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete b;
+    return RFGPU_ERR_CUDA;
+  }
+  const int block = 128;
+  std::vector<Tile> ct, ft, bt;
+  for (int i = 0; i < n; ++i) {
+    rfgpu_region_s *h = regions[i];
+    cudaStreamSynchronize(h->stream);
+    auto a = make_tiles(i, h->nCells, block), f = make_tiles(i, h->nFaces, block),
+         c = make_tiles(i, h->nBFaces, block);
+    ct.insert(ct.end(), a.begin(), a.end());
+    ft.insert(ft.end(), f.begin(), f.end());
+    bt.insert(bt.end(), c.begin(), c.end());
+    b->spaceOrder = std::max(b->spaceOrder, h->spaceOrder);
+    b->reconst = std::max(b->reconst, h->reconst);
+    if (i == 0) b->nSteps = h->nSteps;
+    if (h->nSteps != b->nSteps) {
+      cudaStreamDestroy(b->stream);
+      delete b;
+      return RFGPU_ERR_UNSUPPORTED;
+    }
+  }
+  try {
+    Tile *dct = b->mem.upload(ct, b->stream), *dft = b->mem.upload(ft, b->stream),
+         *dbt = b->mem.upload(bt, b->stream);
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n};
+    if (prec) {
+      std::vector<RegionDev<float>> v;
+      for (int i = 0; i < n; ++i) v.push_back(regions[i]->rd32);
+      b->regsDev = b->mem.upload(v, b->stream);
+    } else {
+      std::vector<RegionDev<double>> v;
+      for (int i = 0; i < n; ++i) v.push_back(regions[i]->rd64);
+      b->regsDev = b->mem.upload(v, b->stream);
+    }
+    cudaStreamSynchronize(b->stream);
+  } catch (const std::bad_alloc &) {
+    b->mem.free_all();
+    cudaStreamDestroy(b->stream);
+    delete b;
+    return RFGPU_ERR_NOMEM;
+  }
+  *out = b;
+  return RFGPU_OK;
+}
+
+int rfgpu_batch_destroy(rfgpu_batch_t b) {
+  if (!b) return RFGPU_ERR_ARG;
+  cudaStreamSynchronize(b->stream);
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->mem.free_all();
+  cudaStreamDestroy(b->stream);
+  delete b;
+  return RFGPU_OK;
+}
+
+static void batch_step_launch(rfgpu_batch_t b, double cfl, double dtImposed, double dtMinLimit,
+                              double endTime) {
+  DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
+  if (b->prec)
+    launch_dt<float>((const RegionDev<float> *)b->regsDev, b->work, da, b->stream, &b->launches);
+  else
+    launch_dt<double>((const RegionDev<double> *)b->regsDev, b->work, da, b->stream, &b->launches);
+  for (int is = 1; is <= b->nSteps; ++is) {
+    StepArgs sa{is, 1, 0.0, 0, 1};
+    if (b->prec)
+      launch_stage<float>((const RegionDev<float> *)b->regsDev, b->work, sa, b->stream,
+                          &b->launches, b->spaceOrder, b->reconst);
+    else
+      launch_stage<double>((const RegionDev<double> *)b->regsDev, b->work, sa, b->stream,
+                           &b->launches, b->spaceOrder, b->reconst);
+  }
+}
+
+int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMinLimit,
+                     double endTime) {
+  if (!b) return RFGPU_ERR_ARG;
+  batch_step_launch(b, cfl, dtImposed, dtMinLimit, endTime);
+  return cuda_rc(cudaGetLastError());
+}
+
+int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtImposed,
+                            double dtMinLimit, double endTime) {
+  if (!b || nSteps < 0) return RFGPU_ERR_ARG;
+  double key[4] = {cfl, dtImposed, dtMinLimit, endTime};
+  if (!b->graph || std::memcmp(key, b->gkey, sizeof(key)) != 0) {
+    if (b->graph) {
+      cudaGraphExecDestroy(b->graph);
+      b->graph = nullptr;
+    }
+    cudaGraph_t g;
+    if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    long long before = b->launches;
+    batch_step_launch(b, cfl, dtImposed, dtMinLimit, endTime);
+    b->perStep = b->launches - before;  // counted at replay
+    b->launches = before;
+    if (cudaStreamEndCapture(b->stream, &g) != cudaSuccess) return RFGPU_ERR_CUDA;
+    cudaError_t e = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) return RFGPU_ERR_CUDA;
+    std::memcpy(b->gkey, key, sizeof(key));
+  }
+  for (int i = 0; i < nSteps; ++i)
+    if (cudaGraphLaunch(b->graph, b->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  b->launches += b->perStep * nSteps;
+  return RFGPU_OK;
+}
+
+int rfgpu_batch_sync(rfgpu_batch_t b) {
+  if (!b) return RFGPU_ERR_ARG;
+  return cuda_rc(cudaStreamSynchronize(b->stream));
+}
+
+void *rfgpu_batch_stream(rfgpu_batch_t b) { return b ? (void *)b->stream : nullptr; }
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// rfgpu_internal.h - device-side data layout shared by the engine's
+// translation units (host API, FP64 kernels, mixed-precision kernels).
+//
+// Layout in HBM (per region, N = nCells, F = nFaces, B = nBFaces):
+//   cell state   cv[5][N], rhsSum[5][N], dv[3][N] (p,T,a)     FP64, SoA
+//   working      prim[5][N] (rho,u,v,w,p), grad[15][N] ((3*v+d)*N + c)   R
+//   stencil      SELL-32: member k of cell c at stOff[c/32] + 32*k + c%32;
+//                stIdx (0-based), stW[3][stTotal] WLSQ weights   R
+//   cell->face   SELL-32 list in the reference accumulation order (interior
+//                faces ascending, then boundary faces by patch); code >= 0:
+//                2*face + side, code < 0: -(bface+1); cfNb = other cell,
+//                cfD[3] = cofg - fc (limiter vector)
+//   faces        f2c[2][F], fn[4][F], fdl/fdr[3][F] = fc - cofg(c1/c2)
+//   boundary     bf2c[B], bfn[4][B], bfd[3][B], bkind[B], bpout[B]
+//   scratch      flux[5][F], bflux[5][B] (R), srad[F], sradb[B] (FP64)
+// R is double on the FP64 path and float on the mixed path.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace rfgpu {
+
+constexpr int kSlice = 32;
+
+// boundary kind bits
+enum { BK_SLIP = 0, BK_OUTFLOW = 1 };
+__host__ __device__ inline int bk_pack(int type, int order, int opt) {
+  return type | (order << 4) | (opt << 8);
+}
+
+struct Phys {
+  double refCp, refGamma, gcRef;    // flux kernels: cp, g, R = cp - cp/g
+  double gvR, gvG, gvCp, gvMol;     // EOS / conversions: R = 8314.3/M, g = cp/(cp-R)
+  double epsentr, dissFact;
+  double ark[5], grk[5];
+  int nSteps, rkScheme, spaceDiscr, spaceOrder, reconst, venkatGuard;
+};
+
+template <typename R>
+struct RegionDev {
+  int nCells, nFaces, nBFaces, pad_;
+  // state
+  double *cv, *cvOld, *rhsSum, *dv, *rhs;
+  R *prim, *grad;
+  // geometry
+  const double *vol;
+  const R *epsq;
+  // stencil (SELL-32)
+  const long long *stOff;
+  const int *stCnt, *stIdx;
+  const R *stW;
+  long long stTotal;
+  // cell -> face (SELL-32)
+  const long long *cfOff;
+  const int *cfCnt, *cfCode, *cfNb;
+  const R *cfD;
+  long long cfTotal;
+  // faces
+  const int *f2c;
+  const R *fn;
+  const double *fn64;
+  const R *fdl, *fdr;
+  R *flux;
+  // boundary faces
+  const int *bf2c;
+  const R *bfn;
+  const double *bfn64;
+  const R *bfd;
+  const int *bkind;
+  const double *bpout;
+  R *bflux;
+  // time step
+  double *srad, *sradb;
+  unsigned long long *dtBits;
+  double *scal;   // [0] dtMin, [1] current time, [2] dtMin of the previous step
+  unsigned *status;
+  Phys ph;
+};
+
+// A tile of work: blockDim.x consecutive items of one region.
+struct Tile {
+  int region;
+  int first;
+};
+
+struct Work {
+  const Tile *cellTiles, *faceTiles, *bfaceTiles;
+  int nCellTiles, nFaceTiles, nBFaceTiles;
+  int grid;     // blocks per launch (persistent when smaller than the tile count)
+  int block;    // items per tile == threads per block
+  int nRegions;
+};
+
+// step parameters (host-side values; dt may alternatively come from the device)
+struct StepArgs {
+  int istage;
+  int useDeviceDt;   // 1: dtMin from scal[0]
+  double dtHost;
+  int writeRhs;      // 1: store the residual into rhs
+  int update;        // 0: residual only (no RK update)
+};
+
+struct DtArgs {
+  double cfl, dtImposed, dtMinLimit, endTime;
+  int useDeviceTime;  // 1: current time from scal[1] and advance it
+  double timeHost;
+};
+
+// Launchers, instantiated for R = double (FP64 unit, no FMA contraction) and
+// R = float (mixed unit).  `regs` is a device array of RegionDev<R>.
+template <typename R>
+void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
+template <typename R>
+void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
+                  long long *launches, int spaceOrder, int reconst);
+template <typename R>
+void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
+               long long *launches);
+
+// Setup kernels of the FP64 unit.  WLSQ weights of every stencil member,
+// w64[3][stTotal], with the arithmetic of RFLU_ComputeGradCellsFast_3D
+// (modflu/RFLU_ModDifferentiationCells.F90:1029-1080); cofg is [3][N] SoA,
+// moms [6][N] (r11,r12,r22,r13,r23,r33).
+void launch_weights64(const long long *stOff, const int *stCnt, const int *stIdx, int nCells,
+                      const double *cofg, const double *moms, double *w64, cudaStream_t s,
+                      long long stTotal);
+void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s);
+// Fortran image a(ncomp,N) <-> SoA [ncomp][N]
+void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, cudaStream_t s);
+void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, cudaStream_t s);
+void launch_soa_to_aos_f32(const float *soa, double *aos, int N, int ncomp, cudaStream_t s);
+
+}  // namespace rfgpu

@@ -1,0 +1,863 @@
+// rfgpu_kernels.cuh - residual / RK-stage kernels, templated on the working
+// precision R of reconstruction, limiter and flux arithmetic.  Included by
+// rfgpu_fp64.cu (R = double, built with --fmad=false so every expression
+// rounds exactly like the unfused reference expression) and rfgpu_mixed.cu
+// (R = float).  Residual accumulation, RK update, EOS and time step are FP64
+// in both.
+//
+// Every kernel walks a tile list (region, first item); a tile is blockDim.x
+// consecutive cells / faces / boundary faces of one region, so one launch
+// covers one region or a whole batch of regions.  Grids smaller than the tile
+// count walk the list persistently.
+#pragma once
+
+#include "rfgpu_internal.h"
+
+namespace rfgpu {
+
+template <typename R> __device__ __forceinline__ R rmin(R a, R b) { return b < a ? b : a; }
+template <typename R> __device__ __forceinline__ R rmax(R a, R b) { return b > a ? b : a; }
+
+// ---- perfect-gas relations (libfloflu/MixtPerf_*.F90) ----------------------
+template <typename R>
+__device__ __forceinline__ R eo_dgpuvw(R D, R G, R P, R U, R V, R W) {
+  return P / (D * (G - R(1))) + R(0.5) * (U * U + V * V + W * W) + R(0);
+}
+
+// ---- flux functions on reconstructed states ----------------------------------
+
+// AUSM+ (modflu/RFLU_ModAUSMFlux.F90:282-367 with the state set-up of :2787-2846)
+template <typename R>
+__device__ __forceinline__ void ausm_flux(const Phys &ph, const R L[5], const R Rt[5],
+                                          R nx, R ny, R nz, R nm, R flx[5]) {
+  const R cp = R(ph.refCp), g = R(ph.refGamma), gc = R(ph.gcRef), fs = R(0);
+  R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
+  R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
+  R tl = pl / (rl * gc);
+  R al = sqrt(g * gc * tl);
+  R Hl = cp * tl + R(0.5) * (ul * ul + vl * vl + wl * wl) + R(0);
+  R tr = pr / (rr * gc);
+  R ar = sqrt(g * gc * tr);
+  R Hr = cp * tr + R(0.5) * (ur * ur + vr * vr + wr * wr) + R(0);
+  R ql = ul * nx + vl * ny + wl * nz - fs;
+  R qr = ur * nx + vr * ny + wr * nz - fs;
+  R af = R(0.5) * (al + ar);
+  R ml = ql / af, mla = fabs(ml);
+  R mr = qr / af, mra = fabs(mr);
+  R mlp, wtl, mrm, wtr;
+  if (mla <= R(1)) {
+    mlp = R(0.25) * (ml + R(1)) * (ml + R(1)) + R(0.125) * (ml * ml - R(1)) * (ml * ml - R(1));
+    wtl = R(0.25) * (ml + R(1)) * (ml + R(1)) * (R(2) - ml) +
+          R(0.1875) * ml * (ml * ml - R(1)) * (ml * ml - R(1));
+  } else {
+    mlp = R(0.5) * (ml + mla);
+    wtl = R(0.5) * (R(1) + ml / mla);
+  }
+  if (mra <= R(1)) {
+    mrm = -(R(0.25) * (mr - R(1)) * (mr - R(1))) - R(0.125) * (mr * mr - R(1)) * (mr * mr - R(1));
+    wtr = R(0.25) * (mr - R(1)) * (mr - R(1)) * (R(2) + mr) -
+          R(0.1875) * mr * (mr * mr - R(1)) * (mr * mr - R(1));
+  } else {
+    mrm = R(0.5) * (mr - mra);
+    wtr = R(0.5) * (R(1) - mr / mra);
+  }
+  R mf = mlp + mrm, mfa = fabs(mf);
+  R mfp = R(0.5) * (mf + mfa), mfm = R(0.5) * (mf - mfa);
+  R pf = wtl * pl + wtr * pr;
+  flx[0] = (af * (mfp * rl + mfm * rr)) * nm;
+  flx[1] = (af * (mfp * rl * ul + mfm * rr * ur) + pf * nx) * nm;
+  flx[2] = (af * (mfp * rl * vl + mfm * rr * vr) + pf * ny) * nm;
+  flx[3] = (af * (mfp * rl * wl + mfm * rr * wr) + pf * nz) * nm;
+  flx[4] = (af * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
+}
+
+template <typename R>
+__device__ __forceinline__ R entropy_fix(R l, R d) {  // RFLU_ModEntropyFixes.F90:95-106
+  return (l > d) ? l : (l * l + d * d) / (R(2) * d);
+}
+
+// Roe with the Harten-Hyman entropy fix (modflu/RFLU_ModRoeFlux.F90:2725-2855)
+template <typename R>
+__device__ __forceinline__ void roe_flux(const Phys &ph, const R L[5], const R Rt[5], R nx,
+                                         R ny, R nz, R nm, R flx[5]) {
+  const R cp = R(ph.refCp), g = R(ph.refGamma), gc = R(ph.gcRef), fs = R(0);
+  R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
+  R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
+  R tl = pl / (rl * gc);
+  R Hl = cp * tl + R(0.5) * (ul * ul + vl * vl + wl * wl) + R(0);
+  R ql = ul * nx + vl * ny + wl * nz - fs;
+  R tr = pr / (rr * gc);
+  R Hr = cp * tr + R(0.5) * (ur * ur + vr * vr + wr * wr) + R(0);
+  R qr = ur * nx + vr * ny + wr * nz - fs;
+  R rh = sqrt(rl * rr);
+  R wt = rl / (rl + rh);
+  R uh = wt * ul + (R(1) - wt) * ur;
+  R vh = wt * vl + (R(1) - wt) * vr;
+  R wh = wt * wl + (R(1) - wt) * wr;
+  R Hh = wt * Hl + (R(1) - wt) * Hr;
+  R qh = uh * nx + vh * ny + wh * nz - fs;
+  R sh = R(0.5) * (uh * uh + vh * vh + wh * wh);
+  R ah = sqrt((g - R(1)) * (Hh - R(0.5) * (R(2) * sh)));
+  R l1 = fabs(qh - ah), l2 = fabs(qh), l5 = fabs(qh + ah);
+  R efc = R(ph.epsentr) * l5;
+  l1 = entropy_fix(l1, efc);
+  l2 = entropy_fix(l2, efc);
+  l5 = entropy_fix(l5, efc);
+  R dr = rr - rl, du = ur - ul, de = vr - vl, dw = wr - wl, dp = pr - pl;
+  R dq = du * nx + de * ny + dw * nz;
+  R dv1 = (dp - rh * ah * dq) / (R(2) * ah * ah);
+  R dv5 = (dp + rh * ah * dq) / (R(2) * ah * ah);
+  R dv2 = dr - dp / (ah * ah);
+  R t1 = l1 * dv1, t2 = l2 * dv2, t3 = l2 * rh, t5 = l5 * dv5;
+  R df = R(ph.dissFact);
+  flx[0] = R(0.5) * (ql * rl + qr * rr) * nm - R(0.5) * df * (t1 + t2 + t5) * nm;
+  flx[1] = R(0.5) * (ql * rl * ul + pl * nx + qr * rr * ur + pr * nx) * nm -
+           R(0.5) * df * (t1 * (uh - nx * ah) + t2 * uh + t3 * (du - nx * dq) + t5 * (uh + nx * ah)) * nm;
+  flx[2] = R(0.5) * (ql * rl * vl + pl * ny + qr * rr * vr + pr * ny) * nm -
+           R(0.5) * df * (t1 * (vh - ny * ah) + t2 * vh + t3 * (de - ny * dq) + t5 * (vh + ny * ah)) * nm;
+  flx[3] = R(0.5) * (ql * rl * wl + pl * nz + qr * rr * wr + pr * nz) * nm -
+           R(0.5) * df * (t1 * (wh - nz * ah) + t2 * wh + t3 * (dw - nz * dq) + t5 * (wh + nz * ah)) * nm;
+  flx[4] = R(0.5) * (ql * rl * Hl + pl * fs + qr * rr * Hr + pr * fs) * nm -
+           R(0.5) * df * (t1 * (Hh - qh * ah) + t2 * sh + t3 * (uh * du + vh * de + wh * dw - qh * dq) +
+                          t5 * (Hh + qh * ah)) * nm;
+}
+
+// HLLC (modflu/RFLU_ModHLLCFlux.F90:2296-2409); irl/irr are the reciprocal
+// cell densities before reconstruction, as the reference uses in Hl/Hr.
+template <typename R>
+__device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R Rt[5], R irl,
+                                          R irr, R nx, R ny, R nz, R nm, R flx[5]) {
+  const R g = R(ph.refGamma), fs = R(0);
+  R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
+  R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
+  R el = eo_dgpuvw(rl, g, pl, ul, vl, wl);
+  R al = sqrt(g * pl / rl);
+  R ql = ul * nx + vl * ny + wl * nz - fs;
+  R Hl = el + irl * pl;
+  R er = eo_dgpuvw(rr, g, pr, ur, vr, wr);
+  R ar = sqrt(g * pr / rr);
+  R qr = ur * nx + vr * ny + wr * nz - fs;
+  R Hr = er + irr * pr;
+  R wt1 = sqrt(rr / rl);
+  R wt2 = R(1) / (R(1) + wt1);
+  R us = wt2 * (ul + wt1 * ur);
+  R vs = wt2 * (vl + wt1 * vr);
+  R ws = wt2 * (wl + wt1 * wr);
+  R qs = wt2 * (ql + wt1 * qr);
+  R Hs = wt2 * (Hl + wt1 * Hr);
+  R Vms = us * us + vs * vs + ws * ws;
+  R as = sqrt((g - R(1)) * (Hs - R(0.5) * Vms));
+  R sl = rmin(ql - al, qs - as);
+  R sr = rmax(qr + ar, qs + as);
+  if (sl > R(0)) {
+    flx[0] = ql * rl * nm;
+    flx[1] = (ql * rl * ul + pl * nx) * nm;
+    flx[2] = (ql * rl * vl + pl * ny) * nm;
+    flx[3] = (ql * rl * wl + pl * nz) * nm;
+    flx[4] = (ql * (rl * el + pl) + pl * fs) * nm;
+  } else if (sr < R(0)) {
+    flx[0] = qr * rr * nm;
+    flx[1] = (qr * rr * ur + pr * nx) * nm;
+    flx[2] = (qr * rr * vr + pr * ny) * nm;
+    flx[3] = (qr * rr * wr + pr * nz) * nm;
+    flx[4] = (qr * (rr * er + pr) + pr * fs) * nm;
+  } else {
+    R sm = (rr * qr * (sr - qr) - rl * ql * (sl - ql) - pr + pl) / (rr * (sr - qr) - rl * (sl - ql));
+    R ps = pl + rl * (ql - sl) * (ql - sm);
+    R rs, rus, rvs, rws, res, term;
+    if (sm > R(0)) {
+      term = R(1) / (sl - sm);
+      rs = term * (sl - ql) * rl;
+      rus = term * ((sl - ql) * rl * ul + (ps - pl) * nx);
+      rvs = term * ((sl - ql) * rl * vl + (ps - pl) * ny);
+      rws = term * ((sl - ql) * rl * wl + (ps - pl) * nz);
+      res = term * ((sl - ql) * rl * el + (ps * sm - pl * ql));
+    } else {
+      term = R(1) / (sr - sm);
+      rs = term * (sr - qr) * rr;
+      rus = term * ((sr - qr) * rr * ur + (ps - pr) * nx);
+      rvs = term * ((sr - qr) * rr * vr + (ps - pr) * ny);
+      rws = term * ((sr - qr) * rr * wr + (ps - pr) * nz);
+      res = term * ((sr - qr) * rr * er + (ps * sm - pr * qr));
+    }
+    flx[0] = sm * rs * nm;
+    flx[1] = (sm * rus + ps * nx) * nm;
+    flx[2] = (sm * rvs + ps * ny) * nm;
+    flx[3] = (sm * rws + ps * nz) * nm;
+    flx[4] = (sm * (res + ps) - ps * fs) * nm;
+  }
+}
+
+// Cell-centre values the *_ComputeFlux2_TCP loops start from: rho, u = rhou *
+// (1/rho) with rhou the conserved momentum as CellGradientsMP's Prim2Cons
+// left it (rho * u_prim), p from dv.  On the mixed path the FP32 primitive
+// state is used directly.
+template <typename R>
+__device__ __forceinline__ void cell_values(const RegionDev<R> &g, int c, R S[5], R &ir) {
+  const int N = g.nCells;
+  R rho = g.prim[c];
+  ir = R(1) / rho;
+  S[0] = rho;
+  if (sizeof(R) == 8) {
+    if (g.ph.spaceOrder > 1) {
+      S[1] = (rho * g.prim[N + c]) * ir;
+      S[2] = (rho * g.prim[2 * N + c]) * ir;
+      S[3] = (rho * g.prim[3 * N + c]) * ir;
+    } else {
+      S[1] = R(g.cv[N + c]) * ir;
+      S[2] = R(g.cv[2 * N + c]) * ir;
+      S[3] = R(g.cv[3 * N + c]) * ir;
+    }
+  } else {
+    S[1] = g.prim[N + c];
+    S[2] = g.prim[2 * N + c];
+    S[3] = g.prim[3 * N + c];
+  }
+  S[4] = g.prim[4 * N + c];
+}
+
+template <typename R>
+__device__ __forceinline__ void reconstruct(const RegionDev<R> &g, int c, R dx, R dy, R dz, R S[5]) {
+  const int N = g.nCells;
+#pragma unroll
+  for (int v = 0; v < 5; ++v)
+    S[v] = S[v] + g.grad[(3 * v) * N + c] * dx + g.grad[(3 * v + 1) * N + c] * dy +
+           g.grad[(3 * v + 2) * N + c] * dz;
+}
+
+// One face term of RFLU_ComputeLimiterVenkat (modflu/RFLU_ModLimiters.F90:482-504).
+// guard = 0 keeps the reference's denom + TINY; guard = 1 adds TINY with the
+// sign of denom (for d2 < 0 the reference sum can cancel).
+template <typename R>
+__device__ __forceinline__ void venkat_term(R d2, R dmax, R dmin, R epsq, R &lim, int guard) {
+  const R TINY = R(1.0e-12);
+  if (d2 > R(0)) {
+    R numer = (dmax * dmax + epsq) * d2 + R(2) * d2 * d2 * dmax;
+    R denom = d2 * (dmax * dmax + R(2) * d2 * d2 + dmax * d2 + epsq);
+    R term = numer / (denom + TINY);
+    lim = rmin(term, lim);
+  } else if (d2 < R(0)) {
+    R numer = (dmin * dmin + epsq) * d2 + R(2) * d2 * d2 * dmin;
+    R denom = d2 * (dmin * dmin + R(2) * d2 * d2 + dmin * d2 + epsq);
+    R term = numer / (denom + (guard ? -TINY : TINY));
+    lim = rmin(term, lim);
+  }
+}
+
+// ---- kernels ------------------------------------------------------------------
+
+#define RF_TILE_LOOP(tiles, nTiles)                                   \
+  for (int t_ = blockIdx.x; t_ < (nTiles); t_ += gridDim.x)
+
+// Cons2Prim (modflu/RFLU_ModConvertCv.F90:221-231) of the uploaded state, and
+// optionally the EOS first (libflu/RFLU_SetDependentVars.F90:256-287).
+template <typename R>
+__global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+                       int nTiles, int computeDv) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N) continue;
+    double q0 = g.cv[c], q1 = g.cv[N + c], q2 = g.cv[2 * N + c], q3 = g.cv[3 * N + c],
+           q4 = g.cv[4 * N + c];
+    double ir = 1.0 / q0;
+    if (computeDv) {
+      double gc = g.ph.gvR, gg = g.ph.gvG;
+      double Eo = ir * q4;
+      double Vm2 = ir * ir * (q1 * q1 + q2 * q2 + q3 * q3);
+      double p = (gg - 1.0) * q0 * (Eo - 0.5 * Vm2 - 0.0);
+      double T = p / (q0 * gc);
+      g.dv[c] = p;
+      g.dv[N + c] = T;
+      g.dv[2 * N + c] = sqrt(gg * gc * T);
+    }
+    g.prim[c] = R(q0);
+    g.prim[N + c] = R(ir * q1);
+    g.prim[2 * N + c] = R(ir * q2);
+    g.prim[3 * N + c] = R(ir * q3);
+    g.prim[4 * N + c] = R(g.dv[c]);
+  }
+}
+
+// WLSQ gradients of (rho,u,v,w,p), RFLU_ComputeGradCellsFast_3D
+// (modflu/RFLU_ModDifferentiationCells.F90:1021-1149), weights precomputed.
+// One thread per cell, members in stored order: the summation order of the
+// reference.
+template <typename R>
+__global__ void __launch_bounds__(128) k_gradient(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N) continue;
+    const R *__restrict__ prim = g.prim;
+    R p0[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) p0[v] = prim[v * N + c];
+    R acc[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) acc[k] = R(0);
+    const long long T = g.stTotal;
+    long long e = g.stOff[c >> 5] + (c & 31);
+    const int n = g.stCnt[c];
+    for (int k = 0; k < n; ++k, e += kSlice) {
+      const int nb = g.stIdx[e];
+      const R wx = g.stW[e], wy = g.stW[T + e], wz = g.stW[2 * T + e];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        R dVar = prim[v * N + nb] - p0[v];
+        acc[3 * v] = acc[3 * v] + wx * dVar;
+        acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
+        acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 15; ++k) g.grad[k * N + c] = acc[k];
+  }
+}
+
+// Venkatakrishnan limiter + RFLU_LimitGradCells (modflu/RFLU_ModLimiters.F90:
+// 339-532, 707-760) as a per-cell gather over the cell's interior faces:
+// min/max and the MIN over faces do not depend on the face order, so this
+// equals the reference's two face loops.  In place on grad.
+template <typename R>
+__global__ void __launch_bounds__(128) k_limiter(const RegionDev<R> *__restrict__ regs,
+                                                 const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N || g.ph.reconst != 11) continue;
+    const R *__restrict__ prim = g.prim;
+    R p0[5], vmin[5], vmax[5], lim[5];
+#pragma unroll
+    for (int v = 0; v < 5; ++v) {
+      p0[v] = prim[v * N + c];
+      vmin[v] = p0[v];
+      vmax[v] = p0[v];
+      lim[v] = R(1);
+    }
+    const long long T = g.cfTotal;
+    const long long e0 = g.cfOff[c >> 5] + (c & 31);
+    const int n = g.cfCnt[c];
+    for (int k = 0; k < n; ++k) {
+      const long long e = e0 + (long long)k * kSlice;
+      if (g.cfCode[e] < 0) continue;
+      const int nb = g.cfNb[e];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        R x = prim[v * N + nb];
+        vmin[v] = rmin(vmin[v], x);
+        vmax[v] = rmax(vmax[v], x);
+      }
+    }
+    R G[15];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) G[k] = g.grad[k * N + c];
+    const R epsq = g.epsq[c];
+    const int guard = g.ph.venkatGuard;
+    for (int k = 0; k < n; ++k) {
+      const long long e = e0 + (long long)k * kSlice;
+      if (g.cfCode[e] < 0) continue;
+      const R dx = g.cfD[e], dy = g.cfD[T + e], dz = g.cfD[2 * T + e];
+#pragma unroll
+      for (int v = 0; v < 5; ++v) {
+        R d2 = G[3 * v] * dx + G[3 * v + 1] * dy + G[3 * v + 2] * dz;
+        venkat_term(d2, vmax[v] - p0[v], vmin[v] - p0[v], epsq, lim[v], guard);
+      }
+    }
+#pragma unroll
+    for (int v = 0; v < 5; ++v)
+#pragma unroll
+      for (int d = 0; d < 3; ++d) g.grad[(3 * v + d) * N + c] = lim[v] * G[3 * v + d];
+  }
+}
+
+// Interior face fluxes, *_ComputeFlux2_TCP face loops (AUSM+ :2726-2846,
+// Roe :2646-2855, HLLC :2239-2409), written to the face flux buffer.
+template <typename R>
+__global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restrict__ regs,
+                                                   const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int f = tl.first + threadIdx.x;
+    const int F = g.nFaces;
+    if (f >= F) continue;
+    const int c1 = g.f2c[f], c2 = g.f2c[F + f];
+    const R nx = g.fn[f], ny = g.fn[F + f], nz = g.fn[2 * F + f], nm = g.fn[3 * F + f];
+    R L[5], Rt[5], irl, irr;
+    cell_values(g, c1, L, irl);
+    cell_values(g, c2, Rt, irr);
+    if (g.ph.spaceOrder > 1) {
+      reconstruct(g, c1, g.fdl[f], g.fdl[F + f], g.fdl[2 * F + f], L);
+      reconstruct(g, c2, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
+    }
+    R flx[5];
+    const int sd = g.ph.spaceDiscr;
+    if (sd == 4)
+      ausm_flux(g.ph, L, Rt, nx, ny, nz, nm, flx);
+    else if (sd == 1)
+      roe_flux(g.ph, L, Rt, nx, ny, nz, nm, flx);
+    else
+      hllc_flux(g.ph, L, Rt, irl, irr, nx, ny, nz, nm, flx);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) g.flux[k * F + f] = flx[k];
+  }
+}
+
+// Outflow boundary state, libfloflu/BcondOutflowPerf.F90:88-160 (ksg = 0).
+template <typename R>
+__device__ __forceinline__ void bcond_outflow(int bcOpt, R pout, R sxn, R syn, R szn, R gamma,
+                                              R rho, R rhou, R rhov, R rhow, R rhoe, R press,
+                                              R &rhob, R &rhoub, R &rhovb, R &rhowb, R &rhoeb) {
+  R u = rhou / rho, v = rhov / rho, w = rhow / rho;
+  R csound = sqrt(gamma * press / rho);
+  R mach = sqrt(u * u + v * v + w * w) / csound;
+  if (mach < R(1) && (bcOpt == 1 || bcOpt == 2)) {
+    R rrhoc = R(1) / (rho * csound);
+    R deltp = press - pout;
+    rhob = rho - deltp / (csound * csound);
+    R ub = u + sxn * deltp * rrhoc;
+    R vb = v + syn * deltp * rrhoc;
+    R wb = w + szn * deltp * rrhoc;
+    R vnd = ub * sxn + vb * syn + wb * szn;
+    if (vnd < R(0)) {
+      ub = copysign(R(1), u) * rmax(fabs(ub), fabs(u));
+      vb = copysign(R(1), v) * rmax(fabs(vb), fabs(v));
+      wb = copysign(R(1), w) * rmax(fabs(wb), fabs(w));
+    }
+    rhoub = rhob * ub;
+    rhovb = rhob * vb;
+    rhowb = rhob * wb;
+    rhoeb = rhob * eo_dgpuvw(rhob, gamma, pout, ub, vb, wb);
+  } else {
+    rhob = rho;
+    rhoub = rhou;
+    rhovb = rhov;
+    rhowb = rhow;
+    rhoeb = rhoe;
+  }
+}
+
+// Boundary face fluxes: slip wall and outflow patches of
+// rocflu/RFLU_CentralSecondPatch.F90:638-1013 (ORDER 2) and
+// rocflu/RFLU_CentralFirstPatch.F90:575-946 (ORDER 1).  Slip walls store -0.0
+// as mass flux, the exact additive identity, since the reference leaves the
+// mass residual untouched there.
+template <typename R>
+__global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restrict__ regs,
+                                                    const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int b = tl.first + threadIdx.x;
+    const int B = g.nBFaces;
+    if (b >= B) continue;
+    const int N = g.nCells;
+    const int c = g.bf2c[b];
+    const int kind = g.bkind[b];
+    const int type = kind & 15, order = (kind >> 4) & 15, opt = kind >> 8;
+    const R nx = g.bfn[b], ny = g.bfn[B + b], nz = g.bfn[2 * B + b], nm = g.bfn[3 * B + b];
+    const R fs = R(0);
+    R flx[5];
+    R S[5], ir;
+    cell_values(g, c, S, ir);
+    if (order == 2) reconstruct(g, c, g.bfd[b], g.bfd[B + b], g.bfd[2 * B + b], S);
+    if (type == BK_SLIP) {
+      R pl = S[4];
+      flx[0] = R(-0.0);
+      flx[1] = pl * nx * nm;
+      flx[2] = pl * ny * nm;
+      flx[3] = pl * nz * nm;
+      flx[4] = pl * fs * nm;
+    } else {
+      const R gvG = R(g.ph.gvG);
+      R rl, rul, rvl, rwl, rel, pl;
+      if (order == 2) {
+        rl = S[0];
+        pl = S[4];
+        rul = rl * S[1];
+        rvl = rl * S[2];
+        rwl = rl * S[3];
+        rel = rl * eo_dgpuvw(rl, gvG, pl, S[1], S[2], S[3]);
+      } else {
+        rl = g.prim[c];
+        pl = g.prim[4 * N + c];
+        if (sizeof(R) == 8 && g.ph.spaceOrder == 1) {  // no conversion round trip
+          rul = R(g.cv[N + c]);
+          rvl = R(g.cv[2 * N + c]);
+          rwl = R(g.cv[3 * N + c]);
+          rel = R(g.cv[4 * N + c]);
+        } else {  // cv as CellGradientsMP's Prim2Cons left it
+          R u = g.prim[N + c], v = g.prim[2 * N + c], w = g.prim[3 * N + c];
+          rul = rl * u;
+          rvl = rl * v;
+          rwl = rl * w;
+          rel = rl * eo_dgpuvw(rl, gvG, pl, u, v, w);
+        }
+      }
+      R pr = (opt != 0) ? R(g.bpout[b]) : pl;
+      R rr, rur, rvr, rwr, rer;
+      bcond_outflow(opt, pr, nx, ny, nz, gvG, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer);
+      R ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+      R qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+      flx[0] = R(0.5) * (ql * rl + qr * rr) * nm;
+      flx[1] = R(0.5) * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+      flx[2] = R(0.5) * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+      flx[3] = R(0.5) * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+      flx[4] = R(0.5) * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+    }
+#pragma unroll
+    for (int k = 0; k < 5; ++k) g.bflux[k * B + b] = flx[k];
+  }
+}
+
+// AfterUpdateMP checks for one cell (libfloflu/AfterUpdateMP.F90:134-136):
+// RFLU_CheckValidity, RFLU_EnforceBounds (libflu/RFLU_EnforceBounds.F90:163-232),
+// RFLU_CheckPositivity (libflu/RFLU_CheckPositivity.F90).  Returns status bits.
+__device__ __forceinline__ unsigned after_update(double gc, double gg, double q[5], double d[3]) {
+  unsigned st = 0;
+  {
+    double rho = q[0], rrho = 1.0 / rho;
+    double u = rrho * q[1], v = rrho * q[2], w = rrho * q[3];
+    if (isnan(rho) || isnan(u) || isnan(v) || isnan(w) || isnan(d[0]) || isnan(d[1])) st |= 1u;
+  }
+  {
+    const double pTol = 1.0e-12;
+    double rr = q[0], ir = 1.0 / rr;
+    double u = ir * q[1], v = ir * q[2], w = ir * q[3], Eo = ir * q[4];
+    double Vm2 = u * u + v * v + w * w;
+    double p = (gg - 1.0) * rr * (Eo - 0.5 * Vm2 - 0.0);
+    if (p <= 0.0 && fabs(p) <= pTol) {
+      p = pTol;
+      q[4] = rr * (p / (rr * (gg - 1.0)) + 0.5 * (u * u + v * v + w * w) + 0.0);
+      st |= 8u;
+    }
+  }
+  {
+    double rho = q[0], rrho = 1.0 / rho;
+    double u = rrho * q[1], v = rrho * q[2], w = rrho * q[3];
+    double Vm2 = u * u + v * v + w * w;
+    double p = d[0];
+    if (p <= 0.0) {
+      double Eo = 1.0e4 + 0.5 * Vm2 + 0.0;
+      p = (gg - 1.0) * rho * (Eo - 0.5 * Vm2 - 0.0);
+      d[0] = p;
+      d[1] = p / (rho * gc);
+      q[4] = rho * Eo;
+      st |= 4u;
+    }
+    if (rho <= 0.0 || p <= 0.0) st |= 2u;
+  }
+  return st;
+}
+
+// Face->cell residual gather in the reference accumulation order, then the
+// RK update (libfloflu/RkUpdateGeneric.F90:229-314), EOS
+// (libflu/RFLU_SetDependentVars.F90:256-287), AfterUpdate checks and
+// Cons2Prim of the new state for the next stage.  With update = 0 only the
+// residual is written (rfgpu_residual).
+template <typename R>
+__global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__restrict__ regs,
+                                                       const Tile *__restrict__ tiles,
+                                                       int nTiles, StepArgs a) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N) continue;
+    const int F = g.nFaces, B = g.nBFaces;
+    double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
+    const long long e0 = g.cfOff[c >> 5] + (c & 31);
+    const int n = g.cfCnt[c];
+    for (int k = 0; k < n; ++k) {
+      const int code = g.cfCode[e0 + (long long)k * kSlice];
+      if (code >= 0) {
+        const int f = code >> 1;
+        if (code & 1) {
+#pragma unroll
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(g.flux[j * F + f]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(g.flux[j * F + f]);
+        }
+      } else {
+        const int b = -code - 1;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(g.bflux[j * B + b]);
+      }
+    }
+    if (a.writeRhs) {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = acc[j];
+    }
+    if (!a.update) continue;
+    const Phys &ph = g.ph;
+    const double dtMin = a.useDeviceDt ? g.scal[0] : a.dtHost;
+    const int is = a.istage;
+    const double fac = ph.ark[is - 1] * dtMin;
+    const double adtv = fac / g.vol[c];
+    double q[5], old[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
+    if (ph.rkScheme == 1) {  // RK4: cvOld saved at stage 1 only
+      if (is == 1) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) {
+          old[j] = q[j];
+          g.cvOld[j * N + c] = q[j];
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) old[j] = g.cvOld[j * N + c];
+      }
+    } else {  // Wray / Euler: cvOld = cv at every stage start
+#pragma unroll
+      for (int j = 0; j < 5; ++j) old[j] = q[j];
+    }
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const double rhs = acc[j];
+      if (ph.rkScheme == 2) {
+        if (is == 1) {
+          q[j] = old[j] - adtv * rhs;
+          g.rhsSum[j * N + c] = rhs;
+        } else if (is == 2) {
+          q[j] = old[j] - adtv * (rhs - ph.grk[is - 1] * g.rhsSum[j * N + c]);
+          g.rhsSum[j * N + c] = rhs;
+        } else {
+          q[j] = old[j] - adtv * (rhs - ph.grk[is - 1] * g.rhsSum[j * N + c]);
+        }
+      } else if (ph.rkScheme == 1) {
+        if (is == 1) {
+          q[j] = old[j] - adtv * rhs;
+          g.rhsSum[j * N + c] = rhs;
+        } else if (is == ph.nSteps) {
+          q[j] = old[j] - adtv * (rhs + g.rhsSum[j * N + c]);
+        } else {
+          q[j] = old[j] - adtv * rhs;
+          g.rhsSum[j * N + c] = g.rhsSum[j * N + c] + ph.grk[is - 1] * rhs;
+        }
+      } else {
+        q[j] = old[j] - adtv * rhs;
+      }
+    }
+    // EOS
+    const double gc = ph.gvR, gg = ph.gvG;
+    double d[3];
+    {
+      double rr = q[0];
+      double ir = 1.0 / rr;
+      double Eo = ir * q[4];
+      double Vm2 = ir * ir * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+      d[0] = (gg - 1.0) * rr * (Eo - 0.5 * Vm2 - 0.0);
+      d[1] = d[0] / (rr * gc);
+      d[2] = sqrt(gg * gc * d[1]);
+    }
+    unsigned st = after_update(gc, gg, q, d);
+    if (st) atomicOr(g.status, st);
+#pragma unroll
+    for (int j = 0; j < 5; ++j) g.cv[j * N + c] = q[j];
+    g.dv[c] = d[0];
+    g.dv[N + c] = d[1];
+    g.dv[2 * N + c] = d[2];
+    const double ir = 1.0 / q[0];
+    g.prim[c] = R(q[0]);
+    g.prim[N + c] = R(ir * q[1]);
+    g.prim[2 * N + c] = R(ir * q[2]);
+    g.prim[3 * N + c] = R(ir * q[3]);
+    g.prim[4 * N + c] = R(d[0]);
+  }
+}
+
+// ---- time step: RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:165-327)
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_dt_face(const RegionDev<R> *__restrict__ regs,
+                                                 const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int f = tl.first + threadIdx.x;
+    const int F = g.nFaces, N = g.nCells;
+    if (f >= F) continue;
+    const int c1 = g.f2c[f], c2 = g.f2c[F + f];
+    const double *cv = g.cv;
+    double ir1 = 1.0 / cv[c1], ir2 = 1.0 / cv[c2];
+    double u1 = cv[N + c1] * ir1, v1 = cv[2 * N + c1] * ir1, w1 = cv[3 * N + c1] * ir1;
+    double a1 = g.dv[2 * N + c1];
+    double u2 = cv[N + c2] * ir2, v2 = cv[2 * N + c2] * ir2, w2 = cv[3 * N + c2] * ir2;
+    double a2 = g.dv[2 * N + c2];
+    double nx = g.fn64[f], ny = g.fn64[F + f], nz = g.fn64[2 * F + f], nm = g.fn64[3 * F + f];
+    double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
+    double as = 0.5 * (a1 + a2);
+    g.srad[f] = (fabs(vc - 0.0) + as) * nm;
+  }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_dt_bface(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int b = tl.first + threadIdx.x;
+    const int B = g.nBFaces, N = g.nCells;
+    if (b >= B) continue;
+    const int c = g.bf2c[b];
+    const double *cv = g.cv;
+    double ir1 = 1.0 / cv[c];
+    double u1 = cv[N + c] * ir1, v1 = cv[2 * N + c] * ir1, w1 = cv[3 * N + c] * ir1;
+    double a1 = g.dv[2 * N + c];
+    double nx = g.bfn64[b], ny = g.bfn64[B + b], nz = g.bfn64[2 * B + b], nm = g.bfn64[3 * B + b];
+    double vc = u1 * nx + v1 * ny + w1 * nz;
+    g.sradb[b] = (fabs(vc - 0.0) + a1) * nm;
+  }
+}
+
+// dt(c) = vol / sum over the cell's faces in the reference order; block
+// minimum, then an atomic minimum on the bit pattern (dt > 0, so the IEEE
+// order equals the unsigned integer order).
+template <typename R>
+__global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict__ regs,
+                                                 const Tile *__restrict__ tiles, int nTiles) {
+  __shared__ unsigned long long smin[32];
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    unsigned long long bits = 0x7FF0000000000000ull;  // +inf
+    if (c < N) {
+      double acc = 0.0;
+      const long long e0 = g.cfOff[c >> 5] + (c & 31);
+      const int n = g.cfCnt[c];
+      for (int k = 0; k < n; ++k) {
+        const int code = g.cfCode[e0 + (long long)k * kSlice];
+        acc = acc + (code >= 0 ? g.srad[code >> 1] : g.sradb[-code - 1]);
+      }
+      double dtc = g.vol[c] / acc;
+      bits = (unsigned long long)__double_as_longlong(dtc);
+    }
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long x = __shfl_down_sync(0xffffffffu, bits, o);
+      bits = x < bits ? x : bits;
+    }
+    if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = bits;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      unsigned long long v = threadIdx.x < (blockDim.x >> 5) ? smin[threadIdx.x] : 0x7FF0000000000000ull;
+      for (int o = 16; o > 0; o >>= 1) {
+        unsigned long long x = __shfl_down_sync(0xffffffffu, v, o);
+        v = x < v ? x : v;
+      }
+      if (threadIdx.x == 0) atomicMin(g.dtBits, v);
+    }
+    __syncthreads();
+  }
+}
+
+// RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:131-146,235-241) and the
+// end-time clip of rocflu/RFLU_TimeStepping.F90:490-493; one thread per region.
+template <typename R>
+__global__ void k_dt_finalize(const RegionDev<R> *__restrict__ regs, int nRegions, DtArgs a) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRegions) return;
+  const RegionDev<R> &g = regs[r];
+  double dtMin = __longlong_as_double((long long)*g.dtBits);
+  *g.dtBits = 0x7FF0000000000000ull;
+  const double t = a.useDeviceTime ? g.scal[1] : a.timeHost;
+  dtMin = a.cfl * dtMin;
+  double wI = 0.0, wC = 0.0;
+  if (t <= 1.0e-08) wI = 1.0; else wC = 1.0;
+  dtMin = wI / a.dtImposed + wC / dtMin;
+  dtMin = 1.0 / dtMin;
+  if (dtMin <= 0.0) dtMin = 6.0e-12;
+  dtMin = (a.dtMinLimit > dtMin) ? a.dtMinLimit : dtMin;
+  double tNew = t + dtMin;
+  if (a.endTime > 0.0 && t + dtMin > a.endTime) {
+    dtMin = a.endTime - t;
+    tNew = a.endTime;
+  }
+  if (a.endTime > 0.0 && t >= a.endTime) {  // finished: later stages leave cv as is
+    dtMin = 0.0;
+    tNew = t;
+  }
+  g.scal[0] = dtMin;
+  g.scal[2] = dtMin;
+  if (a.useDeviceTime) g.scal[1] = tNew;
+}
+
+// ---- launchers ----------------------------------------------------------------
+
+template <typename R>
+void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s) {
+  int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
+  if (grid > 0) k_prim<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, computeDv);
+}
+
+template <typename R>
+void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
+                  long long *launches, int spaceOrder, int reconst) {
+  auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
+  long long n = 0;
+  if (spaceOrder > 1 && w.nCellTiles > 0) {
+    k_gradient<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    ++n;
+    if (reconst == 11) {
+      k_limiter<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+      ++n;
+    }
+  }
+  if (w.nFaceTiles > 0) {
+    k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
+    ++n;
+  }
+  if (w.nBFaceTiles > 0) {
+    k_bface_flux<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
+    ++n;
+  }
+  if (w.nCellTiles > 0) {
+    k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a);
+    ++n;
+  }
+  if (launches) *launches += n;
+}
+
+template <typename R>
+void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
+               long long *launches) {
+  auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
+  long long n = 0;
+  if (w.nFaceTiles > 0) {
+    k_dt_face<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
+    ++n;
+  }
+  if (w.nBFaceTiles > 0) {
+    k_dt_bface<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
+    ++n;
+  }
+  if (w.nCellTiles > 0) {
+    k_dt_cell<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    ++n;
+  }
+  k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a);
+  ++n;
+  if (launches) *launches += n;
+}
+
+#define RFGPU_INSTANTIATE(R)                                                                  \
+  template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
+  template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
+                                cudaStream_t, long long *, int, int);                         \
+  template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
+                             long long *);
+
+}  // namespace rfgpu

@@ -1,0 +1,756 @@
+// rfmesh.cpp - host mesh builder for the residual engine (see include/rfmesh.h).
+//
+// Compiled with -ffp-contract=off so the geometry is bit-identical on every
+// host (x86_64 here, aarch64 on the GPU nodes) and matches the unfused
+// Fortran arithmetic it restates.
+#include "rfmesh.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <new>
+#include <random>
+#include <stdexcept>
+#include <vector>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+namespace {
+
+enum { T_TET = 0, T_HEX = 1, T_PRI = 2, T_PYR = 3 };
+const int kNV[4] = {4, 8, 6, 5};
+const int kNF[4] = {4, 6, 5, 5};
+// local faces, cyclic vertex order, -1 padded (tri faces)
+const int kFaces[4][6][4] = {
+    {{0, 2, 1, -1}, {0, 1, 3, -1}, {1, 2, 3, -1}, {0, 3, 2, -1}},
+    {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}},
+    {{0, 2, 1, -1}, {3, 4, 5, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}},
+    {{0, 3, 2, 1}, {0, 1, 4, -1}, {1, 2, 4, -1}, {2, 3, 4, -1}, {3, 0, 4, -1}}};
+
+struct Patch {
+  std::vector<int> bf2c;    // 0-based internally
+  std::vector<int> bf2v;    // 4 per face
+  std::vector<double> fn, fc;
+  std::vector<int> bf2c1;   // 1-based export
+};
+
+}  // namespace
+
+struct rfmesh_s {
+  int kind = 0;
+  double lo[3], hi[3];
+  std::vector<double> xyz;
+  // cells grouped by type; global numbering tets, hexes, prisms, pyramids
+  std::vector<int> c2v[4];
+  long long nOfType[4] = {0, 0, 0, 0};
+  long long nCells = 0;
+  std::vector<int> ctype, cloc;  // per global cell: type, local index
+  std::vector<double> cofgApp, cofg, vol;
+  std::vector<int> f2c;          // 2 per interior face, 0-based
+  std::vector<int> f2v;          // 4 per interior face
+  std::vector<double> fn, fc;
+  std::vector<int> f2c1;         // 1-based export
+  Patch patch[RFMESH_NPATCH];
+  std::vector<int> v2cOff, v2c;
+  std::vector<int> csOff, csMem, csMem1;
+  std::vector<double> moms;
+  int maxMembs = 0;
+
+  int nv(long long icg) const { return kNV[ctype[icg]]; }
+  const int *verts(long long icg) const {
+    int t = ctype[icg];
+    return &c2v[t][(size_t)cloc[icg] * kNV[t]];
+  }
+};
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Sorting restated from modfloflu/ModSortSearch.F90:898-990 (Wirth's
+// non-recursive quicksort).  The unstable tie-breaking decides which of the
+// equal-fraction vertex neighbours survive stencil truncation on tet meshes.
+// Arrays are 1-based in the Fortran; here a[0..n-1] with the same index math
+// shifted by one.
+void quicksort_real_int(double *a, int *b, int n) {
+  if (n <= 0) return;
+  int stackl[50], stackr[50];
+  int s = 1;
+  stackl[0] = 1;
+  stackr[0] = n;
+  int l, r;
+L10:
+  l = stackl[s - 1];
+  r = stackr[s - 1];
+  s = s - 1;
+L20: {
+  int i = l, j = r;
+  int k = (l + r) / 2;
+  double x = a[k - 1];
+  for (;;) {
+    while (a[i - 1] < x) i = i + 1;
+    while (x < a[j - 1]) j = j - 1;
+    if (i <= j) {
+      double w = a[i - 1];
+      a[i - 1] = a[j - 1];
+      a[j - 1] = w;
+      int v = b[i - 1];
+      b[i - 1] = b[j - 1];
+      b[j - 1] = v;
+      i = i + 1;
+      j = j - 1;
+      if (i > j) break;
+    } else {
+      break;
+    }
+  }
+  if (j - l >= r - i) {
+    if (l < j) {
+      s = s + 1;
+      stackl[s - 1] = l;
+      stackr[s - 1] = j;
+    }
+    l = i;
+  } else {
+    if (i < r) {
+      s = s + 1;
+      stackl[s - 1] = i;
+      stackr[s - 1] = r;
+    }
+    r = j;
+  }
+  if (l < r) goto L20;
+  if (s != 0) goto L10;
+}
+}
+
+// Singular values (descending) of a column-scaled rows x 4 matrix, from the
+// eigenvalues of A^T A by cyclic Jacobi.  Used only for the layer-growth test
+// of libflu/RFLU_InvertMatrixSVD.F90:150-190 (ratio of successive singular
+// values against 0.01, first one against 100*eps), where LAPACK dgesdd is
+// replaced by this 4x4 symmetric eigen solve.
+void singular_values4(const std::vector<double> &A, int rows, double s[4]) {
+  double g[4][4] = {{0}};
+  for (int i = 0; i < 4; ++i)
+    for (int j = 0; j < 4; ++j) {
+      double acc = 0.0;
+      for (int r = 0; r < rows; ++r) acc += A[r * 4 + i] * A[r * 4 + j];
+      g[i][j] = acc;
+    }
+  for (int sweep = 0; sweep < 60; ++sweep) {
+    double off = 0.0;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 4; ++q) off += g[p][q] * g[p][q];
+    if (off < 1e-300) break;
+    for (int p = 0; p < 4; ++p)
+      for (int q = p + 1; q < 4; ++q) {
+        if (g[p][q] == 0.0) continue;
+        double theta = (g[q][q] - g[p][p]) / (2.0 * g[p][q]);
+        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
+        double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
+        for (int k = 0; k < 4; ++k) {
+          double gkp = g[k][p], gkq = g[k][q];
+          g[k][p] = c * gkp - sn * gkq;
+          g[k][q] = sn * gkp + c * gkq;
+        }
+        for (int k = 0; k < 4; ++k) {
+          double gpk = g[p][k], gqk = g[q][k];
+          g[p][k] = c * gpk - sn * gqk;
+          g[q][k] = sn * gpk + c * gqk;
+        }
+      }
+  }
+  for (int i = 0; i < 4; ++i) s[i] = std::sqrt(std::max(g[i][i], 0.0));
+  std::sort(s, s + 4, [](double a, double b) { return a > b; });
+}
+
+int svd_scount(const std::vector<double> &A, int rows) {
+  double s[4];
+  singular_values4(A, rows, s);
+  const double eps = std::numeric_limits<double>::epsilon();
+  int sCount = 0;
+  if (!(s[0] > 100.0 * eps)) sCount = 1;
+  for (int i = 1; i < 4; ++i) {
+    if (s[i] > 0.01 * s[i - 1]) continue;
+    sCount += 4 - i;
+    break;
+  }
+  return sCount;
+}
+
+// FaceVectorTria / FaceVectorQuad (libfloflu/FaceVector.F90:79-136) and
+// FaceCentroidTria / FaceCentroidQuad (libfloflu/FaceCentroid.F90:77-122).
+void face_vec_cen(const double *xyz, const int *fv, double S[3], double C[3]) {
+  if (fv[3] < 0) {
+    const double *p1 = xyz + 3 * (size_t)fv[0], *p2 = xyz + 3 * (size_t)fv[1],
+                 *p3 = xyz + 3 * (size_t)fv[2];
+    double dxa = p1[0] - p2[0], dya = p1[1] - p2[1], dza = p1[2] - p2[2];
+    double dxb = p1[0] - p3[0], dyb = p1[1] - p3[1], dzb = p1[2] - p3[2];
+    S[0] = 0.5 * (dya * dzb - dyb * dza);
+    S[1] = -0.5 * (dxa * dzb - dxb * dza);
+    S[2] = 0.5 * (dxa * dyb - dxb * dya);
+    const double thrd = 1.0 / 3.0;
+    C[0] = thrd * (p1[0] + p2[0] + p3[0]);
+    C[1] = thrd * (p1[1] + p2[1] + p3[1]);
+    C[2] = thrd * (p1[2] + p2[2] + p3[2]);
+  } else {
+    const double *p1 = xyz + 3 * (size_t)fv[0], *p2 = xyz + 3 * (size_t)fv[1],
+                 *p3 = xyz + 3 * (size_t)fv[2], *p4 = xyz + 3 * (size_t)fv[3];
+    double dxa = p3[0] - p1[0], dya = p3[1] - p1[1], dza = p3[2] - p1[2];
+    double dxb = p2[0] - p4[0], dyb = p2[1] - p4[1], dzb = p2[2] - p4[2];
+    S[0] = 0.5 * (dza * dyb - dya * dzb);
+    S[1] = 0.5 * (dxa * dzb - dza * dxb);
+    S[2] = 0.5 * (dya * dxb - dxa * dyb);
+    C[0] = 0.25 * (p1[0] + p2[0] + p3[0] + p4[0]);
+    C[1] = 0.25 * (p1[1] + p2[1] + p3[1] + p4[1]);
+    C[2] = 0.25 * (p1[2] + p2[2] + p3[2] + p4[2]);
+  }
+}
+
+inline uint64_t vid(int i, int j, int k, int nx, int ny) {
+  return (uint64_t)i + (uint64_t)(nx + 1) * ((uint64_t)j + (uint64_t)(ny + 1) * (uint64_t)k);
+}
+
+// ---------------------------------------------------------------------------
+// generators
+
+struct Gen {
+  int nx, ny, nz;
+  std::vector<int> cells[4];  // vertex lists per type, in creation order
+};
+
+void add_cell(Gen &g, int t, const int *v) {
+  for (int i = 0; i < kNV[t]; ++i) g.cells[t].push_back(v[i]);
+}
+
+void generate(rfmesh_s *m, int nx, int ny, int nz, double jitter, unsigned long long seed) {
+  long long nvBase = (long long)(nx + 1) * (ny + 1) * (nz + 1);
+  double h[3] = {(m->hi[0] - m->lo[0]) / nx, (m->hi[1] - m->lo[1]) / ny,
+                 (m->hi[2] - m->lo[2]) / nz};
+  m->xyz.resize(3 * (size_t)nvBase);
+  std::mt19937_64 rng(seed);
+  const double two53 = 1.0 / 9007199254740992.0;
+  for (int k = 0; k <= nz; ++k)
+    for (int j = 0; j <= ny; ++j)
+      for (int i = 0; i <= nx; ++i) {
+        uint64_t v = vid(i, j, k, nx, ny);
+        double p[3] = {m->lo[0] + h[0] * i, m->lo[1] + h[1] * j, m->lo[2] + h[2] * k};
+        if (i == nx) p[0] = m->hi[0];
+        if (j == ny) p[1] = m->hi[1];
+        if (k == nz) p[2] = m->hi[2];
+        bool interior = i > 0 && i < nx && j > 0 && j < ny && k > 0 && k < nz;
+        if (jitter > 0.0 && interior) {
+          for (int d = 0; d < 3; ++d) {
+            double u = (double)(rng() >> 11) * two53;  // [0,1)
+            p[d] += (2.0 * u - 1.0) * jitter * h[d];
+          }
+        }
+        m->xyz[3 * v + 0] = p[0];
+        m->xyz[3 * v + 1] = p[1];
+        m->xyz[3 * v + 2] = p[2];
+      }
+  Gen g;
+  int midx = nx / 2, midz = nz / 2;
+  static const int kuhn[6][4] = {{0, 1, 2, 6}, {0, 1, 5, 6}, {0, 3, 2, 6},
+                                 {0, 3, 7, 6}, {0, 4, 5, 6}, {0, 4, 7, 6}};
+  // hex faces (cyclic) and their Freudenthal diagonal split into two triangles
+  static const int quadFace[6][4] = {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4},
+                                     {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}};
+  static const int kuhnTri[6][2][3] = {{{0, 1, 2}, {0, 2, 3}}, {{4, 5, 6}, {4, 6, 7}},
+                                       {{0, 1, 5}, {0, 5, 4}}, {{1, 2, 6}, {1, 6, 5}},
+                                       {{3, 2, 6}, {3, 6, 7}}, {{0, 4, 7}, {0, 7, 3}}};
+  auto region = [&](int i, int k) -> int {  // 0 hex, 1 prism, 2 tet (mixed mesh)
+    if (m->kind == RFMESH_HEX) return 0;
+    if (m->kind == RFMESH_TET) return 2;
+    if (i >= midx) return 1;
+    if (k >= midz) return 2;
+    return 0;
+  };
+  for (int k = 0; k < nz; ++k)
+    for (int j = 0; j < ny; ++j)
+      for (int i = 0; i < nx; ++i) {
+        int cv[8] = {(int)vid(i, j, k, nx, ny),         (int)vid(i + 1, j, k, nx, ny),
+                     (int)vid(i + 1, j + 1, k, nx, ny), (int)vid(i, j + 1, k, nx, ny),
+                     (int)vid(i, j, k + 1, nx, ny),     (int)vid(i + 1, j, k + 1, nx, ny),
+                     (int)vid(i + 1, j + 1, k + 1, nx, ny), (int)vid(i, j + 1, k + 1, nx, ny)};
+        int reg = region(i, k);
+        if (reg == 0) {
+          add_cell(g, T_HEX, cv);
+        } else if (reg == 1) {
+          int p0[6] = {cv[0], cv[1], cv[2], cv[4], cv[5], cv[6]};
+          int p1[6] = {cv[0], cv[2], cv[3], cv[4], cv[6], cv[7]};
+          add_cell(g, T_PRI, p0);
+          add_cell(g, T_PRI, p1);
+        } else {
+          // quad neighbours across the -z face (hex below) and +x face (prism)
+          bool quad[6] = {false, false, false, false, false, false};
+          if (m->kind == RFMESH_MIXED) {
+            if (k - 1 >= 0 && region(i, k - 1) != 2) quad[0] = true;
+            if (i + 1 < nx && region(i + 1, k) != 2) quad[3] = true;
+          }
+          bool transition = false;
+          for (int f = 0; f < 6; ++f) transition |= quad[f];
+          if (!transition) {
+            for (int t = 0; t < 6; ++t) {
+              int tv[4] = {cv[kuhn[t][0]], cv[kuhn[t][1]], cv[kuhn[t][2]], cv[kuhn[t][3]]};
+              add_cell(g, T_TET, tv);
+            }
+          } else {
+            // centroid vertex, then a pyramid on each quad face and two tets on
+            // every other face (split along its Freudenthal diagonal)
+            int c = (int)(m->xyz.size() / 3);
+            double pc[3] = {0, 0, 0};
+            for (int a = 0; a < 8; ++a)
+              for (int d = 0; d < 3; ++d) pc[d] += m->xyz[3 * (size_t)cv[a] + d];
+            for (int d = 0; d < 3; ++d) m->xyz.push_back(0.125 * pc[d]);
+            for (int f = 0; f < 6; ++f) {
+              if (quad[f]) {
+                int pv[5] = {cv[quadFace[f][0]], cv[quadFace[f][1]], cv[quadFace[f][2]],
+                             cv[quadFace[f][3]], c};
+                add_cell(g, T_PYR, pv);
+              } else {
+                for (int s = 0; s < 2; ++s) {
+                  int tv[4] = {cv[kuhnTri[f][s][0]], cv[kuhnTri[f][s][1]],
+                               cv[kuhnTri[f][s][2]], c};
+                  add_cell(g, T_TET, tv);
+                }
+              }
+            }
+          }
+        }
+      }
+  for (int t = 0; t < 4; ++t) {
+    m->nOfType[t] = (long long)(g.cells[t].size() / kNV[t]);
+    m->c2v[t].swap(g.cells[t]);
+  }
+}
+
+// ---------------------------------------------------------------------------
+
+void build(rfmesh_s *m, int nThreads) {
+  (void)nThreads;
+  m->nCells = m->nOfType[0] + m->nOfType[1] + m->nOfType[2] + m->nOfType[3];
+  const long long nC = m->nCells;
+  const long long nV = (long long)(m->xyz.size() / 3);
+  m->ctype.resize(nC);
+  m->cloc.resize(nC);
+  {
+    long long icg = 0;
+    for (int t = 0; t < 4; ++t)
+      for (long long l = 0; l < m->nOfType[t]; ++l, ++icg) {
+        m->ctype[icg] = t;
+        m->cloc[icg] = (int)l;
+      }
+  }
+  // approximate centroids: vertex averages (RFLU_ModGeometry.F90:1277-1460)
+  m->cofgApp.assign(3 * (size_t)nC, 0.0);
+  for (long long icg = 0; icg < nC; ++icg) {
+    int n = m->nv(icg);
+    const int *v = m->verts(icg);
+    double term = 1.0 / (double)n;
+    for (int d = 0; d < 3; ++d) {
+      double s = 0.0;
+      for (int a = 0; a < n; ++a) s = s + m->xyz[3 * (size_t)v[a] + d];
+      m->cofgApp[3 * icg + d] = term * s;
+    }
+  }
+  // face list: first encounter sweeping cells in global order; faces keyed by
+  // their sorted vertex set, chained on the smallest vertex id
+  std::vector<int> fvAll;    // 4 per face
+  std::vector<int> fc1, fc2;
+  std::vector<int64_t> head(nV, -1), next;
+  std::vector<int> keyAll;   // sorted key, 4 per face
+  fvAll.reserve(4 * (size_t)nC * 3);
+  for (long long icg = 0; icg < nC; ++icg) {
+    int t = m->ctype[icg];
+    const int *v = m->verts(icg);
+    for (int f = 0; f < kNF[t]; ++f) {
+      int fv[4];
+      for (int a = 0; a < 4; ++a) fv[a] = kFaces[t][f][a] < 0 ? -1 : v[kFaces[t][f][a]];
+      int key[4] = {fv[0], fv[1], fv[2], fv[3]};
+      int nk = key[3] < 0 ? 3 : 4;
+      std::sort(key, key + nk);
+      if (nk == 3) key[3] = -1;
+      int64_t hit = -1;
+      for (int64_t e = head[key[0]]; e >= 0; e = next[e]) {
+        const int *k2 = &keyAll[4 * e];
+        if (k2[1] == key[1] && k2[2] == key[2] && k2[3] == key[3]) {
+          hit = e;
+          break;
+        }
+      }
+      if (hit >= 0) {
+        fc2[hit] = (int)icg;
+      } else {
+        int64_t e = (int64_t)fc1.size();
+        fc1.push_back((int)icg);
+        fc2.push_back(-1);
+        for (int a = 0; a < 4; ++a) {
+          fvAll.push_back(fv[a]);
+          keyAll.push_back(key[a]);
+        }
+        next.push_back(head[key[0]]);
+        head[key[0]] = e;
+      }
+    }
+  }
+  std::vector<int64_t>().swap(head);
+  std::vector<int64_t>().swap(next);
+  std::vector<int>().swap(keyAll);
+  const int64_t nAll = (int64_t)fc1.size();
+  // orient every face outward from its first cell, then split interior/boundary
+  const double tolx = 1e-9 * (m->hi[0] - m->lo[0]), toly = 1e-9 * (m->hi[1] - m->lo[1]),
+               tolz = 1e-9 * (m->hi[2] - m->lo[2]);
+  for (int64_t e = 0; e < nAll; ++e) {
+    int *fv = &fvAll[4 * e];
+    double S[3], C[3];
+    face_vec_cen(m->xyz.data(), fv, S, C);
+    const double *ca = &m->cofgApp[3 * (size_t)fc1[e]];
+    double dot = (C[0] - ca[0]) * S[0] + (C[1] - ca[1]) * S[1] + (C[2] - ca[2]) * S[2];
+    if (dot < 0.0) {
+      if (fv[3] < 0)
+        std::swap(fv[1], fv[2]);
+      else
+        std::swap(fv[1], fv[3]);
+    }
+    if (fc2[e] >= 0) {
+      m->f2c.push_back(fc1[e]);
+      m->f2c.push_back(fc2[e]);
+      for (int a = 0; a < 4; ++a) m->f2v.push_back(fv[a]);
+    } else {
+      int ip = -1;
+      if (std::fabs(C[0] - m->lo[0]) < tolx) ip = RFMESH_XLO;
+      else if (std::fabs(C[0] - m->hi[0]) < tolx) ip = RFMESH_XHI;
+      else if (std::fabs(C[1] - m->lo[1]) < toly) ip = RFMESH_YLO;
+      else if (std::fabs(C[1] - m->hi[1]) < toly) ip = RFMESH_YHI;
+      else if (std::fabs(C[2] - m->lo[2]) < tolz) ip = RFMESH_ZLO;
+      else if (std::fabs(C[2] - m->hi[2]) < tolz) ip = RFMESH_ZHI;
+      if (ip < 0) throw std::runtime_error("boundary face off the box surface");
+      m->patch[ip].bf2c.push_back(fc1[e]);
+      for (int a = 0; a < 4; ++a) m->patch[ip].bf2v.push_back(fv[a]);
+    }
+  }
+  const int64_t nF = (int64_t)(m->f2c.size() / 2);
+  // geometry (RFLU_ModGeometry.F90:307-672)
+  m->vol.assign(nC, 0.0);
+  m->cofg.assign(3 * (size_t)nC, 0.0);
+  m->fn.resize(4 * (size_t)nF);
+  m->fc.resize(3 * (size_t)nF);
+  auto contrib = [&](int c, const double S[3], const double C[3], double sgn) {
+    const double *ca = &m->cofgApp[3 * (size_t)c];
+    double term = (C[0] - ca[0]) * S[0] + (C[1] - ca[1]) * S[1] + (C[2] - ca[2]) * S[2];
+    if (sgn > 0) m->vol[c] = m->vol[c] + term; else m->vol[c] = m->vol[c] - term;
+    term = C[0] * S[0] + C[1] * S[1] + C[2] * S[2];
+    for (int d = 0; d < 3; ++d) {
+      if (sgn > 0) m->cofg[3 * (size_t)c + d] = m->cofg[3 * (size_t)c + d] + term * C[d];
+      else m->cofg[3 * (size_t)c + d] = m->cofg[3 * (size_t)c + d] - term * C[d];
+    }
+  };
+  for (int64_t f = 0; f < nF; ++f) {
+    double S[3], C[3];
+    face_vec_cen(m->xyz.data(), &m->f2v[4 * f], S, C);
+    double fVecM = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+    double term = 1.0 / fVecM;
+    m->fn[4 * f + 0] = S[0] * term;
+    m->fn[4 * f + 1] = S[1] * term;
+    m->fn[4 * f + 2] = S[2] * term;
+    m->fn[4 * f + 3] = fVecM;
+    m->fc[3 * f + 0] = C[0];
+    m->fc[3 * f + 1] = C[1];
+    m->fc[3 * f + 2] = C[2];
+    contrib(m->f2c[2 * f], S, C, 1.0);
+    contrib(m->f2c[2 * f + 1], S, C, -1.0);
+  }
+  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) {
+    Patch &p = m->patch[ip];
+    size_t nb = p.bf2c.size();
+    p.fn.resize(4 * nb);
+    p.fc.resize(3 * nb);
+    for (size_t f = 0; f < nb; ++f) {
+      double S[3], C[3];
+      face_vec_cen(m->xyz.data(), &p.bf2v[4 * f], S, C);
+      double fVecM = std::sqrt(S[0] * S[0] + S[1] * S[1] + S[2] * S[2]);
+      double term = 1.0 / fVecM;
+      p.fn[4 * f + 0] = S[0] * term;
+      p.fn[4 * f + 1] = S[1] * term;
+      p.fn[4 * f + 2] = S[2] * term;
+      p.fn[4 * f + 3] = fVecM;
+      p.fc[3 * f + 0] = C[0];
+      p.fc[3 * f + 1] = C[1];
+      p.fc[3 * f + 2] = C[2];
+      contrib(p.bf2c[f], S, C, 1.0);
+    }
+  }
+  const double THRD = 1.0 / 3.0;
+  for (long long c = 0; c < nC; ++c) {
+    m->vol[c] = THRD * m->vol[c];
+    if (!(m->vol[c] > 0.0)) throw std::runtime_error("non-positive cell volume");
+    double term = 1.0 / (4.0 * m->vol[c]);
+    for (int d = 0; d < 3; ++d) m->cofg[3 * c + d] = term * m->cofg[3 * c + d];
+  }
+  // vertex-to-cell lists, ascending cell id
+  m->v2cOff.assign(nV + 1, 0);
+  for (long long c = 0; c < nC; ++c) {
+    const int *v = m->verts(c);
+    for (int a = 0; a < m->nv(c); ++a) m->v2cOff[v[a] + 1]++;
+  }
+  for (long long v = 0; v < nV; ++v) m->v2cOff[v + 1] += m->v2cOff[v];
+  m->v2c.resize(m->v2cOff[nV]);
+  {
+    std::vector<int> fill(m->v2cOff.begin(), m->v2cOff.end() - 1);
+    for (long long c = 0; c < nC; ++c) {
+      const int *v = m->verts(c);
+      for (int a = 0; a < m->nv(c); ++a) m->v2c[fill[v[a]]++] = (int)c;
+    }
+  }
+  // c2c stencils (RFLU_ModStencilsCells.F90:750-1416) and moments
+  // (RFLU_ModWeights.F90:1770-1894)
+  const int stencilSizeMin = 4;  // RFLU_ComputeStencilSize(3,1,1) = 2*3*4/6
+  const int stencilSizeMax = 10 * stencilSizeMin;
+  const int nLayersMax = 6;
+  std::vector<int> cnt(nC, 0);
+  std::vector<int> memb((size_t)nC * stencilSizeMax);
+  m->moms.assign(10 * (size_t)nC, 0.0);
+#pragma omp parallel
+  {
+    std::vector<int> tmp, tmp2, help, sorted;
+    std::vector<double> frac, A;
+    int c2cs[40];
+#pragma omp for schedule(dynamic, 1024)
+    for (long long icg = 0; icg < nC; ++icg) {
+      int nVert = m->nv(icg);
+      const int *v = m->verts(icg);
+      double iNVert = 1.0 / (double)nVert;
+      tmp.clear();
+      for (int a = 0; a < nVert; ++a)
+        for (int e = m->v2cOff[v[a]]; e < m->v2cOff[v[a] + 1]; ++e) tmp.push_back(m->v2c[e]);
+      std::sort(tmp.begin(), tmp.end());
+      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
+      tmp.erase(std::lower_bound(tmp.begin(), tmp.end(), (int)icg));
+      int vs[8];
+      for (int a = 0; a < nVert; ++a) vs[a] = v[a];
+      std::sort(vs, vs + nVert);
+      int nC2 = (int)tmp.size();
+      frac.resize(nC2);
+      for (int q = 0; q < nC2; ++q) {
+        int c2 = tmp[q];
+        int n2 = m->nv(c2);
+        int vs2[8];
+        const int *v2 = m->verts(c2);
+        for (int a = 0; a < n2; ++a) vs2[a] = v2[a];
+        std::sort(vs2, vs2 + n2);
+        int common = 0, ia = 0, ib = 0;
+        while (ia < nVert && ib < n2) {
+          if (vs[ia] == vs2[ib]) { ++common; ++ia; ++ib; }
+          else if (vs[ia] < vs2[ib]) ++ia;
+          else ++ib;
+        }
+        frac[q] = (double)common * iNVert;
+      }
+      quicksort_real_int(frac.data(), tmp.data(), nC2);
+      int degr = 0;
+      for (int q = nC2; q >= std::max(nC2 - stencilSizeMax + 1, 1); --q) c2cs[degr++] = tmp[q - 1];
+      std::sort(c2cs, c2cs + degr);
+      int layBeg = 0, layEnd = degr;  // previous layer [beg,end)
+      for (int iLayer = 2; iLayer <= nLayersMax; ++iLayer) {
+        int sCount = 0;
+        if (degr >= stencilSizeMin) {
+          A.assign((size_t)degr * 4, 0.0);
+          const double *c0 = &m->cofg[3 * (size_t)icg];
+          for (int s = 0; s < degr; ++s) {
+            const double *c1 = &m->cofg[3 * (size_t)c2cs[s]];
+            double dx = c1[0] - c0[0], dy = c1[1] - c0[1], dz = c1[2] - c0[2];
+            double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+            A[4 * s + 0] = term;
+            A[4 * s + 1] = term * dx;
+            A[4 * s + 2] = term * dy;
+            A[4 * s + 3] = term * dz;
+          }
+          for (int col = 0; col < 4; ++col) {
+            double cm = -std::numeric_limits<double>::max();
+            for (int s = 0; s < degr; ++s) cm = std::max(cm, std::fabs(A[4 * s + col]));
+            for (int s = 0; s < degr; ++s) A[4 * s + col] = A[4 * s + col] / cm;
+          }
+          sCount = svd_scount(A, degr);
+        }
+        if (sCount != 0 || degr < stencilSizeMin) {
+          // RFLU_AddCellLayer (RFLU_ModStencilsUtils.F90:696-979)
+          sorted.assign(c2cs, c2cs + degr);
+          std::sort(sorted.begin(), sorted.end());
+          help.clear();
+          bool full = false;
+          for (int s = layBeg; s < layEnd && !full; ++s) {
+            int c1 = c2cs[s];
+            const int *v1 = m->verts(c1);
+            for (int a = 0; a < m->nv(c1) && !full; ++a)
+              for (int e = m->v2cOff[v1[a]]; e < m->v2cOff[v1[a] + 1]; ++e) {
+                int c2 = m->v2c[e];
+                if (c2 == (int)icg) continue;
+                if (std::binary_search(sorted.begin(), sorted.end(), c2)) continue;
+                if (std::binary_search(help.begin(), help.end(), c2)) continue;
+                if ((int)help.size() < stencilSizeMax) {
+                  help.insert(std::upper_bound(help.begin(), help.end(), c2), c2);
+                } else {
+                  full = true;
+                  break;
+                }
+              }
+          }
+          int newBeg = degr;
+          for (size_t s = 0; s < help.size(); ++s)
+            if (degr < stencilSizeMax) c2cs[degr++] = help[s];
+          layBeg = newBeg;
+          layEnd = degr;
+        } else {
+          break;
+        }
+      }
+      cnt[icg] = degr;
+      for (int s = 0; s < degr; ++s) memb[(size_t)icg * stencilSizeMax + s] = c2cs[s];
+      // moments
+      double mo[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+      const double *c0 = &m->cofg[3 * (size_t)icg];
+      for (int s = 0; s < degr; ++s) {
+        const double *c1 = &m->cofg[3 * (size_t)c2cs[s]];
+        double dx = c1[0] - c0[0], dy = c1[1] - c0[1], dz = c1[2] - c0[2];
+        double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
+        dx = wt * dx;
+        dy = wt * dy;
+        dz = wt * dz;
+        mo[0] = mo[0] + dx * dx;
+        mo[1] = mo[1] + dx * dy;
+        mo[2] = mo[2] + dy * dy;
+        mo[3] = mo[3] + dx * dz;
+        mo[4] = mo[4] + dy * dz;
+        mo[5] = mo[5] + dz * dz;
+        mo[6] = mo[6] + wt * dx;
+        mo[7] = mo[7] + wt * dy;
+        mo[8] = mo[8] + wt * dz;
+        mo[9] = mo[9] + wt * wt;
+      }
+      double r11 = std::sqrt(mo[0]);
+      double ir11 = 1.0 / r11;
+      double r12 = ir11 * mo[1];
+      double r22 = std::sqrt(mo[2] - r12 * r12);
+      double ir22 = 1.0 / r22;
+      double r13 = ir11 * mo[3];
+      double r23 = ir22 * (mo[4] - r12 * r13);
+      double r33 = std::sqrt(mo[5] - (r13 * r13 + r23 * r23));
+      double ir33 = 1.0 / r33;
+      double r14 = ir11 * mo[6];
+      double r24 = ir22 * (mo[7] - r12 * r14);
+      double r34 = ir33 * (mo[8] - (r13 * r14 + r23 * r24));
+      double r44 = std::sqrt(mo[9] - (r14 * r14 + r24 * r24 + r34 * r34));
+      double *out = &m->moms[10 * (size_t)icg];
+      out[0] = r11; out[1] = r12; out[2] = r22; out[3] = r13; out[4] = r23;
+      out[5] = r33; out[6] = r14; out[7] = r24; out[8] = r34; out[9] = r44;
+    }
+  }
+  m->csOff.assign(nC + 1, 0);
+  for (long long c = 0; c < nC; ++c) {
+    m->csOff[c + 1] = m->csOff[c] + cnt[c];
+    m->maxMembs = std::max(m->maxMembs, cnt[c]);
+  }
+  m->csMem1.resize(m->csOff[nC]);
+  for (long long c = 0; c < nC; ++c)
+    for (int s = 0; s < cnt[c]; ++s)
+      m->csMem1[m->csOff[c] + s] = memb[(size_t)c * stencilSizeMax + s] + 1;
+  // 1-based exports
+  m->f2c1.resize(m->f2c.size());
+  for (size_t i = 0; i < m->f2c.size(); ++i) m->f2c1[i] = m->f2c[i] + 1;
+  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) {
+    Patch &p = m->patch[ip];
+    p.bf2c1.resize(p.bf2c.size());
+    for (size_t i = 0; i < p.bf2c.size(); ++i) p.bf2c1[i] = p.bf2c[i] + 1;
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3], const double hi[3],
+                      double jitter, unsigned long long seed, int nThreads, rfmesh_t *out) {
+  if (!out || !lo || !hi || nx < 1 || ny < 1 || nz < 1 || kind < 0 || kind > 2 || jitter < 0 ||
+      jitter >= 0.25)
+    return RFMESH_ERR_ARG;
+  *out = nullptr;
+  rfmesh_s *m = new (std::nothrow) rfmesh_s();
+  if (!m) return RFMESH_ERR_NOMEM;
+  m->kind = kind;
+  for (int d = 0; d < 3; ++d) {
+    m->lo[d] = lo[d];
+    m->hi[d] = hi[d];
+  }
+#ifdef _OPENMP
+  int saved = omp_get_max_threads();
+  if (nThreads > 0) omp_set_num_threads(nThreads);
+#endif
+  int rc = RFMESH_OK;
+  try {
+    generate(m, nx, ny, nz, jitter, seed);
+    build(m, nThreads);
+  } catch (const std::bad_alloc &) {
+    rc = RFMESH_ERR_NOMEM;
+  } catch (...) {
+    rc = RFMESH_ERR_GEOM;
+  }
+#ifdef _OPENMP
+  omp_set_num_threads(saved);
+#endif
+  if (rc != RFMESH_OK) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return RFMESH_OK;
+}
+
+int rfmesh_destroy(rfmesh_t m) {
+  delete m;
+  return RFMESH_OK;
+}
+
+int rfmesh_sizes(rfmesh_t m, long long s[RFMESH_NSIZES]) {
+  if (!m || !s) return RFMESH_ERR_ARG;
+  s[RFMESH_NVERT] = (long long)(m->xyz.size() / 3);
+  s[RFMESH_NCELLS] = m->nCells;
+  s[RFMESH_NFACES] = (long long)(m->f2c.size() / 2);
+  s[RFMESH_NPATCHES] = RFMESH_NPATCH;
+  s[RFMESH_NMEMBS] = (long long)m->csMem1.size();
+  for (int t = 0; t < 4; ++t) s[RFMESH_NTETS + t] = m->nOfType[t];
+  long long nb = 0;
+  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) nb += (long long)m->patch[ip].bf2c.size();
+  s[RFMESH_NBFACES] = nb;
+  s[RFMESH_MAXMEMBS] = m->maxMembs;
+  return RFMESH_OK;
+}
+
+int rfmesh_patch_nbfaces(rfmesh_t m, int ip) {
+  if (!m || ip < 0 || ip >= RFMESH_NPATCH) return -1;
+  return (int)m->patch[ip].bf2c.size();
+}
+
+const double *rfmesh_xyz(rfmesh_t m) { return m ? m->xyz.data() : nullptr; }
+const double *rfmesh_vol(rfmesh_t m) { return m ? m->vol.data() : nullptr; }
+const double *rfmesh_cofg(rfmesh_t m) { return m ? m->cofg.data() : nullptr; }
+const int *rfmesh_f2c(rfmesh_t m) { return m ? m->f2c1.data() : nullptr; }
+const double *rfmesh_fn(rfmesh_t m) { return m ? m->fn.data() : nullptr; }
+const double *rfmesh_fc(rfmesh_t m) { return m ? m->fc.data() : nullptr; }
+const int *rfmesh_c2cs_offsets(rfmesh_t m) { return m ? m->csOff.data() : nullptr; }
+const int *rfmesh_c2cs_members(rfmesh_t m) { return m ? m->csMem1.data() : nullptr; }
+const double *rfmesh_xyzmoms(rfmesh_t m) { return m ? m->moms.data() : nullptr; }
+const int *rfmesh_cell_type(rfmesh_t m) { return m ? m->ctype.data() : nullptr; }
+const int *rfmesh_bf2c(rfmesh_t m, int ip) {
+  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].bf2c1.data() : nullptr;
+}
+const double *rfmesh_bfn(rfmesh_t m, int ip) {
+  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].fn.data() : nullptr;
+}
+const double *rfmesh_bfc(rfmesh_t m, int ip) {
+  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].fc.data() : nullptr;
+}
+
+}  // extern "C"

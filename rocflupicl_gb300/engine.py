@@ -1,0 +1,344 @@
+"""Python front end of the residual engine (include/rfgpu.h).
+
+Mirrors the reference's operator interface for the hot path:
+
+  Region.rk_stage(istage, dtMin)   libfloflu/RungeKuttaMP.F90 per-region stage body
+  Region.time_step(...)            RFLU_TimeStepInviscid + RFLU_MinimumTimeStep
+  Region.residual()                CellGradientsMP + ConvectiveFluxesMP
+  Region.step(...)                 one time step (dt + all stages) on the device
+  Region.solve(...)                the RFLU_TimeStepping loop to an end time / step count
+
+Errors raise `EngineError` carrying the C-ABI code, as the Fortran shim maps
+them onto ErrorStop.  There is no CPU fallback: without the CUDA library or a
+GPU every call fails.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from typing import List, Optional, Sequence
+
+import numpy as np
+
+from . import _build
+from .case import Case, PREC_FP64, PREC_MIXED  # noqa: F401
+
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT = range(7)
+ST_NAN, ST_NEGPOS, ST_PFLOOR, ST_PCLAMP = 1, 2, 4, 8
+_NAMES = {1: "RFGPU_ERR_ARG", 2: "RFGPU_ERR_UNSUPPORTED", 3: "RFGPU_ERR_CUDA",
+          4: "RFGPU_ERR_NOMEM", 5: "RFGPU_ERR_STATE", 6: "RFGPU_ERR_TIMEOUT"}
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code: int, where: str):
+        super().__init__(f"{where}: {_NAMES.get(code, code)}")
+        self.code = code
+
+
+class PatchT(C.Structure):
+    _fields_ = [("bcType", C.c_int), ("spaceOrder", C.c_int), ("bcOptType", C.c_int),
+                ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
+                ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
+                ("distrib", C.c_int)]
+
+
+class RegionDescT(C.Structure):
+    _fields_ = [("nCells", C.c_int), ("nFaces", C.c_int), ("f2cLd", C.c_int),
+                ("f2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
+                ("fc", C.POINTER(C.c_double)), ("cofg", C.POINTER(C.c_double)),
+                ("vol", C.POINTER(C.c_double)), ("c2csOffsets", C.POINTER(C.c_int)),
+                ("c2csMembers", C.POINTER(C.c_int)), ("xyzMoms", C.POINTER(C.c_double)),
+                ("nPatches", C.c_int), ("patches", C.POINTER(PatchT)),
+                ("cv", C.POINTER(C.c_double)), ("dv", C.POINTER(C.c_double)),
+                ("gasModel", C.c_int), ("flowModel", C.c_int),
+                ("spaceDiscr", C.c_int), ("spaceOrder", C.c_int), ("reconst", C.c_int),
+                ("rkScheme", C.c_int), ("refCp", C.c_double), ("refGamma", C.c_double),
+                ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
+                ("dissFact", C.c_double), ("precision", C.c_int), ("venkatGuard", C.c_int)]
+
+
+SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_dt",
+           "rfgpu_step", "rfgpu_steps_graph", "rfgpu_residual", "rfgpu_download",
+           "rfgpu_upload", "rfgpu_download_grad", "rfgpu_time", "rfgpu_set_time",
+           "rfgpu_status", "rfgpu_sync", "rfgpu_stream", "rfgpu_device_bytes",
+           "rfgpu_launch_count", "rfgpu_set_tuning", "rfgpu_batch_create",
+           "rfgpu_batch_destroy", "rfgpu_batch_step", "rfgpu_batch_steps_graph",
+           "rfgpu_batch_sync", "rfgpu_batch_stream"]
+
+_lib = None
+
+
+def load(path: Optional[str] = None):
+    """Load (building if needed) librfgpu.so and declare the C signatures."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    lib = C.CDLL(str(path or _build.build_gpu()))
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.POINTER(C.c_int)
+    d = C.c_double
+    sig = {
+        "rfgpu_region_create": ([C.POINTER(RegionDescT), C.POINTER(vp)], C.c_int),
+        "rfgpu_region_destroy": ([vp], C.c_int),
+        "rfgpu_stage": ([vp, C.c_int, d], C.c_int),
+        "rfgpu_dt": ([vp, d, d, d, d, dp], C.c_int),
+        "rfgpu_step": ([vp, d, d, d, d], C.c_int),
+        "rfgpu_steps_graph": ([vp, C.c_int, d, d, d, d], C.c_int),
+        "rfgpu_residual": ([vp, dp], C.c_int),
+        "rfgpu_download": ([vp, dp, dp], C.c_int),
+        "rfgpu_upload": ([vp, dp, dp], C.c_int),
+        "rfgpu_download_grad": ([vp, dp], C.c_int),
+        "rfgpu_time": ([vp, dp, dp], C.c_int),
+        "rfgpu_set_time": ([vp, d], C.c_int),
+        "rfgpu_status": ([vp, ip], C.c_int),
+        "rfgpu_sync": ([vp], C.c_int),
+        "rfgpu_stream": ([vp], vp),
+        "rfgpu_device_bytes": ([vp], C.c_longlong),
+        "rfgpu_launch_count": ([vp], C.c_longlong),
+        "rfgpu_set_tuning": ([vp, C.c_int, C.c_int], C.c_int),
+        "rfgpu_batch_create": ([C.POINTER(vp), C.c_int, C.POINTER(vp)], C.c_int),
+        "rfgpu_batch_destroy": ([vp], C.c_int),
+        "rfgpu_batch_step": ([vp, d, d, d, d], C.c_int),
+        "rfgpu_batch_steps_graph": ([vp, C.c_int, d, d, d, d], C.c_int),
+        "rfgpu_batch_sync": ([vp], C.c_int),
+        "rfgpu_batch_stream": ([vp], vp),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(lib, name)
+        f.argtypes = args
+        f.restype = res
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _dp(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _ip(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int))
+
+
+def _check(rc: int, where: str):
+    if rc != OK:
+        raise EngineError(rc, where)
+
+
+class Region:
+    """One registered region on the GPU (device-resident state)."""
+
+    def __init__(self, case: Case, precision: Optional[int] = None):
+        self.lib = load()
+        m, num = case.mesh, case.numerics
+        self.case = case
+        self.num = num
+        self.nCells = m.nCells
+        self.precision = num.precision if precision is None else precision
+        keep = []
+
+        def k(a, dt):
+            a = np.ascontiguousarray(a, dtype=dt)
+            keep.append(a)
+            return a
+
+        patches = [(p, bc) for p, bc in zip(m.patches, case.bcs) if p.n > 0]
+        parr = (PatchT * max(1, len(patches)))()
+        for i, (p, bc) in enumerate(patches):
+            P = parr[i]
+            P.bcType, P.spaceOrder, P.bcOptType, P.nBFaces = bc.bcType, bc.spaceOrder, bc.bcOptType, p.n
+            P.bf2c = _ip(k(p.bf2c, np.int32))
+            P.fn = _dp(k(p.fn, np.float64))
+            P.fc = _dp(k(p.fc, np.float64))
+            vals = np.zeros(1) if bc.pout is None else np.atleast_1d(np.asarray(bc.pout, np.float64))
+            P.vals = _dp(k(vals, np.float64))
+            P.distrib = 1 if vals.shape[0] > 1 else 0
+        d = RegionDescT()
+        d.nCells, d.nFaces, d.f2cLd = m.nCells, m.nFaces, 2
+        d.f2c = _ip(k(m.f2c, np.int32))
+        d.fn = _dp(k(m.fn, np.float64))
+        d.fc = _dp(k(m.fc, np.float64))
+        d.cofg = _dp(k(m.cofg, np.float64))
+        d.vol = _dp(k(m.vol, np.float64))
+        d.c2csOffsets = _ip(k(m.c2cs_off, np.int32))
+        d.c2csMembers = _ip(k(m.c2cs_mem, np.int32))
+        d.xyzMoms = _dp(k(m.xyzmoms, np.float64))
+        d.nPatches = len(patches)
+        d.patches = parr
+        d.cv = _dp(k(case.cv, np.float64))
+        d.dv = _dp(k(case.dv, np.float64))
+        d.gasModel, d.flowModel = 1, 0
+        d.spaceDiscr, d.spaceOrder, d.reconst, d.rkScheme = (
+            num.spaceDiscr, num.spaceOrder, num.reconst, num.rkScheme)
+        d.refCp, d.refGamma = num.refCp, num.refGamma
+        d.gvCp, d.gvMol = num.gv
+        d.epsentr, d.dissFact = num.epsentr, num.dissFact
+        d.precision = self.precision
+        d.venkatGuard = num.venkatGuard
+        h = C.c_void_p()
+        _check(self.lib.rfgpu_region_create(C.byref(d), C.byref(h)), "rfgpu_region_create")
+        self.h = h
+        self.nSteps = {1: 4, 2: 3, 3: 1}[num.rkScheme]
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rfgpu_region_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # --- reference-shaped operations -----------------------------------------
+    def rk_stage(self, istage: int, dtMin: float):
+        _check(self.lib.rfgpu_stage(self.h, istage, dtMin), "rfgpu_stage")
+
+    def time_step(self, cfl: float, dtImposed: float, dtMinLimit: float = 0.0,
+                  currentTime: float = 1.0) -> float:
+        out = C.c_double()
+        _check(self.lib.rfgpu_dt(self.h, cfl, dtImposed, dtMinLimit, currentTime, C.byref(out)),
+               "rfgpu_dt")
+        return out.value
+
+    def step(self, cfl: float, dtImposed: float, dtMinLimit: float = 0.0, endTime: float = 0.0):
+        _check(self.lib.rfgpu_step(self.h, cfl, dtImposed, dtMinLimit, endTime), "rfgpu_step")
+
+    def steps_graph(self, n: int, cfl: float, dtImposed: float, dtMinLimit: float = 0.0,
+                    endTime: float = 0.0):
+        _check(self.lib.rfgpu_steps_graph(self.h, n, cfl, dtImposed, dtMinLimit, endTime),
+               "rfgpu_steps_graph")
+
+    def residual(self, to_host: bool = True):
+        if not to_host:
+            _check(self.lib.rfgpu_residual(self.h, None), "rfgpu_residual")
+            return None
+        rhs = np.empty((self.nCells, 5))
+        _check(self.lib.rfgpu_residual(self.h, _dp(rhs)), "rfgpu_residual")
+        return rhs
+
+    def download(self):
+        cv = np.empty((self.nCells, 5))
+        dv = np.empty((self.nCells, 3))
+        _check(self.lib.rfgpu_download(self.h, _dp(cv), _dp(dv)), "rfgpu_download")
+        return cv, dv
+
+    def download_into(self, cv: np.ndarray, dv: Optional[np.ndarray] = None):
+        _check(self.lib.rfgpu_download(self.h, _dp(cv), _dp(dv) if dv is not None else None),
+               "rfgpu_download")
+
+    def upload(self, cv: np.ndarray, dv: Optional[np.ndarray] = None):
+        cv = np.ascontiguousarray(cv, np.float64)
+        dvp = None
+        if dv is not None:
+            dv = np.ascontiguousarray(dv, np.float64)
+            dvp = _dp(dv)
+        _check(self.lib.rfgpu_upload(self.h, _dp(cv), dvp), "rfgpu_upload")
+
+    def gradients(self):
+        g = np.empty((self.nCells, 5, 3))
+        _check(self.lib.rfgpu_download_grad(self.h, _dp(g)), "rfgpu_download_grad")
+        return g
+
+    def time(self):
+        t, dt = C.c_double(), C.c_double()
+        _check(self.lib.rfgpu_time(self.h, C.byref(t), C.byref(dt)), "rfgpu_time")
+        return t.value, dt.value
+
+    def set_time(self, t: float):
+        _check(self.lib.rfgpu_set_time(self.h, t), "rfgpu_set_time")
+
+    def status(self) -> int:
+        fl = C.c_int()
+        rc = self.lib.rfgpu_status(self.h, C.byref(fl))
+        if rc not in (OK, ERR_STATE):
+            raise EngineError(rc, "rfgpu_status")
+        return fl.value
+
+    def sync(self):
+        _check(self.lib.rfgpu_sync(self.h), "rfgpu_sync")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.rfgpu_stream(self.h) or 0
+
+    @property
+    def device_bytes(self) -> int:
+        return self.lib.rfgpu_device_bytes(self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.lib.rfgpu_launch_count(self.h)
+
+    def set_grid_cap(self, blocks: int):
+        _check(self.lib.rfgpu_set_tuning(self.h, blocks, 0), "rfgpu_set_tuning")
+
+    def solve(self, t_end: Optional[float] = None, n_steps: Optional[int] = None,
+              dt_imposed: Optional[float] = None, graph: bool = False):
+        """RFLU_TimeStepping loop: the first step uses dtImposed (the CFL step
+        of the initial state unless given), later steps cfl*min(dt); the last
+        step is clipped to t_end.  Returns (time, steps, status)."""
+        cfl = self.num.cfl
+        if dt_imposed is None:
+            dt_imposed = self.time_step(cfl, 1.0, 0.0, 1.0)
+        self.set_time(0.0)
+        end = t_end if t_end is not None else 0.0
+        k = 0
+        if n_steps is not None:
+            if graph:
+                self.steps_graph(n_steps, cfl, dt_imposed, 0.0, end)
+            else:
+                for _ in range(n_steps):
+                    self.step(cfl, dt_imposed, 0.0, end)
+            k = n_steps
+        else:
+            chunk = 64
+            while True:
+                if graph:
+                    self.steps_graph(chunk, cfl, dt_imposed, 0.0, end)
+                else:
+                    for _ in range(chunk):
+                        self.step(cfl, dt_imposed, 0.0, end)
+                k += chunk
+                t, _ = self.time()
+                if t >= end:
+                    break
+        t, _ = self.time()
+        return t, k, self.status()
+
+
+class Batch:
+    """Many regions advanced together: one launch per pass over all regions."""
+
+    def __init__(self, regions: Sequence[Region]):
+        self.lib = load()
+        self.regions = list(regions)
+        arr = (C.c_void_p * len(self.regions))(*[r.h for r in self.regions])
+        h = C.c_void_p()
+        _check(self.lib.rfgpu_batch_create(arr, len(self.regions), C.byref(h)), "rfgpu_batch_create")
+        self.h = h
+
+    def step(self, cfl, dtImposed, dtMinLimit=0.0, endTime=0.0):
+        _check(self.lib.rfgpu_batch_step(self.h, cfl, dtImposed, dtMinLimit, endTime),
+               "rfgpu_batch_step")
+
+    def steps_graph(self, n, cfl, dtImposed, dtMinLimit=0.0, endTime=0.0):
+        _check(self.lib.rfgpu_batch_steps_graph(self.h, n, cfl, dtImposed, dtMinLimit, endTime),
+               "rfgpu_batch_steps_graph")
+
+    def sync(self):
+        _check(self.lib.rfgpu_batch_sync(self.h), "rfgpu_batch_sync")
+
+    @property
+    def stream(self) -> int:
+        return self.lib.rfgpu_batch_stream(self.h) or 0
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rfgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,138 @@
+"""Python view of the host mesh builder (include/rfmesh.h).
+
+A `BoxMesh` holds the region arrays in the layout the Fortran host passes to
+the engine: Fortran column-major arrays with 1-based cell indices, e.g.
+``f2c`` has shape ``(nFaces, 2)`` in NumPy (C order) which is the memory image
+of the Fortran array ``f2c(2,nFaces)``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+from typing import List
+
+import numpy as np
+
+from . import _build
+
+HEX, TET, MIXED = 0, 1, 2
+XLO, XHI, YLO, YHI, ZLO, ZHI = range(6)
+_NSIZES = 11
+
+_lib = None
+
+
+def _load():
+    global _lib
+    if _lib is None:
+        path = _build.build_mesh()
+        lib = C.CDLL(str(path))
+        vp = C.c_void_p
+        lib.rfmesh_create_box.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int,
+                                          C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                          C.c_double, C.c_ulonglong, C.c_int, C.POINTER(vp)]
+        lib.rfmesh_destroy.argtypes = [vp]
+        lib.rfmesh_sizes.argtypes = [vp, C.POINTER(C.c_longlong)]
+        lib.rfmesh_patch_nbfaces.argtypes = [vp, C.c_int]
+        for name in ("xyz", "vol", "cofg", "fn", "fc", "xyzmoms"):
+            f = getattr(lib, "rfmesh_" + name)
+            f.argtypes = [vp]
+            f.restype = C.POINTER(C.c_double)
+        for name in ("f2c", "c2cs_offsets", "c2cs_members", "cell_type"):
+            f = getattr(lib, "rfmesh_" + name)
+            f.argtypes = [vp]
+            f.restype = C.POINTER(C.c_int)
+        lib.rfmesh_bf2c.argtypes = [vp, C.c_int]
+        lib.rfmesh_bf2c.restype = C.POINTER(C.c_int)
+        for name in ("bfn", "bfc"):
+            f = getattr(lib, "rfmesh_" + name)
+            f.argtypes = [vp, C.c_int]
+            f.restype = C.POINTER(C.c_double)
+        _lib = lib
+    return _lib
+
+
+def _copy(ptr, n, dtype, shape):
+    if n == 0:
+        return np.zeros(shape, dtype=dtype)
+    return np.ctypeslib.as_array(ptr, shape=(n,)).astype(dtype, copy=True).reshape(shape)
+
+
+@dataclass
+class Patch:
+    """One boundary patch: faces bf2c (1-based), fn (nB,4), fc (nB,3)."""
+    bf2c: np.ndarray
+    fn: np.ndarray
+    fc: np.ndarray
+
+    @property
+    def n(self) -> int:
+        return int(self.bf2c.shape[0])
+
+
+@dataclass
+class BoxMesh:
+    kind: int
+    dims: tuple
+    nCells: int
+    nFaces: int
+    xyz: np.ndarray
+    vol: np.ndarray
+    cofg: np.ndarray            # (nCells,3)
+    f2c: np.ndarray             # (nFaces,2) 1-based
+    fn: np.ndarray              # (nFaces,4)
+    fc: np.ndarray              # (nFaces,3)
+    c2cs_off: np.ndarray        # (nCells+1,) 0-based offsets
+    c2cs_mem: np.ndarray        # (nMembs,) 1-based
+    xyzmoms: np.ndarray         # (nCells,10)
+    cell_type: np.ndarray
+    patches: List[Patch] = field(default_factory=list)
+    n_of_type: tuple = (0, 0, 0, 0)
+
+    @property
+    def nBFaces(self) -> int:
+        return sum(p.n for p in self.patches)
+
+    @property
+    def nMembs(self) -> int:
+        return int(self.c2cs_mem.shape[0])
+
+
+def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
+        jitter: float = 0.0, seed: int = 0, threads: int = 0) -> BoxMesh:
+    """Build a box mesh (HEX / Kuhn TET / MIXED) and return its region arrays."""
+    lib = _load()
+    h = C.c_void_p()
+    lo_a = (C.c_double * 3)(*lo)
+    hi_a = (C.c_double * 3)(*hi)
+    rc = lib.rfmesh_create_box(kind, nx, ny, nz, lo_a, hi_a, float(jitter), int(seed),
+                               int(threads), C.byref(h))
+    if rc != 0:
+        raise RuntimeError(f"rfmesh_create_box failed with code {rc}")
+    try:
+        s = (C.c_longlong * _NSIZES)()
+        lib.rfmesh_sizes(h, s)
+        nV, nC, nF, nP, nM = s[0], s[1], s[2], s[3], s[4]
+        m = BoxMesh(
+            kind=kind, dims=(nx, ny, nz), nCells=nC, nFaces=nF,
+            xyz=_copy(lib.rfmesh_xyz(h), 3 * nV, np.float64, (nV, 3)),
+            vol=_copy(lib.rfmesh_vol(h), nC, np.float64, (nC,)),
+            cofg=_copy(lib.rfmesh_cofg(h), 3 * nC, np.float64, (nC, 3)),
+            f2c=_copy(lib.rfmesh_f2c(h), 2 * nF, np.int32, (nF, 2)),
+            fn=_copy(lib.rfmesh_fn(h), 4 * nF, np.float64, (nF, 4)),
+            fc=_copy(lib.rfmesh_fc(h), 3 * nF, np.float64, (nF, 3)),
+            c2cs_off=_copy(lib.rfmesh_c2cs_offsets(h), nC + 1, np.int32, (nC + 1,)),
+            c2cs_mem=_copy(lib.rfmesh_c2cs_members(h), nM, np.int32, (nM,)),
+            xyzmoms=_copy(lib.rfmesh_xyzmoms(h), 10 * nC, np.float64, (nC, 10)),
+            cell_type=_copy(lib.rfmesh_cell_type(h), nC, np.int32, (nC,)),
+            n_of_type=(s[5], s[6], s[7], s[8]),
+        )
+        for ip in range(nP):
+            nb = lib.rfmesh_patch_nbfaces(h, ip)
+            m.patches.append(Patch(
+                bf2c=_copy(lib.rfmesh_bf2c(h, ip), nb, np.int32, (nb,)),
+                fn=_copy(lib.rfmesh_bfn(h, ip), 4 * nb, np.float64, (nb, 4)),
+                fc=_copy(lib.rfmesh_bfc(h, ip), 3 * nb, np.float64, (nb, 3))))
+        return m
+    finally:
+        lib.rfmesh_destroy(h)

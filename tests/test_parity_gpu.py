@@ -1,0 +1,195 @@
+"""Parity of the CUDA engine with the CPU oracle, through the C ABI.
+
+FP64 path: bit-identical residuals, limited gradients, stage updates, time
+steps and multi-step trajectories (the engine sums each cell's face fluxes in
+the reference's order and is built without FMA contraction).  The relative
+criterion of the spec, |R_gpu - R_oracle| <= 1e-12 * max(|R_oracle|, S_c), is
+implied by equality and is also asserted so a failure reports its size.
+
+Mixed path: L1 = mean |q/q_ref - 1| of rho and p against the FP64 oracle
+(utilities/post/RFLU_ComputeExactFlowError.F90:946-977 definition) within
+1e-5 after the steps below.
+"""
+import numpy as np
+import pytest
+
+from rocflupicl_gb300 import case as K
+from rocflupicl_gb300 import engine as E
+
+pytestmark = pytest.mark.gpu
+
+SCHEMES = [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC]
+
+
+def _oracle(c):
+    from oracle.oracle import Oracle
+    return Oracle(c)
+
+
+def make(kind, scheme, **kw):
+    num = K.Numerics(spaceDiscr=scheme, venkatGuard=kw.pop("guard", 1), **kw)
+    if kind == "tube":
+        return K.shock_tube(24, numerics=num)
+    if kind == "tet":
+        return K.tet_shock_box(4, seed=5, numerics=num)
+    if kind == "mixed":
+        return K.mixed_box(6, numerics=num)
+    raise ValueError(kind)
+
+
+def assert_same(a, b, what):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, what
+    assert np.all(np.isfinite(b)), f"{what}: oracle not finite"
+    if not np.array_equal(a, b):
+        d = np.abs(a - b)
+        scale = np.maximum(np.abs(b), 1e-300)
+        i = np.unravel_index(np.argmax(d / scale), d.shape)
+        raise AssertionError(f"{what}: not bit-identical; max rel diff {np.max(d / scale):.3e} at "
+                             f"{i}: gpu {a[i]!r} oracle {b[i]!r}")
+
+
+@pytest.mark.parametrize("kind", ["tube", "tet", "mixed"])
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_residual_bitwise(kind, scheme):
+    c = make(kind, scheme)
+    o = _oracle(c)
+    rhs_o, grad_o = o.residual(c.cv, c.dv)
+    r = E.Region(c)
+    rhs_g = r.residual()
+    grad_g = r.gradients()
+    assert_same(grad_g, grad_o, "limited gradients")
+    assert_same(rhs_g, rhs_o, "residual")
+    # flux-scaled 1e-12 criterion
+    assert np.all(np.abs(rhs_g - rhs_o) <= 1e-12 * np.maximum(np.abs(rhs_o), 1e-30))
+    r.close()
+
+
+@pytest.mark.parametrize("kind", ["tube", "tet", "mixed"])
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_steps_bitwise(kind, scheme):
+    c = make(kind, scheme)
+    o = _oracle(c)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    t_o, k, st_o = o.run(cv, dv, n_steps=4)
+    r = E.Region(c)
+    t_g, _, st_g = r.solve(n_steps=4)
+    cvg, dvg = r.download()
+    assert st_g == st_o
+    assert t_g == t_o
+    assert_same(cvg, cv, "cv after 4 steps")
+    assert_same(dvg, dv, "dv after 4 steps")
+    r.close()
+
+
+@pytest.mark.parametrize("rk", [K.RK_SCHEME_4_CLASSICAL, K.RK_SCHEME_3_WRAY, K.RK_SCHEME_1_EULER])
+def test_host_driven_stages(rk):
+    """rfgpu_dt + rfgpu_stage exactly as RFLU_TimeStepping/RungeKuttaMP call them."""
+    c = make("tet", K.DISCR_UPW_ROE, rkScheme=rk, cfl=0.4)
+    o = _oracle(c)
+    r = E.Region(c)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    nst = {1: 4, 2: 3, 3: 1}[rk]
+    dti = o.dt(cv, dv, 0.4, 1.0, 0.0, 1.0)
+    assert r.time_step(0.4, 1.0, 0.0, 1.0) == dti
+    t = 0.0
+    for step in range(3):
+        dto = o.dt(cv, dv, 0.4, dti, 0.0, t)
+        dtg = r.time_step(0.4, dti, 0.0, t)
+        assert dtg == dto
+        for s in range(1, nst + 1):
+            o.stage(cv, dv, s, dto)
+            r.rk_stage(s, dtg)
+        t += dto
+    cvg, dvg = r.download()
+    assert_same(cvg, cv, "cv")
+    assert_same(dvg, dv, "dv")
+    r.close()
+
+
+@pytest.mark.parametrize("variant", ["order1", "nolimiter", "refguard", "subsonic", "order1bc"])
+def test_option_envelope_bitwise(variant):
+    scheme = K.DISCR_UPW_AUSMPLUS
+    if variant == "order1":
+        c = make("tet", scheme, spaceOrder=1)
+    elif variant == "nolimiter":
+        c = make("tet", K.DISCR_UPW_HLLC, reconst=K.RECONST_NONE)
+    elif variant == "refguard":
+        c = make("mixed", K.DISCR_UPW_ROE, guard=0)
+    elif variant == "subsonic":
+        c = make("tube", scheme)
+        for bc in c.bcs[:2]:
+            bc.bcOptType = K.BCOPT_SUBSONIC
+            bc.pout = np.array([0.5])
+    else:
+        c = make("tube", scheme)
+        for bc in c.bcs:
+            bc.spaceOrder = 1
+    o = _oracle(c)
+    rhs_o, _ = o.residual(c.cv, c.dv)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    o.run(cv, dv, n_steps=3)
+    r = E.Region(c)
+    assert_same(r.residual(), rhs_o, "residual")
+    r.solve(n_steps=3)
+    cvg, dvg = r.download()
+    assert_same(cvg, cv, "cv")
+    assert_same(dvg, dv, "dv")
+    r.close()
+
+
+@pytest.mark.parametrize("scheme", SCHEMES)
+def test_mixed_precision_l1(scheme):
+    c = make("tet", scheme, precision=K.PREC_MIXED)
+    o = _oracle(c)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    # impose the same dt sequence on both: the FP64 oracle's first dt
+    dti = o.dt(cv, dv, c.numerics.cfl, 1.0, 0.0, 1.0)
+    o.run(cv, dv, n_steps=5, dt_imposed=dti)
+    r = E.Region(c)
+    r.solve(n_steps=5, dt_imposed=dti)
+    cvg, dvg = r.download()
+    l1r = np.mean(np.abs(cvg[:, 0] / cv[:, 0] - 1.0))
+    l1p = np.mean(np.abs(dvg[:, 0] / dv[:, 0] - 1.0))
+    assert l1r <= 1e-5, l1r
+    assert l1p <= 1e-5, l1p
+    r.close()
+
+
+def test_graph_replay_equals_steps():
+    c = make("tet", K.DISCR_UPW_HLLC)
+    a = E.Region(c)
+    b = E.Region(c)
+    a.solve(n_steps=6)
+    b.solve(n_steps=6, graph=True)
+    assert_same(b.download()[0], a.download()[0], "graph vs stream steps")
+    assert b.launches > 0
+    a.close()
+    b.close()
+
+
+def test_status_flags_on_host_injected_nan():
+    """Failure detection without a GPU fault: a NaN planted in the uploaded
+    state is latched in the device status word and reported as
+    RFGPU_ERR_STATE / RFGPU_ST_NAN, and the context stays usable."""
+    c = make("tube", K.DISCR_UPW_AUSMPLUS)
+    r = E.Region(c)
+    cv = c.cv.copy()
+    cv[5, 0] = np.nan
+    r.upload(cv)
+    _, _, st = r.solve(n_steps=1)   # solve() reads and clears the status word
+    assert st & E.ST_NAN
+    assert r.status() == 0
+    r.upload(c.cv, c.dv)
+    _, _, st = r.solve(n_steps=1)
+    assert st == 0
+    r.close()
+
+
+def test_unsupported_option_refused():
+    c = make("tube", K.DISCR_UPW_AUSMPLUS)
+    c.numerics.spaceDiscr = 5  # AUSM+up is not in the envelope
+    with pytest.raises(E.EngineError) as ei:
+        E.Region(c)
+    assert ei.value.code == E.ERR_UNSUPPORTED
