@@ -1,0 +1,381 @@
+#!/usr/bin/env python3
+"""Benchmark of the residual engine on its headline workload.
+
+Workload (default): planar Ms=2 shock over a perturbed tetrahedral box, 128^3
+unit-box hexes x 6 Kuhn tets = 12,582,912 cells, interior vertices jittered
+U(+-10% h) from a seed, rho=1.2, p=1e5 times a lognormal density factor
+(sigma 0.1), Rankine-Hugoniot post-shock state for x<0.2; Roe flux, WLSQ
+gradients + Venkatakrishnan limiter, Wray RK3.  All inputs are seeded
+synthetic data of those shapes.
+
+One step = one RK3 time step (device time step + 3 stages) over the whole
+mesh; the metric counts face-flux evaluations (interior + boundary faces per
+stage).  `value` is the mixed-precision path (FP32 reconstruction/flux, FP64
+accumulation/update/EOS) with the state resident in HBM; the FP64 path, the
+L1(rho)/L1(p) error of mixed against FP64 and the end-to-end figure through
+the C ABI with host buffers are reported beside it.
+
+  python bench.py [--gpus N --steps K --warmup W] [--impl reference]
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+from rocflupicl_gb300 import case as K  # noqa: E402
+from rocflupicl_gb300 import perfmodel  # noqa: E402
+
+METRIC = "face-flux evals/s & HBM GB/s, mixed vs FP64 at L1rho<=1e-5; p50/p99 solve latency"
+UNIT = "face-flux evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=128, help="base hexes per direction")
+    ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--l1-steps", type=int, default=10)
+    return ap.parse_args()
+
+
+SCHEME = {"roe": K.DISCR_UPW_ROE, "hllc": K.DISCR_UPW_HLLC, "ausm+": K.DISCR_UPW_AUSMPLUS}
+
+
+class Dist:
+    """torchrun rendezvous (gloo, host side only): barrier and max over ranks."""
+
+    def __init__(self):
+        self.world = int(os.environ.get("WORLD_SIZE", "1"))
+        self.rank = int(os.environ.get("RANK", "0"))
+        self.local = int(os.environ.get("LOCAL_RANK", "0"))
+        self.pg = None
+        if self.world > 1:
+            import torch.distributed as dist
+            dist.init_process_group("gloo")
+            self.pg = dist
+
+    def barrier(self):
+        if self.pg:
+            self.pg.barrier()
+
+    def max(self, x: float) -> float:
+        if not self.pg:
+            return x
+        import torch
+        t = torch.tensor([x], dtype=torch.float64)
+        self.pg.all_reduce(t, op=self.pg.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.pg:
+            self.pg.destroy_process_group()
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.t.join(timeout=2)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def ncu_traffic():
+    """Per-launch DRAM bytes of each kernel from the committed ncu summary."""
+    try:
+        with open(os.path.join(ROOT, "profiles", "traffic.json")) as f:
+            return json.load(f)
+    except Exception:
+        return {}
+
+
+def build_case(a):
+    num = K.Numerics(spaceDiscr=SCHEME[a.scheme], venkatGuard=1, precision=K.PREC_MIXED)
+    return K.tet_shock_box(a.n, numerics=num)
+
+
+def workload_config(c, a):
+    m = c.mesh
+    return {"workload": f"tet_shock_box {a.n}^3x6 Kuhn tets, jitter 0.1h, Ms=2, lognormal rho sigma 0.1; "
+                        f"{a.scheme} flux, WLSQ+Venkatakrishnan, Wray RK3",
+            "cells": m.nCells, "faces": m.nFaces, "bfaces": m.nBFaces, "stencil_members": m.nMembs,
+            "precision": "mixed: FP32 reconstruction/limiter/flux, FP64 geometry/accumulate/update/EOS",
+            "l2": "inputs larger than L2 (working set >10 GB vs 129 MB L2)",
+            "parallelism": "replicas (one independent region per GPU)"}
+
+
+def cpu_sample(c, threads: int):
+    """Oracle (C++ FP64 restatement, OpenMP over cells) on one RK3 step of the
+    same mesh: the bounded CPU sample."""
+    from oracle.oracle import Oracle
+    o = Oracle(c.with_numerics(precision=K.PREC_FP64))
+    cv, dv = c.cv.copy(), c.dv.copy()
+    num = c.numerics
+    t0 = time.perf_counter()
+    dti = o.dt(cv, dv, num.cfl, 1.0, 0.0, 1.0)
+    dtm = o.dt(cv, dv, num.cfl, dti, 0.0, 0.0)
+    for s in (1, 2, 3):
+        o.stage(cv, dv, s, dtm, threads=threads)
+    el = time.perf_counter() - t0
+    evals = 3 * (c.mesh.nFaces + c.mesh.nBFaces)
+    return evals / el, el
+
+
+def run_reference(a, dist):
+    """--impl reference: the reference path's CPU restatement (the Fortran
+    reference cannot be built here), all host threads, rank 0 only."""
+    if dist.rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    c = build_case(a)
+    from oracle.oracle import Oracle
+    o = Oracle(c.with_numerics(precision=K.PREC_FP64))
+    cv, dv = c.cv.copy(), c.dv.copy()
+    num = c.numerics
+    dti = o.dt(cv, dv, num.cfl, 1.0, 0.0, 1.0)
+    dtm = o.dt(cv, dv, num.cfl, dti, 0.0, 0.0)
+    st = 1
+    for _ in range(min(a.warmup, 1)):
+        o.stage(cv, dv, st, dtm, threads=threads)
+        st = st % 3 + 1
+    t0 = time.perf_counter()
+    for _ in range(a.steps):  # one step of this arm = one RK stage of the full mesh
+        o.stage(cv, dv, st, dtm, threads=threads)
+        st = st % 3 + 1
+    el = time.perf_counter() - t0
+    evals = (c.mesh.nFaces + c.mesh.nBFaces) * a.steps
+    v = evals / el
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
+            "steps": a.steps, "warmup": a.warmup, "ms_per_step": el / a.steps * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(c, a),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"{a.steps} RK stages of the full mesh, OpenMP C++ FP64 "
+                                       f"restatement of the reference residual/RK path "
+                                       f"(reference Fortran+MPI not buildable here)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def timed_steps(r, steps, cfl, dti, prof=True):
+    if prof:
+        r.profile(True)
+    l0 = r.launches
+    r.timer_start()
+    for _ in range(steps):
+        r.step(cfl, dti)
+    ms = r.timer_stop()
+    launches = r.launches - l0
+    pr = r.profile_read() if prof else {}
+    if prof:
+        r.profile(False)
+    return ms, launches, pr
+
+
+def main():
+    a = parse()
+    dist = Dist()
+    if a.impl == "reference":
+        run_reference(a, dist)
+        dist.close()
+        return
+    from rocflupicl_gb300 import engine as E
+    E.set_device(dist.local)
+    c = build_case(a)
+    m = c.mesh
+    evals_step = 3 * (m.nFaces + m.nBFaces)
+    cfl = c.numerics.cfl
+    peak, peak_kind = peaks()
+    res = {}
+
+    # ---- mixed path, resident ------------------------------------------------
+    r = E.Region(c)
+    dti = r.time_step(cfl, 1.0, 0.0, 1.0)
+    r.set_time(0.0)
+    for _ in range(a.warmup):
+        r.step(cfl, dti)
+    r.sync()
+    clocks = Clocks(dist.local)
+    dist.barrier()
+    clocks.start()
+    ms, launches, pr = timed_steps(r, a.steps, cfl, dti)
+    clk = clocks.stop()
+    dist.barrier()
+    ms_max = dist.max(ms)
+    status = r.status()
+    value = evals_step * a.steps * dist.world / (ms_max * 1e-3)
+    s = 4
+    kb = perfmodel.kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
+    per = {}
+    for k, (t, n) in pr.items():
+        if n:
+            per[k] = {"ms_total": t, "launches": n, "ms_avg": t / n}
+            if k in kb:
+                per[k]["gbs"] = kb[k] / (t / n * 1e-3) / 1e9
+    dom = max((k for k in per if k in kb), key=lambda k: per[k]["ms_total"])
+    traffic = ncu_traffic().get(dom)
+    achieved = per[dom]["gbs"]
+    stage_b = perfmodel.stage_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
+    step_gbs = 3 * stage_b / (ms / a.steps * 1e-3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "algorithmic_bytes_per_launch": kb[dom],
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
+            "step_gbs": step_gbs, "step_frac": step_gbs / peak}
+
+    # ---- e2e through the C ABI with host buffers --------------------------------
+    e2e = None
+    if not a.no_e2e:
+        cvh = E.PinnedArray((m.nCells, 5))
+        dvh = E.PinnedArray((m.nCells, 3))
+        r.download_into(cvh.array, dvh.array)
+        for _ in range(2):
+            r.upload(cvh.array)
+            r.step(cfl, dti)
+            r.download_into(cvh.array, dvh.array)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            r.upload(cvh.array)
+            r.step(cfl, dti)
+            r.download_into(cvh.array, dvh.array)
+        el = dist.max(time.perf_counter() - t0)
+        e2e = {"value": evals_step * a.steps * dist.world / el, "unit": UNIT,
+               "h2d_bytes_per_step": 40 * m.nCells, "d2h_bytes_per_step": 64 * m.nCells,
+               "ms_per_step": el / a.steps * 1e3,
+               "path": "rfgpu_upload(cv) + rfgpu_step + rfgpu_download(cv,dv), pinned host buffers"}
+        cvh.close()
+        dvh.close()
+    dev_bytes = r.device_bytes
+    r.close()
+
+    # ---- FP64 path and accuracy of mixed vs FP64 -------------------------------
+    fp64 = None
+    if not a.no_fp64:
+        c64 = c.with_numerics(precision=K.PREC_FP64)
+        f = E.Region(c64)
+        for _ in range(min(a.warmup, 2)):
+            f.step(cfl, dti)
+        f.sync()
+        nst = max(2, min(a.steps, 5))
+        ms64, _, pr64 = timed_steps(f, nst, cfl, dti)
+        kb64 = perfmodel.kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, 8)
+        dom64 = max((k for k in pr64 if k in kb64 and pr64[k][1]), key=lambda k: pr64[k][0])
+        t64 = pr64[dom64][0] / pr64[dom64][1]
+        fp64 = {"value": evals_step * nst / (ms64 * 1e-3), "ms_per_step": ms64 / nst,
+                "steps": nst, "dominant_kernel": dom64, "dominant_gbs": kb64[dom64] / (t64 * 1e-3) / 1e9,
+                "bound": "fp64 ALU (GB300 non-tensor FP64 rate), not HBM",
+                "kernel_ms": {k: v[0] / v[1] for k, v in pr64.items() if v[1]}}
+        f.close()
+        # identical dt sequence (from the FP64 path) for both precisions
+        f = E.Region(c64)
+        mm = E.Region(c)
+        t = 0.0
+        for _ in range(a.l1_steps):
+            dt = f.time_step(cfl, dti, 0.0, t)
+            for st in (1, 2, 3):
+                f.rk_stage(st, dt)
+                mm.rk_stage(st, dt)
+            t += dt
+        cvf, dvf = f.download()
+        cvm, dvm = mm.download()
+        fp64["l1_rho"] = float(np.mean(np.abs(cvm[:, 0] / cvf[:, 0] - 1.0)))
+        fp64["l1_p"] = float(np.mean(np.abs(dvm[:, 0] / dvf[:, 0] - 1.0)))
+        fp64["l1_steps"] = a.l1_steps
+        fp64["speedup_mixed_vs_fp64"] = value / dist.world / fp64["value"]
+        f.close()
+        mm.close()
+
+    # ---- CPU baseline (rank 0) --------------------------------------------------
+    cpu = None
+    if not a.no_cpu and dist.rank == 0:
+        th = os.cpu_count() or 1
+        v, el = cpu_sample(c, th)
+        cpu = {"value": v, "unit": UNIT, "cores": th, "kind": "port",
+               "sample": f"1 RK3 step (dt + 3 stages) of the same {m.nCells}-cell mesh, "
+                         f"OpenMP C++ FP64 restatement of the reference path, {el:.1f} s"}
+
+    if dist.rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32 flux / f64 accumulate", "data": "synthetic (seeded)",
+                "config": workload_config(c, a), "roofline": roof, "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": launches, "clocks": clk, "status": status,
+                "kernels": per, "fp64": fp64, "device_bytes": dev_bytes}
+        print(json.dumps(line), flush=True)
+    dist.close()
+
+
+if __name__ == "__main__":
+    main()

@@ -162,6 +162,28 @@ long long rfgpu_launch_count(rfgpu_region_t h);
 /* Launch configuration used by the kernels (block size); 0 = default. */
 int rfgpu_set_tuning(rfgpu_region_t h, int blockCells, int blockFaces);
 
+/* Per-kernel profiler (the engine's counterpart of the reference's ROCPROF
+ * FPROFILER_BEGINS/ENDS markers): while enabled, CUDA events are recorded on
+ * the handle's stream around every kernel; rfgpu_profile_read synchronises and
+ * returns, per kernel class, the summed milliseconds and launch counts, then
+ * resets.  Classes: 0 gradient, 1 limiter, 2 face flux, 3 boundary-face flux,
+ * 4 gather+update, 5 dt faces, 6 dt boundary faces, 7 dt cells, 8 dt finalize.
+ * Graph replays are not profiled. */
+#define RFGPU_NPROF 9
+int rfgpu_profile(rfgpu_region_t h, int enable);
+int rfgpu_profile_read(rfgpu_region_t h, double *ms, long long *count, int n);
+
+/* Stream timers: CUDA events recorded on the handle's stream; stop
+ * synchronises on the stop event and returns the elapsed milliseconds. */
+int rfgpu_timer_start(rfgpu_region_t h);
+int rfgpu_timer_stop(rfgpu_region_t h, double *ms);
+
+/* Device selection for the calling host thread (one process per GPU), and
+ * page-locked host buffers for the host<->device copies of a drop-in caller. */
+int rfgpu_set_device(int device);
+void *rfgpu_host_alloc(long long bytes);
+int rfgpu_host_free(void *p);
+
 /* Batches: many independent regions advanced together, one launch per pass
  * over all regions (a persistent grid walking a tile work list). */
 int rfgpu_batch_create(rfgpu_region_t *regions, int nRegions, rfgpu_batch_t *out);
@@ -172,6 +194,11 @@ int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtIm
                             double dtMinLimit, double endTime);
 int rfgpu_batch_sync(rfgpu_batch_t b);
 void *rfgpu_batch_stream(rfgpu_batch_t b);
+int rfgpu_batch_profile(rfgpu_batch_t b, int enable);
+int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int n);
+long long rfgpu_batch_launch_count(rfgpu_batch_t b);
+int rfgpu_batch_timer_start(rfgpu_batch_t b);
+int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms);
 
 #ifdef __cplusplus
 }

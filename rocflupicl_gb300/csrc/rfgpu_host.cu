@@ -60,6 +60,51 @@ struct Sell {
   long long at(int c, int k) const { return off[c / kSlice] + (long long)k * kSlice + c % kSlice; }
 };
 
+// Per-kernel CUDA-event profiler: a pair of events recorded on the launching
+// stream around every launch while enabled; resolved into per-class totals
+// when read.
+struct ProfState {
+  bool on = false;
+  std::vector<cudaEvent_t> pool;
+  size_t used = 0;
+  std::vector<std::pair<int, std::pair<size_t, size_t>>> spans;  // kind, (start ev, stop ev)
+  size_t open[KP_COUNT] = {0};
+  Prof hook{};
+  cudaEvent_t get() {
+    if (used == pool.size()) {
+      cudaEvent_t e;
+      cudaEventCreate(&e);
+      pool.push_back(e);
+    }
+    return pool[used++];
+  }
+  static void mark(void *ctx, int kind, int phase, cudaStream_t s) {
+    ProfState *p = (ProfState *)ctx;
+    size_t idx = p->used;
+    cudaEvent_t e = p->get();
+    cudaEventRecord(e, s);
+    if (phase == 0)
+      p->open[kind] = idx;
+    else
+      p->spans.push_back({kind, {p->open[kind], idx}});
+  }
+  const Prof *hookp() {
+    if (!on) return nullptr;
+    hook.mark = &ProfState::mark;
+    hook.ctx = this;
+    return &hook;
+  }
+  void reset() {
+    used = 0;
+    spans.clear();
+  }
+  void destroy() {
+    for (auto e : pool) cudaEventDestroy(e);
+    pool.clear();
+    reset();
+  }
+};
+
 }  // namespace
 
 struct rfgpu_region_s {
@@ -79,6 +124,8 @@ struct rfgpu_region_s {
   cudaGraphExec_t graph = nullptr;
   double gkey[4] = {0, 0, 0, 0};
   long long perStep = 0;
+  ProfState prof;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
 };
 
 struct rfgpu_batch_s {
@@ -93,6 +140,8 @@ struct rfgpu_batch_s {
   cudaGraphExec_t graph = nullptr;
   double gkey[4] = {0, 0, 0, 0};
   long long perStep = 0;
+  ProfState prof;
+  cudaEvent_t t0 = nullptr, t1 = nullptr;
 };
 
 namespace {
@@ -367,17 +416,17 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
 void stage_launch(rfgpu_region_s *h, const StepArgs &a) {
   if (h->prec)
     launch_stage<float>(regs_of<float>(h), h->work, a, h->stream, &h->launches, h->spaceOrder,
-                        h->reconst);
+                        h->reconst, h->prof.hookp());
   else
     launch_stage<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches, h->spaceOrder,
-                         h->reconst);
+                         h->reconst, h->prof.hookp());
 }
 
 void dt_launch(rfgpu_region_s *h, const DtArgs &a) {
   if (h->prec)
-    launch_dt<float>(regs_of<float>(h), h->work, a, h->stream, &h->launches);
+    launch_dt<float>(regs_of<float>(h), h->work, a, h->stream, &h->launches, h->prof.hookp());
   else
-    launch_dt<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches);
+    launch_dt<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches, h->prof.hookp());
 }
 
 void step_launch(rfgpu_region_s *h, double cfl, double dtImposed, double dtMinLimit,
@@ -466,6 +515,9 @@ int rfgpu_region_destroy(rfgpu_region_t h) {
   if (!h) return RFGPU_ERR_ARG;
   cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->t0) cudaEventDestroy(h->t0);
+  if (h->t1) cudaEventDestroy(h->t1);
+  h->prof.destroy();
   h->mem.free_all();
   cudaStreamDestroy(h->stream);
   delete h;
@@ -509,7 +561,10 @@ int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed
     if (cudaStreamBeginCapture(h->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return RFGPU_ERR_CUDA;
     long long before = h->launches;
+    bool profOn = h->prof.on;
+    h->prof.on = false;
     step_launch(h, cfl, dtImposed, dtMinLimit, endTime);
+    h->prof.on = profOn;
     h->perStep = h->launches - before;  // counted at replay
     h->launches = before;
     if (cudaStreamEndCapture(h->stream, &g) != cudaSuccess) return RFGPU_ERR_CUDA;
@@ -698,6 +753,9 @@ int rfgpu_batch_destroy(rfgpu_batch_t b) {
   if (!b) return RFGPU_ERR_ARG;
   cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
+  if (b->t0) cudaEventDestroy(b->t0);
+  if (b->t1) cudaEventDestroy(b->t1);
+  b->prof.destroy();
   b->mem.free_all();
   cudaStreamDestroy(b->stream);
   delete b;
@@ -708,17 +766,19 @@ static void batch_step_launch(rfgpu_batch_t b, double cfl, double dtImposed, dou
                               double endTime) {
   DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
   if (b->prec)
-    launch_dt<float>((const RegionDev<float> *)b->regsDev, b->work, da, b->stream, &b->launches);
+    launch_dt<float>((const RegionDev<float> *)b->regsDev, b->work, da, b->stream, &b->launches,
+                     b->prof.hookp());
   else
-    launch_dt<double>((const RegionDev<double> *)b->regsDev, b->work, da, b->stream, &b->launches);
+    launch_dt<double>((const RegionDev<double> *)b->regsDev, b->work, da, b->stream, &b->launches,
+                      b->prof.hookp());
   for (int is = 1; is <= b->nSteps; ++is) {
     StepArgs sa{is, 1, 0.0, 0, 1};
     if (b->prec)
       launch_stage<float>((const RegionDev<float> *)b->regsDev, b->work, sa, b->stream,
-                          &b->launches, b->spaceOrder, b->reconst);
+                          &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
     else
       launch_stage<double>((const RegionDev<double> *)b->regsDev, b->work, sa, b->stream,
-                           &b->launches, b->spaceOrder, b->reconst);
+                           &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
   }
 }
 
@@ -742,7 +802,10 @@ int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtIm
     if (cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
       return RFGPU_ERR_CUDA;
     long long before = b->launches;
+    bool profOn = b->prof.on;
+    b->prof.on = false;
     batch_step_launch(b, cfl, dtImposed, dtMinLimit, endTime);
+    b->prof.on = profOn;
     b->perStep = b->launches - before;  // counted at replay
     b->launches = before;
     if (cudaStreamEndCapture(b->stream, &g) != cudaSuccess) return RFGPU_ERR_CUDA;
@@ -763,5 +826,87 @@ int rfgpu_batch_sync(rfgpu_batch_t b) {
 }
 
 void *rfgpu_batch_stream(rfgpu_batch_t b) { return b ? (void *)b->stream : nullptr; }
+
+static int prof_read(ProfState &p, cudaStream_t s, double *ms, long long *count, int n) {
+  if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
+  for (int k = 0; k < n; ++k) {
+    ms[k] = 0.0;
+    if (count) count[k] = 0;
+  }
+  for (auto &sp : p.spans) {
+    float t = 0.f;
+    if (cudaEventElapsedTime(&t, p.pool[sp.second.first], p.pool[sp.second.second]) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    if (sp.first < n) {
+      ms[sp.first] += t;
+      if (count) count[sp.first] += 1;
+    }
+  }
+  p.reset();
+  return RFGPU_OK;
+}
+
+int rfgpu_profile(rfgpu_region_t h, int enable) {
+  if (!h) return RFGPU_ERR_ARG;
+  cudaStreamSynchronize(h->stream);
+  h->prof.on = enable != 0;
+  h->prof.reset();
+  return RFGPU_OK;
+}
+
+int rfgpu_profile_read(rfgpu_region_t h, double *ms, long long *count, int n) {
+  if (!h || !ms || n < 0) return RFGPU_ERR_ARG;
+  return prof_read(h->prof, h->stream, ms, count, n);
+}
+
+int rfgpu_batch_profile(rfgpu_batch_t b, int enable) {
+  if (!b) return RFGPU_ERR_ARG;
+  cudaStreamSynchronize(b->stream);
+  b->prof.on = enable != 0;
+  b->prof.reset();
+  return RFGPU_OK;
+}
+
+int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int n) {
+  if (!b || !ms || n < 0) return RFGPU_ERR_ARG;
+  return prof_read(b->prof, b->stream, ms, count, n);
+}
+
+long long rfgpu_batch_launch_count(rfgpu_batch_t b) { return b ? b->launches : -1; }
+
+static int timer_start(cudaEvent_t &t0, cudaEvent_t &t1, cudaStream_t s) {
+  if (!t0 && cudaEventCreate(&t0) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (!t1 && cudaEventCreate(&t1) != cudaSuccess) return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaEventRecord(t0, s));
+}
+
+static int timer_stop(cudaEvent_t t0, cudaEvent_t t1, cudaStream_t s, double *ms) {
+  if (!t0 || !t1 || !ms) return RFGPU_ERR_ARG;
+  if (cudaEventRecord(t1, s) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (cudaEventSynchronize(t1) != cudaSuccess) return RFGPU_ERR_CUDA;
+  float f = 0.f;
+  if (cudaEventElapsedTime(&f, t0, t1) != cudaSuccess) return RFGPU_ERR_CUDA;
+  *ms = f;
+  return RFGPU_OK;
+}
+
+int rfgpu_timer_start(rfgpu_region_t h) { return h ? timer_start(h->t0, h->t1, h->stream) : RFGPU_ERR_ARG; }
+int rfgpu_timer_stop(rfgpu_region_t h, double *ms) {
+  return h ? timer_stop(h->t0, h->t1, h->stream, ms) : RFGPU_ERR_ARG;
+}
+int rfgpu_batch_timer_start(rfgpu_batch_t b) { return b ? timer_start(b->t0, b->t1, b->stream) : RFGPU_ERR_ARG; }
+int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms) {
+  return b ? timer_stop(b->t0, b->t1, b->stream, ms) : RFGPU_ERR_ARG;
+}
+
+int rfgpu_set_device(int device) { return cuda_rc(cudaSetDevice(device)); }
+
+void *rfgpu_host_alloc(long long bytes) {
+  void *p = nullptr;
+  if (bytes <= 0 || cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
+  return p;
+}
+
+int rfgpu_host_free(void *p) { return p ? cuda_rc(cudaFreeHost(p)) : RFGPU_ERR_ARG; }
 
 }  // extern "C"

@@ -107,16 +107,27 @@ struct DtArgs {
   double timeHost;
 };
 
+// Kernel classes for the per-kernel event profiler.
+enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
+       KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_COUNT };
+
+// Optional hook called around every kernel launch (phase 0 before, 1 after),
+// used to record CUDA events on the launching stream.
+struct Prof {
+  void (*mark)(void *ctx, int kind, int phase, cudaStream_t s);
+  void *ctx;
+};
+
 // Launchers, instantiated for R = double (FP64 unit, no FMA contraction) and
 // R = float (mixed unit).  `regs` is a device array of RegionDev<R>.
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
-                  long long *launches, int spaceOrder, int reconst);
+                  long long *launches, int spaceOrder, int reconst, const Prof *prof);
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
-               long long *launches);
+               long long *launches, const Prof *prof);
 
 // Setup kernels of the FP64 unit.  WLSQ weights of every stencil member,
 // w64[3][stTotal], with the arithmetic of RFLU_ComputeGradCellsFast_3D

@@ -803,29 +803,42 @@ void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStr
   if (grid > 0) k_prim<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, computeDv);
 }
 
+#define RF_MARK(kind, phase) \
+  if (prof) prof->mark(prof->ctx, (kind), (phase), s)
+
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
-                  long long *launches, int spaceOrder, int reconst) {
+                  long long *launches, int spaceOrder, int reconst, const Prof *prof) {
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   long long n = 0;
   if (spaceOrder > 1 && w.nCellTiles > 0) {
+    RF_MARK(KP_GRADIENT, 0);
     k_gradient<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    RF_MARK(KP_GRADIENT, 1);
     ++n;
     if (reconst == 11) {
+      RF_MARK(KP_LIMITER, 0);
       k_limiter<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+      RF_MARK(KP_LIMITER, 1);
       ++n;
     }
   }
   if (w.nFaceTiles > 0) {
+    RF_MARK(KP_FACE_FLUX, 0);
     k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
+    RF_MARK(KP_FACE_FLUX, 1);
     ++n;
   }
   if (w.nBFaceTiles > 0) {
+    RF_MARK(KP_BFACE_FLUX, 0);
     k_bface_flux<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
+    RF_MARK(KP_BFACE_FLUX, 1);
     ++n;
   }
   if (w.nCellTiles > 0) {
+    RF_MARK(KP_GATHER_UPDATE, 0);
     k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a);
+    RF_MARK(KP_GATHER_UPDATE, 1);
     ++n;
   }
   if (launches) *launches += n;
@@ -833,22 +846,30 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
 
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
-               long long *launches) {
+               long long *launches, const Prof *prof) {
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   long long n = 0;
   if (w.nFaceTiles > 0) {
+    RF_MARK(KP_DT_FACE, 0);
     k_dt_face<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
+    RF_MARK(KP_DT_FACE, 1);
     ++n;
   }
   if (w.nBFaceTiles > 0) {
+    RF_MARK(KP_DT_BFACE, 0);
     k_dt_bface<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
+    RF_MARK(KP_DT_BFACE, 1);
     ++n;
   }
   if (w.nCellTiles > 0) {
+    RF_MARK(KP_DT_CELL, 0);
     k_dt_cell<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    RF_MARK(KP_DT_CELL, 1);
     ++n;
   }
+  RF_MARK(KP_DT_FINAL, 0);
   k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a);
+  RF_MARK(KP_DT_FINAL, 1);
   ++n;
   if (launches) *launches += n;
 }
@@ -856,8 +877,8 @@ void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStr
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
-                                cudaStream_t, long long *, int, int);                         \
+                                cudaStream_t, long long *, int, int, const Prof *);           \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
-                             long long *);
+                             long long *, const Prof *);
 
 }  // namespace rfgpu

@@ -62,7 +62,13 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_status", "rfgpu_sync", "rfgpu_stream", "rfgpu_device_bytes",
            "rfgpu_launch_count", "rfgpu_set_tuning", "rfgpu_batch_create",
            "rfgpu_batch_destroy", "rfgpu_batch_step", "rfgpu_batch_steps_graph",
-           "rfgpu_batch_sync", "rfgpu_batch_stream"]
+           "rfgpu_batch_sync", "rfgpu_batch_stream", "rfgpu_profile", "rfgpu_profile_read",
+           "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
+           "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
+           "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free"]
+
+KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
+           "dt_bface", "dt_cell", "dt_finalize"]
 
 _lib = None
 
@@ -100,6 +106,18 @@ def load(path: Optional[str] = None):
         "rfgpu_batch_steps_graph": ([vp, C.c_int, d, d, d, d], C.c_int),
         "rfgpu_batch_sync": ([vp], C.c_int),
         "rfgpu_batch_stream": ([vp], vp),
+        "rfgpu_profile": ([vp, C.c_int], C.c_int),
+        "rfgpu_profile_read": ([vp, dp, C.POINTER(C.c_longlong), C.c_int], C.c_int),
+        "rfgpu_batch_profile": ([vp, C.c_int], C.c_int),
+        "rfgpu_batch_profile_read": ([vp, dp, C.POINTER(C.c_longlong), C.c_int], C.c_int),
+        "rfgpu_batch_launch_count": ([vp], C.c_longlong),
+        "rfgpu_timer_start": ([vp], C.c_int),
+        "rfgpu_timer_stop": ([vp, dp], C.c_int),
+        "rfgpu_batch_timer_start": ([vp], C.c_int),
+        "rfgpu_batch_timer_stop": ([vp, dp], C.c_int),
+        "rfgpu_set_device": ([C.c_int], C.c_int),
+        "rfgpu_host_alloc": ([C.c_longlong], vp),
+        "rfgpu_host_free": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -121,6 +139,44 @@ def _ip(a):
 def _check(rc: int, where: str):
     if rc != OK:
         raise EngineError(rc, where)
+
+
+def _prof_read(fn, h):
+    n = len(KERNELS)
+    ms = (C.c_double * n)()
+    cnt = (C.c_longlong * n)()
+    _check(fn(h, ms, cnt, n), "rfgpu_profile_read")
+    return {KERNELS[i]: (ms[i], cnt[i]) for i in range(n)}
+
+
+def set_device(device: int):
+    """Select the GPU for this host thread (one process per GPU)."""
+    _check(load().rfgpu_set_device(device), "rfgpu_set_device")
+
+
+class PinnedArray:
+    """A page-locked host buffer viewed as a float64 NumPy array."""
+
+    def __init__(self, shape):
+        self.lib = load()
+        n = int(np.prod(shape))
+        self.ptr = self.lib.rfgpu_host_alloc(8 * n)
+        if not self.ptr:
+            raise EngineError(ERR_NOMEM, "rfgpu_host_alloc")
+        buf = (C.c_double * n).from_address(self.ptr)
+        self.array = np.ctypeslib.as_array(buf).reshape(shape)
+
+    def close(self):
+        if getattr(self, "ptr", None):
+            self.array = None
+            self.lib.rfgpu_host_free(self.ptr)
+            self.ptr = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class Region:
@@ -269,6 +325,21 @@ class Region:
     def launches(self) -> int:
         return self.lib.rfgpu_launch_count(self.h)
 
+    def timer_start(self):
+        _check(self.lib.rfgpu_timer_start(self.h), "rfgpu_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        _check(self.lib.rfgpu_timer_stop(self.h, C.byref(ms)), "rfgpu_timer_stop")
+        return ms.value
+
+    def profile(self, enable: bool = True):
+        _check(self.lib.rfgpu_profile(self.h, int(enable)), "rfgpu_profile")
+
+    def profile_read(self):
+        """{kernel: (total ms, launches)} since profiling was enabled/read."""
+        return _prof_read(self.lib.rfgpu_profile_read, self.h)
+
     def set_grid_cap(self, blocks: int):
         _check(self.lib.rfgpu_set_tuning(self.h, blocks, 0), "rfgpu_set_tuning")
 
@@ -327,6 +398,24 @@ class Batch:
 
     def sync(self):
         _check(self.lib.rfgpu_batch_sync(self.h), "rfgpu_batch_sync")
+
+    def timer_start(self):
+        _check(self.lib.rfgpu_batch_timer_start(self.h), "rfgpu_batch_timer_start")
+
+    def timer_stop(self) -> float:
+        ms = C.c_double()
+        _check(self.lib.rfgpu_batch_timer_stop(self.h, C.byref(ms)), "rfgpu_batch_timer_stop")
+        return ms.value
+
+    def profile(self, enable: bool = True):
+        _check(self.lib.rfgpu_batch_profile(self.h, int(enable)), "rfgpu_batch_profile")
+
+    def profile_read(self):
+        return _prof_read(self.lib.rfgpu_batch_profile_read, self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.lib.rfgpu_batch_launch_count(self.h)
 
     @property
     def stream(self) -> int:
