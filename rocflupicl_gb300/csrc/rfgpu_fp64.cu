@@ -101,4 +101,21 @@ void launch_soa_to_aos_f32(const float *soa, double *aos, int N, int ncomp, cuda
   k_soa_to_aos<float><<<nblk((long long)N * ncomp), 256, 0, s>>>(soa, aos, N, ncomp);
 }
 
+template <typename T>
+__global__ void k_grad_export(const T *__restrict__ g16, double *__restrict__ out, int N) {
+  long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  long long n = (long long)N * 15;
+  for (; i < n; i += (long long)gridDim.x * blockDim.x) {
+    long long c = i / 15, k = i - c * 15;
+    out[i] = (double)g16[16 * c + k];
+  }
+}
+
+void launch_grad_export(const double *g16, double *out, int N, cudaStream_t s) {
+  k_grad_export<double><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N);
+}
+void launch_grad_export_f32(const float *g16, double *out, int N, cudaStream_t s) {
+  k_grad_export<float><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N);
+}
+
 }  // namespace rfgpu

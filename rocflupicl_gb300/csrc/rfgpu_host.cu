@@ -246,6 +246,25 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   }
   g.vol = M.upload(vol, s);
   g.epsq = M.upload(cast<R>(epsq), s);
+  // WLSQ factor terms for the mixed path's on-the-fly weights
+  // (RFLU_ModDifferentiationCells.F90:1029-1042)
+  if (sizeof(R) == 4) {
+    std::vector<double> cw(6 * (size_t)N);
+    for (int c = 0; c < N; ++c) {
+      const double *mo = d->xyzMoms + 10 * (size_t)c;
+      double c11 = 1.0 / mo[0], c22 = 1.0 / mo[2], c33 = 1.0 / mo[5];
+      double c12 = -c11 * mo[1];
+      double c13 = -(c11 * mo[3] + c12 * c22 * mo[4]);
+      double c23 = -c22 * mo[4];
+      cw[c] = c12;
+      cw[(size_t)N + c] = c13;
+      cw[2 * (size_t)N + c] = c23;
+      cw[3 * (size_t)N + c] = c11 * c11;
+      cw[4 * (size_t)N + c] = c22 * c22;
+      cw[5 * (size_t)N + c] = c33 * c33;
+    }
+    g.cwt = M.upload(cast<R>(cw), s);
+  }
   // ---- stencil SELL
   {
     std::vector<int> cnt(N);
@@ -259,29 +278,25 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.stCnt = M.upload(sl.cnt, s);
     g.stIdx = M.upload(idx, s);
     g.stTotal = sl.total;
-    // weights on the device with the reference arithmetic (FP64 unit)
-    double *dcofg = M.alloc<double>(cofg.size());
-    double *dmoms = M.alloc<double>(moms.size());
-    cudaMemcpyAsync(dcofg, cofg.data(), cofg.size() * 8, cudaMemcpyHostToDevice, s);
-    cudaMemcpyAsync(dmoms, moms.data(), moms.size() * 8, cudaMemcpyHostToDevice, s);
-    double *w64 = M.alloc<double>(3 * (size_t)sl.total);
-    launch_weights64(g.stOff, g.stCnt, g.stIdx, N, dcofg, dmoms, w64, s, sl.total);
     if (sizeof(R) == 8) {
+      // weights on the device with the reference arithmetic (FP64 unit)
+      double *dcofg = M.alloc<double>(cofg.size());
+      double *dmoms = M.alloc<double>(moms.size());
+      cudaMemcpyAsync(dcofg, cofg.data(), cofg.size() * 8, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dmoms, moms.data(), moms.size() * 8, cudaMemcpyHostToDevice, s);
+      double *w64 = M.alloc<double>(3 * (size_t)sl.total);
+      launch_weights64(g.stOff, g.stCnt, g.stIdx, N, dcofg, dmoms, w64, s, sl.total);
       g.stW = (const R *)w64;
-    } else {
-      float *w32 = M.alloc<float>(3 * (size_t)sl.total);
-      launch_to_f32(w64, w32, 3 * sl.total, s);
-      g.stW = (const R *)w32;
     }
   }
   // ---- faces
   std::vector<int> f2c(2 * (size_t)F);
-  std::vector<double> fn(4 * (size_t)F), fdl(3 * (size_t)F), fdr(3 * (size_t)F);
+  std::vector<double> fnA(4 * (size_t)F), fdl(3 * (size_t)F), fdr(3 * (size_t)F);
   for (int f = 0; f < F; ++f) {
     int c1 = d->f2c[(long long)f * d->f2cLd] - 1, c2 = d->f2c[(long long)f * d->f2cLd + 1] - 1;
     f2c[f] = c1;
     f2c[(size_t)F + f] = c2;
-    for (int k = 0; k < 4; ++k) fn[(size_t)k * F + f] = d->fn[4 * (size_t)f + k];
+    for (int k = 0; k < 4; ++k) fnA[4 * (size_t)f + k] = d->fn[4 * (size_t)f + k];
     for (int k = 0; k < 3; ++k) {
       double xc = d->fc[3 * (size_t)f + k];
       fdl[(size_t)k * F + f] = xc - d->cofg[3 * (size_t)c1 + k];
@@ -289,12 +304,10 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     }
   }
   g.f2c = M.upload(f2c, s);
-  g.fn64 = M.upload(fn, s);
-  g.fn = sizeof(R) == 8 ? (const R *)g.fn64 : M.upload(cast<R>(fn), s);
+  g.fnA = M.upload(cast<R>(fnA), s);
   g.fdl = M.upload(cast<R>(fdl), s);
   g.fdr = M.upload(cast<R>(fdr), s);
-  g.flux = M.alloc<R>(5 * (size_t)F);
-  g.srad = M.alloc<double>(F);
+  g.flux = M.alloc<R>(8 * (size_t)F);
   // ---- boundary faces, patches in order
   std::vector<int> bf2c, bkind;
   std::vector<double> bfnA, bfdA, bpout;
@@ -314,19 +327,15 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   }
   const int B = (int)bf2c.size();
   g.nBFaces = B;
-  std::vector<double> bfn(4 * (size_t)B), bfd(3 * (size_t)B);
-  for (int b = 0; b < B; ++b) {
-    for (int k = 0; k < 4; ++k) bfn[(size_t)k * B + b] = bfnA[4 * (size_t)b + k];
+  std::vector<double> bfd(3 * (size_t)B);
+  for (int b = 0; b < B; ++b)
     for (int k = 0; k < 3; ++k) bfd[(size_t)k * B + b] = bfdA[3 * (size_t)b + k];
-  }
   g.bf2c = M.upload(bf2c, s);
   g.bkind = M.upload(bkind, s);
   g.bpout = M.upload(bpout, s);
-  g.bfn64 = M.upload(bfn, s);
-  g.bfn = sizeof(R) == 8 ? (const R *)g.bfn64 : M.upload(cast<R>(bfn), s);
+  g.bfnA = M.upload(cast<R>(bfnA), s);
   g.bfd = M.upload(cast<R>(bfd), s);
-  g.bflux = M.alloc<R>(5 * (size_t)B);
-  g.sradb = M.alloc<double>(B);
+  g.bflux = M.alloc<R>(8 * (size_t)B);
   // ---- cell -> face lists in the reference accumulation order
   {
     std::vector<int> cnt(N, 0);
@@ -365,13 +374,23 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   // ---- state
   g.cv = M.alloc<double>(5 * (size_t)N);
   g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
-  g.rhsSum = M.alloc<double>(5 * (size_t)N);
+  if (sizeof(R) == 8) {
+    g.rhsSum = M.alloc<double>(5 * (size_t)N);
+    cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
+  } else {
+    g.rhsSumF = M.alloc<float>(5 * (size_t)N);
+    cudaMemsetAsync(g.rhsSumF, 0, 5 * (size_t)N * sizeof(float), s);
+  }
   g.dv = M.alloc<double>(3 * (size_t)N);
   g.rhs = M.alloc<double>(5 * (size_t)N);
-  g.prim = M.alloc<R>(5 * (size_t)N);
-  g.grad = M.alloc<R>(15 * (size_t)N);
-  cudaMemsetAsync(g.grad, 0, 15 * (size_t)N * sizeof(R), s);
-  cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
+  {
+    std::vector<double> recx(8 * (size_t)N, 0.0);  // centroid slots; state filled by k_prim
+    for (int c = 0; c < N; ++c)
+      for (int k = 0; k < 3; ++k) recx[8 * (size_t)c + 5 + k] = d->cofg[3 * (size_t)c + k];
+    g.rec = M.upload(cast<R>(recx), s);
+  }
+  g.grad = M.alloc<R>(16 * (size_t)N);
+  cudaMemsetAsync(g.grad, 0, 16 * (size_t)N * sizeof(R), s);
   g.dtBits = M.alloc<unsigned long long>(1);
   unsigned long long inf = 0x7FF0000000000000ull;
   cudaMemcpyAsync(g.dtBits, &inf, 8, cudaMemcpyHostToDevice, s);
@@ -605,6 +624,10 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (dv) {
     // stage is reused: wait for the cv copy first
     if (cv && cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+    if (h->prec) {  // mixed path: a stage writes only p; complete T and a
+      launch_dv_complete<float>(regs_of<float>(h), h->work, h->stream);
+      h->launches++;
+    }
     launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(dv, h->stage, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
@@ -626,9 +649,9 @@ int rfgpu_download_grad(rfgpu_region_t h, double *grad) {
   double *tmp = nullptr;
   if (cudaMalloc(&tmp, 15 * (size_t)N * 8) != cudaSuccess) return RFGPU_ERR_NOMEM;
   if (h->prec)
-    launch_soa_to_aos_f32(h->rd32.grad, tmp, N, 15, h->stream);
+    launch_grad_export_f32(h->rd32.grad, tmp, N, h->stream);
   else
-    launch_soa_to_aos(h->rd64.grad, tmp, N, 15, h->stream);
+    launch_grad_export(h->rd64.grad, tmp, N, h->stream);
   h->launches++;
   cudaError_t e = cudaMemcpyAsync(grad, tmp, 15 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);

@@ -1,18 +1,24 @@
 // rfgpu_internal.h - device-side data layout shared by the engine's
 // translation units (host API, FP64 kernels, mixed-precision kernels).
 //
-// Layout in HBM (per region, N = nCells, F = nFaces, B = nBFaces):
-//   cell state   cv[5][N], rhsSum[5][N], dv[3][N] (p,T,a)     FP64, SoA
-//   working      prim[5][N] (rho,u,v,w,p), grad[15][N] ((3*v+d)*N + c)   R
+// Layout in HBM (per region, N = nCells, F = nFaces, B = nBFaces).  Data a
+// thread streams through is SoA (coalesced); data gathered through an index
+// is AoS, one record per cell or face, so a gather touches one 32-byte sector
+// (mixed path) instead of one per component:
+//   cell state   cv[5][N], rhsSum[5][N], dv[3][N] (p,T,a)        FP64 SoA
+//   cell record  rec[N][8] = rho,u,v,w,p,x,y,z                   R    AoS
+//   gradients    grad[N][16] = d(rho,u,v,w,p)/d(x,y,z)           R    AoS
 //   stencil      SELL-32: member k of cell c at stOff[c/32] + 32*k + c%32;
-//                stIdx (0-based), stW[3][stTotal] WLSQ weights   R
+//                stIdx (0-based); stW[3][stTotal] precomputed WLSQ weights
+//                (FP64 path); cwt[6][N] WLSQ factor terms (mixed path,
+//                weights rebuilt on the fly from rec x,y,z)
 //   cell->face   SELL-32 list in the reference accumulation order (interior
 //                faces ascending, then boundary faces by patch); code >= 0:
 //                2*face + side, code < 0: -(bface+1); cfNb = other cell,
 //                cfD[3] = cofg - fc (limiter vector)
-//   faces        f2c[2][F], fn[4][F], fdl/fdr[3][F] = fc - cofg(c1/c2)
-//   boundary     bf2c[B], bfn[4][B], bfd[3][B], bkind[B], bpout[B]
-//   scratch      flux[5][F], bflux[5][B] (R), srad[F], sradb[B] (FP64)
+//   faces        f2c[2][F], fnA[F][4] (normal, area), fdl/fdr[3][F] = fc - cofg(c1/c2)
+//   boundary     bf2c[B], bfnA[B][4], bfd[3][B], bkind[B], bpout[B]
+//   scratch      flux[F][8], bflux[B][8] (R, 5 used)
 // R is double on the FP64 path and float on the mixed path.
 #pragma once
 
@@ -40,16 +46,21 @@ struct Phys {
 template <typename R>
 struct RegionDev {
   int nCells, nFaces, nBFaces, pad_;
-  // state
+  // state (FP64 SoA); the mixed path keeps its RK increment history in FP32
+  // (rhsSumF) and writes only p of dv during a stage (T, a on download)
   double *cv, *cvOld, *rhsSum, *dv, *rhs;
-  R *prim, *grad;
+  float *rhsSumF;
+  // gathered per-cell records (AoS): rec[8*c..] = rho,u,v,w,p,x,y,z;
+  // grad[16*c + 3*v + d] (15 used)
+  R *rec, *grad;
   // geometry
   const double *vol;
   const R *epsq;
+  const R *cwt;   // [6][N] c12,c13,c23,c11^2,c22^2,c33^2 of the WLSQ factor (mixed path)
   // stencil (SELL-32)
   const long long *stOff;
   const int *stCnt, *stIdx;
-  const R *stW;
+  const R *stW;   // [3][stTotal] precomputed weights (FP64 path)
   long long stTotal;
   // cell -> face (SELL-32)
   const long long *cfOff;
@@ -57,21 +68,18 @@ struct RegionDev {
   const R *cfD;
   long long cfTotal;
   // faces
-  const int *f2c;
-  const R *fn;
-  const double *fn64;
-  const R *fdl, *fdr;
-  R *flux;
+  const int *f2c;      // [2][F]
+  const R *fnA;        // [F][4] nx,ny,nz,area
+  const R *fdl, *fdr;  // [3][F]
+  R *flux;             // [F][8] (5 used)
   // boundary faces
   const int *bf2c;
-  const R *bfn;
-  const double *bfn64;
-  const R *bfd;
+  const R *bfnA;       // [B][4]
+  const R *bfd;        // [3][B]
   const int *bkind;
   const double *bpout;
-  R *bflux;
+  R *bflux;            // [B][8]
   // time step
-  double *srad, *sradb;
   unsigned long long *dtBits;
   double *scal;   // [0] dtMin, [1] current time, [2] dtMin of the previous step
   unsigned *status;
@@ -110,6 +118,9 @@ struct DtArgs {
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
        KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_COUNT };
+// KP_GRADIENT times the fused gradient + limiter kernel; KP_LIMITER, KP_DT_FACE
+// and KP_DT_BFACE are no longer launched separately (kept for the ABI's
+// class numbering).
 
 // Optional hook called around every kernel launch (phase 0 before, 1 after),
 // used to record CUDA events on the launching stream.
@@ -122,6 +133,8 @@ struct Prof {
 // R = float (mixed unit).  `regs` is a device array of RegionDev<R>.
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
+template <typename R>
+void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof);
@@ -141,5 +154,8 @@ void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s);
 void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, cudaStream_t s);
 void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, cudaStream_t s);
 void launch_soa_to_aos_f32(const float *soa, double *aos, int N, int ncomp, cudaStream_t s);
+// grad[N][16] -> grad(3,5,N) Fortran image in FP64
+void launch_grad_export(const double *g16, double *out, int N, cudaStream_t s);
+void launch_grad_export_f32(const float *g16, double *out, int N, cudaStream_t s);
 
 }  // namespace rfgpu

@@ -188,41 +188,79 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
   }
 }
 
+// ---- vector access to AoS records --------------------------------------------
+__device__ __forceinline__ void ld8(const float *__restrict__ p, float v[8]) {
+  float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+__device__ __forceinline__ void ld8(const double *__restrict__ p, double v[8]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    double2 a = reinterpret_cast<const double2 *>(p)[i];
+    v[2 * i] = a.x;
+    v[2 * i + 1] = a.y;
+  }
+}
+__device__ __forceinline__ void ld4(const float *__restrict__ p, float v[4]) {
+  float4 a = *reinterpret_cast<const float4 *>(p);
+  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+__device__ __forceinline__ void ld4(const double *__restrict__ p, double v[4]) {
+  double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
+  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
+}
+__device__ __forceinline__ void st8(float *p, const float v[8]) {
+  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  *reinterpret_cast<float4 *>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+}
+__device__ __forceinline__ void st8(double *p, const double v[8]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i) reinterpret_cast<double2 *>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+}
+template <typename R>
+__device__ __forceinline__ void ld16(const R *__restrict__ p, R v[16]) {
+  ld8(p, v);
+  ld8(p + 8, v + 8);
+}
+template <typename R>
+__device__ __forceinline__ void st16(R *p, const R v[16]) {
+  st8(p, v);
+  st8(p + 8, v + 8);
+}
+
 // Cell-centre values the *_ComputeFlux2_TCP loops start from: rho, u = rhou *
 // (1/rho) with rhou the conserved momentum as CellGradientsMP's Prim2Cons
 // left it (rho * u_prim), p from dv.  On the mixed path the FP32 primitive
-// state is used directly.
+// state is used directly.  rc = the cell's record.
 template <typename R>
-__device__ __forceinline__ void cell_values(const RegionDev<R> &g, int c, R S[5], R &ir) {
+__device__ __forceinline__ void cell_values(const RegionDev<R> &g, int c, const R rc[8], R S[5],
+                                            R &ir) {
   const int N = g.nCells;
-  R rho = g.prim[c];
+  R rho = rc[0];
   ir = R(1) / rho;
   S[0] = rho;
   if (sizeof(R) == 8) {
     if (g.ph.spaceOrder > 1) {
-      S[1] = (rho * g.prim[N + c]) * ir;
-      S[2] = (rho * g.prim[2 * N + c]) * ir;
-      S[3] = (rho * g.prim[3 * N + c]) * ir;
+      S[1] = (rho * rc[1]) * ir;
+      S[2] = (rho * rc[2]) * ir;
+      S[3] = (rho * rc[3]) * ir;
     } else {
       S[1] = R(g.cv[N + c]) * ir;
       S[2] = R(g.cv[2 * N + c]) * ir;
       S[3] = R(g.cv[3 * N + c]) * ir;
     }
   } else {
-    S[1] = g.prim[N + c];
-    S[2] = g.prim[2 * N + c];
-    S[3] = g.prim[3 * N + c];
+    S[1] = rc[1];
+    S[2] = rc[2];
+    S[3] = rc[3];
   }
-  S[4] = g.prim[4 * N + c];
+  S[4] = rc[4];
 }
 
 template <typename R>
-__device__ __forceinline__ void reconstruct(const RegionDev<R> &g, int c, R dx, R dy, R dz, R S[5]) {
-  const int N = g.nCells;
+__device__ __forceinline__ void reconstruct(const R G[16], R dx, R dy, R dz, R S[5]) {
 #pragma unroll
-  for (int v = 0; v < 5; ++v)
-    S[v] = S[v] + g.grad[(3 * v) * N + c] * dx + g.grad[(3 * v + 1) * N + c] * dy +
-           g.grad[(3 * v + 2) * N + c] * dz;
+  for (int v = 0; v < 5; ++v) S[v] = S[v] + G[3 * v] * dx + G[3 * v + 1] * dy + G[3 * v + 2] * dz;
 }
 
 // One face term of RFLU_ComputeLimiterVenkat (modflu/RFLU_ModLimiters.F90:482-504).
@@ -250,7 +288,8 @@ __device__ __forceinline__ void venkat_term(R d2, R dmax, R dmin, R epsq, R &lim
   for (int t_ = blockIdx.x; t_ < (nTiles); t_ += gridDim.x)
 
 // Cons2Prim (modflu/RFLU_ModConvertCv.F90:221-231) of the uploaded state, and
-// optionally the EOS first (libflu/RFLU_SetDependentVars.F90:256-287).
+// optionally the EOS first (libflu/RFLU_SetDependentVars.F90:256-287).  The
+// record's centroid slots are kept.
 template <typename R>
 __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
                        int nTiles, int computeDv) {
@@ -273,20 +312,29 @@ __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__rest
       g.dv[N + c] = T;
       g.dv[2 * N + c] = sqrt(gg * gc * T);
     }
-    g.prim[c] = R(q0);
-    g.prim[N + c] = R(ir * q1);
-    g.prim[2 * N + c] = R(ir * q2);
-    g.prim[3 * N + c] = R(ir * q3);
-    g.prim[4 * N + c] = R(g.dv[c]);
+    R r[8];
+    ld8(g.rec + 8 * (size_t)c, r);
+    r[0] = R(q0);
+    r[1] = R(ir * q1);
+    r[2] = R(ir * q2);
+    r[3] = R(ir * q3);
+    r[4] = R(g.dv[c]);
+    st8(g.rec + 8 * (size_t)c, r);
   }
 }
 
-// WLSQ gradients of (rho,u,v,w,p), RFLU_ComputeGradCellsFast_3D
-// (modflu/RFLU_ModDifferentiationCells.F90:1021-1149), weights precomputed.
-// One thread per cell, members in stored order: the summation order of the
-// reference.
+// WLSQ gradients of (rho,u,v,w,p) (RFLU_ComputeGradCellsFast_3D,
+// modflu/RFLU_ModDifferentiationCells.F90:1021-1149) fused with the
+// Venkatakrishnan limiter and RFLU_LimitGradCells (modflu/RFLU_ModLimiters.F90:
+// 339-532, 707-760).  One thread per cell; stencil members in stored order
+// (the reference's summation order).  The limiter of a cell needs only its own
+// unlimited gradient and its face neighbours' values, and min/max and the MIN
+// over faces do not depend on the face order, so the per-cell gather equals
+// the reference's two face loops.  FP64 path: precomputed weights (bitwise the
+// reference's); mixed path: weights rebuilt in FP32 from the records'
+// centroids and the cell's WLSQ factor terms.
 template <typename R>
-__global__ void __launch_bounds__(128) k_gradient(const RegionDev<R> *__restrict__ regs,
+__global__ void __launch_bounds__(128) k_grad_lim(const RegionDev<R> *__restrict__ regs,
                                                   const Tile *__restrict__ tiles, int nTiles) {
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
@@ -294,87 +342,129 @@ __global__ void __launch_bounds__(128) k_gradient(const RegionDev<R> *__restrict
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     if (c >= N) continue;
-    const R *__restrict__ prim = g.prim;
-    R p0[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) p0[v] = prim[v * N + c];
+    const R *__restrict__ rec = g.rec;
+    R r0[8];
+    ld8(rec + 8 * (size_t)c, r0);
     R acc[15];
 #pragma unroll
     for (int k = 0; k < 15; ++k) acc[k] = R(0);
-    const long long T = g.stTotal;
     long long e = g.stOff[c >> 5] + (c & 31);
     const int n = g.stCnt[c];
-    for (int k = 0; k < n; ++k, e += kSlice) {
-      const int nb = g.stIdx[e];
-      const R wx = g.stW[e], wy = g.stW[T + e], wz = g.stW[2 * T + e];
+    // members are accumulated in stored order; the loads of U consecutive
+    // members are issued together so their gathers overlap
+    if (sizeof(R) == 8) {
+      const long long T = g.stTotal;
+      auto member = [&](const R rn[8], long long ee) {
+        const R wx = g.stW[ee], wy = g.stW[T + ee], wz = g.stW[2 * T + ee];
 #pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        R dVar = prim[v * N + nb] - p0[v];
-        acc[3 * v] = acc[3 * v] + wx * dVar;
-        acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
-        acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+        for (int v = 0; v < 5; ++v) {
+          R dVar = rn[v] - r0[v];
+          acc[3 * v] = acc[3 * v] + wx * dVar;
+          acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
+          acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+        }
+      };
+      int k = 0;
+      for (; k + 2 <= n; k += 2, e += 2 * kSlice) {
+        const int nb0 = g.stIdx[e], nb1 = g.stIdx[e + kSlice];
+        R ra[8], rb[8];
+        ld8(rec + 8 * (size_t)nb0, ra);
+        ld8(rec + 8 * (size_t)nb1, rb);
+        member(ra, e);
+        member(rb, e + kSlice);
+      }
+      for (; k < n; ++k, e += kSlice) {
+        R ra[8];
+        ld8(rec + 8 * (size_t)g.stIdx[e], ra);
+        member(ra, e);
+      }
+    } else {
+      const R c12 = g.cwt[c], c13 = g.cwt[N + c], c23 = g.cwt[2 * N + c];
+      const R c1111 = g.cwt[3 * N + c], c2222 = g.cwt[4 * N + c], c3333 = g.cwt[5 * N + c];
+      auto member = [&](const R rn[8]) {
+        R dx = rn[5] - r0[5], dy = rn[6] - r0[6], dz = rn[7] - r0[7];
+        R term = rsqrtf(float(dx * dx + dy * dy + dz * dz));
+        dx = term * dx;
+        dy = term * dy;
+        dz = term * dz;
+        R term1 = c1111 * dx;
+        R term2 = c2222 * (dy + c12 * dx);
+        R term3 = c3333 * (dz + c23 * dy + c13 * dx);
+        R wx = term * (term1 + c12 * term2 + c13 * term3);
+        R wy = term * (term2 + c23 * term3);
+        R wz = term * term3;
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          R dVar = rn[v] - r0[v];
+          acc[3 * v] = acc[3 * v] + wx * dVar;
+          acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
+          acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+        }
+      };
+      int k = 0;
+      for (; k + 4 <= n; k += 4, e += 4 * kSlice) {
+        const int nb0 = g.stIdx[e], nb1 = g.stIdx[e + kSlice], nb2 = g.stIdx[e + 2 * kSlice],
+                  nb3 = g.stIdx[e + 3 * kSlice];
+        R ra[8], rb[8], rc[8], rd[8];
+        ld8(rec + 8 * (size_t)nb0, ra);
+        ld8(rec + 8 * (size_t)nb1, rb);
+        ld8(rec + 8 * (size_t)nb2, rc);
+        ld8(rec + 8 * (size_t)nb3, rd);
+        member(ra);
+        member(rb);
+        member(rc);
+        member(rd);
+      }
+      for (; k < n; ++k, e += kSlice) {
+        R ra[8];
+        ld8(rec + 8 * (size_t)g.stIdx[e], ra);
+        member(ra);
       }
     }
-#pragma unroll
-    for (int k = 0; k < 15; ++k) g.grad[k * N + c] = acc[k];
-  }
-}
-
-// Venkatakrishnan limiter + RFLU_LimitGradCells (modflu/RFLU_ModLimiters.F90:
-// 339-532, 707-760) as a per-cell gather over the cell's interior faces:
-// min/max and the MIN over faces do not depend on the face order, so this
-// equals the reference's two face loops.  In place on grad.
-template <typename R>
-__global__ void __launch_bounds__(128) k_limiter(const RegionDev<R> *__restrict__ regs,
-                                                 const Tile *__restrict__ tiles, int nTiles) {
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    const int c = tl.first + threadIdx.x;
-    const int N = g.nCells;
-    if (c >= N || g.ph.reconst != 11) continue;
-    const R *__restrict__ prim = g.prim;
-    R p0[5], vmin[5], vmax[5], lim[5];
-#pragma unroll
-    for (int v = 0; v < 5; ++v) {
-      p0[v] = prim[v * N + c];
-      vmin[v] = p0[v];
-      vmax[v] = p0[v];
-      lim[v] = R(1);
-    }
-    const long long T = g.cfTotal;
-    const long long e0 = g.cfOff[c >> 5] + (c & 31);
-    const int n = g.cfCnt[c];
-    for (int k = 0; k < n; ++k) {
-      const long long e = e0 + (long long)k * kSlice;
-      if (g.cfCode[e] < 0) continue;
-      const int nb = g.cfNb[e];
+    if (g.ph.reconst == 11) {
+      R vmin[5], vmax[5], lim[5];
 #pragma unroll
       for (int v = 0; v < 5; ++v) {
-        R x = prim[v * N + nb];
-        vmin[v] = rmin(vmin[v], x);
-        vmax[v] = rmax(vmax[v], x);
+        vmin[v] = r0[v];
+        vmax[v] = r0[v];
+        lim[v] = R(1);
       }
-    }
-    R G[15];
+      const long long T = g.cfTotal;
+      const long long e0 = g.cfOff[c >> 5] + (c & 31);
+      const int nf = g.cfCnt[c];
+      for (int k = 0; k < nf; ++k) {
+        const long long ee = e0 + (long long)k * kSlice;
+        if (g.cfCode[ee] < 0) continue;
+        R rn[8];
+        ld8(rec + 8 * (size_t)g.cfNb[ee], rn);
 #pragma unroll
-    for (int k = 0; k < 15; ++k) G[k] = g.grad[k * N + c];
-    const R epsq = g.epsq[c];
-    const int guard = g.ph.venkatGuard;
-    for (int k = 0; k < n; ++k) {
-      const long long e = e0 + (long long)k * kSlice;
-      if (g.cfCode[e] < 0) continue;
-      const R dx = g.cfD[e], dy = g.cfD[T + e], dz = g.cfD[2 * T + e];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        R d2 = G[3 * v] * dx + G[3 * v + 1] * dy + G[3 * v + 2] * dz;
-        venkat_term(d2, vmax[v] - p0[v], vmin[v] - p0[v], epsq, lim[v], guard);
+        for (int v = 0; v < 5; ++v) {
+          vmin[v] = rmin(vmin[v], rn[v]);
+          vmax[v] = rmax(vmax[v], rn[v]);
+        }
       }
+      const R epsq = g.epsq[c];
+      const int guard = g.ph.venkatGuard;
+      for (int k = 0; k < nf; ++k) {
+        const long long ee = e0 + (long long)k * kSlice;
+        if (g.cfCode[ee] < 0) continue;
+        const R dx = g.cfD[ee], dy = g.cfD[T + ee], dz = g.cfD[2 * T + ee];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          R d2 = acc[3 * v] * dx + acc[3 * v + 1] * dy + acc[3 * v + 2] * dz;
+          venkat_term(d2, vmax[v] - r0[v], vmin[v] - r0[v], epsq, lim[v], guard);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < 5; ++v)
+#pragma unroll
+        for (int d = 0; d < 3; ++d) acc[3 * v + d] = lim[v] * acc[3 * v + d];
     }
+    R out[16];
 #pragma unroll
-    for (int v = 0; v < 5; ++v)
-#pragma unroll
-      for (int d = 0; d < 3; ++d) g.grad[(3 * v + d) * N + c] = lim[v] * G[3 * v + d];
+    for (int k = 0; k < 15; ++k) out[k] = acc[k];
+    out[15] = R(0);
+    st16(g.grad + 16 * (size_t)c, out);
   }
 }
 
@@ -390,24 +480,31 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
     const int F = g.nFaces;
     if (f >= F) continue;
     const int c1 = g.f2c[f], c2 = g.f2c[F + f];
-    const R nx = g.fn[f], ny = g.fn[F + f], nz = g.fn[2 * F + f], nm = g.fn[3 * F + f];
+    R nrm[4];
+    ld4(g.fnA + 4 * (size_t)f, nrm);
+    R r1[8], r2[8];
+    ld8(g.rec + 8 * (size_t)c1, r1);
+    ld8(g.rec + 8 * (size_t)c2, r2);
     R L[5], Rt[5], irl, irr;
-    cell_values(g, c1, L, irl);
-    cell_values(g, c2, Rt, irr);
+    cell_values(g, c1, r1, L, irl);
+    cell_values(g, c2, r2, Rt, irr);
     if (g.ph.spaceOrder > 1) {
-      reconstruct(g, c1, g.fdl[f], g.fdl[F + f], g.fdl[2 * F + f], L);
-      reconstruct(g, c2, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
+      R G[16];
+      ld16(g.grad + 16 * (size_t)c1, G);
+      reconstruct(G, g.fdl[f], g.fdl[F + f], g.fdl[2 * F + f], L);
+      ld16(g.grad + 16 * (size_t)c2, G);
+      reconstruct(G, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
     }
-    R flx[5];
+    R flx[8];
     const int sd = g.ph.spaceDiscr;
     if (sd == 4)
-      ausm_flux(g.ph, L, Rt, nx, ny, nz, nm, flx);
+      ausm_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
     else if (sd == 1)
-      roe_flux(g.ph, L, Rt, nx, ny, nz, nm, flx);
+      roe_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
     else
-      hllc_flux(g.ph, L, Rt, irl, irr, nx, ny, nz, nm, flx);
-#pragma unroll
-    for (int k = 0; k < 5; ++k) g.flux[k * F + f] = flx[k];
+      hllc_flux(g.ph, L, Rt, irl, irr, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+    flx[5] = flx[6] = flx[7] = R(0);
+    st8(g.flux + 8 * (size_t)f, flx);
   }
 }
 
@@ -463,12 +560,20 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
     const int c = g.bf2c[b];
     const int kind = g.bkind[b];
     const int type = kind & 15, order = (kind >> 4) & 15, opt = kind >> 8;
-    const R nx = g.bfn[b], ny = g.bfn[B + b], nz = g.bfn[2 * B + b], nm = g.bfn[3 * B + b];
+    R nrm[4];
+    ld4(g.bfnA + 4 * (size_t)b, nrm);
+    const R nx = nrm[0], ny = nrm[1], nz = nrm[2], nm = nrm[3];
     const R fs = R(0);
-    R flx[5];
+    R flx[8];
+    R rc[8];
+    ld8(g.rec + 8 * (size_t)c, rc);
     R S[5], ir;
-    cell_values(g, c, S, ir);
-    if (order == 2) reconstruct(g, c, g.bfd[b], g.bfd[B + b], g.bfd[2 * B + b], S);
+    cell_values(g, c, rc, S, ir);
+    if (order == 2) {
+      R G[16];
+      ld16(g.grad + 16 * (size_t)c, G);
+      reconstruct(G, g.bfd[b], g.bfd[B + b], g.bfd[2 * B + b], S);
+    }
     if (type == BK_SLIP) {
       R pl = S[4];
       flx[0] = R(-0.0);
@@ -487,15 +592,15 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
         rwl = rl * S[3];
         rel = rl * eo_dgpuvw(rl, gvG, pl, S[1], S[2], S[3]);
       } else {
-        rl = g.prim[c];
-        pl = g.prim[4 * N + c];
+        rl = rc[0];
+        pl = rc[4];
         if (sizeof(R) == 8 && g.ph.spaceOrder == 1) {  // no conversion round trip
           rul = R(g.cv[N + c]);
           rvl = R(g.cv[2 * N + c]);
           rwl = R(g.cv[3 * N + c]);
           rel = R(g.cv[4 * N + c]);
         } else {  // cv as CellGradientsMP's Prim2Cons left it
-          R u = g.prim[N + c], v = g.prim[2 * N + c], w = g.prim[3 * N + c];
+          R u = rc[1], v = rc[2], w = rc[3];
           rul = rl * u;
           rvl = rl * v;
           rwl = rl * w;
@@ -513,8 +618,8 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       flx[3] = R(0.5) * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
       flx[4] = R(0.5) * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
     }
-#pragma unroll
-    for (int k = 0; k < 5; ++k) g.bflux[k * B + b] = flx[k];
+    flx[5] = flx[6] = flx[7] = R(0);
+    st8(g.bflux + 8 * (size_t)b, flx);
   }
 }
 
@@ -558,6 +663,138 @@ __device__ __forceinline__ unsigned after_update(double gc, double gg, double q[
   return st;
 }
 
+// Error-free transformation of a + b (Knuth's TwoSum); lo collects the
+// rounding errors, so hi + lo carries about twice the FP32 significand.
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
+  float s = hi + x;
+  float bb = s - hi;
+  float err = (hi - (s - bb)) + (x - bb);
+  hi = s;
+  lo += err;
+}
+
+// Mixed-path gather + update.  The FP32 face fluxes are summed with
+// compensated (TwoSum) accumulation, so the residual is the FP32-rounded exact
+// sum of the fluxes regardless of cancellation; the RK increment
+// dU = a*dt/V (rhs - g rhsSum) is formed in FP32 and applied to the FP64
+// conserved state, and the pressure is recovered in FP64 from
+// E - |m|^2/(2 rho), where cancellation at strong shocks needs it (1/rho: FP32
+// reciprocal refined by one FP64 Newton step).  Cells whose density or
+// pressure is not clearly positive take the exact FP64 checks of
+// AfterUpdateMP.  T and a of dv are completed on download.
+__device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, int c,
+                                                    const StepArgs &a) {
+  const int N = g.nCells;
+  float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const long long e0 = g.cfOff[c >> 5] + (c & 31);
+  const int n = g.cfCnt[c];
+  for (int k = 0; k < n; ++k) {
+    const int code = g.cfCode[e0 + (long long)k * kSlice];
+    float fl[8];
+    if (code >= 0) {
+      ld8(g.flux + 8 * (size_t)(code >> 1), fl);
+      const float sg = (code & 1) ? -1.f : 1.f;
+#pragma unroll
+      for (int j = 0; j < 5; ++j) two_sum_acc(hi[j], lo[j], sg * fl[j]);
+    } else {
+      ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) two_sum_acc(hi[j], lo[j], fl[j]);
+    }
+  }
+  if (a.writeRhs) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = double(hi[j]) + double(lo[j]);
+  }
+  if (!a.update) return;
+  float rhs[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) rhs[j] = hi[j] + lo[j];
+  const Phys &ph = g.ph;
+  const double dtMin = a.useDeviceDt ? g.scal[0] : a.dtHost;
+  const int is = a.istage;
+  const float adtv = float(ph.ark[is - 1] * dtMin) / float(g.vol[c]);
+  const float grk = float(ph.grk[is - 1]);
+  double q[5], old[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
+  if (ph.rkScheme == 1) {
+    if (is == 1) {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) {
+        old[j] = q[j];
+        g.cvOld[j * N + c] = q[j];
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < 5; ++j) old[j] = g.cvOld[j * N + c];
+    }
+  } else {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) old[j] = q[j];
+  }
+  float *rs = g.rhsSumF;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    float dU;
+    if (ph.rkScheme == 2) {
+      if (is == 1) {
+        dU = adtv * rhs[j];
+        rs[j * N + c] = rhs[j];
+      } else if (is == 2) {
+        dU = adtv * (rhs[j] - grk * rs[j * N + c]);
+        rs[j * N + c] = rhs[j];
+      } else {
+        dU = adtv * (rhs[j] - grk * rs[j * N + c]);
+      }
+    } else if (ph.rkScheme == 1) {
+      if (is == 1) {
+        dU = adtv * rhs[j];
+        rs[j * N + c] = rhs[j];
+      } else if (is == ph.nSteps) {
+        dU = adtv * (rhs[j] + rs[j * N + c]);
+      } else {
+        dU = adtv * rhs[j];
+        rs[j * N + c] = rs[j * N + c] + grk * rhs[j];
+      }
+    } else {
+      dU = adtv * rhs[j];
+    }
+    q[j] = old[j] - double(dU);
+  }
+  const double gg = ph.gvG;
+  const double rho = q[0];
+  const float rf = float(rho);
+  const float irf = 1.0f / rf;
+  double ir = double(irf);
+  ir = fma(ir, fma(-rho, ir, 1.0), ir);
+  const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
+  double p = (gg - 1.0) * (q[4] - 0.5 * m2 * ir);
+  float pf = float(p);
+  const float uf = float(q[1]) * irf, vf = float(q[2]) * irf, wf = float(q[3]) * irf;
+  if (!(rf > 0.f) || !(pf > 1.0e-12f) || isnan(uf) || isnan(vf) || isnan(wf)) {
+    double d[3];
+    d[0] = p;
+    d[1] = p / (rho * ph.gvR);
+    d[2] = 0.0;
+    unsigned st = after_update(ph.gvR, gg, q, d);
+    if (st) atomicOr(g.status, st);
+    p = d[0];
+    pf = float(p);
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) g.cv[j * N + c] = q[j];
+  g.dv[c] = p;
+  float r[8];
+  ld8(g.rec + 8 * (size_t)c, r);
+  r[0] = rf;
+  r[1] = uf;
+  r[2] = vf;
+  r[3] = wf;
+  r[4] = pf;
+  st8(g.rec + 8 * (size_t)c, r);
+}
+
 // Face->cell residual gather in the reference accumulation order, then the
 // RK update (libfloflu/RkUpdateGeneric.F90:229-314), EOS
 // (libflu/RFLU_SetDependentVars.F90:256-287), AfterUpdate checks and
@@ -573,25 +810,29 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     if (c >= N) continue;
-    const int F = g.nFaces, B = g.nBFaces;
+    if constexpr (sizeof(R) == 4) {
+      gather_update_mixed(g, c, a);
+      continue;
+    }
     double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
     const long long e0 = g.cfOff[c >> 5] + (c & 31);
     const int n = g.cfCnt[c];
     for (int k = 0; k < n; ++k) {
       const int code = g.cfCode[e0 + (long long)k * kSlice];
+      R fl[8];
       if (code >= 0) {
-        const int f = code >> 1;
+        ld8(g.flux + 8 * (size_t)(code >> 1), fl);
         if (code & 1) {
 #pragma unroll
-          for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(g.flux[j * F + f]);
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(fl[j]);
         } else {
 #pragma unroll
-          for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(g.flux[j * F + f]);
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
         }
       } else {
-        const int b = -code - 1;
+        ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
 #pragma unroll
-        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(g.bflux[j * B + b]);
+        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
       }
     }
     if (a.writeRhs) {
@@ -669,62 +910,41 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
     g.dv[N + c] = d[1];
     g.dv[2 * N + c] = d[2];
     const double ir = 1.0 / q[0];
-    g.prim[c] = R(q[0]);
-    g.prim[N + c] = R(ir * q[1]);
-    g.prim[2 * N + c] = R(ir * q[2]);
-    g.prim[3 * N + c] = R(ir * q[3]);
-    g.prim[4 * N + c] = R(d[0]);
+    R r[8];
+    ld8(g.rec + 8 * (size_t)c, r);
+    r[0] = R(q[0]);
+    r[1] = R(ir * q[1]);
+    r[2] = R(ir * q[2]);
+    r[3] = R(ir * q[3]);
+    r[4] = R(d[0]);
+    st8(g.rec + 8 * (size_t)c, r);
+  }
+}
+
+// T and a of dv from cv and p (mixed path: a stage writes only p of dv).
+template <typename R>
+__global__ void k_dv_complete(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+                              int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N) continue;
+    const double gc = g.ph.gvR, gg = g.ph.gvG;
+    double T = g.dv[c] / (g.cv[c] * gc);
+    g.dv[N + c] = T;
+    g.dv[2 * N + c] = sqrt(gg * gc * T);
   }
 }
 
 // ---- time step: RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:165-327)
-
-template <typename R>
-__global__ void __launch_bounds__(128) k_dt_face(const RegionDev<R> *__restrict__ regs,
-                                                 const Tile *__restrict__ tiles, int nTiles) {
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    const int f = tl.first + threadIdx.x;
-    const int F = g.nFaces, N = g.nCells;
-    if (f >= F) continue;
-    const int c1 = g.f2c[f], c2 = g.f2c[F + f];
-    const double *cv = g.cv;
-    double ir1 = 1.0 / cv[c1], ir2 = 1.0 / cv[c2];
-    double u1 = cv[N + c1] * ir1, v1 = cv[2 * N + c1] * ir1, w1 = cv[3 * N + c1] * ir1;
-    double a1 = g.dv[2 * N + c1];
-    double u2 = cv[N + c2] * ir2, v2 = cv[2 * N + c2] * ir2, w2 = cv[3 * N + c2] * ir2;
-    double a2 = g.dv[2 * N + c2];
-    double nx = g.fn64[f], ny = g.fn64[F + f], nz = g.fn64[2 * F + f], nm = g.fn64[3 * F + f];
-    double vc = 0.5 * ((u1 + u2) * nx + (v1 + v2) * ny + (w1 + w2) * nz);
-    double as = 0.5 * (a1 + a2);
-    g.srad[f] = (fabs(vc - 0.0) + as) * nm;
-  }
-}
-
-template <typename R>
-__global__ void __launch_bounds__(128) k_dt_bface(const RegionDev<R> *__restrict__ regs,
-                                                  const Tile *__restrict__ tiles, int nTiles) {
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    const int b = tl.first + threadIdx.x;
-    const int B = g.nBFaces, N = g.nCells;
-    if (b >= B) continue;
-    const int c = g.bf2c[b];
-    const double *cv = g.cv;
-    double ir1 = 1.0 / cv[c];
-    double u1 = cv[N + c] * ir1, v1 = cv[2 * N + c] * ir1, w1 = cv[3 * N + c] * ir1;
-    double a1 = g.dv[2 * N + c];
-    double nx = g.bfn64[b], ny = g.bfn64[B + b], nz = g.bfn64[2 * B + b], nm = g.bfn64[3 * B + b];
-    double vc = u1 * nx + v1 * ny + w1 * nz;
-    g.sradb[b] = (fabs(vc - 0.0) + a1) * nm;
-  }
-}
-
-// dt(c) = vol / sum over the cell's faces in the reference order; block
-// minimum, then an atomic minimum on the bit pattern (dt > 0, so the IEEE
-// order equals the unsigned integer order).
+// as a per-cell gather: dt(c) = vol / sum over the cell's faces, in the
+// reference order, of (|v_n| + a) * area with face-averaged velocity and
+// sound speed (interior) or the cell's own (boundary).  u = rhou*(1/rho) is
+// the record's velocity; a is dv(SOUN) on the FP64 path and sqrt(g p/rho) in
+// FP32 on the mixed path.  Block minimum, then an atomic minimum on the bit
+// pattern (dt > 0: the IEEE order equals the unsigned integer order).
 template <typename R>
 __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict__ regs,
                                                  const Tile *__restrict__ tiles, int nTiles) {
@@ -736,14 +956,39 @@ __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict_
     const int N = g.nCells;
     unsigned long long bits = 0x7FF0000000000000ull;  // +inf
     if (c < N) {
-      double acc = 0.0;
+      const R gg = R(g.ph.gvG);
+      R r0[8];
+      ld8(g.rec + 8 * (size_t)c, r0);
+      const R a0 = sizeof(R) == 8 ? R(g.dv[2 * N + c]) : R(sqrtf(float(gg * r0[4] / r0[0])));
+      R acc = R(0);
       const long long e0 = g.cfOff[c >> 5] + (c & 31);
       const int n = g.cfCnt[c];
       for (int k = 0; k < n; ++k) {
-        const int code = g.cfCode[e0 + (long long)k * kSlice];
-        acc = acc + (code >= 0 ? g.srad[code >> 1] : g.sradb[-code - 1]);
+        const long long e = e0 + (long long)k * kSlice;
+        const int code = g.cfCode[e];
+        R nrm[4];
+        if (code >= 0) {
+          const int nb = g.cfNb[e];
+          ld4(g.fnA + 4 * (size_t)(code >> 1), nrm);
+          R rn[8];
+          ld8(g.rec + 8 * (size_t)nb, rn);
+          const R an = sizeof(R) == 8 ? R(g.dv[2 * N + nb]) : R(sqrtf(float(gg * rn[4] / rn[0])));
+          // the face's c1 values first, as in the reference
+          const bool first = (code & 1) == 0;
+          const R u1 = first ? r0[1] : rn[1], u2 = first ? rn[1] : r0[1];
+          const R v1 = first ? r0[2] : rn[2], v2 = first ? rn[2] : r0[2];
+          const R w1 = first ? r0[3] : rn[3], w2 = first ? rn[3] : r0[3];
+          const R a1 = first ? a0 : an, a2 = first ? an : a0;
+          R vc = R(0.5) * ((u1 + u2) * nrm[0] + (v1 + v2) * nrm[1] + (w1 + w2) * nrm[2]);
+          R as = R(0.5) * (a1 + a2);
+          acc = acc + (fabs(vc - R(0)) + as) * nrm[3];
+        } else {
+          ld4(g.bfnA + 4 * (size_t)(-code - 1), nrm);
+          R vc = r0[1] * nrm[0] + r0[2] * nrm[1] + r0[3] * nrm[2];
+          acc = acc + (fabs(vc - R(0)) + a0) * nrm[3];
+        }
       }
-      double dtc = g.vol[c] / acc;
+      double dtc = sizeof(R) == 8 ? double(R(g.vol[c]) / acc) : double(float(g.vol[c]) / float(acc));
       bits = (unsigned long long)__double_as_longlong(dtc);
     }
     for (int o = 16; o > 0; o >>= 1) {
@@ -810,18 +1055,13 @@ template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof) {
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
+  (void)reconst;
   long long n = 0;
   if (spaceOrder > 1 && w.nCellTiles > 0) {
     RF_MARK(KP_GRADIENT, 0);
-    k_gradient<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    k_grad_lim<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
     RF_MARK(KP_GRADIENT, 1);
     ++n;
-    if (reconst == 11) {
-      RF_MARK(KP_LIMITER, 0);
-      k_limiter<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
-      RF_MARK(KP_LIMITER, 1);
-      ++n;
-    }
   }
   if (w.nFaceTiles > 0) {
     RF_MARK(KP_FACE_FLUX, 0);
@@ -849,18 +1089,6 @@ void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStr
                long long *launches, const Prof *prof) {
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   long long n = 0;
-  if (w.nFaceTiles > 0) {
-    RF_MARK(KP_DT_FACE, 0);
-    k_dt_face<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
-    RF_MARK(KP_DT_FACE, 1);
-    ++n;
-  }
-  if (w.nBFaceTiles > 0) {
-    RF_MARK(KP_DT_BFACE, 0);
-    k_dt_bface<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
-    RF_MARK(KP_DT_BFACE, 1);
-    ++n;
-  }
   if (w.nCellTiles > 0) {
     RF_MARK(KP_DT_CELL, 0);
     k_dt_cell<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
@@ -874,8 +1102,15 @@ void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStr
   if (launches) *launches += n;
 }
 
+template <typename R>
+void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+  int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
+  if (grid > 0) k_dv_complete<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+}
+
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
+  template void launch_dv_complete<R>(const RegionDev<R> *, const Work &, cudaStream_t);      \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
                                 cudaStream_t, long long *, int, int, const Prof *);           \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \

@@ -1,0 +1,107 @@
+"""C-ABI libraries: they load, export every entry point the headers declare,
+and the host-side validation answers without touching the GPU."""
+import ctypes as C
+import os
+import re
+
+import numpy as np
+import pytest
+
+from rocflupicl_gb300 import case as K
+from rocflupicl_gb300 import engine as E
+from rocflupicl_gb300 import mesh as M
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared(header):
+    txt = open(os.path.join(ROOT, "include", header)).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(rf(?:gpu|mesh)_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_engine_exports_every_declared_symbol():
+    lib = E.load()
+    names = declared("rfgpu.h")
+    assert len(names) >= 30
+    for n in names:
+        assert hasattr(lib, n), n
+    assert set(names) == set(E.SYMBOLS)
+
+
+def test_mesh_exports_every_declared_symbol():
+    lib = M._load()
+    for n in declared("rfmesh.h"):
+        assert hasattr(lib, n), n
+
+
+def _desc(c, **over):
+    """Descriptor through the same path Region uses, without creating it."""
+    lib = E.load()
+    m = c.mesh
+    keep = []
+
+    def k(a, dt):
+        a = np.ascontiguousarray(a, dtype=dt)
+        keep.append(a)
+        return a
+
+    d = E.RegionDescT()
+    d.nCells, d.nFaces, d.f2cLd = m.nCells, m.nFaces, 2
+    d.f2c = E._ip(k(m.f2c, np.int32))
+    d.fn, d.fc = E._dp(k(m.fn, np.float64)), E._dp(k(m.fc, np.float64))
+    d.cofg, d.vol = E._dp(k(m.cofg, np.float64)), E._dp(k(m.vol, np.float64))
+    d.c2csOffsets = E._ip(k(m.c2cs_off, np.int32))
+    d.c2csMembers = E._ip(k(m.c2cs_mem, np.int32))
+    d.xyzMoms = E._dp(k(m.xyzmoms, np.float64))
+    d.nPatches = 0
+    d.cv = E._dp(k(c.cv, np.float64))
+    d.dv = E._dp(k(c.dv, np.float64))
+    d.gasModel, d.flowModel = 1, 0
+    d.spaceDiscr, d.spaceOrder, d.reconst, d.rkScheme = 4, 2, 11, 2
+    d.refCp, d.refGamma = 1004.5, 1.4
+    d.gvCp, d.gvMol = c.numerics.gv
+    d.epsentr, d.dissFact, d.precision = 0.05, 1.0, 0
+    for key, val in over.items():
+        setattr(d, key, val)
+    return lib, d, keep
+
+
+@pytest.mark.parametrize("field,value", [("spaceDiscr", 5), ("spaceOrder", 3), ("reconst", 1),
+                                         ("rkScheme", 7), ("gasModel", 2), ("flowModel", 1),
+                                         ("precision", 9)])
+def test_unsupported_options_refused_before_any_cuda_call(field, value):
+    c = K.shock_tube(6)
+    lib, d, keep = _desc(c, **{field: value})
+    h = C.c_void_p()
+    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_UNSUPPORTED
+    assert not h.value
+
+
+def test_bad_indices_refused():
+    c = K.shock_tube(6)
+    bad = c.mesh.f2c.copy()
+    bad[3, 1] = c.mesh.nCells + 1
+    lib, d, keep = _desc(c)
+    keep.append(bad)
+    d.f2c = E._ip(bad)
+    h = C.c_void_p()
+    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_ARG
+    lib2, d2, keep2 = _desc(c, nCells=0)
+    assert lib2.rfgpu_region_create(C.byref(d2), C.byref(h)) == E.ERR_ARG
+    assert lib.rfgpu_region_create(None, C.byref(h)) == E.ERR_ARG
+
+
+def test_null_handles_are_errors():
+    lib = E.load()
+    assert lib.rfgpu_stage(None, 1, 1.0) == E.ERR_ARG
+    assert lib.rfgpu_sync(None) == E.ERR_ARG
+    assert lib.rfgpu_region_destroy(None) == E.ERR_ARG
+    assert lib.rfgpu_launch_count(None) == -1
+
+
+def test_perfmodel_matches_pass_totals():
+    from rocflupicl_gb300 import perfmodel as P
+    nc, nf, nb, m = 1000, 2000, 100, 40000
+    assert P.stage_bytes(nc, nf, nb, m, 8) == 964 * nc + 4 * m + 112 * nf + 64 * nb
+    assert P.stage_bytes(nc, nf, nb, m, 4) == 664 * nc + 4 * m + 112 * nf + 64 * nb
