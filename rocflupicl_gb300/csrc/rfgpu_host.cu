@@ -126,6 +126,7 @@ struct rfgpu_region_s {
   long long perStep = 0;
   ProfState prof;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  int maxStW = 0;
 };
 
 struct rfgpu_batch_s {
@@ -206,6 +207,10 @@ int check_desc(const rfgpu_region_desc_t *d) {
     if (d->c2csOffsets[c + 1] < d->c2csOffsets[c]) return RFGPU_ERR_ARG;
   for (long long e = 0; e < d->c2csOffsets[N]; ++e)
     if (d->c2csMembers[e] < 1 || d->c2csMembers[e] > N) return RFGPU_ERR_ARG;
+  // stencils are at most 10x the minimum size (RFLU_ModStencilsCells.F90:2865-2873)
+  // in the reference; the engine stages up to 400 members per cell on chip
+  for (long long c = 0; c < N; ++c)
+    if (d->c2csOffsets[c + 1] - d->c2csOffsets[c] > 400) return RFGPU_ERR_UNSUPPORTED;
   for (int ip = 0; ip < d->nPatches; ++ip)
     for (int b = 0; b < d->patches[ip].nBFaces; ++b)
       if (d->patches[ip].bf2c[b] < 1 || d->patches[ip].bf2c[b] > N) return RFGPU_ERR_ARG;
@@ -245,6 +250,11 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     for (int k = 0; k < 6; ++k) moms[(size_t)k * N + c] = d->xyzMoms[10 * (size_t)c + k];
   }
   g.vol = M.upload(vol, s);
+  {
+    std::vector<float> iv(N);
+    for (int c = 0; c < N; ++c) iv[c] = (float)(1.0 / vol[c]);
+    g.ivolF = M.upload(iv, s);
+  }
   g.epsq = M.upload(cast<R>(epsq), s);
   // WLSQ factor terms for the mixed path's on-the-fly weights
   // (RFLU_ModDifferentiationCells.F90:1029-1042)
@@ -278,6 +288,8 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.stCnt = M.upload(sl.cnt, s);
     g.stIdx = M.upload(idx, s);
     g.stTotal = sl.total;
+    for (size_t q = 0; q + 1 < sl.off.size(); ++q)
+      h->maxStW = std::max(h->maxStW, (int)((sl.off[q + 1] - sl.off[q]) / kSlice));
     if (sizeof(R) == 8) {
       // weights on the device with the reference arithmetic (FP64 unit)
       double *dcofg = M.alloc<double>(cofg.size());
@@ -394,8 +406,8 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.dtBits = M.alloc<unsigned long long>(1);
   unsigned long long inf = 0x7FF0000000000000ull;
   cudaMemcpyAsync(g.dtBits, &inf, 8, cudaMemcpyHostToDevice, s);
-  g.scal = M.alloc<double>(4);
-  cudaMemsetAsync(g.scal, 0, 4 * sizeof(double), s);
+  g.scal = M.alloc<double>(8);
+  cudaMemsetAsync(g.scal, 0, 8 * sizeof(double), s);
   g.status = M.alloc<unsigned>(1);
   cudaMemsetAsync(g.status, 0, sizeof(unsigned), s);
   h->nBFaces = B;
@@ -451,11 +463,12 @@ void dt_launch(rfgpu_region_s *h, const DtArgs &a) {
 void step_launch(rfgpu_region_s *h, double cfl, double dtImposed, double dtMinLimit,
                  double endTime) {
   DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
-  dt_launch(h, da);
-  for (int is = 1; is <= h->nSteps; ++is) {
-    StepArgs sa{is, 1, 0.0, 0, 1};
-    stage_launch(h, sa);
-  }
+  if (h->prec)
+    launch_step<float>(regs_of<float>(h), h->work, da, h->nSteps, h->stream, &h->launches,
+                       h->spaceOrder, h->reconst, h->prof.hookp());
+  else
+    launch_step<double>(regs_of<double>(h), h->work, da, h->nSteps, h->stream, &h->launches,
+                        h->spaceOrder, h->reconst, h->prof.hookp());
 }
 
 }  // namespace
@@ -509,7 +522,10 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
     h->faceTiles = h->mem.upload(ft, h->stream);
     h->bfaceTiles = h->mem.upload(bt, h->stream);
     h->work = Work{h->cellTiles, h->faceTiles, h->bfaceTiles, (int)ct.size(), (int)ft.size(),
-                   (int)bt.size(), 0, block, 1};
+                   (int)bt.size(), 0, block, 1, h->maxStW};
+    if ((h->prec ? configure_grad_smem<float>(h->maxStW, block)
+                 : configure_grad_smem<double>(h->maxStW, block)) != 0)
+      throw std::bad_alloc();
     h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
     cudaStreamSynchronize(h->stream);
   } catch (const std::bad_alloc &) {
@@ -545,7 +561,7 @@ int rfgpu_region_destroy(rfgpu_region_t h) {
 
 int rfgpu_stage(rfgpu_region_t h, int istage, double dtMin) {
   if (!h || istage < 1 || istage > h->nSteps) return RFGPU_ERR_ARG;
-  StepArgs a{istage, 0, dtMin, 0, 1};
+  StepArgs a{istage, 0, dtMin, 0, 1, 0, DtArgs{}};
   stage_launch(h, a);
   return cuda_rc(cudaGetLastError());
 }
@@ -600,7 +616,7 @@ int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed
 
 int rfgpu_residual(rfgpu_region_t h, double *rhs) {
   if (!h) return RFGPU_ERR_ARG;
-  StepArgs a{1, 0, 0.0, 1, 0};
+  StepArgs a{1, 0, 0.0, 1, 0, 0, DtArgs{}};
   stage_launch(h, a);
   if (!rhs) return cuda_rc(cudaGetLastError());
   const int N = h->nCells;
@@ -751,7 +767,10 @@ int rfgpu_batch_create(rfgpu_region_t *regions, int n, rfgpu_batch_t *out) {
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n};
+    int maxW = 0;
+    for (int i = 0; i < n; ++i) maxW = std::max(maxW, regions[i]->maxStW);
+    b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n,
+                   maxW};
     if (prec) {
       std::vector<RegionDev<float>> v;
       for (int i = 0; i < n; ++i) v.push_back(regions[i]->rd32);
@@ -789,20 +808,11 @@ static void batch_step_launch(rfgpu_batch_t b, double cfl, double dtImposed, dou
                               double endTime) {
   DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
   if (b->prec)
-    launch_dt<float>((const RegionDev<float> *)b->regsDev, b->work, da, b->stream, &b->launches,
-                     b->prof.hookp());
+    launch_step<float>((const RegionDev<float> *)b->regsDev, b->work, da, b->nSteps, b->stream,
+                       &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
   else
-    launch_dt<double>((const RegionDev<double> *)b->regsDev, b->work, da, b->stream, &b->launches,
-                      b->prof.hookp());
-  for (int is = 1; is <= b->nSteps; ++is) {
-    StepArgs sa{is, 1, 0.0, 0, 1};
-    if (b->prec)
-      launch_stage<float>((const RegionDev<float> *)b->regsDev, b->work, sa, b->stream,
-                          &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
-    else
-      launch_stage<double>((const RegionDev<double> *)b->regsDev, b->work, sa, b->stream,
-                           &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
-  }
+    launch_step<double>((const RegionDev<double> *)b->regsDev, b->work, da, b->nSteps, b->stream,
+                        &b->launches, b->spaceOrder, b->reconst, b->prof.hookp());
 }
 
 int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMinLimit,

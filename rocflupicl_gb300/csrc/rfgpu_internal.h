@@ -55,6 +55,7 @@ struct RegionDev {
   R *rec, *grad;
   // geometry
   const double *vol;
+  const float *ivolF;  // 1/vol in FP32 (mixed-path update)
   const R *epsq;
   const R *cwt;   // [6][N] c12,c13,c23,c11^2,c22^2,c33^2 of the WLSQ factor (mixed path)
   // stencil (SELL-32)
@@ -81,7 +82,8 @@ struct RegionDev {
   R *bflux;            // [B][8]
   // time step
   unsigned long long *dtBits;
-  double *scal;   // [0] dtMin, [1] current time, [2] dtMin of the previous step
+  double *scal;   // [0] dtMin, [1] current time, [2] dtMin of the previous step,
+                  // [3..7] ark(1..5)*dtMin of the current step
   unsigned *status;
   Phys ph;
 };
@@ -98,6 +100,13 @@ struct Work {
   int grid;     // blocks per launch (persistent when smaller than the tile count)
   int block;    // items per tile == threads per block
   int nRegions;
+  int maxStW;   // widest stencil SELL slice over the regions (shared-memory staging)
+};
+
+struct DtArgs {
+  double cfl, dtImposed, dtMinLimit, endTime;
+  int useDeviceTime;  // 1: current time from scal[1] and advance it
+  double timeHost;
 };
 
 // step parameters (host-side values; dt may alternatively come from the device)
@@ -107,13 +116,10 @@ struct StepArgs {
   double dtHost;
   int writeRhs;      // 1: store the residual into rhs
   int update;        // 0: residual only (no RK update)
+  int fuseDt;        // 1: the gradient pass also reduces the time step (stage 1)
+  DtArgs dt;         // time-step parameters when fuseDt
 };
 
-struct DtArgs {
-  double cfl, dtImposed, dtMinLimit, endTime;
-  int useDeviceTime;  // 1: current time from scal[1] and advance it
-  double timeHost;
-};
 
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
@@ -136,11 +142,19 @@ void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStr
 template <typename R>
 void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
 template <typename R>
+int configure_grad_smem(int maxW, int block);
+template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof);
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
                long long *launches, const Prof *prof);
+// One time step: stage 1 with the time-step reduction fused into its gradient
+// pass (finalized before the stage's update), then the remaining stages.
+template <typename R>
+void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int nStages,
+                 cudaStream_t s, long long *launches, int spaceOrder, int reconst,
+                 const Prof *prof);
 
 // Setup kernels of the FP64 unit.  WLSQ weights of every stencil member,
 // w64[3][stTotal], with the arithmetic of RFLU_ComputeGradCellsFast_3D

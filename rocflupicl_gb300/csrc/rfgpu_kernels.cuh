@@ -334,137 +334,218 @@ __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__rest
 // reference's); mixed path: weights rebuilt in FP32 from the records'
 // centroids and the cell's WLSQ factor terms.
 template <typename R>
-__global__ void __launch_bounds__(128) k_grad_lim(const RegionDev<R> *__restrict__ regs,
-                                                  const Tile *__restrict__ tiles, int nTiles) {
+__device__ __forceinline__ void dt_block_min(unsigned long long bits, unsigned long long *smin,
+                                             unsigned long long *dst) {
+  for (int o = 16; o > 0; o >>= 1) {
+    unsigned long long x = __shfl_down_sync(0xffffffffu, bits, o);
+    bits = x < bits ? x : bits;
+  }
+  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = bits;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    unsigned long long v = threadIdx.x < (blockDim.x >> 5) ? smin[threadIdx.x] : 0x7FF0000000000000ull;
+    for (int o = 16; o > 0; o >>= 1) {
+      unsigned long long x = __shfl_down_sync(0xffffffffu, v, o);
+      v = x < v ? x : v;
+    }
+    if (threadIdx.x == 0) atomicMin(dst, v);
+  }
+  __syncthreads();
+}
+
+// Local time-step sum of RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:
+// 165-297) for one cell, as a gather over its faces in the reference order:
+// sum of (|v_n| + a) * area with face-averaged velocity and sound speed
+// (interior faces) or the cell's own (boundary faces).  u = rhou*(1/rho) is
+// the record's velocity; a is dv(SOUN) on the FP64 path and sqrt(g p/rho) in
+// FP32 on the mixed path.  Returns dt(c) = vol / sum.
+template <typename R>
+__device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R r0[8]) {
+  const int N = g.nCells;
+  const R gg = R(g.ph.gvG);
+  const R a0 = sizeof(R) == 8 ? R(g.dv[2 * N + c]) : R(sqrtf(float(gg * r0[4] / r0[0])));
+  R acc = R(0);
+  const long long e0 = g.cfOff[c >> 5] + (c & 31);
+  const int n = g.cfCnt[c];
+  for (int k = 0; k < n; ++k) {
+    const long long e = e0 + (long long)k * kSlice;
+    const int code = g.cfCode[e];
+    R nrm[4];
+    if (code >= 0) {
+      const int nb = g.cfNb[e];
+      ld4(g.fnA + 4 * (size_t)(code >> 1), nrm);
+      R rn[8];
+      ld8(g.rec + 8 * (size_t)nb, rn);
+      const R an = sizeof(R) == 8 ? R(g.dv[2 * N + nb]) : R(sqrtf(float(gg * rn[4] / rn[0])));
+      // the face's c1 values first, as in the reference
+      const bool first = (code & 1) == 0;
+      const R u1 = first ? r0[1] : rn[1], u2 = first ? rn[1] : r0[1];
+      const R v1 = first ? r0[2] : rn[2], v2 = first ? rn[2] : r0[2];
+      const R w1 = first ? r0[3] : rn[3], w2 = first ? rn[3] : r0[3];
+      const R a1 = first ? a0 : an, a2 = first ? an : a0;
+      R vc = R(0.5) * ((u1 + u2) * nrm[0] + (v1 + v2) * nrm[1] + (w1 + w2) * nrm[2]);
+      R as = R(0.5) * (a1 + a2);
+      acc = acc + (fabs(vc - R(0)) + as) * nrm[3];
+    } else {
+      ld4(g.bfnA + 4 * (size_t)(-code - 1), nrm);
+      R vc = r0[1] * nrm[0] + r0[2] * nrm[1] + r0[3] * nrm[2];
+      acc = acc + (fabs(vc - R(0)) + a0) * nrm[3];
+    }
+  }
+  return sizeof(R) == 8 ? double(R(g.vol[c]) / acc) : double(float(g.vol[c]) / float(acc));
+}
+
+// WLSQ gradients of (rho,u,v,w,p) (RFLU_ComputeGradCellsFast_3D,
+// modflu/RFLU_ModDifferentiationCells.F90:1021-1149) fused with the
+// Venkatakrishnan limiter and RFLU_LimitGradCells (modflu/RFLU_ModLimiters.F90:
+// 339-532, 707-760).  One thread per cell; stencil members in stored order
+// (the reference's summation order); the stencil indices are read from the
+// SELL slice (coalesced across the warp) and the record gathers of
+// consecutive members are issued together.  The limiter of a cell needs only its
+// own unlimited gradient and its face neighbours' values, and min/max and the
+// MIN over faces do not depend on the face order, so the per-cell gather
+// equals the reference's two face loops.  FP64 path: precomputed weights
+// (bitwise the reference's); mixed path: weights rebuilt in FP32 from the
+// records' centroids and the cell's WLSQ factor terms.  With fuseDt the pass
+// also reduces the time step (stage 1 of a step).
+template <typename R>
+__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? 8 : 4) k_grad_lim(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles,
+                                                  int maxW, int fuseDt) {
+  __shared__ unsigned long long smin[32];
+  (void)maxW;
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
-    if (c >= N) continue;
-    const R *__restrict__ rec = g.rec;
-    R r0[8];
-    ld8(rec + 8 * (size_t)c, r0);
-    R acc[15];
+    const bool valid = c < N;
+    const long long base = valid ? g.stOff[c >> 5] + (c & 31) : 0;
+    const int *__restrict__ sidx = g.stIdx + base;
+    unsigned long long dtbits = 0x7FF0000000000000ull;
+    if (valid) {
+      const R *__restrict__ rec = g.rec;
+      R r0[8];
+      ld8(rec + 8 * (size_t)c, r0);
+      R acc[15];
 #pragma unroll
-    for (int k = 0; k < 15; ++k) acc[k] = R(0);
-    long long e = g.stOff[c >> 5] + (c & 31);
-    const int n = g.stCnt[c];
-    // members are accumulated in stored order; the loads of U consecutive
-    // members are issued together so their gathers overlap
-    if (sizeof(R) == 8) {
-      const long long T = g.stTotal;
-      auto member = [&](const R rn[8], long long ee) {
-        const R wx = g.stW[ee], wy = g.stW[T + ee], wz = g.stW[2 * T + ee];
+      for (int k = 0; k < 15; ++k) acc[k] = R(0);
+      const int n = g.stCnt[c];
+      // members accumulated in stored order; loads of consecutive members are
+      // issued together so their gathers overlap
+      if (sizeof(R) == 8) {
+        const long long T = g.stTotal;
+        auto member = [&](const R rn[8], long long ee) {
+          const R wx = g.stW[ee], wy = g.stW[T + ee], wz = g.stW[2 * T + ee];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            R dVar = rn[v] - r0[v];
+            acc[3 * v] = acc[3 * v] + wx * dVar;
+            acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
+            acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+          }
+        };
+        int k = 0;
+        for (; k + 2 <= n; k += 2) {
+          R ra[8], rb[8];
+          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
+          ld8(rec + 8 * (size_t)sidx[(k + 1) * kSlice], rb);
+          member(ra, base + (long long)k * kSlice);
+          member(rb, base + (long long)(k + 1) * kSlice);
+        }
+        for (; k < n; ++k) {
+          R ra[8];
+          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
+          member(ra, base + (long long)k * kSlice);
+        }
+      } else {
+        const R c12 = g.cwt[c], c13 = g.cwt[N + c], c23 = g.cwt[2 * N + c];
+        const R c1111 = g.cwt[3 * N + c], c2222 = g.cwt[4 * N + c], c3333 = g.cwt[5 * N + c];
+        auto member = [&](const R rn[8]) {
+          R dx = rn[5] - r0[5], dy = rn[6] - r0[6], dz = rn[7] - r0[7];
+          R term = rsqrtf(float(dx * dx + dy * dy + dz * dz));
+          dx = term * dx;
+          dy = term * dy;
+          dz = term * dz;
+          R term1 = c1111 * dx;
+          R term2 = c2222 * (dy + c12 * dx);
+          R term3 = c3333 * (dz + c23 * dy + c13 * dx);
+          R wx = term * (term1 + c12 * term2 + c13 * term3);
+          R wy = term * (term2 + c23 * term3);
+          R wz = term * term3;
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            R dVar = rn[v] - r0[v];
+            acc[3 * v] = acc[3 * v] + wx * dVar;
+            acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
+            acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+          }
+        };
+        int k = 0;
+        for (; k + 4 <= n; k += 4) {
+          R ra[8], rb[8], rc[8], rd[8];
+          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
+          ld8(rec + 8 * (size_t)sidx[(k + 1) * kSlice], rb);
+          ld8(rec + 8 * (size_t)sidx[(k + 2) * kSlice], rc);
+          ld8(rec + 8 * (size_t)sidx[(k + 3) * kSlice], rd);
+          member(ra);
+          member(rb);
+          member(rc);
+          member(rd);
+        }
+        for (; k < n; ++k) {
+          R ra[8];
+          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
+          member(ra);
+        }
+      }
+      if (g.ph.reconst == 11) {
+        R vmin[5], vmax[5], lim[5];
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
-          R dVar = rn[v] - r0[v];
-          acc[3 * v] = acc[3 * v] + wx * dVar;
-          acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
-          acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+          vmin[v] = r0[v];
+          vmax[v] = r0[v];
+          lim[v] = R(1);
         }
-      };
-      int k = 0;
-      for (; k + 2 <= n; k += 2, e += 2 * kSlice) {
-        const int nb0 = g.stIdx[e], nb1 = g.stIdx[e + kSlice];
-        R ra[8], rb[8];
-        ld8(rec + 8 * (size_t)nb0, ra);
-        ld8(rec + 8 * (size_t)nb1, rb);
-        member(ra, e);
-        member(rb, e + kSlice);
-      }
-      for (; k < n; ++k, e += kSlice) {
-        R ra[8];
-        ld8(rec + 8 * (size_t)g.stIdx[e], ra);
-        member(ra, e);
-      }
-    } else {
-      const R c12 = g.cwt[c], c13 = g.cwt[N + c], c23 = g.cwt[2 * N + c];
-      const R c1111 = g.cwt[3 * N + c], c2222 = g.cwt[4 * N + c], c3333 = g.cwt[5 * N + c];
-      auto member = [&](const R rn[8]) {
-        R dx = rn[5] - r0[5], dy = rn[6] - r0[6], dz = rn[7] - r0[7];
-        R term = rsqrtf(float(dx * dx + dy * dy + dz * dz));
-        dx = term * dx;
-        dy = term * dy;
-        dz = term * dz;
-        R term1 = c1111 * dx;
-        R term2 = c2222 * (dy + c12 * dx);
-        R term3 = c3333 * (dz + c23 * dy + c13 * dx);
-        R wx = term * (term1 + c12 * term2 + c13 * term3);
-        R wy = term * (term2 + c23 * term3);
-        R wz = term * term3;
+        const long long T = g.cfTotal;
+        const long long e0 = g.cfOff[c >> 5] + (c & 31);
+        const int nf = g.cfCnt[c];
+        for (int k = 0; k < nf; ++k) {
+          const long long ee = e0 + (long long)k * kSlice;
+          if (g.cfCode[ee] < 0) continue;
+          R rn[8];
+          ld8(rec + 8 * (size_t)g.cfNb[ee], rn);
 #pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          R dVar = rn[v] - r0[v];
-          acc[3 * v] = acc[3 * v] + wx * dVar;
-          acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
-          acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+          for (int v = 0; v < 5; ++v) {
+            vmin[v] = rmin(vmin[v], rn[v]);
+            vmax[v] = rmax(vmax[v], rn[v]);
+          }
         }
-      };
-      int k = 0;
-      for (; k + 4 <= n; k += 4, e += 4 * kSlice) {
-        const int nb0 = g.stIdx[e], nb1 = g.stIdx[e + kSlice], nb2 = g.stIdx[e + 2 * kSlice],
-                  nb3 = g.stIdx[e + 3 * kSlice];
-        R ra[8], rb[8], rc[8], rd[8];
-        ld8(rec + 8 * (size_t)nb0, ra);
-        ld8(rec + 8 * (size_t)nb1, rb);
-        ld8(rec + 8 * (size_t)nb2, rc);
-        ld8(rec + 8 * (size_t)nb3, rd);
-        member(ra);
-        member(rb);
-        member(rc);
-        member(rd);
+        const R epsq = g.epsq[c];
+        const int guard = g.ph.venkatGuard;
+        for (int k = 0; k < nf; ++k) {
+          const long long ee = e0 + (long long)k * kSlice;
+          if (g.cfCode[ee] < 0) continue;
+          const R dx = g.cfD[ee], dy = g.cfD[T + ee], dz = g.cfD[2 * T + ee];
+#pragma unroll
+          for (int v = 0; v < 5; ++v) {
+            R d2 = acc[3 * v] * dx + acc[3 * v + 1] * dy + acc[3 * v + 2] * dz;
+            venkat_term(d2, vmax[v] - r0[v], vmin[v] - r0[v], epsq, lim[v], guard);
+          }
+        }
+#pragma unroll
+        for (int v = 0; v < 5; ++v)
+#pragma unroll
+          for (int d = 0; d < 3; ++d) acc[3 * v + d] = lim[v] * acc[3 * v + d];
       }
-      for (; k < n; ++k, e += kSlice) {
-        R ra[8];
-        ld8(rec + 8 * (size_t)g.stIdx[e], ra);
-        member(ra);
-      }
+      R out[16];
+#pragma unroll
+      for (int k = 0; k < 15; ++k) out[k] = acc[k];
+      out[15] = R(0);
+      st16(g.grad + 16 * (size_t)c, out);
+      if (fuseDt) dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
     }
-    if (g.ph.reconst == 11) {
-      R vmin[5], vmax[5], lim[5];
-#pragma unroll
-      for (int v = 0; v < 5; ++v) {
-        vmin[v] = r0[v];
-        vmax[v] = r0[v];
-        lim[v] = R(1);
-      }
-      const long long T = g.cfTotal;
-      const long long e0 = g.cfOff[c >> 5] + (c & 31);
-      const int nf = g.cfCnt[c];
-      for (int k = 0; k < nf; ++k) {
-        const long long ee = e0 + (long long)k * kSlice;
-        if (g.cfCode[ee] < 0) continue;
-        R rn[8];
-        ld8(rec + 8 * (size_t)g.cfNb[ee], rn);
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          vmin[v] = rmin(vmin[v], rn[v]);
-          vmax[v] = rmax(vmax[v], rn[v]);
-        }
-      }
-      const R epsq = g.epsq[c];
-      const int guard = g.ph.venkatGuard;
-      for (int k = 0; k < nf; ++k) {
-        const long long ee = e0 + (long long)k * kSlice;
-        if (g.cfCode[ee] < 0) continue;
-        const R dx = g.cfD[ee], dy = g.cfD[T + ee], dz = g.cfD[2 * T + ee];
-#pragma unroll
-        for (int v = 0; v < 5; ++v) {
-          R d2 = acc[3 * v] * dx + acc[3 * v + 1] * dy + acc[3 * v + 2] * dz;
-          venkat_term(d2, vmax[v] - r0[v], vmin[v] - r0[v], epsq, lim[v], guard);
-        }
-      }
-#pragma unroll
-      for (int v = 0; v < 5; ++v)
-#pragma unroll
-        for (int d = 0; d < 3; ++d) acc[3 * v + d] = lim[v] * acc[3 * v + d];
-    }
-    R out[16];
-#pragma unroll
-    for (int k = 0; k < 15; ++k) out[k] = acc[k];
-    out[15] = R(0);
-    st16(g.grad + 16 * (size_t)c, out);
+    if (fuseDt) dt_block_min<R>(dtbits, smin, g.dtBits);
   }
 }
 
@@ -685,6 +766,21 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
 __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, int c,
                                                     const StepArgs &a) {
   const int N = g.nCells;
+  const Phys &ph = g.ph;
+  const int is = a.istage;
+  // own-cell loads first: they are independent of the flux gathers below
+  double q[5];
+  float rsOld[5];
+  float r[8];
+  float ivol = 0.f;
+  if (a.update) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) rsOld[j] = (is > 1) ? g.rhsSumF[j * N + c] : 0.f;
+    ld8(g.rec + 8 * (size_t)c, r);
+    ivol = g.ivolF[c];
+  }
   float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
@@ -710,14 +806,10 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   float rhs[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) rhs[j] = hi[j] + lo[j];
-  const Phys &ph = g.ph;
-  const double dtMin = a.useDeviceDt ? g.scal[0] : a.dtHost;
-  const int is = a.istage;
-  const float adtv = float(ph.ark[is - 1] * dtMin) / float(g.vol[c]);
+  const float fac = a.useDeviceDt ? float(g.scal[3 + is - 1]) : float(ph.ark[is - 1] * a.dtHost);
+  const float adtv = fac * ivol;
   const float grk = float(ph.grk[is - 1]);
-  double q[5], old[5];
-#pragma unroll
-  for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
+  double old[5];
   if (ph.rkScheme == 1) {
     if (is == 1) {
 #pragma unroll
@@ -742,20 +834,20 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
         dU = adtv * rhs[j];
         rs[j * N + c] = rhs[j];
       } else if (is == 2) {
-        dU = adtv * (rhs[j] - grk * rs[j * N + c]);
+        dU = adtv * (rhs[j] - grk * rsOld[j]);
         rs[j * N + c] = rhs[j];
       } else {
-        dU = adtv * (rhs[j] - grk * rs[j * N + c]);
+        dU = adtv * (rhs[j] - grk * rsOld[j]);
       }
     } else if (ph.rkScheme == 1) {
       if (is == 1) {
         dU = adtv * rhs[j];
         rs[j * N + c] = rhs[j];
       } else if (is == ph.nSteps) {
-        dU = adtv * (rhs[j] + rs[j * N + c]);
+        dU = adtv * (rhs[j] + rsOld[j]);
       } else {
         dU = adtv * rhs[j];
-        rs[j * N + c] = rs[j * N + c] + grk * rhs[j];
+        rs[j * N + c] = rsOld[j] + grk * rhs[j];
       }
     } else {
       dU = adtv * rhs[j];
@@ -785,8 +877,6 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
 #pragma unroll
   for (int j = 0; j < 5; ++j) g.cv[j * N + c] = q[j];
   g.dv[c] = p;
-  float r[8];
-  ld8(g.rec + 8 * (size_t)c, r);
   r[0] = rf;
   r[1] = uf;
   r[2] = vf;
@@ -841,9 +931,8 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
     }
     if (!a.update) continue;
     const Phys &ph = g.ph;
-    const double dtMin = a.useDeviceDt ? g.scal[0] : a.dtHost;
     const int is = a.istage;
-    const double fac = ph.ark[is - 1] * dtMin;
+    const double fac = a.useDeviceDt ? g.scal[3 + is - 1] : ph.ark[is - 1] * a.dtHost;
     const double adtv = fac / g.vol[c];
     double q[5], old[5];
 #pragma unroll
@@ -938,13 +1027,9 @@ __global__ void k_dv_complete(const RegionDev<R> *__restrict__ regs, const Tile 
   }
 }
 
-// ---- time step: RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:165-327)
-// as a per-cell gather: dt(c) = vol / sum over the cell's faces, in the
-// reference order, of (|v_n| + a) * area with face-averaged velocity and
-// sound speed (interior) or the cell's own (boundary).  u = rhou*(1/rho) is
-// the record's velocity; a is dv(SOUN) on the FP64 path and sqrt(g p/rho) in
-// FP32 on the mixed path.  Block minimum, then an atomic minimum on the bit
-// pattern (dt > 0: the IEEE order equals the unsigned integer order).
+// ---- time step (standalone pass): per-cell gather of cell_dt, block minimum,
+// then an atomic minimum on the bit pattern (dt > 0: the IEEE order equals
+// the unsigned integer order).
 template <typename R>
 __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict__ regs,
                                                  const Tile *__restrict__ tiles, int nTiles) {
@@ -953,59 +1038,13 @@ __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict_
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
-    const int N = g.nCells;
     unsigned long long bits = 0x7FF0000000000000ull;  // +inf
-    if (c < N) {
-      const R gg = R(g.ph.gvG);
+    if (c < g.nCells) {
       R r0[8];
       ld8(g.rec + 8 * (size_t)c, r0);
-      const R a0 = sizeof(R) == 8 ? R(g.dv[2 * N + c]) : R(sqrtf(float(gg * r0[4] / r0[0])));
-      R acc = R(0);
-      const long long e0 = g.cfOff[c >> 5] + (c & 31);
-      const int n = g.cfCnt[c];
-      for (int k = 0; k < n; ++k) {
-        const long long e = e0 + (long long)k * kSlice;
-        const int code = g.cfCode[e];
-        R nrm[4];
-        if (code >= 0) {
-          const int nb = g.cfNb[e];
-          ld4(g.fnA + 4 * (size_t)(code >> 1), nrm);
-          R rn[8];
-          ld8(g.rec + 8 * (size_t)nb, rn);
-          const R an = sizeof(R) == 8 ? R(g.dv[2 * N + nb]) : R(sqrtf(float(gg * rn[4] / rn[0])));
-          // the face's c1 values first, as in the reference
-          const bool first = (code & 1) == 0;
-          const R u1 = first ? r0[1] : rn[1], u2 = first ? rn[1] : r0[1];
-          const R v1 = first ? r0[2] : rn[2], v2 = first ? rn[2] : r0[2];
-          const R w1 = first ? r0[3] : rn[3], w2 = first ? rn[3] : r0[3];
-          const R a1 = first ? a0 : an, a2 = first ? an : a0;
-          R vc = R(0.5) * ((u1 + u2) * nrm[0] + (v1 + v2) * nrm[1] + (w1 + w2) * nrm[2]);
-          R as = R(0.5) * (a1 + a2);
-          acc = acc + (fabs(vc - R(0)) + as) * nrm[3];
-        } else {
-          ld4(g.bfnA + 4 * (size_t)(-code - 1), nrm);
-          R vc = r0[1] * nrm[0] + r0[2] * nrm[1] + r0[3] * nrm[2];
-          acc = acc + (fabs(vc - R(0)) + a0) * nrm[3];
-        }
-      }
-      double dtc = sizeof(R) == 8 ? double(R(g.vol[c]) / acc) : double(float(g.vol[c]) / float(acc));
-      bits = (unsigned long long)__double_as_longlong(dtc);
+      bits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
     }
-    for (int o = 16; o > 0; o >>= 1) {
-      unsigned long long x = __shfl_down_sync(0xffffffffu, bits, o);
-      bits = x < bits ? x : bits;
-    }
-    if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = bits;
-    __syncthreads();
-    if (threadIdx.x < 32) {
-      unsigned long long v = threadIdx.x < (blockDim.x >> 5) ? smin[threadIdx.x] : 0x7FF0000000000000ull;
-      for (int o = 16; o > 0; o >>= 1) {
-        unsigned long long x = __shfl_down_sync(0xffffffffu, v, o);
-        v = x < v ? x : v;
-      }
-      if (threadIdx.x == 0) atomicMin(g.dtBits, v);
-    }
-    __syncthreads();
+    dt_block_min<R>(bits, smin, g.dtBits);
   }
 }
 
@@ -1037,6 +1076,7 @@ __global__ void k_dt_finalize(const RegionDev<R> *__restrict__ regs, int nRegion
   }
   g.scal[0] = dtMin;
   g.scal[2] = dtMin;
+  for (int i = 0; i < 5; ++i) g.scal[3 + i] = g.ph.ark[i] * dtMin;  // fac of RkUpdateGeneric
   if (a.useDeviceTime) g.scal[1] = tNew;
 }
 
@@ -1057,10 +1097,18 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   (void)reconst;
   long long n = 0;
-  if (spaceOrder > 1 && w.nCellTiles > 0) {
+  const bool grad = spaceOrder > 1 && w.nCellTiles > 0;
+  if (grad) {
     RF_MARK(KP_GRADIENT, 0);
-    k_grad_lim<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    k_grad_lim<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles,
+                                                        w.maxStW, a.fuseDt);
     RF_MARK(KP_GRADIENT, 1);
+    ++n;
+  }
+  if (a.fuseDt && grad) {
+    RF_MARK(KP_DT_FINAL, 0);
+    k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a.dt);
+    RF_MARK(KP_DT_FINAL, 1);
     ++n;
   }
   if (w.nFaceTiles > 0) {
@@ -1103,6 +1151,28 @@ void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStr
 }
 
 template <typename R>
+void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int nStages,
+                 cudaStream_t s, long long *launches, int spaceOrder, int reconst,
+                 const Prof *prof) {
+  const bool fuse = spaceOrder > 1 && w.nCellTiles > 0;
+  if (!fuse) launch_dt<R>(regs, w, da, s, launches, prof);
+  for (int is = 1; is <= nStages; ++is) {
+    StepArgs sa{is, 1, 0.0, 0, 1, (fuse && is == 1) ? 1 : 0, da};
+    launch_stage<R>(regs, w, sa, s, launches, spaceOrder, reconst, prof);
+  }
+}
+
+// Shared-memory configuration of the gradient pass.  Staging the stencil
+// indices in shared memory was measured slower (the carve-out shrinks the L1
+// that serves the neighbour-record gathers), so none is requested.
+template <typename R>
+int configure_grad_smem(int maxW, int block) {
+  (void)maxW;
+  (void)block;
+  return 0;  // the gradient pass keeps L1 for record gathers: no dynamic smem
+}
+
+template <typename R>
 void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
   int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
   if (grid > 0) k_dv_complete<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
@@ -1111,9 +1181,12 @@ void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s)
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
   template void launch_dv_complete<R>(const RegionDev<R> *, const Work &, cudaStream_t);      \
+  template int configure_grad_smem<R>(int, int);                                              \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
                                 cudaStream_t, long long *, int, int, const Prof *);           \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
-                             long long *, const Prof *);
+                             long long *, const Prof *);                                      \
+  template void launch_step<R>(const RegionDev<R> *, const Work &, const DtArgs &, int,       \
+                               cudaStream_t, long long *, int, int, const Prof *);
 
 }  // namespace rfgpu
