@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--l1-steps", type=int, default=10)
+    ap.add_argument("--serve-requests", type=int, default=16,
+                    help="requests of the serving measurement (0 disables it)")
+    ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson rate, requests/s")
+    ap.add_argument("--serve-tend", type=float, default=2.0e-4, help="end time of each solve")
     return ap.parse_args()
 
 
@@ -275,7 +279,7 @@ def main():
     status = r.status()
     value = evals_step * a.steps * dist.world / (ms_max * 1e-3)
     s = 4
-    kb = perfmodel.kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
+    kb = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
     per = {}
     for k, (t, n) in pr.items():
         if n:
@@ -329,7 +333,7 @@ def main():
         f.sync()
         nst = max(2, min(a.steps, 5))
         ms64, _, pr64 = timed_steps(f, nst, cfl, dti)
-        kb64 = perfmodel.kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, 8)
+        kb64 = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, 8)
         dom64 = max((k for k in pr64 if k in kb64 and pr64[k][1]), key=lambda k: pr64[k][0])
         t64 = pr64[dom64][0] / pr64[dom64][1]
         fp64 = {"value": evals_step * nst / (ms64 * 1e-3), "ms_per_step": ms64 / nst,
@@ -356,6 +360,22 @@ def main():
         f.close()
         mm.close()
 
+    # ---- serving: continuous batching of a seeded Poisson stream ---------------
+    serving = None
+    if a.serve_requests > 0:
+        from rocflupicl_gb300 import serving as S
+        reqs = S.poisson_requests(a.serve_requests, a.serve_rate, seed=17 + dist.rank)
+        srv = S.Server(a.serve_tend, prepare_workers=4, mesh_threads=4)
+        t0 = time.perf_counter()
+        rs = srv.run(reqs)
+        wall = time.perf_counter() - t0
+        serving = S.summarize(rs, wall)
+        serving.update({"rate_per_s": a.serve_rate, "t_end": a.serve_tend,
+                        "max_active": srv.max_active, "batch_iterations": srv.iterations,
+                        "cells": "6k^3, log-uniform 10k-4M", "precision": "mixed",
+                        "latency": "arrival -> state read back, including host mesh "
+                                   "preparation and queueing"})
+
     # ---- CPU baseline (rank 0) --------------------------------------------------
     cpu = None
     if not a.no_cpu and dist.rank == 0:
@@ -372,7 +392,7 @@ def main():
                 "dtype": "f32 flux / f64 accumulate", "data": "synthetic (seeded)",
                 "config": workload_config(c, a), "roofline": roof, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "status": status,
-                "kernels": per, "fp64": fp64, "device_bytes": dev_bytes}
+                "kernels": per, "fp64": fp64, "device_bytes": dev_bytes, "serving": serving}
         print(json.dumps(line), flush=True)
     dist.close()
 

@@ -181,6 +181,8 @@ int rfgpu_timer_stop(rfgpu_region_t h, double *ms);
 /* Device selection for the calling host thread (one process per GPU), and
  * page-locked host buffers for the host<->device copies of a drop-in caller. */
 int rfgpu_set_device(int device);
+/* Free and total device memory of the current GPU (admission control). */
+int rfgpu_mem_info(long long *freeBytes, long long *totalBytes);
 void *rfgpu_host_alloc(long long bytes);
 int rfgpu_host_free(void *p);
 

@@ -508,6 +508,13 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   ph.spaceOrder = d->spaceOrder;
   ph.reconst = h->reconst;
   ph.venkatGuard = d->venkatGuard;
+  ph.refCpF = (float)ph.refCp;
+  ph.refGammaF = (float)ph.refGamma;
+  ph.gcRefF = (float)ph.gcRef;
+  ph.gvGF = (float)ph.gvG;
+  ph.epsentrF = (float)ph.epsentr;
+  ph.dissFactF = (float)ph.dissFact;
+  for (int i = 0; i < 5; ++i) ph.grkF[i] = (float)ph.grk[i];
   h->nSteps = ph.nSteps;
   try {
     if (h->prec)
@@ -933,6 +940,14 @@ int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms) {
 }
 
 int rfgpu_set_device(int device) { return cuda_rc(cudaSetDevice(device)); }
+
+int rfgpu_mem_info(long long *freeBytes, long long *totalBytes) {
+  size_t f = 0, t = 0;
+  if (cudaMemGetInfo(&f, &t) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (freeBytes) *freeBytes = (long long)f;
+  if (totalBytes) *totalBytes = (long long)t;
+  return RFGPU_OK;
+}
 
 void *rfgpu_host_alloc(long long bytes) {
   void *p = nullptr;

@@ -41,6 +41,8 @@ struct Phys {
   double epsentr, dissFact;
   double ark[5], grk[5];
   int nSteps, rkScheme, spaceDiscr, spaceOrder, reconst, venkatGuard;
+  // FP32 copies for the mixed-path kernels (no per-thread FP64 conversions)
+  float refCpF, refGammaF, gcRefF, gvGF, epsentrF, dissFactF, grkF[5];
 };
 
 template <typename R>

@@ -24,13 +24,36 @@ __device__ __forceinline__ R eo_dgpuvw(R D, R G, R P, R U, R V, R W) {
   return P / (D * (G - R(1))) + R(0.5) * (U * U + V * V + W * W) + R(0);
 }
 
+// Physical constants in the working precision: the FP64 values on the FP64
+// path, their FP32 copies on the mixed path (no per-thread conversions).
+template <typename R> struct PC;
+template <> struct PC<double> {
+  const Phys &p;
+  __device__ double cp() const { return p.refCp; }
+  __device__ double g() const { return p.refGamma; }
+  __device__ double gc() const { return p.gcRef; }
+  __device__ double gvG() const { return p.gvG; }
+  __device__ double eps() const { return p.epsentr; }
+  __device__ double diss() const { return p.dissFact; }
+};
+template <> struct PC<float> {
+  const Phys &p;
+  __device__ float cp() const { return p.refCpF; }
+  __device__ float g() const { return p.refGammaF; }
+  __device__ float gc() const { return p.gcRefF; }
+  __device__ float gvG() const { return p.gvGF; }
+  __device__ float eps() const { return p.epsentrF; }
+  __device__ float diss() const { return p.dissFactF; }
+};
+
 // ---- flux functions on reconstructed states ----------------------------------
 
 // AUSM+ (modflu/RFLU_ModAUSMFlux.F90:282-367 with the state set-up of :2787-2846)
 template <typename R>
 __device__ __forceinline__ void ausm_flux(const Phys &ph, const R L[5], const R Rt[5],
                                           R nx, R ny, R nz, R nm, R flx[5]) {
-  const R cp = R(ph.refCp), g = R(ph.refGamma), gc = R(ph.gcRef), fs = R(0);
+  const PC<R> k{ph};
+  const R cp = k.cp(), g = k.g(), gc = k.gc(), fs = R(0);
   R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
   R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
   R tl = pl / (rl * gc);
@@ -80,7 +103,8 @@ __device__ __forceinline__ R entropy_fix(R l, R d) {  // RFLU_ModEntropyFixes.F9
 template <typename R>
 __device__ __forceinline__ void roe_flux(const Phys &ph, const R L[5], const R Rt[5], R nx,
                                          R ny, R nz, R nm, R flx[5]) {
-  const R cp = R(ph.refCp), g = R(ph.refGamma), gc = R(ph.gcRef), fs = R(0);
+  const PC<R> k{ph};
+  const R cp = k.cp(), g = k.g(), gc = k.gc(), fs = R(0);
   R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
   R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
   R tl = pl / (rl * gc);
@@ -99,7 +123,7 @@ __device__ __forceinline__ void roe_flux(const Phys &ph, const R L[5], const R R
   R sh = R(0.5) * (uh * uh + vh * vh + wh * wh);
   R ah = sqrt((g - R(1)) * (Hh - R(0.5) * (R(2) * sh)));
   R l1 = fabs(qh - ah), l2 = fabs(qh), l5 = fabs(qh + ah);
-  R efc = R(ph.epsentr) * l5;
+  R efc = k.eps() * l5;
   l1 = entropy_fix(l1, efc);
   l2 = entropy_fix(l2, efc);
   l5 = entropy_fix(l5, efc);
@@ -109,7 +133,7 @@ __device__ __forceinline__ void roe_flux(const Phys &ph, const R L[5], const R R
   R dv5 = (dp + rh * ah * dq) / (R(2) * ah * ah);
   R dv2 = dr - dp / (ah * ah);
   R t1 = l1 * dv1, t2 = l2 * dv2, t3 = l2 * rh, t5 = l5 * dv5;
-  R df = R(ph.dissFact);
+  R df = k.diss();
   flx[0] = R(0.5) * (ql * rl + qr * rr) * nm - R(0.5) * df * (t1 + t2 + t5) * nm;
   flx[1] = R(0.5) * (ql * rl * ul + pl * nx + qr * rr * ur + pr * nx) * nm -
            R(0.5) * df * (t1 * (uh - nx * ah) + t2 * uh + t3 * (du - nx * dq) + t5 * (uh + nx * ah)) * nm;
@@ -127,7 +151,7 @@ __device__ __forceinline__ void roe_flux(const Phys &ph, const R L[5], const R R
 template <typename R>
 __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R Rt[5], R irl,
                                           R irr, R nx, R ny, R nz, R nm, R flx[5]) {
-  const R g = R(ph.refGamma), fs = R(0);
+  const R g = PC<R>{ph}.g(), fs = R(0);
   R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
   R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
   R el = eo_dgpuvw(rl, g, pl, ul, vl, wl);
@@ -362,7 +386,7 @@ __device__ __forceinline__ void dt_block_min(unsigned long long bits, unsigned l
 template <typename R>
 __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R r0[8]) {
   const int N = g.nCells;
-  const R gg = R(g.ph.gvG);
+  const R gg = PC<R>{g.ph}.gvG();
   const R a0 = sizeof(R) == 8 ? R(g.dv[2 * N + c]) : R(sqrtf(float(gg * r0[4] / r0[0])));
   R acc = R(0);
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
@@ -663,7 +687,7 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       flx[3] = pl * nz * nm;
       flx[4] = pl * fs * nm;
     } else {
-      const R gvG = R(g.ph.gvG);
+      const R gvG = PC<R>{g.ph}.gvG();
       R rl, rul, rvl, rwl, rel, pl;
       if (order == 2) {
         rl = S[0];
@@ -808,7 +832,7 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   for (int j = 0; j < 5; ++j) rhs[j] = hi[j] + lo[j];
   const float fac = a.useDeviceDt ? float(g.scal[3 + is - 1]) : float(ph.ark[is - 1] * a.dtHost);
   const float adtv = fac * ivol;
-  const float grk = float(ph.grk[is - 1]);
+  const float grk = ph.grkF[is - 1];
   double old[5];
   if (ph.rkScheme == 1) {
     if (is == 1) {

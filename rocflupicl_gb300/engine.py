@@ -65,7 +65,8 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_sync", "rfgpu_batch_stream", "rfgpu_profile", "rfgpu_profile_read",
            "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
-           "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free"]
+           "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
+           "rfgpu_mem_info"]
 
 KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
            "dt_bface", "dt_cell", "dt_finalize"]
@@ -118,6 +119,7 @@ def load(path: Optional[str] = None):
         "rfgpu_set_device": ([C.c_int], C.c_int),
         "rfgpu_host_alloc": ([C.c_longlong], vp),
         "rfgpu_host_free": ([vp], C.c_int),
+        "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -152,6 +154,13 @@ def _prof_read(fn, h):
 def set_device(device: int):
     """Select the GPU for this host thread (one process per GPU)."""
     _check(load().rfgpu_set_device(device), "rfgpu_set_device")
+
+
+def mem_info():
+    """(free, total) device bytes of the current GPU."""
+    f, t = C.c_longlong(), C.c_longlong()
+    _check(load().rfgpu_mem_info(C.byref(f), C.byref(t)), "rfgpu_mem_info")
+    return f.value, t.value
 
 
 class PinnedArray:
@@ -363,7 +372,7 @@ class Region:
             k = n_steps
         else:
             chunk = 64
-            while True:
+            while k < 10_000_000:
                 if graph:
                     self.steps_graph(chunk, cfl, dt_imposed, 0.0, end)
                 else:
@@ -371,6 +380,8 @@ class Region:
                         self.step(cfl, dt_imposed, 0.0, end)
                 k += chunk
                 t, _ = self.time()
+                if not np.isfinite(t):
+                    raise EngineError(ERR_STATE, "solve: non-finite time")
                 if t >= end:
                     break
         t, _ = self.time()

@@ -40,6 +40,14 @@ def stage_bytes(nc: int, nf: int, nb: int, m: int, s: int) -> int:
     return sum(kernel_bytes(nc, nf, nb, m, s).values())
 
 
+def engine_kernel_bytes(nc: int, nf: int, nb: int, m: int, s: int) -> dict:
+    """Algorithmic bytes per launch of the engine's kernels: the gradient
+    kernel fuses the limiter, so it carries P1 + P2."""
+    kb = kernel_bytes(nc, nf, nb, m, s)
+    return {"gradient": kb["gradient"] + kb["limiter"], "face_flux": kb["face_flux"],
+            "bface_flux": kb["bface_flux"], "gather_update": kb["gather_update"]}
+
+
 def residual_bytes(nc: int, nf: int, nb: int, m: int, s: int) -> int:
     """Single residual evaluation: P1 + P2 + P3 without the update columns
     (cv, rhsSum, vol, p, a)."""
