@@ -36,7 +36,8 @@ enum {
   RFGPU_ERR_CUDA = 3,         /* CUDA runtime error */
   RFGPU_ERR_NOMEM = 4,        /* device allocation failed */
   RFGPU_ERR_STATE = 5,        /* invalid flow state detected on the device */
-  RFGPU_ERR_TIMEOUT = 6       /* a bounded device wait expired */
+  RFGPU_ERR_TIMEOUT = 6,      /* a bounded device wait expired */
+  RFGPU_ERR_NOALLOC_LIMIT = 7 /* problem larger than rfgpu_residual_noalloc's fixed scratch */
 };
 
 /* status bits returned by rfgpu_status */
@@ -201,6 +202,27 @@ int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int 
 long long rfgpu_batch_launch_count(rfgpu_batch_t b);
 int rfgpu_batch_timer_start(rfgpu_batch_t b);
 int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms);
+
+/* Residual that allocates nothing (no counterpart in the reference; an
+ * addition of this library).  For callers that may not allocate device
+ * memory: a Fortran or C host whose device memory is budgeted once at start-up
+ * (a server admitting work by its HBM footprint, a solver sized to fill the
+ * GPU), or code running where the CUDA runtime must not be asked for memory,
+ * such as a host callback.  Same result as rfgpu_residual(h, rhs): the
+ * CellGradientsMP + ConvectiveFluxesMP residual of the resident state into the
+ * caller's host array rhs(5,nCells).  The face fluxes and the residual are
+ * staged in one static device array of RFGPU_NOALLOC_SCRATCH_BYTES (32 MiB)
+ * that every GPU loading the library reserves until the process exits; a
+ * region needs 8*sizeof(working precision) bytes per interior face (rounded
+ * up to 256) plus 40 bytes per cell, and larger regions get
+ * RFGPU_ERR_NOALLOC_LIMIT before anything runs.  The first call on a device
+ * looks up the array's device address (cudaGetSymbolAddress) with that
+ * device current; make that first call before any stream capture.  All calls
+ * share the one array, which keeps the last call's contents: calls whose work
+ * overlaps on the GPU (other threads, other handles' streams) race on it and
+ * must be serialised by the caller.  Synchronous, like rfgpu_residual. */
+#define RFGPU_NOALLOC_SCRATCH_BYTES (32u << 20)
+int rfgpu_residual_noalloc(rfgpu_region_t h, double *rhs);
 
 #ifdef __cplusplus
 }

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -956,5 +957,57 @@ void *rfgpu_host_alloc(long long bytes) {
 }
 
 int rfgpu_host_free(void *p) { return p ? cuda_rc(cudaFreeHost(p)) : RFGPU_ERR_ARG; }
+
+// ---- residual without device allocation -----------------------------------------
+// Fixed scratch for rfgpu_residual_noalloc: RFGPU_NOALLOC_SCRATCH_BYTES of
+// device memory, reserved in every GPU that loads the library until the
+// process exits.  It holds the face fluxes (8 working-precision values per
+// interior face) followed by the residual (5 doubles per cell).  Host code must
+// not use the symbol itself as a device address: the address comes from
+// cudaGetSymbolAddress, taken once per device with that device current.
+
+}  // extern "C"
+
+static __device__ __align__(256) unsigned char g_noallocScratch[RFGPU_NOALLOC_SCRATCH_BYTES];
+
+namespace {
+std::mutex g_noallocMutex;
+void *g_noallocPtr[256] = {nullptr};
+}  // namespace
+
+extern "C" {
+
+int rfgpu_residual_noalloc(rfgpu_region_t h, double *rhs) {
+  if (!h || !rhs) return RFGPU_ERR_ARG;
+  const long long N = h->nCells, F = h->nFaces;
+  const long long fluxBytes = F * 8 * (h->prec ? 4 : 8);
+  const long long fluxAligned = (fluxBytes + 255) / 256 * 256;
+  if (fluxAligned + N * 5 * 8 > (long long)RFGPU_NOALLOC_SCRATCH_BYTES) return RFGPU_ERR_NOALLOC_LIMIT;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return RFGPU_ERR_CUDA;
+  void *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_noallocMutex);
+    if (!g_noallocPtr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noallocScratch) != cudaSuccess || !p) return RFGPU_ERR_CUDA;
+      g_noallocPtr[dev] = p;
+    }
+    base = g_noallocPtr[dev];
+  }
+  double *drhs = (double *)((unsigned char *)base + fluxAligned);
+  // every face flux and every residual entry is written before it is read, so
+  // nothing left from an earlier call needs clearing
+  if (h->prec)
+    launch_residual_scratch<float>(regs_of<float>(h), h->rd32, h->work, h->spaceOrder,
+                                   (float *)base, drhs, h->stream);
+  else
+    launch_residual_scratch<double>(regs_of<double>(h), h->rd64, h->work, h->spaceOrder,
+                                    (double *)base, drhs, h->stream);
+  if (cudaGetLastError() != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (cudaMemcpyAsync(rhs, drhs, (size_t)N * 5 * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
 
 }  // extern "C"

@@ -145,6 +145,11 @@ template <typename R>
 void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
 template <typename R>
 int configure_grad_smem(int maxW, int block);
+// Residual with the face fluxes and the result in caller-supplied scratch
+// (used by rfgpu_residual_noalloc): rhs in the Fortran layout rhs(5,nCells).
+template <typename R>
+void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
+                             int spaceOrder, R *flux, double *rhs, cudaStream_t s);
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof);

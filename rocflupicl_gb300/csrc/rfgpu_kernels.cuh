@@ -1202,10 +1202,116 @@ void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s)
   if (grid > 0) k_dv_complete<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
 }
 
+// ---- residual without device allocation ---------------------------------------
+// Variant of the face-flux and residual-gather passes for rfgpu_residual_noalloc:
+// the face fluxes go to a caller-supplied scratch area (the library's static
+// device array) and the residual to the same area, in the Fortran layout
+// rhs(5,nCells), instead of the region's own buffers.  The region is passed by
+// value, so no device-side descriptor has to be written.
+template <typename R>
+__global__ void __launch_bounds__(128) k_face_flux_scratch(const RegionDev<R> g,
+                                                           R *__restrict__ flux) {
+  const int f = blockIdx.x * blockDim.x + threadIdx.x;
+  const int F = g.nFaces;
+  if (f >= F) return;
+  const int c1 = g.f2c[f], c2 = g.f2c[F + f];
+  R nrm[4];
+  ld4(g.fnA + 4 * (size_t)f, nrm);
+  R r1[8], r2[8];
+  ld8(g.rec + 8 * (size_t)c1, r1);
+  ld8(g.rec + 8 * (size_t)c2, r2);
+  R L[5], Rt[5], irl, irr;
+  cell_values(g, c1, r1, L, irl);
+  cell_values(g, c2, r2, Rt, irr);
+  if (g.ph.spaceOrder > 1) {
+    R G[16];
+    ld16(g.grad + 16 * (size_t)c1, G);
+    reconstruct(G, g.fdl[f], g.fdl[F + f], g.fdl[2 * F + f], L);
+    ld16(g.grad + 16 * (size_t)c2, G);
+    reconstruct(G, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
+  }
+  R flx[8];
+  const int sd = g.ph.spaceDiscr;
+  if (sd == 4)
+    ausm_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  else if (sd == 1)
+    roe_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  else
+    hllc_flux(g.ph, L, Rt, irl, irr, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  flx[5] = flx[6] = flx[7] = R(0);
+  st8(flux + 8 * (size_t)f, flx);
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g,
+                                                            const R *__restrict__ flux,
+                                                            double *__restrict__ rhs) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= g.nCells) return;
+  const long long e0 = g.cfOff[c >> 5] + (c & 31);
+  const int n = g.cfCnt[c];
+  if constexpr (sizeof(R) == 8) {
+    double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
+    for (int k = 0; k < n; ++k) {
+      const int code = g.cfCode[e0 + (long long)k * kSlice];
+      R fl[8];
+      if (code >= 0) {
+        ld8(flux + 8 * (size_t)(code >> 1), fl);
+        if (code & 1) {
+#pragma unroll
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(fl[j]);
+        } else {
+#pragma unroll
+          for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
+        }
+      } else {
+        ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 5; ++j) rhs[5 * (size_t)c + j] = acc[j];
+  } else {
+    float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < n; ++k) {
+      const int code = g.cfCode[e0 + (long long)k * kSlice];
+      float fl[8];
+      if (code >= 0) {
+        ld8(flux + 8 * (size_t)(code >> 1), fl);
+        const float sg = (code & 1) ? -1.f : 1.f;
+#pragma unroll
+        for (int j = 0; j < 5; ++j) two_sum_acc(hi[j], lo[j], sg * fl[j]);
+      } else {
+        ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
+#pragma unroll
+        for (int j = 0; j < 5; ++j) two_sum_acc(hi[j], lo[j], fl[j]);
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < 5; ++j) rhs[5 * (size_t)c + j] = double(hi[j]) + double(lo[j]);
+  }
+}
+
+// Gradients (the region's own pass), face fluxes into `flux`, boundary fluxes,
+// residual into `rhs`; all on stream s.
+template <typename R>
+void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
+                             int spaceOrder, R *flux, double *rhs, cudaStream_t s) {
+  if (spaceOrder > 1 && w.nCellTiles > 0)
+    k_grad_lim<R><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, w.maxStW, 0);
+  if (g.nFaces > 0) k_face_flux_scratch<R><<<(g.nFaces + 127) / 128, 128, 0, s>>>(g, flux);
+  if (w.nBFaceTiles > 0)
+    k_bface_flux<R><<<w.nBFaceTiles, w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
+  k_gather_rhs_scratch<R><<<(g.nCells + 127) / 128, 128, 0, s>>>(g, flux, rhs);
+}
+
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
   template void launch_dv_complete<R>(const RegionDev<R> *, const Work &, cudaStream_t);      \
   template int configure_grad_smem<R>(int, int);                                              \
+  template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
+                                           const Work &, int, R *, double *, cudaStream_t);    \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
                                 cudaStream_t, long long *, int, int, const Prof *);           \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \

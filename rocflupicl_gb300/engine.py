@@ -22,10 +22,12 @@ import numpy as np
 from . import _build
 from .case import Case, PREC_FP64, PREC_MIXED  # noqa: F401
 
-OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT = range(7)
+OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NOALLOC_LIMIT = range(8)
+NOALLOC_SCRATCH_BYTES = 32 << 20
 ST_NAN, ST_NEGPOS, ST_PFLOOR, ST_PCLAMP = 1, 2, 4, 8
 _NAMES = {1: "RFGPU_ERR_ARG", 2: "RFGPU_ERR_UNSUPPORTED", 3: "RFGPU_ERR_CUDA",
-          4: "RFGPU_ERR_NOMEM", 5: "RFGPU_ERR_STATE", 6: "RFGPU_ERR_TIMEOUT"}
+          4: "RFGPU_ERR_NOMEM", 5: "RFGPU_ERR_STATE", 6: "RFGPU_ERR_TIMEOUT",
+          7: "RFGPU_ERR_NOALLOC_LIMIT"}
 
 
 class EngineError(RuntimeError):
@@ -66,7 +68,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
-           "rfgpu_mem_info"]
+           "rfgpu_mem_info", "rfgpu_residual_noalloc"]
 
 KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
            "dt_bface", "dt_cell", "dt_finalize"]
@@ -120,6 +122,7 @@ def load(path: Optional[str] = None):
         "rfgpu_host_alloc": ([C.c_longlong], vp),
         "rfgpu_host_free": ([vp], C.c_int),
         "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
+        "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -279,6 +282,14 @@ class Region:
             return None
         rhs = np.empty((self.nCells, 5))
         _check(self.lib.rfgpu_residual(self.h, _dp(rhs)), "rfgpu_residual")
+        return rhs
+
+    def residual_noalloc(self):
+        """rfgpu_residual_noalloc: the residual with no device allocation, its
+        scratch in the library's fixed static device array (see include/rfgpu.h
+        for who needs it and its size limit)."""
+        rhs = np.empty((self.nCells, 5))
+        _check(self.lib.rfgpu_residual_noalloc(self.h, _dp(rhs)), "rfgpu_residual_noalloc")
         return rhs
 
     def download(self):
