@@ -46,6 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--workload", default="tet", choices=["tet", "sod", "mixed", "tubes", "serving"],
+                    help="tet: the headline line; the others print their own measurement")
     ap.add_argument("--n", type=int, default=128, help="base hexes per direction")
     ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
     ap.add_argument("--no-fp64", action="store_true")
@@ -108,7 +110,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
-                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except Exception:
@@ -246,11 +248,41 @@ def timed_steps(r, steps, cfl, dti, prof=True):
     return ms, launches, pr
 
 
+def run_secondary(a, dist):
+    """Secondary workloads: one JSON object per run (not the headline line)."""
+    from rocflupicl_gb300 import engine as E
+    from rocflupicl_gb300 import workloads as W
+    E.set_device(dist.local)
+    if a.workload == "sod":
+        out = W.run_sod()
+    elif a.workload == "mixed":
+        out = W.run_mixed_residual(repeats=a.steps)
+    elif a.workload == "tubes":
+        out = W.run_tubes(steps=a.steps)
+    else:
+        from rocflupicl_gb300 import serving as S
+        out = {"workload": "serving sweep", "rates": {}}
+        for lam in (1.0, 4.0, 16.0):
+            reqs = S.poisson_requests(a.serve_requests, lam, seed=23)
+            srv = S.Server(a.serve_tend, prepare_workers=6, mesh_threads=4)
+            t0 = time.perf_counter()
+            rs = srv.run(reqs)
+            o = S.summarize(rs, time.perf_counter() - t0)
+            o["max_active"] = srv.max_active
+            out["rates"][str(lam)] = o
+    if dist.rank == 0:
+        print(json.dumps({"impl": "ours", "secondary": a.workload, **out}), flush=True)
+
+
 def main():
     a = parse()
     dist = Dist()
     if a.impl == "reference":
         run_reference(a, dist)
+        dist.close()
+        return
+    if a.workload != "tet":
+        run_secondary(a, dist)
         dist.close()
         return
     from rocflupicl_gb300 import engine as E
@@ -266,12 +298,15 @@ def main():
     r = E.Region(c)
     dti = r.time_step(cfl, 1.0, 0.0, 1.0)
     r.set_time(0.0)
+    # the clock sampler runs from the warm-up through the timed region (its
+    # 50 ms period is longer than a few steps)
+    clocks = Clocks(dist.local)
+    clocks.start()
+    time.sleep(0.3)
     for _ in range(a.warmup):
         r.step(cfl, dti)
     r.sync()
-    clocks = Clocks(dist.local)
     dist.barrier()
-    clocks.start()
     ms, launches, pr = timed_steps(r, a.steps, cfl, dti)
     clk = clocks.stop()
     dist.barrier()

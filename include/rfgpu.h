@@ -196,6 +196,9 @@ int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMin
 int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtImposed,
                             double dtMinLimit, double endTime);
 int rfgpu_batch_sync(rfgpu_batch_t b);
+/* Persistent grid size of the batch's launches (blocks; 0 = one block per
+ * tile).  Chosen by the autotuner (rocflupicl_gb300/autotune.py). */
+int rfgpu_batch_set_tuning(rfgpu_batch_t b, int gridCap);
 void *rfgpu_batch_stream(rfgpu_batch_t b);
 int rfgpu_batch_profile(rfgpu_batch_t b, int enable);
 int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int n);

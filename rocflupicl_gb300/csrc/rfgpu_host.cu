@@ -861,6 +861,16 @@ int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtIm
   return RFGPU_OK;
 }
 
+int rfgpu_batch_set_tuning(rfgpu_batch_t b, int gridCap) {
+  if (!b || gridCap < 0) return RFGPU_ERR_ARG;
+  b->work.grid = gridCap;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return RFGPU_OK;
+}
+
 int rfgpu_batch_sync(rfgpu_batch_t b) {
   if (!b) return RFGPU_ERR_ARG;
   return cuda_rc(cudaStreamSynchronize(b->stream));

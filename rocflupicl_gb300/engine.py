@@ -68,7 +68,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
-           "rfgpu_mem_info", "rfgpu_residual_noalloc"]
+           "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning"]
 
 KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
            "dt_bface", "dt_cell", "dt_finalize"]
@@ -123,6 +123,7 @@ def load(path: Optional[str] = None):
         "rfgpu_host_free": ([vp], C.c_int),
         "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
+        "rfgpu_batch_set_tuning": ([vp, C.c_int], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -428,6 +429,9 @@ class Batch:
         ms = C.c_double()
         _check(self.lib.rfgpu_batch_timer_stop(self.h, C.byref(ms)), "rfgpu_batch_timer_stop")
         return ms.value
+
+    def set_grid_cap(self, blocks: int):
+        _check(self.lib.rfgpu_batch_set_tuning(self.h, blocks), "rfgpu_batch_set_tuning")
 
     def profile(self, enable: bool = True):
         _check(self.lib.rfgpu_batch_profile(self.h, int(enable)), "rfgpu_batch_profile")
