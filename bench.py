@@ -50,6 +50,8 @@ def parse():
                     help="tet: the headline line; the others print their own measurement")
     ap.add_argument("--n", type=int, default=128, help="base hexes per direction")
     ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
+    ap.add_argument("--cell-order", default="locality", choices=["locality", "host"],
+                    help="device numbering of cells and faces (results are identical)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -177,6 +179,7 @@ def workload_config(c, a):
             "cells": m.nCells, "faces": m.nFaces, "bfaces": m.nBFaces, "stencil_members": m.nMembs,
             "precision": "mixed: FP32 reconstruction/limiter/flux, FP64 geometry/accumulate/update/EOS",
             "l2": "inputs larger than L2 (working set >10 GB vs 129 MB L2)",
+            "cell_order": getattr(a, "cell_order", "locality"),
             "parallelism": "replicas (one independent region per GPU)"}
 
 
@@ -295,7 +298,8 @@ def main():
     res = {}
 
     # ---- mixed path, resident ------------------------------------------------
-    r = E.Region(c)
+    order = E.ORDER_LOCALITY if a.cell_order == "locality" else E.ORDER_HOST
+    r = E.Region(c, cell_order=order)
     dti = r.time_step(cfl, 1.0, 0.0, 1.0)
     r.set_time(0.0)
     # the clock sampler runs from the warm-up through the timed region (its
@@ -362,7 +366,7 @@ def main():
     fp64 = None
     if not a.no_fp64:
         c64 = c.with_numerics(precision=K.PREC_FP64)
-        f = E.Region(c64)
+        f = E.Region(c64, cell_order=order)
         for _ in range(min(a.warmup, 2)):
             f.step(cfl, dti)
         f.sync()
@@ -377,8 +381,8 @@ def main():
                 "kernel_ms": {k: v[0] / v[1] for k, v in pr64.items() if v[1]}}
         f.close()
         # identical dt sequence (from the FP64 path) for both precisions
-        f = E.Region(c64)
-        mm = E.Region(c)
+        f = E.Region(c64, cell_order=order)
+        mm = E.Region(c, cell_order=order)
         t = 0.0
         for _ in range(a.l1_steps):
             dt = f.time_step(cfl, dti, 0.0, t)

@@ -57,8 +57,16 @@ enum {
   RFGPU_BCOPT_SUPERSONIC = 0, RFGPU_BCOPT_SUBSONIC = 1, RFGPU_BCOPT_MIXED = 2,
   RFGPU_GAS_MODEL_TCPERF = 1, RFGPU_FLOW_EULER = 0,
   RFGPU_PREC_FP64 = 0,   /* everything FP64; bit-identical to the reference order */
-  RFGPU_PREC_MIXED = 1   /* FP32 prim/gradients/limiter/flux; FP64 geometry,
+  RFGPU_PREC_MIXED = 1,  /* FP32 prim/gradients/limiter/flux; FP64 geometry,
                             residual accumulation, RK update and EOS */
+  /* Device numbering.  LOCALITY: cells renumbered along a Morton curve of
+   * their centroids and interior faces grouped by their lower-numbered cell,
+   * so a block's stencil and face gathers stay within a compact patch of the
+   * mesh.  Every per-cell summation keeps the host's order (stencil members
+   * as stored, interior faces by ascending host index, then boundary faces),
+   * so results do not depend on this choice; arrays crossing the ABI are
+   * always in the host's numbering.  HOST: keep the host's numbering. */
+  RFGPU_ORDER_LOCALITY = 0, RFGPU_ORDER_HOST = 1
 };
 
 /* One boundary patch (modfloflu/ModBndPatch.F90:112-162). */
@@ -103,6 +111,7 @@ typedef struct {
   int precision;           /* RFGPU_PREC_* */
   int venkatGuard;         /* 0: limiter term exactly as the reference;
                               1: guard added with the sign of the denominator */
+  int cellOrder;           /* RFGPU_ORDER_*: device numbering of cells and faces */
 } rfgpu_region_desc_t;
 
 /* Register a region: copies and reorders the arrays to device-resident SoA.

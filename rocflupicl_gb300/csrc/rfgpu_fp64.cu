@@ -65,24 +65,29 @@ void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s) {
 
 namespace rfgpu {
 
-// Layout conversion between the Fortran image a(ncomp,N) and device SoA.
+// Layout conversion between the Fortran image a(ncomp,N), host numbering,
+// and device SoA in device numbering.  The loop runs over the host image, so
+// its side of the copy is coalesced.
 __global__ void k_aos_to_soa(const double *__restrict__ aos, double *__restrict__ soa, int N,
-                             int ncomp) {
+                             int ncomp, const int *__restrict__ cellNew) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)N * ncomp;
   for (; i < n; i += (long long)gridDim.x * blockDim.x) {
     long long c = i / ncomp, k = i - c * ncomp;
-    soa[k * N + c] = aos[i];
+    const long long cd = cellNew ? cellNew[c] : c;
+    soa[k * N + cd] = aos[i];
   }
 }
 
 template <typename T>
-__global__ void k_soa_to_aos(const T *__restrict__ soa, double *__restrict__ aos, int N, int ncomp) {
+__global__ void k_soa_to_aos(const T *__restrict__ soa, double *__restrict__ aos, int N, int ncomp,
+                             const int *__restrict__ cellNew) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)N * ncomp;
   for (; i < n; i += (long long)gridDim.x * blockDim.x) {
     long long c = i / ncomp, k = i - c * ncomp;
-    aos[i] = (double)soa[k * N + c];
+    const long long cd = cellNew ? cellNew[c] : c;
+    aos[i] = (double)soa[k * N + cd];
   }
 }
 
@@ -91,31 +96,34 @@ static unsigned nblk(long long n) {
   return (unsigned)(b > 65535LL * 16 ? 65535LL * 16 : (b < 1 ? 1 : b));
 }
 
-void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, cudaStream_t s) {
-  k_aos_to_soa<<<nblk((long long)N * ncomp), 256, 0, s>>>(aos, soa, N, ncomp);
+void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, const int *cellNew,
+                       cudaStream_t s) {
+  k_aos_to_soa<<<nblk((long long)N * ncomp), 256, 0, s>>>(aos, soa, N, ncomp, cellNew);
 }
-void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, cudaStream_t s) {
-  k_soa_to_aos<double><<<nblk((long long)N * ncomp), 256, 0, s>>>(soa, aos, N, ncomp);
-}
-void launch_soa_to_aos_f32(const float *soa, double *aos, int N, int ncomp, cudaStream_t s) {
-  k_soa_to_aos<float><<<nblk((long long)N * ncomp), 256, 0, s>>>(soa, aos, N, ncomp);
+void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, const int *cellNew,
+                       cudaStream_t s) {
+  k_soa_to_aos<double><<<nblk((long long)N * ncomp), 256, 0, s>>>(soa, aos, N, ncomp, cellNew);
 }
 
 template <typename T>
-__global__ void k_grad_export(const T *__restrict__ g16, double *__restrict__ out, int N) {
+__global__ void k_grad_export(const T *__restrict__ g16, double *__restrict__ out, int N,
+                              const int *__restrict__ cellNew) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   long long n = (long long)N * 15;
   for (; i < n; i += (long long)gridDim.x * blockDim.x) {
     long long c = i / 15, k = i - c * 15;
-    out[i] = (double)g16[16 * c + k];
+    const long long cd = cellNew ? cellNew[c] : c;
+    out[i] = (double)g16[16 * cd + k];
   }
 }
 
-void launch_grad_export(const double *g16, double *out, int N, cudaStream_t s) {
-  k_grad_export<double><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N);
+void launch_grad_export(const double *g16, double *out, int N, const int *cellNew,
+                        cudaStream_t s) {
+  k_grad_export<double><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N, cellNew);
 }
-void launch_grad_export_f32(const float *g16, double *out, int N, cudaStream_t s) {
-  k_grad_export<float><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N);
+void launch_grad_export_f32(const float *g16, double *out, int N, const int *cellNew,
+                            cudaStream_t s) {
+  k_grad_export<float><<<nblk((long long)N * 15), 256, 0, s>>>(g16, out, N, cellNew);
 }
 
 }  // namespace rfgpu

@@ -128,6 +128,7 @@ struct rfgpu_region_s {
   ProfState prof;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   int maxStW = 0;
+  const int *cellNew = nullptr, *cellOld = nullptr;  // device numbering (null: host's)
 };
 
 struct rfgpu_batch_s {
@@ -187,6 +188,8 @@ int check_desc(const rfgpu_region_desc_t *d) {
     return RFGPU_ERR_UNSUPPORTED;
   if (d->rkScheme < 1 || d->rkScheme > 3) return RFGPU_ERR_UNSUPPORTED;
   if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED) return RFGPU_ERR_UNSUPPORTED;
+  if (d->cellOrder != RFGPU_ORDER_LOCALITY && d->cellOrder != RFGPU_ORDER_HOST)
+    return RFGPU_ERR_UNSUPPORTED;
   for (int ip = 0; ip < d->nPatches; ++ip) {
     const rfgpu_patch_t &p = d->patches[ip];
     if (p.nBFaces < 0 || (p.nBFaces > 0 && (!p.bf2c || !p.fn || !p.fc))) return RFGPU_ERR_ARG;
@@ -230,9 +233,116 @@ RegionDev<double> &rd<double>(rfgpu_region_s *h) { return h->rd64; }
 template <>
 RegionDev<float> &rd<float>(rfgpu_region_s *h) { return h->rd32; }
 
-// Fill device arrays of precision R.
+// Device numbering of cells and interior faces.  Empty maps: the host's.
+struct Order {
+  std::vector<int> cOld, cNew;  // device cell -> host cell, host cell -> device cell
+  std::vector<int> fOld, fNew;  // the same for interior faces
+  int oc(int c) const { return cOld.empty() ? c : cOld[c]; }
+  int nc(int c) const { return cNew.empty() ? c : cNew[c]; }
+  int of(int f) const { return fOld.empty() ? f : fOld[f]; }
+  int nf(int f) const { return fNew.empty() ? f : fNew[f]; }
+};
+
+// Interleave the low 21 bits of v with two zero bits between each.
+unsigned long long spread3(unsigned long long v) {
+  v &= 0x1fffffull;
+  v = (v | v << 32) & 0x1f00000000ffffull;
+  v = (v | v << 16) & 0x1f0000ff0000ffull;
+  v = (v | v << 8) & 0x100f00f00f00f00full;
+  v = (v | v << 4) & 0x10c30c30c30c30c3ull;
+  v = (v | v << 2) & 0x1249249249249249ull;
+  return v;
+}
+
+// Locality numbering.  Cells: ascending 63-bit Morton key of the centroid
+// (one scale for all three axes, so the curve follows physical distance),
+// ties by host index, by a stable LSD radix sort (6 passes of 11 bits).
+// Interior faces: grouped by their lower device cell, ascending, then by the
+// higher one (a counting sort on the lower cell, short runs sorted in place).
+Order locality_order(const rfgpu_region_desc_t *d) {
+  Order o;
+  const int N = d->nCells, F = d->nFaces;
+  double lo[3], hi[3];
+  for (int k = 0; k < 3; ++k) lo[k] = hi[k] = d->cofg[k];
+  for (int c = 0; c < N; ++c)
+    for (int k = 0; k < 3; ++k) {
+      const double x = d->cofg[3 * (size_t)c + k];
+      lo[k] = x < lo[k] ? x : lo[k];
+      hi[k] = x > hi[k] ? x : hi[k];
+    }
+  double ext = 0.0;
+  for (int k = 0; k < 3; ++k) ext = hi[k] - lo[k] > ext ? hi[k] - lo[k] : ext;
+  const double scale = ext > 0.0 ? 2097151.0 / ext : 0.0;
+  std::vector<unsigned long long> key(N), key2(N);
+  std::vector<int> idx(N), idx2(N);
+  for (int c = 0; c < N; ++c) {
+    unsigned long long m = 0;
+    for (int k = 0; k < 3; ++k) {
+      double q = (d->cofg[3 * (size_t)c + k] - lo[k]) * scale;
+      q = q < 0.0 ? 0.0 : (q > 2097151.0 ? 2097151.0 : q);
+      m |= spread3((unsigned long long)q) << k;
+    }
+    key[c] = m;
+    idx[c] = c;
+  }
+  std::vector<int> count(2048);
+  for (int pass = 0; pass < 6; ++pass) {
+    const int sh = 11 * pass;
+    std::fill(count.begin(), count.end(), 0);
+    for (int i = 0; i < N; ++i) count[(key[i] >> sh) & 2047]++;
+    int run = 0;
+    for (int b = 0; b < 2048; ++b) {
+      const int t = count[b];
+      count[b] = run;
+      run += t;
+    }
+    for (int i = 0; i < N; ++i) {
+      const int dst = count[(key[i] >> sh) & 2047]++;
+      key2[dst] = key[i];
+      idx2[dst] = idx[i];
+    }
+    key.swap(key2);
+    idx.swap(idx2);
+  }
+  o.cOld = idx;
+  o.cNew.assign(N, 0);
+  for (int i = 0; i < N; ++i) o.cNew[o.cOld[i]] = i;
+  // faces
+  std::vector<int> lowOf(F), highOf(F), start(N + 1, 0);
+  for (int f = 0; f < F; ++f) {
+    const int a = o.cNew[d->f2c[(long long)f * d->f2cLd] - 1];
+    const int b = o.cNew[d->f2c[(long long)f * d->f2cLd + 1] - 1];
+    lowOf[f] = a < b ? a : b;
+    highOf[f] = a < b ? b : a;
+    start[lowOf[f] + 1]++;
+  }
+  for (int c = 0; c < N; ++c) start[c + 1] += start[c];
+  o.fOld.assign(F, 0);
+  {
+    std::vector<int> fill(start.begin(), start.end() - 1);
+    for (int f = 0; f < F; ++f) o.fOld[fill[lowOf[f]]++] = f;
+  }
+  for (int c = 0; c < N; ++c) {
+    // insertion sort of the run by the higher cell, ties by host index
+    for (int i = start[c] + 1; i < start[c + 1]; ++i) {
+      const int f = o.fOld[i];
+      int j = i - 1;
+      while (j >= start[c] && (highOf[o.fOld[j]] > highOf[f] ||
+                               (highOf[o.fOld[j]] == highOf[f] && o.fOld[j] > f))) {
+        o.fOld[j + 1] = o.fOld[j];
+        --j;
+      }
+      o.fOld[j + 1] = f;
+    }
+  }
+  o.fNew.assign(F, 0);
+  for (int i = 0; i < F; ++i) o.fNew[o.fOld[i]] = i;
+  return o;
+}
+
+// Fill device arrays of precision R, in the device numbering o.
 template <typename R>
-void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &ph) {
+void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &ph, const Order &o) {
   cudaStream_t s = h->stream;
   DevAlloc &M = h->mem;
   const int N = d->nCells, F = d->nFaces;
@@ -243,12 +353,13 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   // ---- cells
   std::vector<double> cofg(3 * (size_t)N), vol(N), epsq(N), moms(6 * (size_t)N);
   for (int c = 0; c < N; ++c) {
-    for (int k = 0; k < 3; ++k) cofg[(size_t)k * N + c] = d->cofg[3 * (size_t)c + k];
-    vol[c] = d->vol[c];
+    const size_t oc = (size_t)o.oc(c);
+    for (int k = 0; k < 3; ++k) cofg[(size_t)k * N + c] = d->cofg[3 * oc + k];
+    vol[c] = d->vol[oc];
     // eps^2 = (K*vol^(1/3))^3, K = 1 (modflu/RFLU_ModLimiters.F90:386,459-462)
-    double ds = std::pow(d->vol[c], 1.0 / 3.0);
+    double ds = std::pow(d->vol[oc], 1.0 / 3.0);
     epsq[c] = ds * ds * ds;
-    for (int k = 0; k < 6; ++k) moms[(size_t)k * N + c] = d->xyzMoms[10 * (size_t)c + k];
+    for (int k = 0; k < 6; ++k) moms[(size_t)k * N + c] = d->xyzMoms[10 * oc + k];
   }
   g.vol = M.upload(vol, s);
   {
@@ -257,34 +368,38 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.ivolF = M.upload(iv, s);
   }
   g.epsq = M.upload(cast<R>(epsq), s);
-  // WLSQ factor terms for the mixed path's on-the-fly weights
-  // (RFLU_ModDifferentiationCells.F90:1029-1042)
+  // Mixed path: the WLSQ weight of a member is A d / |d|^2, A the symmetric
+  // matrix of the cell's factor terms (RFLU_ModDifferentiationCells.F90:
+  // 1029-1042, 1064-1076 expanded): cwt = Axx, Axy, Axz, Ayy, Ayz, Azz
   if (sizeof(R) == 4) {
     std::vector<double> cw(6 * (size_t)N);
     for (int c = 0; c < N; ++c) {
-      const double *mo = d->xyzMoms + 10 * (size_t)c;
+      const double *mo = d->xyzMoms + 10 * (size_t)o.oc(c);
       double c11 = 1.0 / mo[0], c22 = 1.0 / mo[2], c33 = 1.0 / mo[5];
       double c12 = -c11 * mo[1];
       double c13 = -(c11 * mo[3] + c12 * c22 * mo[4]);
       double c23 = -c22 * mo[4];
-      cw[c] = c12;
-      cw[(size_t)N + c] = c13;
-      cw[2 * (size_t)N + c] = c23;
-      cw[3 * (size_t)N + c] = c11 * c11;
-      cw[4 * (size_t)N + c] = c22 * c22;
-      cw[5 * (size_t)N + c] = c33 * c33;
+      const double q1 = c11 * c11, q2 = c22 * c22, q3 = c33 * c33;
+      cw[c] = q1 + c12 * c12 * q2 + c13 * c13 * q3;
+      cw[(size_t)N + c] = c12 * q2 + c13 * c23 * q3;
+      cw[2 * (size_t)N + c] = c13 * q3;
+      cw[3 * (size_t)N + c] = q2 + c23 * c23 * q3;
+      cw[4 * (size_t)N + c] = c23 * q3;
+      cw[5 * (size_t)N + c] = q3;
     }
     g.cwt = M.upload(cast<R>(cw), s);
   }
   // ---- stencil SELL
   {
     std::vector<int> cnt(N);
-    for (int c = 0; c < N; ++c) cnt[c] = d->c2csOffsets[c + 1] - d->c2csOffsets[c];
+    for (int c = 0; c < N; ++c) cnt[c] = d->c2csOffsets[o.oc(c) + 1] - d->c2csOffsets[o.oc(c)];
     Sell sl;
     sl.build(cnt);
     std::vector<int> idx(sl.total, 0);
-    for (int c = 0; c < N; ++c)
-      for (int k = 0; k < cnt[c]; ++k) idx[sl.at(c, k)] = d->c2csMembers[d->c2csOffsets[c] + k] - 1;
+    for (int c = 0; c < N; ++c) {
+      const int *mem = d->c2csMembers + d->c2csOffsets[o.oc(c)];
+      for (int k = 0; k < cnt[c]; ++k) idx[sl.at(c, k)] = o.nc(mem[k] - 1);  // stored order
+    }
     g.stOff = M.upload(sl.off, s);
     g.stCnt = M.upload(sl.cnt, s);
     g.stIdx = M.upload(idx, s);
@@ -306,14 +421,15 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   std::vector<int> f2c(2 * (size_t)F);
   std::vector<double> fnA(4 * (size_t)F), fdl(3 * (size_t)F), fdr(3 * (size_t)F);
   for (int f = 0; f < F; ++f) {
-    int c1 = d->f2c[(long long)f * d->f2cLd] - 1, c2 = d->f2c[(long long)f * d->f2cLd + 1] - 1;
+    const long long of = o.of(f);
+    int c1 = o.nc(d->f2c[of * d->f2cLd] - 1), c2 = o.nc(d->f2c[of * d->f2cLd + 1] - 1);
     f2c[f] = c1;
     f2c[(size_t)F + f] = c2;
-    for (int k = 0; k < 4; ++k) fnA[4 * (size_t)f + k] = d->fn[4 * (size_t)f + k];
+    for (int k = 0; k < 4; ++k) fnA[4 * (size_t)f + k] = d->fn[4 * of + k];
     for (int k = 0; k < 3; ++k) {
-      double xc = d->fc[3 * (size_t)f + k];
-      fdl[(size_t)k * F + f] = xc - d->cofg[3 * (size_t)c1 + k];
-      fdr[(size_t)k * F + f] = xc - d->cofg[3 * (size_t)c2 + k];
+      double xc = d->fc[3 * of + k];
+      fdl[(size_t)k * F + f] = xc - cofg[(size_t)k * N + c1];
+      fdr[(size_t)k * F + f] = xc - cofg[(size_t)k * N + c2];
     }
   }
   g.f2c = M.upload(f2c, s);
@@ -328,14 +444,14 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     const rfgpu_patch_t &p = d->patches[ip];
     int type = p.bcType == RFGPU_BC_SLIPWALL ? BK_SLIP : BK_OUTFLOW;
     for (int b = 0; b < p.nBFaces; ++b) {
-      int c = p.bf2c[b] - 1;
+      int c = o.nc(p.bf2c[b] - 1);
       bf2c.push_back(c);
       bkind.push_back(bk_pack(type, p.spaceOrder, type == BK_OUTFLOW ? p.bcOptType : 0));
       double pout = 0.0;
       if (type == BK_OUTFLOW && p.bcOptType != RFGPU_BCOPT_SUPERSONIC) pout = p.vals[p.distrib ? b : 0];
       bpout.push_back(pout);
       for (int k = 0; k < 4; ++k) bfnA.push_back(p.fn[4 * (size_t)b + k]);
-      for (int k = 0; k < 3; ++k) bfdA.push_back(p.fc[3 * (size_t)b + k] - d->cofg[3 * (size_t)c + k]);
+      for (int k = 0; k < 3; ++k) bfdA.push_back(p.fc[3 * (size_t)b + k] - cofg[(size_t)k * N + c]);
     }
   }
   const int B = (int)bf2c.size();
@@ -362,7 +478,8 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     std::vector<int> code(sl.total, 0), nb(sl.total, -1);
     std::vector<double> cd(3 * (size_t)sl.total, 0.0);
     std::vector<int> fill(N, 0);
-    for (int f = 0; f < F; ++f) {
+    for (int fh = 0; fh < F; ++fh) {  // host face order: the reference's accumulation order
+      const int f = o.nf(fh);
       for (int side = 0; side < 2; ++side) {
         int c = f2c[(size_t)side * F + f];
         long long e = sl.at(c, fill[c]++);
@@ -399,7 +516,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   {
     std::vector<double> recx(8 * (size_t)N, 0.0);  // centroid slots; state filled by k_prim
     for (int c = 0; c < N; ++c)
-      for (int k = 0; k < 3; ++k) recx[8 * (size_t)c + 5 + k] = d->cofg[3 * (size_t)c + k];
+      for (int k = 0; k < 3; ++k) recx[8 * (size_t)c + 5 + k] = cofg[(size_t)k * N + c];
     g.rec = M.upload(cast<R>(recx), s);
   }
   g.grad = M.alloc<R>(16 * (size_t)N);
@@ -411,6 +528,12 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   cudaMemsetAsync(g.scal, 0, 8 * sizeof(double), s);
   g.status = M.alloc<unsigned>(1);
   cudaMemsetAsync(g.status, 0, sizeof(unsigned), s);
+  if (!o.cOld.empty()) {
+    g.cellNew = M.upload(o.cNew, s);
+    g.cellOld = M.upload(o.cOld, s);
+  }
+  h->cellNew = g.cellNew;
+  h->cellOld = g.cellOld;
   h->nBFaces = B;
   rd<R>(h) = g;
   RegionDev<R> *dregs = M.alloc<RegionDev<R>>(1);
@@ -431,11 +554,11 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
   double *ddv = h->prec ? h->rd32.dv : h->rd64.dv;
   if (cudaMemcpyAsync(h->stage, cv, 5 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
     return RFGPU_ERR_CUDA;
-  launch_aos_to_soa(h->stage, dcv, N, 5, s);
+  launch_aos_to_soa(h->stage, dcv, N, 5, h->cellNew, s);
   if (dv) {
     if (cudaMemcpyAsync(h->stage, dv, 3 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
       return RFGPU_ERR_CUDA;
-    launch_aos_to_soa(h->stage, ddv, N, 3, s);
+    launch_aos_to_soa(h->stage, ddv, N, 3, h->cellNew, s);
   }
   if (h->prec)
     launch_prim<float>(regs_of<float>(h), h->work, dv ? 0 : 1, s);
@@ -518,10 +641,11 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   for (int i = 0; i < 5; ++i) ph.grkF[i] = (float)ph.grk[i];
   h->nSteps = ph.nSteps;
   try {
+    const Order order = d->cellOrder == RFGPU_ORDER_LOCALITY ? locality_order(d) : Order{};
     if (h->prec)
-      build_region<float>(h, d, ph);
+      build_region<float>(h, d, ph, order);
     else
-      build_region<double>(h, d, ph);
+      build_region<double>(h, d, ph, order);
     const int block = 128;
     auto ct = make_tiles(0, h->nCells, block);
     auto ft = make_tiles(0, h->nFaces, block);
@@ -629,7 +753,7 @@ int rfgpu_residual(rfgpu_region_t h, double *rhs) {
   if (!rhs) return cuda_rc(cudaGetLastError());
   const int N = h->nCells;
   double *drhs = h->prec ? h->rd32.rhs : h->rd64.rhs;
-  launch_soa_to_aos(drhs, h->stage, N, 5, h->stream);
+  launch_soa_to_aos(drhs, h->stage, N, 5, h->cellNew, h->stream);
   h->launches++;
   if (cudaMemcpyAsync(rhs, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
     return RFGPU_ERR_CUDA;
@@ -640,7 +764,7 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (!h) return RFGPU_ERR_ARG;
   const int N = h->nCells;
   if (cv) {
-    launch_soa_to_aos(h->prec ? h->rd32.cv : h->rd64.cv, h->stage, N, 5, h->stream);
+    launch_soa_to_aos(h->prec ? h->rd32.cv : h->rd64.cv, h->stage, N, 5, h->cellNew, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(cv, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
       return RFGPU_ERR_CUDA;
@@ -652,7 +776,7 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
       launch_dv_complete<float>(regs_of<float>(h), h->work, h->stream);
       h->launches++;
     }
-    launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->stream);
+    launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->cellNew, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(dv, h->stage, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
       return RFGPU_ERR_CUDA;
@@ -673,9 +797,9 @@ int rfgpu_download_grad(rfgpu_region_t h, double *grad) {
   double *tmp = nullptr;
   if (cudaMalloc(&tmp, 15 * (size_t)N * 8) != cudaSuccess) return RFGPU_ERR_NOMEM;
   if (h->prec)
-    launch_grad_export_f32(h->rd32.grad, tmp, N, h->stream);
+    launch_grad_export_f32(h->rd32.grad, tmp, N, h->cellNew, h->stream);
   else
-    launch_grad_export(h->rd64.grad, tmp, N, h->stream);
+    launch_grad_export(h->rd64.grad, tmp, N, h->cellNew, h->stream);
   h->launches++;
   cudaError_t e = cudaMemcpyAsync(grad, tmp, 15 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(h->stream);

@@ -19,6 +19,9 @@
 //   faces        f2c[2][F], fnA[F][4] (normal, area), fdl/fdr[3][F] = fc - cofg(c1/c2)
 //   boundary     bf2c[B], bfnA[B][4], bfd[3][B], bkind[B], bpout[B]
 //   scratch      flux[F][8], bflux[B][8] (R, 5 used)
+// Cells and faces are in the device numbering (the host's, or a locality
+// order chosen at registration, cellNew/cellOld); the face indices stored in
+// the cell->face lists keep each cell's host summation order.
 // R is double on the FP64 path and float on the mixed path.
 #pragma once
 
@@ -59,7 +62,7 @@ struct RegionDev {
   const double *vol;
   const float *ivolF;  // 1/vol in FP32 (mixed-path update)
   const R *epsq;
-  const R *cwt;   // [6][N] c12,c13,c23,c11^2,c22^2,c33^2 of the WLSQ factor (mixed path)
+  const R *cwt;   // [6][N] Axx,Axy,Axz,Ayy,Ayz,Azz: weight = A d/|d|^2 (mixed path)
   // stencil (SELL-32)
   const long long *stOff;
   const int *stCnt, *stIdx;
@@ -87,6 +90,9 @@ struct RegionDev {
   double *scal;   // [0] dtMin, [1] current time, [2] dtMin of the previous step,
                   // [3..7] ark(1..5)*dtMin of the current step
   unsigned *status;
+  // device numbering (null when it is the host's): cellNew[hostCell],
+  // cellOld[deviceCell]
+  const int *cellNew, *cellOld;
   Phys ph;
 };
 
@@ -146,7 +152,7 @@ void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s)
 template <typename R>
 int configure_grad_smem(int maxW, int block);
 // Residual with the face fluxes and the result in caller-supplied scratch
-// (used by rfgpu_residual_noalloc): rhs in the Fortran layout rhs(5,nCells).
+// (used by rfgpu_residual_noalloc): rhs in the Fortran layout rhs(5,nCells), host numbering.
 template <typename R>
 void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
                              int spaceOrder, R *flux, double *rhs, cudaStream_t s);
@@ -171,12 +177,16 @@ void launch_weights64(const long long *stOff, const int *stCnt, const int *stIdx
                       const double *cofg, const double *moms, double *w64, cudaStream_t s,
                       long long stTotal);
 void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s);
-// Fortran image a(ncomp,N) <-> SoA [ncomp][N]
-void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, cudaStream_t s);
-void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, cudaStream_t s);
-void launch_soa_to_aos_f32(const float *soa, double *aos, int N, int ncomp, cudaStream_t s);
-// grad[N][16] -> grad(3,5,N) Fortran image in FP64
-void launch_grad_export(const double *g16, double *out, int N, cudaStream_t s);
-void launch_grad_export_f32(const float *g16, double *out, int N, cudaStream_t s);
+// Fortran image a(ncomp,N) in host numbering <-> SoA [ncomp][N] in device
+// numbering; cellNew maps a host cell to its device cell (null: identity)
+void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, const int *cellNew,
+                       cudaStream_t s);
+void launch_soa_to_aos(const double *soa, double *aos, int N, int ncomp, const int *cellNew,
+                       cudaStream_t s);
+// grad[N][16] -> grad(3,5,N) Fortran image in FP64, host numbering
+void launch_grad_export(const double *g16, double *out, int N, const int *cellNew,
+                        cudaStream_t s);
+void launch_grad_export_f32(const float *g16, double *out, int N, const int *cellNew,
+                            cudaStream_t s);
 
 }  // namespace rfgpu

@@ -213,33 +213,57 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 }
 
 // ---- vector access to AoS records --------------------------------------------
+// Records are 32-byte aligned, so one record row of 8 floats (or 4 doubles) is
+// a single 256-bit access: one request per warp touching each 32-byte sector
+// once, where two 128-bit halves would issue two requests over the same
+// sectors.  ld8/ld4 read through the non-coherent path and are for data no
+// thread writes during the kernel; ld8_rw is the coherent form for a thread's
+// own record that the same kernel rewrites.
 __device__ __forceinline__ void ld8(const float *__restrict__ p, float v[8]) {
-  float4 a = *reinterpret_cast<const float4 *>(p), b = *reinterpret_cast<const float4 *>(p + 4);
-  v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+  asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+      : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
+        "=f"(v[7])
+      : "l"(p));
+}
+__device__ __forceinline__ void ld4(const double *__restrict__ p, double v[4]) {
+  asm("ld.global.nc.v4.f64 {%0,%1,%2,%3}, [%4];"
+      : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3])
+      : "l"(p));
 }
 __device__ __forceinline__ void ld8(const double *__restrict__ p, double v[8]) {
+  ld4(p, v);
+  ld4(p + 4, v + 4);
+}
+__device__ __forceinline__ void ld8_rw(const float *p, float v[8]) {
+  asm volatile("ld.global.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+               : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]),
+                 "=f"(v[6]), "=f"(v[7])
+               : "l"(p)
+               : "memory");
+}
+__device__ __forceinline__ void ld8_rw(const double *p, double v[8]) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    double2 a = reinterpret_cast<const double2 *>(p)[i];
-    v[2 * i] = a.x;
-    v[2 * i + 1] = a.y;
-  }
+  for (int i = 0; i < 2; ++i)
+    asm volatile("ld.global.v4.f64 {%0,%1,%2,%3}, [%4];"
+                 : "=d"(v[4 * i]), "=d"(v[4 * i + 1]), "=d"(v[4 * i + 2]), "=d"(v[4 * i + 3])
+                 : "l"(p + 4 * i)
+                 : "memory");
 }
 __device__ __forceinline__ void ld4(const float *__restrict__ p, float v[4]) {
   float4 a = *reinterpret_cast<const float4 *>(p);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
 }
-__device__ __forceinline__ void ld4(const double *__restrict__ p, double v[4]) {
-  double2 a = reinterpret_cast<const double2 *>(p)[0], b = reinterpret_cast<const double2 *>(p)[1];
-  v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y;
-}
 __device__ __forceinline__ void st8(float *p, const float v[8]) {
-  *reinterpret_cast<float4 *>(p) = make_float4(v[0], v[1], v[2], v[3]);
-  *reinterpret_cast<float4 *>(p + 4) = make_float4(v[4], v[5], v[6], v[7]);
+  asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]),
+               "f"(v[2]), "f"(v[3]), "f"(v[4]), "f"(v[5]), "f"(v[6]), "f"(v[7])
+               : "memory");
 }
 __device__ __forceinline__ void st8(double *p, const double v[8]) {
 #pragma unroll
-  for (int i = 0; i < 4; ++i) reinterpret_cast<double2 *>(p)[i] = make_double2(v[2 * i], v[2 * i + 1]);
+  for (int i = 0; i < 2; ++i)
+    asm volatile("st.global.v4.f64 [%0], {%1,%2,%3,%4};" ::"l"(p + 4 * i), "d"(v[4 * i]),
+                 "d"(v[4 * i + 1]), "d"(v[4 * i + 2]), "d"(v[4 * i + 3])
+                 : "memory");
 }
 template <typename R>
 __device__ __forceinline__ void ld16(const R *__restrict__ p, R v[16]) {
@@ -337,7 +361,7 @@ __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__rest
       g.dv[2 * N + c] = sqrt(gg * gc * T);
     }
     R r[8];
-    ld8(g.rec + 8 * (size_t)c, r);
+    ld8_rw(g.rec + 8 * (size_t)c, r);
     r[0] = R(q0);
     r[1] = R(ir * q1);
     r[2] = R(ir * q2);
@@ -432,8 +456,14 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 // (bitwise the reference's); mixed path: weights rebuilt in FP32 from the
 // records' centroids and the cell's WLSQ factor terms.  With fuseDt the pass
 // also reduces the time step (stage 1 of a step).
+#ifndef RF_GRAD_UNROLL
+#define RF_GRAD_UNROLL 4   // record gathers issued together (mixed path)
+#endif
+#ifndef RF_GRAD_MINB
+#define RF_GRAD_MINB 8     // resident 128-thread blocks per SM (mixed path)
+#endif
 template <typename R>
-__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? 8 : 4) k_grad_lim(const RegionDev<R> *__restrict__ regs,
+__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? RF_GRAD_MINB : 4) k_grad_lim(const RegionDev<R> *__restrict__ regs,
                                                   const Tile *__restrict__ tiles, int nTiles,
                                                   int maxW, int fuseDt) {
   __shared__ unsigned long long smin[32];
@@ -483,44 +513,49 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? 8 : 4) k_grad_lim(cons
           member(ra, base + (long long)k * kSlice);
         }
       } else {
-        const R c12 = g.cwt[c], c13 = g.cwt[N + c], c23 = g.cwt[2 * N + c];
-        const R c1111 = g.cwt[3 * N + c], c2222 = g.cwt[4 * N + c], c3333 = g.cwt[5 * N + c];
+        // The reference's weight of member m is w = A d/|d|^2 with d the
+        // centroid offset and A the cell's symmetric inverse-moment matrix
+        // built from its WLSQ factor (c11^2 + c12^2 c22^2 + c13^2 c33^2, ...).
+        // A is the same for every member, so the member loop accumulates
+        // S_v = sum (q_v,m - q_v,0) d/|d|^2 and the gradient is A S_v: the
+        // reference's sum reassociated, about a quarter fewer operations per
+        // member.
         auto member = [&](const R rn[8]) {
           R dx = rn[5] - r0[5], dy = rn[6] - r0[6], dz = rn[7] - r0[7];
-          R term = rsqrtf(float(dx * dx + dy * dy + dz * dz));
-          dx = term * dx;
-          dy = term * dy;
-          dz = term * dz;
-          R term1 = c1111 * dx;
-          R term2 = c2222 * (dy + c12 * dx);
-          R term3 = c3333 * (dz + c23 * dy + c13 * dx);
-          R wx = term * (term1 + c12 * term2 + c13 * term3);
-          R wy = term * (term2 + c23 * term3);
-          R wz = term * term3;
+          R t = rsqrtf(float(dx * dx + dy * dy + dz * dz));
+          t = t * t;
+          dx = t * dx;
+          dy = t * dy;
+          dz = t * dz;
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             R dVar = rn[v] - r0[v];
-            acc[3 * v] = acc[3 * v] + wx * dVar;
-            acc[3 * v + 1] = acc[3 * v + 1] + wy * dVar;
-            acc[3 * v + 2] = acc[3 * v + 2] + wz * dVar;
+            acc[3 * v] = acc[3 * v] + dx * dVar;
+            acc[3 * v + 1] = acc[3 * v + 1] + dy * dVar;
+            acc[3 * v + 2] = acc[3 * v + 2] + dz * dVar;
           }
         };
         int k = 0;
-        for (; k + 4 <= n; k += 4) {
-          R ra[8], rb[8], rc[8], rd[8];
-          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
-          ld8(rec + 8 * (size_t)sidx[(k + 1) * kSlice], rb);
-          ld8(rec + 8 * (size_t)sidx[(k + 2) * kSlice], rc);
-          ld8(rec + 8 * (size_t)sidx[(k + 3) * kSlice], rd);
-          member(ra);
-          member(rb);
-          member(rc);
-          member(rd);
+        for (; k + RF_GRAD_UNROLL <= n; k += RF_GRAD_UNROLL) {
+          R ra[RF_GRAD_UNROLL][8];
+#pragma unroll
+          for (int u = 0; u < RF_GRAD_UNROLL; ++u) ld8(rec + 8 * (size_t)sidx[(k + u) * kSlice], ra[u]);
+#pragma unroll
+          for (int u = 0; u < RF_GRAD_UNROLL; ++u) member(ra[u]);
         }
         for (; k < n; ++k) {
           R ra[8];
           ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
           member(ra);
+        }
+        const R axx = g.cwt[c], axy = g.cwt[N + c], axz = g.cwt[2 * N + c];
+        const R ayy = g.cwt[3 * N + c], ayz = g.cwt[4 * N + c], azz = g.cwt[5 * N + c];
+#pragma unroll
+        for (int v = 0; v < 5; ++v) {
+          const R sx = acc[3 * v], sy = acc[3 * v + 1], sz = acc[3 * v + 2];
+          acc[3 * v] = axx * sx + axy * sy + axz * sz;
+          acc[3 * v + 1] = axy * sx + ayy * sy + ayz * sz;
+          acc[3 * v + 2] = axz * sx + ayz * sy + azz * sz;
         }
       }
       if (g.ph.reconst == 11) {
@@ -802,7 +837,7 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
     for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
 #pragma unroll
     for (int j = 0; j < 5; ++j) rsOld[j] = (is > 1) ? g.rhsSumF[j * N + c] : 0.f;
-    ld8(g.rec + 8 * (size_t)c, r);
+    ld8_rw(g.rec + 8 * (size_t)c, r);
     ivol = g.ivolF[c];
   }
   float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
@@ -1024,7 +1059,7 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
     g.dv[2 * N + c] = d[2];
     const double ir = 1.0 / q[0];
     R r[8];
-    ld8(g.rec + 8 * (size_t)c, r);
+    ld8_rw(g.rec + 8 * (size_t)c, r);
     r[0] = R(q[0]);
     r[1] = R(ir * q[1]);
     r[2] = R(ir * q[2]);
@@ -1250,6 +1285,7 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
   if (c >= g.nCells) return;
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
+  const size_t hc = g.cellOld ? (size_t)g.cellOld[c] : (size_t)c;  // host numbering
   if constexpr (sizeof(R) == 8) {
     double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
     for (int k = 0; k < n; ++k) {
@@ -1271,7 +1307,7 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
       }
     }
 #pragma unroll
-    for (int j = 0; j < 5; ++j) rhs[5 * (size_t)c + j] = acc[j];
+    for (int j = 0; j < 5; ++j) rhs[5 * hc + j] = acc[j];
   } else {
     float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int k = 0; k < n; ++k) {
@@ -1289,7 +1325,7 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
       }
     }
 #pragma unroll
-    for (int j = 0; j < 5; ++j) rhs[5 * (size_t)c + j] = double(hi[j]) + double(lo[j]);
+    for (int j = 0; j < 5; ++j) rhs[5 * hc + j] = double(hi[j]) + double(lo[j]);
   }
 }
 

@@ -55,7 +55,12 @@ class RegionDescT(C.Structure):
                 ("spaceDiscr", C.c_int), ("spaceOrder", C.c_int), ("reconst", C.c_int),
                 ("rkScheme", C.c_int), ("refCp", C.c_double), ("refGamma", C.c_double),
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
-                ("dissFact", C.c_double), ("precision", C.c_int), ("venkatGuard", C.c_int)]
+                ("dissFact", C.c_double), ("precision", C.c_int), ("venkatGuard", C.c_int),
+                ("cellOrder", C.c_int)]
+
+
+# device numbering of cells and faces (rfgpu.h RFGPU_ORDER_*)
+ORDER_LOCALITY, ORDER_HOST = 0, 1
 
 
 SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_dt",
@@ -195,7 +200,8 @@ class PinnedArray:
 class Region:
     """One registered region on the GPU (device-resident state)."""
 
-    def __init__(self, case: Case, precision: Optional[int] = None):
+    def __init__(self, case: Case, precision: Optional[int] = None,
+                 cell_order: int = ORDER_LOCALITY):
         self.lib = load()
         m, num = case.mesh, case.numerics
         self.case = case
@@ -242,6 +248,7 @@ class Region:
         d.epsentr, d.dissFact = num.epsentr, num.dissFact
         d.precision = self.precision
         d.venkatGuard = num.venkatGuard
+        d.cellOrder = cell_order
         h = C.c_void_p()
         _check(self.lib.rfgpu_region_create(C.byref(d), C.byref(h)), "rfgpu_region_create")
         self.h = h

@@ -193,3 +193,24 @@ def test_unsupported_option_refused():
     with pytest.raises(E.EngineError) as ei:
         E.Region(c)
     assert ei.value.code == E.ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED])
+@pytest.mark.parametrize("kind", ["tube", "tet", "mixed"])
+def test_locality_order_equals_host_order(prec, kind):
+    """The engine's locality numbering changes where cells and faces live in
+    HBM, not any per-cell summation order: residual, gradients and a short
+    trajectory are bit-identical to the host numbering on both paths."""
+    c = make(kind, K.DISCR_UPW_ROE, precision=prec)
+    out = {}
+    for order in (E.ORDER_HOST, E.ORDER_LOCALITY):
+        r = E.Region(c, cell_order=order)
+        rhs = r.residual()
+        grad = r.gradients()
+        t, steps, st = r.solve(n_steps=4)
+        cv, dv = r.download()
+        out[order] = (rhs, grad, cv, dv, t, st)
+        r.close()
+    for a, b, what in zip(out[E.ORDER_LOCALITY], out[E.ORDER_HOST],
+                          ("rhs", "grad", "cv", "dv", "time", "status")):
+        assert_same(a, b, f"{what} (prec {prec})")
