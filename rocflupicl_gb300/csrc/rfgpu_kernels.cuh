@@ -332,6 +332,81 @@ __device__ __forceinline__ void venkat_term(R d2, R dmax, R dmin, R epsq, R &lim
 
 // ---- kernels ------------------------------------------------------------------
 
+// Bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes): one
+// instruction per contiguous range, issued by one lane.
+__device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
+  const size_t a = ((size_t)p + 15) & ~(size_t)15, e = ((size_t)p + bytes) & ~(size_t)15;
+  if (e > a)
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(a), "r"((unsigned)(e - a))
+                 : "memory");
+}
+
+// Tile prefetches.  The streamed index and geometry arrays a tile reads
+// (SELL slices of stencil members and cell->face lists, face tables, own-cell
+// rows) are pulled into L2 in bulk, so the block does not wait on DRAM for
+// each index before the gather it feeds can issue: the gradient pass at the
+// start of its own tile, the face and update passes one wave of blocks
+// ahead.  Lane 0 of each warp issues its 32-cell slice; thread 0 issues the
+// per-tile face rows.
+template <typename R>
+__device__ __forceinline__ void prefetch_grad_tile(const RegionDev<R> &g, int first, bool faces) {
+  if ((threadIdx.x & 31) != 0) return;
+  const int N = g.nCells;
+  const int sl = (first >> 5) + (threadIdx.x >> 5);
+  if (sl * kSlice >= N) return;
+  const long long s0 = g.stOff[sl], s1 = g.stOff[sl + 1];
+  prefetch_l2(g.stIdx + s0, (size_t)(s1 - s0) * sizeof(int));
+  if (sizeof(R) == 8)
+    for (int k = 0; k < 3; ++k) prefetch_l2(g.stW + k * g.stTotal + s0, (size_t)(s1 - s0) * sizeof(R));
+  if (faces) {
+    const long long f0 = g.cfOff[sl], f1 = g.cfOff[sl + 1];
+    const size_t nb = (size_t)(f1 - f0);
+    prefetch_l2(g.cfCode + f0, nb * sizeof(int));
+    prefetch_l2(g.cfNb + f0, nb * sizeof(int));
+    for (int k = 0; k < 3; ++k) prefetch_l2(g.cfD + k * g.cfTotal + f0, nb * sizeof(R));
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void prefetch_face_tile(const RegionDev<R> &g, int first) {
+  if (threadIdx.x != 0) return;
+  const int F = g.nFaces;
+  if (first >= F) return;
+  const size_t n = (size_t)(F - first < (int)blockDim.x ? F - first : (int)blockDim.x);
+  prefetch_l2(g.f2c + first, n * sizeof(int));
+  prefetch_l2(g.f2c + F + first, n * sizeof(int));
+  prefetch_l2(g.fnA + 4 * (size_t)first, n * 4 * sizeof(R));
+  for (int k = 0; k < 3; ++k) {
+    prefetch_l2(g.fdl + (size_t)k * F + first, n * sizeof(R));
+    prefetch_l2(g.fdr + (size_t)k * F + first, n * sizeof(R));
+  }
+}
+
+template <typename R>
+__device__ __forceinline__ void prefetch_update_tile(const RegionDev<R> &g, int first) {
+  if ((threadIdx.x & 31) != 0) return;
+  const int N = g.nCells;
+  const int sl = (first >> 5) + (threadIdx.x >> 5);
+  if (sl * kSlice >= N) return;
+  const long long f0 = g.cfOff[sl], f1 = g.cfOff[sl + 1];
+  prefetch_l2(g.cfCode + f0, (size_t)(f1 - f0) * sizeof(int));
+  const int c0 = sl * kSlice, nc = N - c0 < kSlice ? N - c0 : kSlice;
+  for (int j = 0; j < 5; ++j) prefetch_l2(g.cv + (size_t)j * N + c0, (size_t)nc * sizeof(double));
+  if (sizeof(R) == 4) {
+    for (int j = 0; j < 5; ++j) prefetch_l2(g.rhsSumF + (size_t)j * N + c0, (size_t)nc * sizeof(float));
+    prefetch_l2(g.ivolF + c0, (size_t)nc * sizeof(float));
+  }
+}
+
+// Calls pf(tile) for the tile a block works on now when it is in the first
+// wave, and for the tile `dist` ahead (the one a block of the next wave, or
+// this block in its next persistent iteration, will take).
+template <typename PF>
+__device__ __forceinline__ void prefetch_ahead(int t, int nTiles, int dist, PF pf) {
+  if (t < dist) pf(t);
+  if (t + dist < nTiles) pf(t + dist);
+}
+
 #define RF_TILE_LOOP(tiles, nTiles)                                   \
   for (int t_ = blockIdx.x; t_ < (nTiles); t_ += gridDim.x)
 
@@ -462,18 +537,23 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #ifndef RF_GRAD_MINB
 #define RF_GRAD_MINB 8     // resident 128-thread blocks per SM (mixed path)
 #endif
-template <typename R>
-__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? RF_GRAD_MINB : 4) k_grad_lim(const RegionDev<R> *__restrict__ regs,
-                                                  const Tile *__restrict__ tiles, int nTiles,
-                                                  int maxW, int fuseDt) {
+#ifndef RF_GRAD_MINB_DT
+#define RF_GRAD_MINB_DT 8  // the same for the stage-1 pass that also reduces the time step
+#endif
+template <typename R, int FUSE_DT>
+__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MINB_DT : RF_GRAD_MINB) : 4)
+    k_grad_lim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles, int nTiles) {
+  constexpr bool fuseDt = FUSE_DT != 0;
   __shared__ unsigned long long smin[32];
-  (void)maxW;
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     const bool valid = c < N;
+    // own tile only: prefetching a wave ahead measured slower here (the
+    // prefetched slices push the neighbour records the gathers reuse out of L2)
+    prefetch_grad_tile(g, tl.first, fuseDt || g.ph.reconst == 11);
     const long long base = valid ? g.stOff[c >> 5] + (c & 31) : 0;
     const int *__restrict__ sidx = g.stIdx + base;
     unsigned long long dtbits = 0x7FF0000000000000ull;
@@ -602,9 +682,9 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? RF_GRAD_MINB : 4) k_gr
       for (int k = 0; k < 15; ++k) out[k] = acc[k];
       out[15] = R(0);
       st16(g.grad + 16 * (size_t)c, out);
-      if (fuseDt) dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
+      if constexpr (fuseDt) dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
     }
-    if (fuseDt) dt_block_min<R>(dtbits, smin, g.dtBits);
+    if constexpr (fuseDt) dt_block_min<R>(dtbits, smin, g.dtBits);
   }
 }
 
@@ -612,10 +692,16 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? RF_GRAD_MINB : 4) k_gr
 // Roe :2646-2855, HLLC :2239-2409), written to the face flux buffer.
 template <typename R>
 __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restrict__ regs,
-                                                   const Tile *__restrict__ tiles, int nTiles) {
+                                                   const Tile *__restrict__ tiles, int nTiles,
+                                                   int pfDist) {
+  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
+    prefetch_ahead(t_, nTiles, dist, [&](int t) {
+      const Tile tp = tiles[t];
+      prefetch_face_tile(regs[tp.region], tp.first);
+    });
     const int f = tl.first + threadIdx.x;
     const int F = g.nFaces;
     if (f >= F) continue;
@@ -952,10 +1038,15 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
 template <typename R>
 __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__restrict__ regs,
                                                        const Tile *__restrict__ tiles,
-                                                       int nTiles, StepArgs a) {
+                                                       int nTiles, StepArgs a, int pfDist) {
+  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
+    prefetch_ahead(t_, nTiles, dist, [&](int t) {
+      const Tile tp = tiles[t];
+      prefetch_update_tile(regs[tp.region], tp.first);
+    });
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     if (c >= N) continue;
@@ -1150,17 +1241,32 @@ void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStr
 #define RF_MARK(kind, phase) \
   if (prof) prof->mark(prof->ctx, (kind), (phase), s)
 
+// Blocks of `kernel` (128 threads) resident on the whole device at once: the
+// prefetch distance in tiles.
+template <typename K>
+int resident_blocks(K kernel) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  return per > 0 && nsm > 0 ? per * nsm : 1;
+}
+
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof) {
+  static const int pfFace = resident_blocks(k_face_flux<R>);
+  static const int pfUpd = resident_blocks(k_gather_update<R>);
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   (void)reconst;
   long long n = 0;
   const bool grad = spaceOrder > 1 && w.nCellTiles > 0;
   if (grad) {
     RF_MARK(KP_GRADIENT, 0);
-    k_grad_lim<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles,
-                                                        w.maxStW, a.fuseDt);
+    if (a.fuseDt)
+      k_grad_lim<R, 1><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    else
+      k_grad_lim<R, 0><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
     RF_MARK(KP_GRADIENT, 1);
     ++n;
   }
@@ -1172,7 +1278,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   }
   if (w.nFaceTiles > 0) {
     RF_MARK(KP_FACE_FLUX, 0);
-    k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles);
+    k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles, pfFace);
     RF_MARK(KP_FACE_FLUX, 1);
     ++n;
   }
@@ -1184,7 +1290,8 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   }
   if (w.nCellTiles > 0) {
     RF_MARK(KP_GATHER_UPDATE, 0);
-    k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a);
+    k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a,
+                                                              pfUpd);
     RF_MARK(KP_GATHER_UPDATE, 1);
     ++n;
   }
@@ -1335,7 +1442,7 @@ template <typename R>
 void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
                              int spaceOrder, R *flux, double *rhs, cudaStream_t s) {
   if (spaceOrder > 1 && w.nCellTiles > 0)
-    k_grad_lim<R><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, w.maxStW, 0);
+    k_grad_lim<R, 0><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
   if (g.nFaces > 0) k_face_flux_scratch<R><<<(g.nFaces + 127) / 128, 128, 0, s>>>(g, flux);
   if (w.nBFaceTiles > 0)
     k_bface_flux<R><<<w.nBFaceTiles, w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
