@@ -510,6 +510,8 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   } else {
     g.rhsSumF = M.alloc<float>(5 * (size_t)N);
     cudaMemsetAsync(g.rhsSumF, 0, 5 * (size_t)N * sizeof(float), s);
+    g.cvF = M.alloc<float>(10 * (size_t)N);
+    if (ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL) g.cvOldF = M.alloc<float>(10 * (size_t)N);
   }
   g.dv = M.alloc<double>(3 * (size_t)N);
   g.rhs = M.alloc<double>(5 * (size_t)N);
@@ -560,11 +562,13 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
       return RFGPU_ERR_CUDA;
     launch_aos_to_soa(h->stage, ddv, N, 3, h->cellNew, s);
   }
-  if (h->prec)
+  if (h->prec) {
     launch_prim<float>(regs_of<float>(h), h->work, dv ? 0 : 1, s);
-  else
+    launch_state_split<float>(regs_of<float>(h), h->work, s);
+  } else {
     launch_prim<double>(regs_of<double>(h), h->work, dv ? 0 : 1, s);
-  h->launches += dv ? 3 : 2;
+  }
+  h->launches += (dv ? 3 : 2) + (h->prec ? 1 : 0);
   return cuda_rc(cudaGetLastError());
 }
 
@@ -763,6 +767,10 @@ int rfgpu_residual(rfgpu_region_t h, double *rhs) {
 int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (!h) return RFGPU_ERR_ARG;
   const int N = h->nCells;
+  if (h->prec && (cv || dv)) {  // mixed path: FP64 cv and dv from the float-float state
+    launch_state_join<float>(regs_of<float>(h), h->work, h->stream);
+    h->launches++;
+  }
   if (cv) {
     launch_soa_to_aos(h->prec ? h->rd32.cv : h->rd64.cv, h->stage, N, 5, h->cellNew, h->stream);
     h->launches++;
@@ -772,10 +780,6 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (dv) {
     // stage is reused: wait for the cv copy first
     if (cv && cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
-    if (h->prec) {  // mixed path: a stage writes only p; complete T and a
-      launch_dv_complete<float>(regs_of<float>(h), h->work, h->stream);
-      h->launches++;
-    }
     launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->cellNew, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(dv, h->stage, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)

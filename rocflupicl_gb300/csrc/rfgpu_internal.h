@@ -51,10 +51,13 @@ struct Phys {
 template <typename R>
 struct RegionDev {
   int nCells, nFaces, nBFaces, pad_;
-  // state (FP64 SoA); the mixed path keeps its RK increment history in FP32
-  // (rhsSumF) and writes only p of dv during a stage (T, a on download)
+  // state (FP64 SoA).  The mixed path advances its state as float-float
+  // pairs, cvF[2][5][N] (hi rows, then lo rows; the pair's sum carries about
+  // 48 significand bits) with the RK increment history in FP32 (rhsSumF);
+  // cv and dv are its FP64 exchange copies, filled on upload / download.
   double *cv, *cvOld, *rhsSum, *dv, *rhs;
   float *rhsSumF;
+  float *cvF, *cvOldF;
   // gathered per-cell records (AoS): rec[8*c..] = rho,u,v,w,p,x,y,z;
   // grad[16*c + 3*v + d] (15 used)
   R *rec, *grad;
@@ -147,8 +150,13 @@ struct Prof {
 // R = float (mixed unit).  `regs` is a device array of RegionDev<R>.
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
+// Mixed path: split the FP64 exchange copy cv into the float-float state
+// (after an upload) / join it back into cv and evaluate dv = p, T, a in FP64
+// (before a download).
 template <typename R>
-void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
+void launch_state_split(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
+template <typename R>
+void launch_state_join(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
 template <typename R>
 int configure_grad_smem(int maxW, int block);
 // Residual with the face fluxes and the result in caller-supplied scratch

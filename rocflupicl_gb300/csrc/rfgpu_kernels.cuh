@@ -899,28 +899,48 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float x) {
   lo += err;
 }
 
+// (hi, lo) - d for a float-float pair: TwoSum of hi and -d, the low part and
+// the rounding error added, then renormalised with TwoSum.  Additions only, so
+// no contraction into FMA can change it.
+__device__ __forceinline__ void ff_sub(float &hi, float &lo, float d) {
+  const float s = hi - d;
+  const float bb = s - hi;
+  const float e = (hi - (s - bb)) + (-d - bb);
+  const float t = lo + e;
+  const float h2 = s + t;
+  const float b2 = h2 - s;
+  lo = (s - (h2 - b2)) + (t - b2);
+  hi = h2;
+}
+
 // Mixed-path gather + update.  The FP32 face fluxes are summed with
 // compensated (TwoSum) accumulation, so the residual is the FP32-rounded exact
 // sum of the fluxes regardless of cancellation; the RK increment
-// dU = a*dt/V (rhs - g rhsSum) is formed in FP32 and applied to the FP64
-// conserved state, and the pressure is recovered in FP64 from
-// E - |m|^2/(2 rho), where cancellation at strong shocks needs it (1/rho: FP32
-// reciprocal refined by one FP64 Newton step).  Cells whose density or
-// pressure is not clearly positive take the exact FP64 checks of
-// AfterUpdateMP.  T and a of dv are completed on download.
+// dU = a*dt/V (rhs - g rhsSum) is formed in FP32 and subtracted from the
+// float-float conserved state exactly (ff_sub), so the state carries about 48
+// significand bits without FP64 arithmetic (GB300's FP64 rate is a small
+// fraction of its FP32 rate).  The pressure for the cell record is
+// (g-1)((E_hi - |m|^2/(2 rho)) + E_lo) in FP32: the total energy keeps its low
+// part and only the kinetic term is rounded.  Cells whose density or pressure
+// is not clearly positive take the exact FP64 checks of AfterUpdateMP on the
+// joined state.  dv (p, T, a) is evaluated in FP64 on download.
 __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, int c,
                                                     const StepArgs &a) {
   const int N = g.nCells;
   const Phys &ph = g.ph;
   const int is = a.istage;
+  const float *cvF = g.cvF;
   // own-cell loads first: they are independent of the flux gathers below
-  double q[5];
+  float qh[5], ql[5];
   float rsOld[5];
   float r[8];
   float ivol = 0.f;
   if (a.update) {
 #pragma unroll
-    for (int j = 0; j < 5; ++j) q[j] = g.cv[j * N + c];
+    for (int j = 0; j < 5; ++j) {
+      qh[j] = cvF[(size_t)j * N + c];
+      ql[j] = cvF[(size_t)(5 + j) * N + c];
+    }
 #pragma unroll
     for (int j = 0; j < 5; ++j) rsOld[j] = (is > 1) ? g.rhsSumF[j * N + c] : 0.f;
     ld8_rw(g.rec + 8 * (size_t)c, r);
@@ -954,21 +974,29 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   const float fac = a.useDeviceDt ? float(g.scal[3 + is - 1]) : float(ph.ark[is - 1] * a.dtHost);
   const float adtv = fac * ivol;
   const float grk = ph.grkF[is - 1];
-  double old[5];
+  float oh[5], ol[5];
   if (ph.rkScheme == 1) {
     if (is == 1) {
 #pragma unroll
       for (int j = 0; j < 5; ++j) {
-        old[j] = q[j];
-        g.cvOld[j * N + c] = q[j];
+        oh[j] = qh[j];
+        ol[j] = ql[j];
+        g.cvOldF[(size_t)j * N + c] = qh[j];
+        g.cvOldF[(size_t)(5 + j) * N + c] = ql[j];
       }
     } else {
 #pragma unroll
-      for (int j = 0; j < 5; ++j) old[j] = g.cvOld[j * N + c];
+      for (int j = 0; j < 5; ++j) {
+        oh[j] = g.cvOldF[(size_t)j * N + c];
+        ol[j] = g.cvOldF[(size_t)(5 + j) * N + c];
+      }
     }
   } else {
 #pragma unroll
-    for (int j = 0; j < 5; ++j) old[j] = q[j];
+    for (int j = 0; j < 5; ++j) {
+      oh[j] = qh[j];
+      ol[j] = ql[j];
+    }
   }
   float *rs = g.rhsSumF;
 #pragma unroll
@@ -997,31 +1025,43 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
     } else {
       dU = adtv * rhs[j];
     }
-    q[j] = old[j] - double(dU);
+    qh[j] = oh[j];
+    ql[j] = ol[j];
+    ff_sub(qh[j], ql[j], dU);
   }
-  const double gg = ph.gvG;
-  const double rho = q[0];
-  const float rf = float(rho);
+  // EOS of the new state in FP32 from the pairs (the total energy keeps its
+  // low part, so p loses only the kinetic term's rounding)
+  const float rf = qh[0];
   const float irf = 1.0f / rf;
-  double ir = double(irf);
-  ir = fma(ir, fma(-rho, ir, 1.0), ir);
-  const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
-  double p = (gg - 1.0) * (q[4] - 0.5 * m2 * ir);
-  float pf = float(p);
-  const float uf = float(q[1]) * irf, vf = float(q[2]) * irf, wf = float(q[3]) * irf;
+  const float uf = qh[1] * irf, vf = qh[2] * irf, wf = qh[3] * irf;
+  const float kin = 0.5f * (qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]) * irf;
+  float pf = (ph.gvGF - 1.0f) * ((qh[4] - kin) + ql[4]);
   if (!(rf > 0.f) || !(pf > 1.0e-12f) || isnan(uf) || isnan(vf) || isnan(wf)) {
+    // exact FP64 checks and bounds of AfterUpdateMP on the joined state
+    const double gg = ph.gvG;
+    double q[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = double(qh[j]) + double(ql[j]);
+    const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
     double d[3];
-    d[0] = p;
-    d[1] = p / (rho * ph.gvR);
+    d[0] = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
+    d[1] = d[0] / (q[0] * ph.gvR);
     d[2] = 0.0;
     unsigned st = after_update(ph.gvR, gg, q, d);
     if (st) atomicOr(g.status, st);
-    p = d[0];
-    pf = float(p);
-  }
+    pf = float(d[0]);
 #pragma unroll
-  for (int j = 0; j < 5; ++j) g.cv[j * N + c] = q[j];
-  g.dv[c] = p;
+    for (int j = 0; j < 5; ++j) {
+      qh[j] = float(q[j]);
+      ql[j] = float(q[j] - double(qh[j]));
+    }
+  }
+  float *cvW = g.cvF;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    cvW[(size_t)j * N + c] = qh[j];
+    cvW[(size_t)(5 + j) * N + c] = ql[j];
+  }
   r[0] = rf;
   r[1] = uf;
   r[2] = vf;
@@ -1160,9 +1200,12 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
   }
 }
 
-// T and a of dv from cv and p (mixed path: a stage writes only p of dv).
+// Mixed path: float-float state <-> FP64 exchange copy.  split: hi = the
+// double rounded to float, lo = the rest rounded to float.  join: cv = hi + lo
+// in FP64, then dv from it with the FP64 update's EOS (p = (g-1)(rhoE -
+// 0.5 |rho v|^2 / rho), T = p / (rho R), a = sqrt(g R T)).
 template <typename R>
-__global__ void k_dv_complete(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+__global__ void k_state_split(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
                               int nTiles) {
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
@@ -1170,8 +1213,36 @@ __global__ void k_dv_complete(const RegionDev<R> *__restrict__ regs, const Tile 
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     if (c >= N) continue;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      const double q = g.cv[j * N + c];
+      const float hi = (float)q;
+      g.cvF[(size_t)j * N + c] = hi;
+      g.cvF[(size_t)(5 + j) * N + c] = (float)(q - (double)hi);
+    }
+  }
+}
+
+template <typename R>
+__global__ void k_state_join(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+                             int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    const int N = g.nCells;
+    if (c >= N) continue;
+    double q[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+      g.cv[j * N + c] = q[j];
+    }
     const double gc = g.ph.gvR, gg = g.ph.gvG;
-    double T = g.dv[c] / (g.cv[c] * gc);
+    const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
+    const double p = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
+    const double T = p / (q[0] * gc);
+    g.dv[c] = p;
     g.dv[N + c] = T;
     g.dv[2 * N + c] = sqrt(gg * gc * T);
   }
@@ -1339,9 +1410,14 @@ int configure_grad_smem(int maxW, int block) {
 }
 
 template <typename R>
-void launch_dv_complete(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+void launch_state_split(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
   int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
-  if (grid > 0) k_dv_complete<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+  if (grid > 0) k_state_split<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+}
+template <typename R>
+void launch_state_join(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+  int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
+  if (grid > 0) k_state_join<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
 }
 
 // ---- residual without device allocation ---------------------------------------
@@ -1451,7 +1527,8 @@ void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, co
 
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
-  template void launch_dv_complete<R>(const RegionDev<R> *, const Work &, cudaStream_t);      \
+  template void launch_state_split<R>(const RegionDev<R> *, const Work &, cudaStream_t);      \
+  template void launch_state_join<R>(const RegionDev<R> *, const Work &, cudaStream_t);       \
   template int configure_grad_smem<R>(int, int);                                              \
   template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
                                            const Work &, int, R *, double *, cudaStream_t);    \
