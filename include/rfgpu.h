@@ -57,8 +57,9 @@ enum {
   RFGPU_BCOPT_SUPERSONIC = 0, RFGPU_BCOPT_SUBSONIC = 1, RFGPU_BCOPT_MIXED = 2,
   RFGPU_GAS_MODEL_TCPERF = 1, RFGPU_FLOW_EULER = 0,
   RFGPU_PREC_FP64 = 0,   /* everything FP64; bit-identical to the reference order */
-  RFGPU_PREC_MIXED = 1,  /* FP32 prim/gradients/limiter/flux; FP64 geometry,
-                            residual accumulation, RK update and EOS */
+  RFGPU_PREC_MIXED = 1,  /* FP32 prim/gradients/limiter/flux with compensated
+                            residual sums; float-float (~48-bit) conserved
+                            state and RK update; FP64 cv/dv on download */
   /* Device numbering.  LOCALITY: cells renumbered along a Morton curve of
    * their centroids and interior faces grouped by their lower-numbered cell,
    * so a block's stencil and face gathers stay within a compact patch of the
