@@ -119,7 +119,8 @@ struct rfgpu_region_s {
   void *regsDev = nullptr;  // RegionDev<R>[1]
   Tile *cellTiles = nullptr, *faceTiles = nullptr, *bfaceTiles = nullptr;
   Work work{};
-  double *stage = nullptr;  // staging for AoS transfers, 5*N doubles
+  double *stage = nullptr;   // staging for AoS transfers, 5*N doubles
+  double *stage2 = nullptr;  // second staging buffer (dv), 3*N doubles, mixed path
   long long launches = 0;
   // graph cache
   cudaGraphExec_t graph = nullptr;
@@ -501,10 +502,11 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.cfD = M.upload(cast<R>(cd), s);
     g.cfTotal = sl.total;
   }
-  // ---- state
-  g.cv = M.alloc<double>(5 * (size_t)N);
-  g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
+  // ---- state (FP64 SoA on the FP64 path; float-float pairs on the mixed path)
   if (sizeof(R) == 8) {
+    g.cv = M.alloc<double>(5 * (size_t)N);
+    g.dv = M.alloc<double>(3 * (size_t)N);
+    g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
     g.rhsSum = M.alloc<double>(5 * (size_t)N);
     cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
   } else {
@@ -513,7 +515,6 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.cvF = M.alloc<float>(10 * (size_t)N);
     if (ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL) g.cvOldF = M.alloc<float>(10 * (size_t)N);
   }
-  g.dv = M.alloc<double>(3 * (size_t)N);
   g.rhs = M.alloc<double>(5 * (size_t)N);
   {
     std::vector<double> recx(8 * (size_t)N, 0.0);  // centroid slots; state filled by k_prim
@@ -552,23 +553,27 @@ const RegionDev<R> *regs_of(rfgpu_region_s *h) {
 int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
   cudaStream_t s = h->stream;
   const int N = h->nCells;
-  double *dcv = h->prec ? h->rd32.cv : h->rd64.cv;
-  double *ddv = h->prec ? h->rd32.dv : h->rd64.dv;
+  if (h->prec) {  // mixed: DMA copies into the staging buffers, one fused conversion pass
+    if (cudaMemcpyAsync(h->stage, cv, 5 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    if (dv && cudaMemcpyAsync(h->stage2, dv, 3 * (size_t)N * 8, cudaMemcpyHostToDevice, s) !=
+                  cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    launch_upload_direct<float>(regs_of<float>(h), h->work, h->stage, dv ? h->stage2 : nullptr, s);
+    h->launches++;
+    return cuda_rc(cudaGetLastError());
+  }
+  // FP64 path: staged copies into the SoA state, then records (and dv) from it
   if (cudaMemcpyAsync(h->stage, cv, 5 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
     return RFGPU_ERR_CUDA;
-  launch_aos_to_soa(h->stage, dcv, N, 5, h->cellNew, s);
+  launch_aos_to_soa(h->stage, h->rd64.cv, N, 5, h->cellNew, s);
   if (dv) {
     if (cudaMemcpyAsync(h->stage, dv, 3 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
       return RFGPU_ERR_CUDA;
-    launch_aos_to_soa(h->stage, ddv, N, 3, h->cellNew, s);
+    launch_aos_to_soa(h->stage, h->rd64.dv, N, 3, h->cellNew, s);
   }
-  if (h->prec) {
-    launch_prim<float>(regs_of<float>(h), h->work, dv ? 0 : 1, s);
-    launch_state_split<float>(regs_of<float>(h), h->work, s);
-  } else {
-    launch_prim<double>(regs_of<double>(h), h->work, dv ? 0 : 1, s);
-  }
-  h->launches += (dv ? 3 : 2) + (h->prec ? 1 : 0);
+  launch_prim<double>(regs_of<double>(h), h->work, dv ? 0 : 1, s);
+  h->launches += dv ? 3 : 2;
   return cuda_rc(cudaGetLastError());
 }
 
@@ -663,6 +668,7 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
                  : configure_grad_smem<double>(h->maxStW, block)) != 0)
       throw std::bad_alloc();
     h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
+    if (h->prec) h->stage2 = h->mem.alloc<double>(3 * (size_t)h->nCells);
     cudaStreamSynchronize(h->stream);
   } catch (const std::bad_alloc &) {
     h->mem.free_all();
@@ -767,12 +773,21 @@ int rfgpu_residual(rfgpu_region_t h, double *rhs) {
 int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (!h) return RFGPU_ERR_ARG;
   const int N = h->nCells;
-  if (h->prec && (cv || dv)) {  // mixed path: FP64 cv and dv from the float-float state
-    launch_state_join<float>(regs_of<float>(h), h->work, h->stream);
+  if (h->prec) {  // mixed: one fused pass into the staging buffers, then the DMA copies
+    if (!cv && !dv) return RFGPU_OK;
+    launch_download_direct<float>(regs_of<float>(h), h->work, cv ? h->stage : nullptr,
+                                  dv ? h->stage2 : nullptr, h->stream);
     h->launches++;
+    if (cv && cudaMemcpyAsync(cv, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost,
+                              h->stream) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    if (dv && cudaMemcpyAsync(dv, h->stage2, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost,
+                              h->stream) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    return cuda_rc(cudaStreamSynchronize(h->stream));
   }
   if (cv) {
-    launch_soa_to_aos(h->prec ? h->rd32.cv : h->rd64.cv, h->stage, N, 5, h->cellNew, h->stream);
+    launch_soa_to_aos(h->rd64.cv, h->stage, N, 5, h->cellNew, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(cv, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
       return RFGPU_ERR_CUDA;
@@ -780,7 +795,7 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (dv) {
     // stage is reused: wait for the cv copy first
     if (cv && cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
-    launch_soa_to_aos(h->prec ? h->rd32.dv : h->rd64.dv, h->stage, N, 3, h->cellNew, h->stream);
+    launch_soa_to_aos(h->rd64.dv, h->stage, N, 3, h->cellNew, h->stream);
     h->launches++;
     if (cudaMemcpyAsync(dv, h->stage, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess)
       return RFGPU_ERR_CUDA;

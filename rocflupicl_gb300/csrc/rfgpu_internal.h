@@ -51,10 +51,11 @@ struct Phys {
 template <typename R>
 struct RegionDev {
   int nCells, nFaces, nBFaces, pad_;
-  // state (FP64 SoA).  The mixed path advances its state as float-float
-  // pairs, cvF[2][5][N] (hi rows, then lo rows; the pair's sum carries about
-  // 48 significand bits) with the RK increment history in FP32 (rhsSumF);
-  // cv and dv are its FP64 exchange copies, filled on upload / download.
+  // state.  FP64 path: SoA cv, dv, rhsSum.  The mixed path advances its state
+  // as float-float pairs, cvF[2][5][N] (hi rows, then lo rows; the pair's sum
+  // carries about 48 significand bits) with the RK increment history in FP32
+  // (rhsSumF); its cv and dv exist only as host images, converted in one pass
+  // on upload / download.
   double *cv, *cvOld, *rhsSum, *dv, *rhs;
   float *rhsSumF;
   float *cvF, *cvOldF;
@@ -150,13 +151,15 @@ struct Prof {
 // R = float (mixed unit).  `regs` is a device array of RegionDev<R>.
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
-// Mixed path: split the FP64 exchange copy cv into the float-float state
-// (after an upload) / join it back into cv and evaluate dv = p, T, a in FP64
-// (before a download).
+// Mixed path: fused conversion between the Fortran images cv(5,N), dv(3,N)
+// (host numbering, in device staging buffers) and the device state; either
+// buffer may be null where the call allows it.
 template <typename R>
-void launch_state_split(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
+void launch_upload_direct(const RegionDev<R> *regs, const Work &w, const double *cvH,
+                          const double *dvH, cudaStream_t s);
 template <typename R>
-void launch_state_join(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
+void launch_download_direct(const RegionDev<R> *regs, const Work &w, double *cvH, double *dvH,
+                            cudaStream_t s);
 template <typename R>
 int configure_grad_smem(int maxW, int block);
 // Residual with the face fluxes and the result in caller-supplied scratch
