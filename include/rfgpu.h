@@ -237,6 +237,22 @@ int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms);
 #define RFGPU_NOALLOC_SCRATCH_BYTES (32u << 20)
 int rfgpu_residual_noalloc(rfgpu_region_t h, double *rhs);
 
+/* Device-side mesh preprocessing: the c2c stencils and WLSQ moments of every
+ * cell (RFLU_BuildC2CStencilWrapper, RFLU_ModStencilsCells.F90:750-1416, and
+ * the moments of RFLU_ModWeights.F90:1770-1894), one GPU thread per cell,
+ * with the same per-cell routine as the host builder of rfmesh.h, so members
+ * and moments are identical to it bit for bit.  Inputs (0-based): cell
+ * vertices padded to 8 with -1 (8,nCells), vertex counts (nCells),
+ * vertex-to-cell lists in ascending cell order (offsets (nVerts+1), cells),
+ * centroids cofg(3,nCells).  Outputs: c2csOffsets (nCells+1, 0-based),
+ * c2csMembers (1-based, room for 40 per cell), xyzMoms (10,nCells).  Every
+ * index is validated on the host first (RFGPU_ERR_ARG); a cell with more
+ * than 256 vertex-neighbour entries gives RFGPU_ERR_UNSUPPORTED.
+ * Synchronous; allocates and frees its own device buffers. */
+int rfgpu_mesh_stencils(int nCells, int nVerts, const int *cellVerts, const int *cellNVerts,
+                        const int *v2cOffsets, const int *v2c, const double *cofg,
+                        int *c2csOffsets, int *c2csMembers, double *xyzMoms);
+
 #ifdef __cplusplus
 }
 #endif

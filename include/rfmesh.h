@@ -61,12 +61,22 @@ enum {
 /* Return codes */
 enum { RFMESH_OK = 0, RFMESH_ERR_ARG = 1, RFMESH_ERR_GEOM = 2, RFMESH_ERR_NOMEM = 3 };
 
+/* flags of rfmesh_create_box_ex */
+enum {
+  RFMESH_DEFER_STENCILS = 1  /* build everything but the c2c stencils and moments; supply
+                                them with rfmesh_set_stencils (e.g. from the GPU builder
+                                rfgpu_mesh_stencils, which runs the same per-cell routine) */
+};
+
 /* Build a box mesh over [lo,hi] with nx*ny*nz base hexes.  Interior vertices
  * are displaced by U(-jitter,+jitter)*h per coordinate from a 64-bit Mersenne
  * twister seeded with `seed`.  nThreads <= 0 uses all host threads. */
 int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3],
                       const double hi[3], double jitter, unsigned long long seed,
                       int nThreads, rfmesh_t *out);
+int rfmesh_create_box_ex(int kind, int nx, int ny, int nz, const double lo[3],
+                         const double hi[3], double jitter, unsigned long long seed,
+                         int nThreads, int flags, rfmesh_t *out);
 int rfmesh_destroy(rfmesh_t m);
 int rfmesh_sizes(rfmesh_t m, long long sizes[RFMESH_NSIZES]);
 int rfmesh_patch_nbfaces(rfmesh_t m, int iPatch);
@@ -85,6 +95,20 @@ const int *rfmesh_cell_type(rfmesh_t m);   /* (nCells) 0 tet 1 hex 2 pri 3 pyr *
 const int *rfmesh_bf2c(rfmesh_t m, int iPatch);   /* (nBFaces), 1-based */
 const double *rfmesh_bfn(rfmesh_t m, int iPatch); /* (4,nBFaces) */
 const double *rfmesh_bfc(rfmesh_t m, int iPatch); /* (3,nBFaces) */
+
+/* Connectivity the stencil builders take (0-based): cell vertices padded to
+ * 8 with -1 (8,nCells), vertex counts (nCells), vertex-to-cell lists in
+ * ascending cell order (offsets (nVert+1), cells (offsets[nVert])), and the
+ * centroids (3,nCells) (the same array as rfmesh_cofg). */
+const int *rfmesh_cell_verts(rfmesh_t m);
+const int *rfmesh_cell_nverts(rfmesh_t m);
+const int *rfmesh_v2c_offsets(rfmesh_t m);
+const int *rfmesh_v2c(rfmesh_t m);
+const double *rfmesh_cofg_view(rfmesh_t m);
+
+/* Install c2c stencils (0-based CSR offsets (nCells+1), 1-based members, at
+ * most 40 per cell) and moments (10,nCells) built elsewhere. */
+int rfmesh_set_stencils(rfmesh_t m, const int *offsets, const int *members, const double *moms);
 
 #ifdef __cplusplus
 }

@@ -117,10 +117,11 @@ def tube_bcs(order: int = 2) -> List[PatchBC]:
 def shock_tube(n: int = 1000, ny: int = 2, nz: int = 2, length=(1.0, 0.01, 0.01),
                left=(1.0, 0.0, 1.0), right=(0.125, 0.0, 0.1), x0: float = 0.5,
                numerics: Optional[Numerics] = None, bc_order: int = 2, t_end: float = 0.2,
-               threads: int = 0) -> Case:
-    """Sod-type tube of n*ny*nz hexes: (rho,u,p) = left for x < x0, right otherwise."""
+               threads: int = 0, stencils: str = "host") -> Case:
+    """Sod-type tube of n*ny*nz hexes: (rho,u,p) = left for x < x0, right otherwise.
+    stencils="device" builds the stencils and moments on the GPU (same output)."""
     num = numerics or Numerics()
-    m = _mesh.box(_mesh.HEX, n, ny, nz, hi=length, threads=threads)
+    m = _mesh.box(_mesh.HEX, n, ny, nz, hi=length, threads=threads, stencils=stencils)
     x = m.cofg[:, 0]
     L = x < x0 * length[0]
     r = np.where(L, left[0], right[0])
@@ -146,14 +147,14 @@ def rankine_hugoniot(Ms: float, gamma: float, rho1: float, p1: float):
 
 def tet_shock_box(n: int = 128, seed: int = 2024, jitter: float = 0.1, Ms: float = 2.0,
                   sigma: float = 0.1, x_shock: float = 0.2, numerics: Optional[Numerics] = None,
-                  n_steps: int = 100, threads: int = 0) -> Case:
+                  n_steps: int = 100, threads: int = 0, stencils: str = "host") -> Case:
     """Planar Ms shock over a perturbed tetrahedral box: n^3 hexes x 6 Kuhn tets,
     interior vertices jittered by U(+-jitter*h); quiescent air rho=1.2, p=1e5
     times a per-cell lognormal density factor exp(sigma*Z); Rankine-Hugoniot
     post-shock state for x < x_shock.  Slip walls on y/z, supersonic outflow
     (extrapolation) on the x ends."""
     num = numerics or Numerics(spaceDiscr=DISCR_UPW_ROE)
-    m = _mesh.box(_mesh.TET, n, n, n, jitter=jitter, seed=seed, threads=threads)
+    m = _mesh.box(_mesh.TET, n, n, n, jitter=jitter, seed=seed, threads=threads, stencils=stencils)
     rng = np.random.default_rng(seed)
     rho1, p1 = 1.2, 1.0e5
     r = rho1 * np.exp(sigma * rng.standard_normal(m.nCells))
@@ -192,12 +193,12 @@ def fourier_state(xyz: np.ndarray, seed: int, n_modes: int = 8):
 
 
 def mixed_box(n: int = 96, seed: int = 7, numerics: Optional[Numerics] = None,
-              threads: int = 0) -> Case:
+              threads: int = 0, stencils: str = "host") -> Case:
     """n^3 box: hexes with x > 0.5 split into 2 prisms, hexes with z > 0.5 into 6
     tets (prism precedence), pyramid transition cubes where tets meet quad faces;
     smooth seeded Fourier state.  Slip walls everywhere (residual benchmark)."""
     num = numerics or Numerics()
-    m = _mesh.box(_mesh.MIXED, n, n, n, threads=threads)
+    m = _mesh.box(_mesh.MIXED, n, n, n, threads=threads, stencils=stencils)
     r, u, v, w, p = fourier_state(m.cofg, seed)
     cv = prim_to_cv(num, r, u, v, w, p)
     bcs = [PatchBC(BC_SLIPWALL, 2) for _ in range(6)]

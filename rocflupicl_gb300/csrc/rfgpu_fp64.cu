@@ -3,6 +3,7 @@
 // the per-cell summation orders equal the reference's, so the residual and
 // the stage update are bit-identical to the CPU restatement.
 #include "rfgpu_kernels.cuh"
+#include "rfmesh_stencil.h"
 
 namespace rfgpu {
 
@@ -52,6 +53,35 @@ void launch_weights64(const long long *stOff, const int *stCnt, const int *stIdx
 __global__ void k_to_f32(const double *__restrict__ src, float *__restrict__ dst, long long n) {
   long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   for (; i < n; i += (long long)gridDim.x * blockDim.x) dst[i] = (float)src[i];
+}
+
+// c2c stencils and WLSQ moments of every cell, one thread per cell, with the
+// per-cell routine the host mesh builder runs (rfmesh_stencil.h); this unit
+// is built without contraction, so the moments match the host's bit for bit.
+__global__ void __launch_bounds__(128) k_mesh_stencils(rfm::CellView m, int N, int *cnt, int *memb,
+                                                       double *moms, int *overflow) {
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= N) return;
+  rfm::Scratch w;
+  int c2cs[rfm::kStencilMax];
+  double mo[10];
+  const int degr = rfm::cell_stencil(m, c, c2cs, mo, w);
+  if (degr < 0) {
+    atomicAdd(overflow, 1);
+    cnt[c] = 0;
+    return;
+  }
+  cnt[c] = degr;
+  for (int s = 0; s < degr; ++s) memb[(size_t)c * rfm::kStencilMax + s] = c2cs[s];
+  for (int k = 0; k < 10; ++k) moms[10 * (size_t)c + k] = mo[k];
+}
+
+void launch_mesh_stencils(const double *cofg, const int *cv, const int *nv, const int *v2cOff,
+                          const int *v2c, int nCells, int *cnt, int *memb, double *moms,
+                          int *overflow, cudaStream_t s) {
+  if (nCells <= 0) return;
+  rfm::CellView m{cofg, cv, nv, v2cOff, v2c};
+  k_mesh_stencils<<<(nCells + 127) / 128, 128, 0, s>>>(m, nCells, cnt, memb, moms, overflow);
 }
 
 void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s) {

@@ -1163,4 +1163,79 @@ int rfgpu_residual_noalloc(rfgpu_region_t h, double *rhs) {
   return cuda_rc(cudaStreamSynchronize(h->stream));
 }
 
+int rfgpu_mesh_stencils(int nCells, int nVerts, const int *cellVerts, const int *cellNVerts,
+                        const int *v2cOffsets, const int *v2c, const double *cofg,
+                        int *c2csOffsets, int *c2csMembers, double *xyzMoms) {
+  if (nCells <= 0 || nVerts <= 0 || !cellVerts || !cellNVerts || !v2cOffsets || !v2c || !cofg ||
+      !c2csOffsets || !c2csMembers || !xyzMoms)
+    return RFGPU_ERR_ARG;
+  // every index the kernel follows is checked here first
+  for (long long c = 0; c < nCells; ++c) {
+    const int n = cellNVerts[c];
+    if (n < 1 || n > 8) return RFGPU_ERR_ARG;
+    for (int a = 0; a < n; ++a)
+      if (cellVerts[8 * c + a] < 0 || cellVerts[8 * c + a] >= nVerts) return RFGPU_ERR_ARG;
+  }
+  if (v2cOffsets[0] != 0) return RFGPU_ERR_ARG;
+  for (long long v = 0; v < nVerts; ++v)
+    if (v2cOffsets[v + 1] < v2cOffsets[v]) return RFGPU_ERR_ARG;
+  const long long nV2c = v2cOffsets[nVerts];
+  for (long long e = 0; e < nV2c; ++e)
+    if (v2c[e] < 0 || v2c[e] >= nCells) return RFGPU_ERR_ARG;
+  const size_t N = (size_t)nCells, K = 40;
+  // stream-ordered allocations: no device-wide synchronisation, so a serving
+  // loop can build stencils for a new request while its batch runs
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) return RFGPU_ERR_CUDA;
+  std::vector<void *> bufs;
+  auto dalloc = [&](size_t bytes) -> void * {
+    void *p = nullptr;
+    if (cudaMallocAsync(&p, bytes ? bytes : 1, s) != cudaSuccess) return nullptr;
+    bufs.push_back(p);
+    return p;
+  };
+  int rc = RFGPU_OK;
+  double *dcofg = (double *)dalloc(3 * N * 8), *dmoms = (double *)dalloc(10 * N * 8);
+  int *dcv = (int *)dalloc(8 * N * 4), *dnv = (int *)dalloc(N * 4);
+  int *doff = (int *)dalloc(((size_t)nVerts + 1) * 4), *dv2c = (int *)dalloc((size_t)nV2c * 4);
+  int *dcnt = (int *)dalloc(N * 4), *dmemb = (int *)dalloc(K * N * 4), *dov = (int *)dalloc(4);
+  if (bufs.size() != 9) {
+    rc = RFGPU_ERR_NOMEM;
+  } else {
+    try {
+      std::vector<int> cnt(N), memb(K * N);
+      int overflow = 0;
+      cudaMemcpyAsync(dcofg, cofg, 3 * N * 8, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dcv, cellVerts, 8 * N * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(dnv, cellNVerts, N * 4, cudaMemcpyHostToDevice, s);
+      cudaMemcpyAsync(doff, v2cOffsets, ((size_t)nVerts + 1) * 4, cudaMemcpyHostToDevice, s);
+      if (nV2c > 0) cudaMemcpyAsync(dv2c, v2c, (size_t)nV2c * 4, cudaMemcpyHostToDevice, s);
+      cudaMemsetAsync(dov, 0, 4, s);
+      launch_mesh_stencils(dcofg, dcv, dnv, doff, dv2c, nCells, dcnt, dmemb, dmoms, dov, s);
+      cudaMemcpyAsync(cnt.data(), dcnt, N * 4, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(memb.data(), dmemb, K * N * 4, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(xyzMoms, dmoms, 10 * N * 8, cudaMemcpyDeviceToHost, s);
+      cudaMemcpyAsync(&overflow, dov, 4, cudaMemcpyDeviceToHost, s);
+      if (cudaStreamSynchronize(s) != cudaSuccess || cudaGetLastError() != cudaSuccess) {
+        rc = RFGPU_ERR_CUDA;
+      } else if (overflow) {
+        rc = RFGPU_ERR_UNSUPPORTED;
+      } else {
+        c2csOffsets[0] = 0;
+        for (size_t c = 0; c < N; ++c) {
+          const int n = cnt[c];
+          for (int k = 0; k < n; ++k) c2csMembers[c2csOffsets[c] + k] = memb[K * c + k] + 1;
+          c2csOffsets[c + 1] = c2csOffsets[c] + n;
+        }
+      }
+    } catch (const std::bad_alloc &) {
+      rc = RFGPU_ERR_NOMEM;
+    }
+  }
+  for (void *p : bufs) cudaFreeAsync(p, s);
+  cudaStreamSynchronize(s);
+  cudaStreamDestroy(s);
+  return rc;
+}
+
 }  // extern "C"

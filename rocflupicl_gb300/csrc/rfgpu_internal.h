@@ -188,6 +188,12 @@ void launch_weights64(const long long *stOff, const int *stCnt, const int *stIdx
                       const double *cofg, const double *moms, double *w64, cudaStream_t s,
                       long long stTotal);
 void launch_to_f32(const double *src, float *dst, long long n, cudaStream_t s);
+// c2c stencils (memb[40*c + s], cnt[c]) and moments (moms[10*c + k]) of every
+// cell from the connectivity views of rfmesh.h; overflow counts cells whose
+// vertex-neighbour list exceeds the builder's capacity.
+void launch_mesh_stencils(const double *cofg, const int *cv, const int *nv, const int *v2cOff,
+                          const int *v2c, int nCells, int *cnt, int *memb, double *moms,
+                          int *overflow, cudaStream_t s);
 // Fortran image a(ncomp,N) in host numbering <-> SoA [ncomp][N] in device
 // numbering; cellNew maps a host cell to its device cell (null: identity)
 void launch_aos_to_soa(const double *aos, double *soa, int N, int ncomp, const int *cellNew,

@@ -4,6 +4,7 @@
 // host (x86_64 here, aarch64 on the GPU nodes) and matches the unfused
 // Fortran arithmetic it restates.
 #include "rfmesh.h"
+#include "rfmesh_stencil.h"
 
 #include <algorithm>
 #include <cmath>
@@ -58,6 +59,8 @@ struct rfmesh_s {
   std::vector<int> csOff, csMem, csMem1;
   std::vector<double> moms;
   int maxMembs = 0;
+  std::vector<int> cv8, nv8;  // connectivity padded to 8 vertices, vertex counts
+  bool skipStencils = false;  // stencils and moments come from rfmesh_set_stencils
 
   int nv(long long icg) const { return kNV[ctype[icg]]; }
   const int *verts(long long icg) const {
@@ -67,118 +70,6 @@ struct rfmesh_s {
 };
 
 namespace {
-
-// ---------------------------------------------------------------------------
-// Sorting restated from modfloflu/ModSortSearch.F90:898-990 (Wirth's
-// non-recursive quicksort).  The unstable tie-breaking decides which of the
-// equal-fraction vertex neighbours survive stencil truncation on tet meshes.
-// Arrays are 1-based in the Fortran; here a[0..n-1] with the same index math
-// shifted by one.
-void quicksort_real_int(double *a, int *b, int n) {
-  if (n <= 0) return;
-  int stackl[50], stackr[50];
-  int s = 1;
-  stackl[0] = 1;
-  stackr[0] = n;
-  int l, r;
-L10:
-  l = stackl[s - 1];
-  r = stackr[s - 1];
-  s = s - 1;
-L20: {
-  int i = l, j = r;
-  int k = (l + r) / 2;
-  double x = a[k - 1];
-  for (;;) {
-    while (a[i - 1] < x) i = i + 1;
-    while (x < a[j - 1]) j = j - 1;
-    if (i <= j) {
-      double w = a[i - 1];
-      a[i - 1] = a[j - 1];
-      a[j - 1] = w;
-      int v = b[i - 1];
-      b[i - 1] = b[j - 1];
-      b[j - 1] = v;
-      i = i + 1;
-      j = j - 1;
-      if (i > j) break;
-    } else {
-      break;
-    }
-  }
-  if (j - l >= r - i) {
-    if (l < j) {
-      s = s + 1;
-      stackl[s - 1] = l;
-      stackr[s - 1] = j;
-    }
-    l = i;
-  } else {
-    if (i < r) {
-      s = s + 1;
-      stackl[s - 1] = i;
-      stackr[s - 1] = r;
-    }
-    r = j;
-  }
-  if (l < r) goto L20;
-  if (s != 0) goto L10;
-}
-}
-
-// Singular values (descending) of a column-scaled rows x 4 matrix, from the
-// eigenvalues of A^T A by cyclic Jacobi.  Used only for the layer-growth test
-// of libflu/RFLU_InvertMatrixSVD.F90:150-190 (ratio of successive singular
-// values against 0.01, first one against 100*eps), where LAPACK dgesdd is
-// replaced by this 4x4 symmetric eigen solve.
-void singular_values4(const std::vector<double> &A, int rows, double s[4]) {
-  double g[4][4] = {{0}};
-  for (int i = 0; i < 4; ++i)
-    for (int j = 0; j < 4; ++j) {
-      double acc = 0.0;
-      for (int r = 0; r < rows; ++r) acc += A[r * 4 + i] * A[r * 4 + j];
-      g[i][j] = acc;
-    }
-  for (int sweep = 0; sweep < 60; ++sweep) {
-    double off = 0.0;
-    for (int p = 0; p < 4; ++p)
-      for (int q = p + 1; q < 4; ++q) off += g[p][q] * g[p][q];
-    if (off < 1e-300) break;
-    for (int p = 0; p < 4; ++p)
-      for (int q = p + 1; q < 4; ++q) {
-        if (g[p][q] == 0.0) continue;
-        double theta = (g[q][q] - g[p][p]) / (2.0 * g[p][q]);
-        double t = (theta >= 0 ? 1.0 : -1.0) / (std::fabs(theta) + std::sqrt(theta * theta + 1.0));
-        double c = 1.0 / std::sqrt(t * t + 1.0), sn = t * c;
-        for (int k = 0; k < 4; ++k) {
-          double gkp = g[k][p], gkq = g[k][q];
-          g[k][p] = c * gkp - sn * gkq;
-          g[k][q] = sn * gkp + c * gkq;
-        }
-        for (int k = 0; k < 4; ++k) {
-          double gpk = g[p][k], gqk = g[q][k];
-          g[p][k] = c * gpk - sn * gqk;
-          g[q][k] = sn * gpk + c * gqk;
-        }
-      }
-  }
-  for (int i = 0; i < 4; ++i) s[i] = std::sqrt(std::max(g[i][i], 0.0));
-  std::sort(s, s + 4, [](double a, double b) { return a > b; });
-}
-
-int svd_scount(const std::vector<double> &A, int rows) {
-  double s[4];
-  singular_values4(A, rows, s);
-  const double eps = std::numeric_limits<double>::epsilon();
-  int sCount = 0;
-  if (!(s[0] > 100.0 * eps)) sCount = 1;
-  for (int i = 1; i < 4; ++i) {
-    if (s[i] > 0.01 * s[i - 1]) continue;
-    sCount += 4 - i;
-    break;
-  }
-  return sCount;
-}
 
 // FaceVectorTria / FaceVectorQuad (libfloflu/FaceVector.F90:79-136) and
 // FaceCentroidTria / FaceCentroidQuad (libfloflu/FaceCentroid.F90:77-122).
@@ -328,6 +219,8 @@ void generate(rfmesh_s *m, int nx, int ny, int nz, double jitter, unsigned long 
 }
 
 // ---------------------------------------------------------------------------
+
+void set_stencils(rfmesh_s *m, const std::vector<int> &cnt, const std::vector<int> &memb);
 
 void build(rfmesh_s *m, int nThreads) {
   (void)nThreads;
@@ -505,158 +398,6 @@ void build(rfmesh_s *m, int nThreads) {
       for (int a = 0; a < m->nv(c); ++a) m->v2c[fill[v[a]]++] = (int)c;
     }
   }
-  // c2c stencils (RFLU_ModStencilsCells.F90:750-1416) and moments
-  // (RFLU_ModWeights.F90:1770-1894)
-  const int stencilSizeMin = 4;  // RFLU_ComputeStencilSize(3,1,1) = 2*3*4/6
-  const int stencilSizeMax = 10 * stencilSizeMin;
-  const int nLayersMax = 6;
-  std::vector<int> cnt(nC, 0);
-  std::vector<int> memb((size_t)nC * stencilSizeMax);
-  m->moms.assign(10 * (size_t)nC, 0.0);
-#pragma omp parallel
-  {
-    std::vector<int> tmp, tmp2, help, sorted;
-    std::vector<double> frac, A;
-    int c2cs[40];
-#pragma omp for schedule(dynamic, 1024)
-    for (long long icg = 0; icg < nC; ++icg) {
-      int nVert = m->nv(icg);
-      const int *v = m->verts(icg);
-      double iNVert = 1.0 / (double)nVert;
-      tmp.clear();
-      for (int a = 0; a < nVert; ++a)
-        for (int e = m->v2cOff[v[a]]; e < m->v2cOff[v[a] + 1]; ++e) tmp.push_back(m->v2c[e]);
-      std::sort(tmp.begin(), tmp.end());
-      tmp.erase(std::unique(tmp.begin(), tmp.end()), tmp.end());
-      tmp.erase(std::lower_bound(tmp.begin(), tmp.end(), (int)icg));
-      int vs[8];
-      for (int a = 0; a < nVert; ++a) vs[a] = v[a];
-      std::sort(vs, vs + nVert);
-      int nC2 = (int)tmp.size();
-      frac.resize(nC2);
-      for (int q = 0; q < nC2; ++q) {
-        int c2 = tmp[q];
-        int n2 = m->nv(c2);
-        int vs2[8];
-        const int *v2 = m->verts(c2);
-        for (int a = 0; a < n2; ++a) vs2[a] = v2[a];
-        std::sort(vs2, vs2 + n2);
-        int common = 0, ia = 0, ib = 0;
-        while (ia < nVert && ib < n2) {
-          if (vs[ia] == vs2[ib]) { ++common; ++ia; ++ib; }
-          else if (vs[ia] < vs2[ib]) ++ia;
-          else ++ib;
-        }
-        frac[q] = (double)common * iNVert;
-      }
-      quicksort_real_int(frac.data(), tmp.data(), nC2);
-      int degr = 0;
-      for (int q = nC2; q >= std::max(nC2 - stencilSizeMax + 1, 1); --q) c2cs[degr++] = tmp[q - 1];
-      std::sort(c2cs, c2cs + degr);
-      int layBeg = 0, layEnd = degr;  // previous layer [beg,end)
-      for (int iLayer = 2; iLayer <= nLayersMax; ++iLayer) {
-        int sCount = 0;
-        if (degr >= stencilSizeMin) {
-          A.assign((size_t)degr * 4, 0.0);
-          const double *c0 = &m->cofg[3 * (size_t)icg];
-          for (int s = 0; s < degr; ++s) {
-            const double *c1 = &m->cofg[3 * (size_t)c2cs[s]];
-            double dx = c1[0] - c0[0], dy = c1[1] - c0[1], dz = c1[2] - c0[2];
-            double term = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
-            A[4 * s + 0] = term;
-            A[4 * s + 1] = term * dx;
-            A[4 * s + 2] = term * dy;
-            A[4 * s + 3] = term * dz;
-          }
-          for (int col = 0; col < 4; ++col) {
-            double cm = -std::numeric_limits<double>::max();
-            for (int s = 0; s < degr; ++s) cm = std::max(cm, std::fabs(A[4 * s + col]));
-            for (int s = 0; s < degr; ++s) A[4 * s + col] = A[4 * s + col] / cm;
-          }
-          sCount = svd_scount(A, degr);
-        }
-        if (sCount != 0 || degr < stencilSizeMin) {
-          // RFLU_AddCellLayer (RFLU_ModStencilsUtils.F90:696-979)
-          sorted.assign(c2cs, c2cs + degr);
-          std::sort(sorted.begin(), sorted.end());
-          help.clear();
-          bool full = false;
-          for (int s = layBeg; s < layEnd && !full; ++s) {
-            int c1 = c2cs[s];
-            const int *v1 = m->verts(c1);
-            for (int a = 0; a < m->nv(c1) && !full; ++a)
-              for (int e = m->v2cOff[v1[a]]; e < m->v2cOff[v1[a] + 1]; ++e) {
-                int c2 = m->v2c[e];
-                if (c2 == (int)icg) continue;
-                if (std::binary_search(sorted.begin(), sorted.end(), c2)) continue;
-                if (std::binary_search(help.begin(), help.end(), c2)) continue;
-                if ((int)help.size() < stencilSizeMax) {
-                  help.insert(std::upper_bound(help.begin(), help.end(), c2), c2);
-                } else {
-                  full = true;
-                  break;
-                }
-              }
-          }
-          int newBeg = degr;
-          for (size_t s = 0; s < help.size(); ++s)
-            if (degr < stencilSizeMax) c2cs[degr++] = help[s];
-          layBeg = newBeg;
-          layEnd = degr;
-        } else {
-          break;
-        }
-      }
-      cnt[icg] = degr;
-      for (int s = 0; s < degr; ++s) memb[(size_t)icg * stencilSizeMax + s] = c2cs[s];
-      // moments
-      double mo[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
-      const double *c0 = &m->cofg[3 * (size_t)icg];
-      for (int s = 0; s < degr; ++s) {
-        const double *c1 = &m->cofg[3 * (size_t)c2cs[s]];
-        double dx = c1[0] - c0[0], dy = c1[1] - c0[1], dz = c1[2] - c0[2];
-        double wt = 1.0 / std::sqrt(dx * dx + dy * dy + dz * dz);
-        dx = wt * dx;
-        dy = wt * dy;
-        dz = wt * dz;
-        mo[0] = mo[0] + dx * dx;
-        mo[1] = mo[1] + dx * dy;
-        mo[2] = mo[2] + dy * dy;
-        mo[3] = mo[3] + dx * dz;
-        mo[4] = mo[4] + dy * dz;
-        mo[5] = mo[5] + dz * dz;
-        mo[6] = mo[6] + wt * dx;
-        mo[7] = mo[7] + wt * dy;
-        mo[8] = mo[8] + wt * dz;
-        mo[9] = mo[9] + wt * wt;
-      }
-      double r11 = std::sqrt(mo[0]);
-      double ir11 = 1.0 / r11;
-      double r12 = ir11 * mo[1];
-      double r22 = std::sqrt(mo[2] - r12 * r12);
-      double ir22 = 1.0 / r22;
-      double r13 = ir11 * mo[3];
-      double r23 = ir22 * (mo[4] - r12 * r13);
-      double r33 = std::sqrt(mo[5] - (r13 * r13 + r23 * r23));
-      double ir33 = 1.0 / r33;
-      double r14 = ir11 * mo[6];
-      double r24 = ir22 * (mo[7] - r12 * r14);
-      double r34 = ir33 * (mo[8] - (r13 * r14 + r23 * r24));
-      double r44 = std::sqrt(mo[9] - (r14 * r14 + r24 * r24 + r34 * r34));
-      double *out = &m->moms[10 * (size_t)icg];
-      out[0] = r11; out[1] = r12; out[2] = r22; out[3] = r13; out[4] = r23;
-      out[5] = r33; out[6] = r14; out[7] = r24; out[8] = r34; out[9] = r44;
-    }
-  }
-  m->csOff.assign(nC + 1, 0);
-  for (long long c = 0; c < nC; ++c) {
-    m->csOff[c + 1] = m->csOff[c] + cnt[c];
-    m->maxMembs = std::max(m->maxMembs, cnt[c]);
-  }
-  m->csMem1.resize(m->csOff[nC]);
-  for (long long c = 0; c < nC; ++c)
-    for (int s = 0; s < cnt[c]; ++s)
-      m->csMem1[m->csOff[c] + s] = memb[(size_t)c * stencilSizeMax + s] + 1;
   // 1-based exports
   m->f2c1.resize(m->f2c.size());
   for (size_t i = 0; i < m->f2c.size(); ++i) m->f2c1[i] = m->f2c[i] + 1;
@@ -665,6 +406,51 @@ void build(rfmesh_s *m, int nThreads) {
     p.bf2c1.resize(p.bf2c.size());
     for (size_t i = 0; i < p.bf2c.size(); ++i) p.bf2c1[i] = p.bf2c[i] + 1;
   }
+  // c2c stencils (RFLU_ModStencilsCells.F90:750-1416) and moments
+  // (RFLU_ModWeights.F90:1770-1894): the per-cell routine shared with the
+  // device builder (rfmesh_stencil.h)
+  m->cv8.assign(8 * (size_t)nC, -1);
+  m->nv8.resize(nC);
+  for (long long c = 0; c < nC; ++c) {
+    m->nv8[c] = m->nv(c);
+    const int *v = m->verts(c);
+    for (int a = 0; a < m->nv(c); ++a) m->cv8[8 * (size_t)c + a] = v[a];
+  }
+  if (m->skipStencils) return;
+  const rfm::CellView view{m->cofg.data(), m->cv8.data(), m->nv8.data(), m->v2cOff.data(),
+                           m->v2c.data()};
+  std::vector<int> cnt(nC, 0);
+  std::vector<int> memb((size_t)nC * rfm::kStencilMax);
+  m->moms.assign(10 * (size_t)nC, 0.0);
+  int overflow = 0;
+#pragma omp parallel reduction(| : overflow)
+  {
+    rfm::Scratch w;
+#pragma omp for schedule(dynamic, 1024)
+    for (long long icg = 0; icg < nC; ++icg) {
+      const int degr = rfm::cell_stencil(view, (int)icg, &memb[(size_t)icg * rfm::kStencilMax],
+                                         &m->moms[10 * (size_t)icg], w);
+      if (degr < 0) overflow = 1;
+      cnt[icg] = degr < 0 ? 0 : degr;
+    }
+  }
+  if (overflow) throw std::runtime_error("vertex-neighbour list longer than the stencil builder holds");
+  set_stencils(m, cnt, memb);
+}
+
+// CSR stencils (1-based members) and the maximum size from per-cell lists of
+// kStencilMax slots.
+void set_stencils(rfmesh_s *m, const std::vector<int> &cnt, const std::vector<int> &memb) {
+  const long long nC = m->nCells;
+  m->csOff.assign(nC + 1, 0);
+  for (long long c = 0; c < nC; ++c) {
+    m->csOff[c + 1] = m->csOff[c] + cnt[c];
+    m->maxMembs = std::max(m->maxMembs, cnt[c]);
+  }
+  m->csMem1.resize(m->csOff[nC]);
+  for (long long c = 0; c < nC; ++c)
+    for (int s = 0; s < cnt[c]; ++s)
+      m->csMem1[m->csOff[c] + s] = memb[(size_t)c * rfm::kStencilMax + s] + 1;
 }
 
 }  // namespace
@@ -673,6 +459,12 @@ extern "C" {
 
 int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3], const double hi[3],
                       double jitter, unsigned long long seed, int nThreads, rfmesh_t *out) {
+  return rfmesh_create_box_ex(kind, nx, ny, nz, lo, hi, jitter, seed, nThreads, 0, out);
+}
+
+int rfmesh_create_box_ex(int kind, int nx, int ny, int nz, const double lo[3], const double hi[3],
+                         double jitter, unsigned long long seed, int nThreads, int flags,
+                         rfmesh_t *out) {
   if (!out || !lo || !hi || nx < 1 || ny < 1 || nz < 1 || kind < 0 || kind > 2 || jitter < 0 ||
       jitter >= 0.25)
     return RFMESH_ERR_ARG;
@@ -680,6 +472,7 @@ int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3], cons
   rfmesh_s *m = new (std::nothrow) rfmesh_s();
   if (!m) return RFMESH_ERR_NOMEM;
   m->kind = kind;
+  m->skipStencils = (flags & RFMESH_DEFER_STENCILS) != 0;
   for (int d = 0; d < 3; ++d) {
     m->lo[d] = lo[d];
     m->hi[d] = hi[d];
@@ -743,6 +536,40 @@ const int *rfmesh_c2cs_offsets(rfmesh_t m) { return m ? m->csOff.data() : nullpt
 const int *rfmesh_c2cs_members(rfmesh_t m) { return m ? m->csMem1.data() : nullptr; }
 const double *rfmesh_xyzmoms(rfmesh_t m) { return m ? m->moms.data() : nullptr; }
 const int *rfmesh_cell_type(rfmesh_t m) { return m ? m->ctype.data() : nullptr; }
+const int *rfmesh_cell_verts(rfmesh_t m) { return m ? m->cv8.data() : nullptr; }
+const int *rfmesh_cell_nverts(rfmesh_t m) { return m ? m->nv8.data() : nullptr; }
+const int *rfmesh_v2c_offsets(rfmesh_t m) { return m ? m->v2cOff.data() : nullptr; }
+const int *rfmesh_v2c(rfmesh_t m) { return m ? m->v2c.data() : nullptr; }
+const double *rfmesh_cofg_view(rfmesh_t m) { return m ? m->cofg.data() : nullptr; }
+
+int rfmesh_set_stencils(rfmesh_t m, const int *offsets, const int *members, const double *moms) {
+  if (!m || !offsets || !members || !moms) return RFMESH_ERR_ARG;
+  const long long nC = m->nCells;
+  if (offsets[0] != 0) return RFMESH_ERR_ARG;
+  for (long long c = 0; c < nC; ++c) {
+    const int k = offsets[c + 1] - offsets[c];
+    if (k < 0 || k > rfm::kStencilMax) return RFMESH_ERR_ARG;
+  }
+  try {
+    std::vector<int> cnt(nC), memb((size_t)nC * rfm::kStencilMax, 0);
+    for (long long c = 0; c < nC; ++c) {
+      cnt[c] = offsets[c + 1] - offsets[c];
+      for (int s = 0; s < cnt[c]; ++s) {
+        const int x = members[offsets[c] + s];
+        if (x < 1 || x > nC) return RFMESH_ERR_ARG;
+        memb[(size_t)c * rfm::kStencilMax + s] = x - 1;
+      }
+    }
+    m->maxMembs = 0;
+    set_stencils(m, cnt, memb);
+    m->moms.assign(moms, moms + 10 * (size_t)nC);
+  } catch (const std::bad_alloc &) {
+    return RFMESH_ERR_NOMEM;
+  }
+  m->skipStencils = false;
+  return RFMESH_OK;
+}
+
 const int *rfmesh_bf2c(rfmesh_t m, int ip) {
   return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].bf2c1.data() : nullptr;
 }

@@ -73,7 +73,8 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
-           "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning"]
+           "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
+           "rfgpu_mesh_stencils"]
 
 KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
            "dt_bface", "dt_cell", "dt_finalize"]
@@ -129,6 +130,7 @@ def load(path: Optional[str] = None):
         "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
         "rfgpu_batch_set_tuning": ([vp, C.c_int], C.c_int),
+        "rfgpu_mesh_stencils": ([C.c_int, C.c_int, ip, ip, ip, ip, dp, ip, ip, dp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -170,6 +172,24 @@ def mem_info():
     f, t = C.c_longlong(), C.c_longlong()
     _check(load().rfgpu_mem_info(C.byref(f), C.byref(t)), "rfgpu_mem_info")
     return f.value, t.value
+
+
+def mesh_stencils(n_cells: int, n_verts: int, cell_verts, cell_nverts, v2c_off, v2c, cofg):
+    """rfgpu_mesh_stencils: c2c stencils and WLSQ moments of every cell built on
+    the GPU with the host builder's per-cell routine.  Returns (offsets
+    (n+1, 0-based), members (1-based), moments (n, 10))."""
+    lib = load()
+    cv = np.ascontiguousarray(cell_verts, np.int32)
+    nv = np.ascontiguousarray(cell_nverts, np.int32)
+    vo = np.ascontiguousarray(v2c_off, np.int32)
+    vc = np.ascontiguousarray(v2c, np.int32)
+    cg = np.ascontiguousarray(cofg, np.float64)
+    off = np.empty(n_cells + 1, np.int32)
+    mem = np.empty(40 * n_cells, np.int32)
+    mom = np.empty((n_cells, 10), np.float64)
+    _check(lib.rfgpu_mesh_stencils(n_cells, n_verts, _ip(cv), _ip(nv), _ip(vo), _ip(vc), _dp(cg),
+                                   _ip(off), _ip(mem), _dp(mom)), "rfgpu_mesh_stencils")
+    return off, mem[:off[-1]].copy(), mom
 
 
 class PinnedArray:

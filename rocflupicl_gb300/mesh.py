@@ -31,6 +31,18 @@ def _load():
         lib.rfmesh_create_box.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int,
                                           C.POINTER(C.c_double), C.POINTER(C.c_double),
                                           C.c_double, C.c_ulonglong, C.c_int, C.POINTER(vp)]
+        lib.rfmesh_create_box_ex.argtypes = [C.c_int, C.c_int, C.c_int, C.c_int,
+                                             C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                             C.c_double, C.c_ulonglong, C.c_int, C.c_int,
+                                             C.POINTER(vp)]
+        for name in ("cell_verts", "cell_nverts", "v2c_offsets", "v2c"):
+            f = getattr(lib, "rfmesh_" + name)
+            f.argtypes = [vp]
+            f.restype = C.POINTER(C.c_int)
+        lib.rfmesh_cofg_view.argtypes = [vp]
+        lib.rfmesh_cofg_view.restype = C.POINTER(C.c_double)
+        lib.rfmesh_set_stencils.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                                            C.POINTER(C.c_double)]
         lib.rfmesh_destroy.argtypes = [vp]
         lib.rfmesh_sizes.argtypes = [vp, C.POINTER(C.c_longlong)]
         lib.rfmesh_patch_nbfaces.argtypes = [vp, C.c_int]
@@ -98,18 +110,42 @@ class BoxMesh:
         return int(self.c2cs_mem.shape[0])
 
 
+RFMESH_DEFER_STENCILS = 1
+
+
 def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
-        jitter: float = 0.0, seed: int = 0, threads: int = 0) -> BoxMesh:
-    """Build a box mesh (HEX / Kuhn TET / MIXED) and return its region arrays."""
+        jitter: float = 0.0, seed: int = 0, threads: int = 0, stencils: str = "host") -> BoxMesh:
+    """Build a box mesh (HEX / Kuhn TET / MIXED) and return its region arrays.
+    stencils="device" builds the c2c stencils and WLSQ moments on the GPU
+    (rfgpu_mesh_stencils: the host builder's per-cell routine, identical
+    output) and the rest on the host."""
+    if stencils not in ("host", "device"):
+        raise ValueError(stencils)
     lib = _load()
     h = C.c_void_p()
     lo_a = (C.c_double * 3)(*lo)
     hi_a = (C.c_double * 3)(*hi)
-    rc = lib.rfmesh_create_box(kind, nx, ny, nz, lo_a, hi_a, float(jitter), int(seed),
-                               int(threads), C.byref(h))
+    flags = RFMESH_DEFER_STENCILS if stencils == "device" else 0
+    rc = lib.rfmesh_create_box_ex(kind, nx, ny, nz, lo_a, hi_a, float(jitter), int(seed),
+                                  int(threads), flags, C.byref(h))
     if rc != 0:
         raise RuntimeError(f"rfmesh_create_box failed with code {rc}")
     try:
+        if stencils == "device":
+            from . import engine
+            s = (C.c_longlong * _NSIZES)()
+            lib.rfmesh_sizes(h, s)
+            nV, nC = s[0], s[1]
+            view = lambda p, n: np.ctypeslib.as_array(p, shape=(n,))
+            vo = view(lib.rfmesh_v2c_offsets(h), nV + 1)
+            off, mem, mom = engine.mesh_stencils(
+                nC, nV, view(lib.rfmesh_cell_verts(h), 8 * nC), view(lib.rfmesh_cell_nverts(h), nC),
+                vo, view(lib.rfmesh_v2c(h), int(vo[-1])), view(lib.rfmesh_cofg_view(h), 3 * nC))
+            rc = lib.rfmesh_set_stencils(h, off.ctypes.data_as(C.POINTER(C.c_int)),
+                                         mem.ctypes.data_as(C.POINTER(C.c_int)),
+                                         mom.ctypes.data_as(C.POINTER(C.c_double)))
+            if rc != 0:
+                raise RuntimeError(f"rfmesh_set_stencils failed with code {rc}")
         s = (C.c_longlong * _NSIZES)()
         lib.rfmesh_sizes(h, s)
         nV, nC, nF, nP, nM = s[0], s[1], s[2], s[3], s[4]

@@ -105,3 +105,41 @@ def test_perfmodel_matches_pass_totals():
     nc, nf, nb, m = 1000, 2000, 100, 40000
     assert P.stage_bytes(nc, nf, nb, m, 8) == 964 * nc + 4 * m + 112 * nf + 64 * nb
     assert P.stage_bytes(nc, nf, nb, m, 4) == 664 * nc + 4 * m + 112 * nf + 64 * nb
+
+
+def test_mesh_stencils_validates_before_any_device_work():
+    """rfgpu_mesh_stencils checks every index on the host: an out-of-range
+    vertex or cell id is refused with RFGPU_ERR_ARG before any CUDA call, so
+    this runs without a GPU."""
+    from rocflupicl_gb300 import engine as E
+    from rocflupicl_gb300 import mesh as M
+    import ctypes as C
+    lib = M._load()
+    h = C.c_void_p()
+    lo = (C.c_double * 3)(0.0, 0.0, 0.0)
+    hi = (C.c_double * 3)(1.0, 1.0, 1.0)
+    assert lib.rfmesh_create_box_ex(M.TET, 2, 2, 2, lo, hi, 0.0, 1, 0, M.RFMESH_DEFER_STENCILS,
+                                    C.byref(h)) == 0
+    try:
+        s = (C.c_longlong * M._NSIZES)()
+        lib.rfmesh_sizes(h, s)
+        nV, nC = s[0], s[1]
+        view = lambda p, n: np.ctypeslib.as_array(p, shape=(n,)).copy()
+        cv = view(lib.rfmesh_cell_verts(h), 8 * nC)
+        nv = view(lib.rfmesh_cell_nverts(h), nC)
+        vo = view(lib.rfmesh_v2c_offsets(h), nV + 1)
+        vc = view(lib.rfmesh_v2c(h), int(vo[-1]))
+        cg = np.ctypeslib.as_array(lib.rfmesh_cofg_view(h), shape=(3 * nC,)).copy()
+    finally:
+        lib.rfmesh_destroy(h)
+    for bad in ("vertex", "cell", "count"):
+        cv2, vc2, nv2 = cv.copy(), vc.copy(), nv.copy()
+        if bad == "vertex":
+            cv2[2] = nV  # a used slot of cell 0 (4 vertices)
+        elif bad == "cell":
+            vc2[3] = nC
+        else:
+            nv2[0] = 9
+        with pytest.raises(E.EngineError) as ei:
+            E.mesh_stencils(nC, nV, cv2, nv2, vo, vc2, cg)
+        assert ei.value.code == E.ERR_ARG

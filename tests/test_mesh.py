@@ -98,3 +98,42 @@ def test_bad_arguments_rejected():
         M.box(M.HEX, 0, 2, 2)
     with pytest.raises(RuntimeError):
         M.box(7, 2, 2, 2)
+
+
+def test_deferred_stencils_roundtrip():
+    """A mesh built with its stencils deferred and then given the host
+    builder's stencils and moments through rfmesh_set_stencils exports the
+    same arrays as a mesh built in one go (the path the GPU builder uses)."""
+    import ctypes as C
+    from rocflupicl_gb300 import mesh as M
+    ref = M.box(M.TET, 4, 3, 3, jitter=0.1, seed=9)
+    lib = M._load()
+    h = C.c_void_p()
+    lo = (C.c_double * 3)(0.0, 0.0, 0.0)
+    hi = (C.c_double * 3)(1.0, 1.0, 1.0)
+    assert lib.rfmesh_create_box_ex(M.TET, 4, 3, 3, lo, hi, 0.1, 9, 0, M.RFMESH_DEFER_STENCILS,
+                                    C.byref(h)) == 0
+    try:
+        off = np.ascontiguousarray(ref.c2cs_off, np.int32)
+        mem = np.ascontiguousarray(ref.c2cs_mem, np.int32)
+        mom = np.ascontiguousarray(ref.xyzmoms, np.float64)
+        assert lib.rfmesh_set_stencils(h, off.ctypes.data_as(C.POINTER(C.c_int)),
+                                       mem.ctypes.data_as(C.POINTER(C.c_int)),
+                                       mom.ctypes.data_as(C.POINTER(C.c_double))) == 0
+        n = ref.nCells
+        got_off = np.ctypeslib.as_array(lib.rfmesh_c2cs_offsets(h), shape=(n + 1,))
+        got_mem = np.ctypeslib.as_array(lib.rfmesh_c2cs_members(h), shape=(int(off[-1]),))
+        got_mom = np.ctypeslib.as_array(lib.rfmesh_xyzmoms(h), shape=(10 * n,))
+        assert np.array_equal(got_off, off) and np.array_equal(got_mem, mem)
+        assert np.array_equal(got_mom, mom.ravel())
+        cv = np.ctypeslib.as_array(lib.rfmesh_cell_verts(h), shape=(8 * n,)).reshape(n, 8)
+        nv = np.ctypeslib.as_array(lib.rfmesh_cell_nverts(h), shape=(n,))
+        assert np.all(nv == 4) and np.all(cv[:, 4:] == -1) and cv[:, :4].min() >= 0
+        # members out of range are refused
+        bad = mem.copy()
+        bad[0] = n + 1
+        assert lib.rfmesh_set_stencils(h, off.ctypes.data_as(C.POINTER(C.c_int)),
+                                       bad.ctypes.data_as(C.POINTER(C.c_int)),
+                                       mom.ctypes.data_as(C.POINTER(C.c_double))) != 0
+    finally:
+        lib.rfmesh_destroy(h)
