@@ -412,8 +412,8 @@ def main():
         serving.update({"rate_per_s": a.serve_rate, "t_end": a.serve_tend,
                         "max_active": srv.max_active, "batch_iterations": srv.iterations,
                         "cells": "6k^3, log-uniform 10k-4M", "precision": "mixed",
-                        "latency": "arrival -> state read back, including host mesh "
-                                   "preparation and queueing"})
+                        "latency": "arrival -> state read back, including mesh preparation "
+                                   "(host face list and geometry, GPU stencils) and queueing"})
 
     # ---- CPU baseline (rank 0) --------------------------------------------------
     cpu = None

@@ -1,8 +1,9 @@
 """Continuous-batching serving loop for solve requests.
 
 Requests (jittered-tet shock boxes of seeded size, Mach number and flux
-scheme) arrive as a Poisson stream.  Each is prepared on the host (mesh,
-stencils, initial state) by a thread pool as soon as it arrives, admitted to
+scheme) arrive as a Poisson stream.  Each is prepared by a thread pool as soon
+as it arrives (mesh, face list and geometry on the host; c2c stencils and
+moments on the GPU; initial state), admitted to
 the GPU when its device footprint fits the HBM budget, takes its first
 (dtImposed) step alone, and then joins the batch: every iteration advances all
 active solves by one time step with one launch per pass over all of them
@@ -69,9 +70,14 @@ def poisson_requests(count: int, lam: float, seed: int, cells_min: int = 10_000,
                     int(seed * 100003 + i)) for i in range(count)]
 
 
-def build_case(req: Request, precision: int = K.PREC_MIXED, threads: int = 4) -> K.Case:
+def build_case(req: Request, precision: int = K.PREC_MIXED, threads: int = 4,
+               stencils: str = "device") -> K.Case:
+    """The request's mesh and initial state.  stencils="device" builds the c2c
+    stencils and WLSQ moments on the GPU (identical to the host builder's),
+    the dominant part of the preparation on the host."""
     num = K.Numerics(spaceDiscr=req.scheme, precision=precision, venkatGuard=1)
-    return K.tet_shock_box(req.n, seed=req.seed, Ms=req.Ms, numerics=num, threads=threads)
+    return K.tet_shock_box(req.n, seed=req.seed, Ms=req.Ms, numerics=num, threads=threads,
+                           stencils=stencils)
 
 
 @dataclass
@@ -90,8 +96,10 @@ class Server:
     def __init__(self, t_end: float, hbm_budget: Optional[int] = None,
                  precision: int = K.PREC_MIXED, prepare_workers: int = 4,
                  mesh_threads: int = 4, keep_state: bool = False,
-                 bytes_per_cell: float = 800.0, max_steps: int = 100000):
+                 bytes_per_cell: float = 800.0, max_steps: int = 100000,
+                 stencils: str = "device"):
         self.t_end = t_end
+        self.stencils = stencils
         self.max_steps = max_steps
         self.precision = precision
         self.keep_state = keep_state
@@ -106,10 +114,21 @@ class Server:
         self.iterations = 0
         self.batch_launches = 0
 
+    @staticmethod
+    def _open(c: K.Case):
+        """Register a prepared case (host-side layout build, device upload) and
+        take its initial CFL time step; runs on a pool thread so the batch
+        keeps stepping meanwhile."""
+        reg = E.Region(c)
+        dti = reg.time_step(c.numerics.cfl, 1.0, 0.0, 1.0)
+        reg.set_time(0.0)
+        return reg, dti
+
     def run(self, requests: List[Request]) -> Dict[int, Result]:
         reqs = sorted(requests, key=lambda r: r.arrival)
         pool = ThreadPoolExecutor(self.prepare_workers)
         preparing = {}
+        opening = {}
         ready: List = []
         active: List[_Active] = []
         results: Dict[int, Result] = {}
@@ -125,26 +144,29 @@ class Server:
                 while nxt < len(reqs) and reqs[nxt].arrival <= now:
                     r = reqs[nxt]
                     preparing[r.rid] = (r, pool.submit(build_case, r, self.precision,
-                                                       self.mesh_threads))
+                                                       self.mesh_threads, self.stencils))
                     nxt += 1
                 for rid in [k for k, (_, f) in preparing.items() if f.done()]:
                     r, f = preparing.pop(rid)
                     ready.append((r, f.result()))
                 ready.sort(key=lambda x: x[0].arrival)
-                # admission: first come first served while the footprint fits
+                # admission: first come first served while the footprint fits; the
+                # footprint is reserved and the region is opened on a pool thread
                 while ready:
                     r, c = ready[0]
                     need = int(self.bytes_per_cell * c.mesh.nCells)
-                    if active and used + need > self.hbm_budget:
+                    if (active or opening) and used + need > self.hbm_budget:
                         break
                     ready.pop(0)
-                    reg = E.Region(c)
+                    used += need
+                    opening[r.rid] = (r, c, need, pool.submit(self._open, c))
+                for rid in [k for k, v in opening.items() if v[3].done()]:
+                    r, c, need, f = opening.pop(rid)
+                    reg, dti = f.result()
                     cfl = c.numerics.cfl
-                    dti = reg.time_step(cfl, 1.0, 0.0, 1.0)
-                    reg.set_time(0.0)
                     reg.step(cfl, dti, 0.0, self.t_end)   # first step: its own dtImposed
                     reg.sync()
-                    used += reg.device_bytes
+                    used += reg.device_bytes - need
                     active.append(_Active(r, c, reg, time.perf_counter() - t0, 1))
                     dirty = True
                 if active:
@@ -179,6 +201,9 @@ class Server:
                     time.sleep(0.0005)
         finally:
             pool.shutdown(wait=True)
+            for _, _, _, f in opening.values():
+                if f.done() and f.exception() is None:
+                    f.result()[0].close()
             if batch is not None:
                 batch.close()
             for a in active:
@@ -202,10 +227,10 @@ class Server:
 
 
 def solve_alone(req: Request, t_end: float, precision: int = K.PREC_MIXED,
-                max_steps: int = 100000):
+                max_steps: int = 100000, stencils: str = "device"):
     """The same request run by itself: first step with its own dtImposed, then
     device steps to the end time."""
-    c = build_case(req, precision)
+    c = build_case(req, precision, stencils=stencils)
     r = E.Region(c)
     cfl = c.numerics.cfl
     dti = r.time_step(cfl, 1.0, 0.0, 1.0)
@@ -227,7 +252,10 @@ def solve_alone(req: Request, t_end: float, precision: int = K.PREC_MIXED,
 def summarize(results: Dict[int, Result], wall: float) -> dict:
     lat = np.array([r.latency for r in results.values()])
     evals = sum(r.face_evals for r in results.values())
+    slow = sorted(results.values(), key=lambda r: -r.latency)[:3]
     return {"requests": len(results), "p50_s": float(np.percentile(lat, 50)),
             "p99_s": float(np.percentile(lat, 99)), "mean_s": float(lat.mean()),
+            "slowest": [{"cells": r.cells, "latency_s": r.latency, "admitted_after_s": r.queue,
+                         "steps": r.steps} for r in slow],
             "face_evals": int(evals), "wall_s": wall, "face_evals_per_s": evals / wall,
             "cells_total": int(sum(r.cells for r in results.values()))}
