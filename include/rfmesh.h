@@ -42,9 +42,10 @@ typedef struct rfmesh_s *rfmesh_t;
 enum {
   RFMESH_HEX = 0,   /* nx*ny*nz hexahedra */
   RFMESH_TET = 1,   /* every hex split into 6 Kuhn (Freudenthal) tets */
-  RFMESH_MIXED = 2  /* hexes; x>mid -> 2 prisms; z>mid -> 6 tets (prism
+  RFMESH_MIXED = 2, /* hexes; x>mid -> 2 prisms; z>mid -> 6 tets (prism
                        precedence); pyramid/tet transition cubes where a tet
                        cube meets a quad face, so the mesh is conforming */
+  RFMESH_GRID = 3   /* any grid of the reference's cell types (rfmesh_create_grid) */
 };
 
 /* patch order of box meshes */
@@ -77,6 +78,27 @@ int rfmesh_create_box(int kind, int nx, int ny, int nz, const double lo[3],
 int rfmesh_create_box_ex(int kind, int nx, int ny, int nz, const double lo[3],
                          const double hi[3], double jitter, unsigned long long seed,
                          int nThreads, int flags, rfmesh_t *out);
+/* Build from a grid in the reference's layout (what a .grda / .grd file
+ * holds, modflu/RFLU_ModReadWriteGrid.F90): xyz(3,nVert); tet2v(4,nTets),
+ * hex2v(8,nHexs), pri2v(6,nPris), pyr2v(5,nPyrs), 1-based, vertex orders of
+ * modflu/RFLU_ModGrid.F90:92-102; per patch its boundary triangles
+ * bTri2v[ip](3,nBTris[ip]) and quads bQuad2v[ip](4,nBQuads[ip]), 1-based.
+ * Cells are numbered tets, hexes, prisms, pyramids in file order; each
+ * boundary face is matched to its patch by vertex set, and a patch's faces
+ * keep the file's order (triangles, then quads).  Every index is validated
+ * (RFMESH_ERR_ARG); a boundary face in no patch, or a patch face that bounds
+ * no cell, gives RFMESH_ERR_GEOM. */
+int rfmesh_create_grid(int nVert, const double *xyz, int nTets, const int *tet2v, int nHexs,
+                       const int *hex2v, int nPris, const int *pri2v, int nPyrs,
+                       const int *pyr2v, int nPatches, const int *nBTris,
+                       const int *const *bTri2v, const int *nBQuads,
+                       const int *const *bQuad2v, int nThreads, int flags, rfmesh_t *out);
+/* cell-to-vertex lists of one type (0 tet, 1 hex, 2 prism, 3 pyramid),
+ * 0-based, (nv,nOfType) */
+const int *rfmesh_cell_conn(rfmesh_t m, int type);
+/* boundary face vertices of a patch, 0-based, (4,nBFaces), -1 for the 4th
+ * vertex of a triangle; oriented outward */
+const int *rfmesh_bf2v(rfmesh_t m, int iPatch);
 int rfmesh_destroy(rfmesh_t m);
 int rfmesh_sizes(rfmesh_t m, long long sizes[RFMESH_NSIZES]);
 int rfmesh_patch_nbfaces(rfmesh_t m, int iPatch);

@@ -227,3 +227,35 @@ def tube_ensemble(count: int = 256, seed: int = 11, n_min: int = 500, n_max: int
         c.n_steps = n_steps
         cases.append(c)
     return cases
+
+
+def from_files(grid_path: str, flow_path: str, bcs: List[PatchBC],
+               numerics: Optional[Numerics] = None, binary: bool = False, endian: str = "<",
+               threads: int = 0, stencils: str = "host") -> Case:
+    """A case from the reference's grid and flow files (.grda/.grd and the v2
+    flow file): the mesh is built from the grid by the same builder as the
+    synthetic meshes, cv comes from the flow file, dv from the EOS; bcs gives
+    each grid patch its boundary condition, in the grid's patch order."""
+    from . import rfluio as IO
+    num = numerics or Numerics()
+    g = IO.read_grid_binary(grid_path, endian) if binary else IO.read_grid_ascii(grid_path)
+    fl = IO.read_flow_binary(flow_path, endian) if binary else IO.read_flow_ascii(flow_path)
+    m = IO.mesh_of_grid(g, threads=threads, stencils=stencils)
+    if fl.cv.shape != (m.nCells, 5):
+        raise ValueError(f"flow file holds {fl.cv.shape}, the grid has {m.nCells} cells x 5")
+    if len(bcs) != len(m.patches):
+        raise ValueError(f"{len(bcs)} boundary conditions for {len(m.patches)} patches")
+    cv = np.ascontiguousarray(fl.cv)
+    return Case(f"files:{grid_path}", m, num, list(bcs), cv, eos_dv(num, cv),
+                meta={"time": fl.time, "grid": grid_path, "flow": flow_path})
+
+
+def write_flow(path: str, cv: np.ndarray, time: float = 0.0, binary: bool = False,
+               endian: str = "<") -> None:
+    """Write a state (nCells, 5) as the reference's v2 flow file."""
+    from . import rfluio as IO
+    fl = IO.Flow(np.ascontiguousarray(cv, np.float64), time=time)
+    if binary:
+        IO.write_flow_binary(path, fl, endian)
+    else:
+        IO.write_flow_ascii(path, fl)

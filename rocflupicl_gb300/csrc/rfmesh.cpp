@@ -7,6 +7,8 @@
 #include "rfmesh_stencil.h"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
@@ -54,7 +56,11 @@ struct rfmesh_s {
   std::vector<int> f2v;          // 4 per interior face
   std::vector<double> fn, fc;
   std::vector<int> f2c1;         // 1-based export
-  Patch patch[RFMESH_NPATCH];
+  std::vector<Patch> patch = std::vector<Patch>(RFMESH_NPATCH);
+  // grid meshes: boundary faces of patch ip, sorted-vertex keys in the grid
+  // file's order (triangles, then quads), and the key -> (patch, position) map
+  bool fromGrid = false;
+  std::vector<std::vector<std::array<int, 4>>> gridPatchKeys;
   std::vector<int> v2cOff, v2c;
   std::vector<int> csOff, csMem, csMem1;
   std::vector<double> moms;
@@ -293,6 +299,15 @@ void build(rfmesh_s *m, int nThreads) {
   std::vector<int64_t>().swap(next);
   std::vector<int>().swap(keyAll);
   const int64_t nAll = (int64_t)fc1.size();
+  // grid meshes: boundary face key -> (patch, position in the patch's file list)
+  std::map<std::array<int, 4>, std::pair<int, int>> gridKey;
+  std::vector<std::vector<std::pair<int, int64_t>>> gridSlot;  // per patch: (position, face)
+  if (m->fromGrid) {
+    gridSlot.resize(m->patch.size());
+    for (size_t ip = 0; ip < m->gridPatchKeys.size(); ++ip)
+      for (size_t q = 0; q < m->gridPatchKeys[ip].size(); ++q)
+        gridKey[m->gridPatchKeys[ip][q]] = {(int)ip, (int)q};
+  }
   // orient every face outward from its first cell, then split interior/boundary
   const double tolx = 1e-9 * (m->hi[0] - m->lo[0]), toly = 1e-9 * (m->hi[1] - m->lo[1]),
                tolz = 1e-9 * (m->hi[2] - m->lo[2]);
@@ -312,6 +327,13 @@ void build(rfmesh_s *m, int nThreads) {
       m->f2c.push_back(fc1[e]);
       m->f2c.push_back(fc2[e]);
       for (int a = 0; a < 4; ++a) m->f2v.push_back(fv[a]);
+    } else if (m->fromGrid) {
+      std::array<int, 4> key{fv[0], fv[1], fv[2], fv[3]};
+      const int nk = key[3] < 0 ? 3 : 4;
+      std::sort(key.begin(), key.begin() + nk);
+      auto it = gridKey.find(key);
+      if (it == gridKey.end()) throw std::runtime_error("boundary face in no patch");
+      gridSlot[it->second.first].push_back({it->second.second, e});
     } else {
       int ip = -1;
       if (std::fabs(C[0] - m->lo[0]) < tolx) ip = RFMESH_XLO;
@@ -323,6 +345,17 @@ void build(rfmesh_s *m, int nThreads) {
       if (ip < 0) throw std::runtime_error("boundary face off the box surface");
       m->patch[ip].bf2c.push_back(fc1[e]);
       for (int a = 0; a < 4; ++a) m->patch[ip].bf2v.push_back(fv[a]);
+    }
+  }
+  if (m->fromGrid) {  // patch faces in the grid file's order
+    for (size_t ip = 0; ip < gridSlot.size(); ++ip) {
+      std::sort(gridSlot[ip].begin(), gridSlot[ip].end());
+      if (gridSlot[ip].size() != m->gridPatchKeys[ip].size())
+        throw std::runtime_error("patch face that bounds no cell");
+      for (auto &sf : gridSlot[ip]) {
+        m->patch[ip].bf2c.push_back(fc1[sf.second]);
+        for (int a = 0; a < 4; ++a) m->patch[ip].bf2v.push_back(fvAll[4 * sf.second + a]);
+      }
     }
   }
   const int64_t nF = (int64_t)(m->f2c.size() / 2);
@@ -356,7 +389,7 @@ void build(rfmesh_s *m, int nThreads) {
     contrib(m->f2c[2 * f], S, C, 1.0);
     contrib(m->f2c[2 * f + 1], S, C, -1.0);
   }
-  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) {
+  for (int ip = 0; ip < (int)m->patch.size(); ++ip) {
     Patch &p = m->patch[ip];
     size_t nb = p.bf2c.size();
     p.fn.resize(4 * nb);
@@ -401,7 +434,7 @@ void build(rfmesh_s *m, int nThreads) {
   // 1-based exports
   m->f2c1.resize(m->f2c.size());
   for (size_t i = 0; i < m->f2c.size(); ++i) m->f2c1[i] = m->f2c[i] + 1;
-  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) {
+  for (int ip = 0; ip < (int)m->patch.size(); ++ip) {
     Patch &p = m->patch[ip];
     p.bf2c1.resize(p.bf2c.size());
     for (size_t i = 0; i < p.bf2c.size(); ++i) p.bf2c1[i] = p.bf2c[i] + 1;
@@ -501,6 +534,97 @@ int rfmesh_create_box_ex(int kind, int nx, int ny, int nz, const double lo[3], c
   return RFMESH_OK;
 }
 
+int rfmesh_create_grid(int nVert, const double *xyz, int nTets, const int *tet2v, int nHexs,
+                       const int *hex2v, int nPris, const int *pri2v, int nPyrs,
+                       const int *pyr2v, int nPatches, const int *nBTris,
+                       const int *const *bTri2v, const int *nBQuads,
+                       const int *const *bQuad2v, int nThreads, int flags, rfmesh_t *out) {
+  if (!out || nVert <= 0 || !xyz || nTets < 0 || nHexs < 0 || nPris < 0 || nPyrs < 0 ||
+      nPatches < 0 || (nPatches > 0 && (!nBTris || !nBQuads || !bTri2v || !bQuad2v)))
+    return RFMESH_ERR_ARG;
+  const int nCt[4] = {nTets, nHexs, nPris, nPyrs};
+  const int *c2v[4] = {tet2v, hex2v, pri2v, pyr2v};
+  for (int t = 0; t < 4; ++t) {
+    if (nCt[t] > 0 && !c2v[t]) return RFMESH_ERR_ARG;
+    for (long long i = 0; i < (long long)nCt[t] * kNV[t]; ++i)
+      if (c2v[t][i] < 1 || c2v[t][i] > nVert) return RFMESH_ERR_ARG;
+  }
+  if ((long long)nTets + nHexs + nPris + nPyrs <= 0) return RFMESH_ERR_ARG;
+  for (int ip = 0; ip < nPatches; ++ip) {
+    if (nBTris[ip] < 0 || nBQuads[ip] < 0 || (nBTris[ip] > 0 && !bTri2v[ip]) ||
+        (nBQuads[ip] > 0 && !bQuad2v[ip]))
+      return RFMESH_ERR_ARG;
+    for (long long i = 0; i < 3LL * nBTris[ip]; ++i)
+      if (bTri2v[ip][i] < 1 || bTri2v[ip][i] > nVert) return RFMESH_ERR_ARG;
+    for (long long i = 0; i < 4LL * nBQuads[ip]; ++i)
+      if (bQuad2v[ip][i] < 1 || bQuad2v[ip][i] > nVert) return RFMESH_ERR_ARG;
+  }
+  *out = nullptr;
+  rfmesh_s *m = new (std::nothrow) rfmesh_s();
+  if (!m) return RFMESH_ERR_NOMEM;
+  int rc = RFMESH_OK;
+#ifdef _OPENMP
+  int saved = omp_get_max_threads();
+  if (nThreads > 0) omp_set_num_threads(nThreads);
+#endif
+  try {
+    m->kind = RFMESH_GRID;
+    m->fromGrid = true;
+    m->skipStencils = (flags & RFMESH_DEFER_STENCILS) != 0;
+    m->xyz.assign(xyz, xyz + 3 * (size_t)nVert);
+    for (int d = 0; d < 3; ++d) {
+      m->lo[d] = m->hi[d] = xyz[d];
+      for (int v = 0; v < nVert; ++v) {
+        m->lo[d] = std::min(m->lo[d], xyz[3 * (size_t)v + d]);
+        m->hi[d] = std::max(m->hi[d], xyz[3 * (size_t)v + d]);
+      }
+    }
+    for (int t = 0; t < 4; ++t) {
+      m->nOfType[t] = nCt[t];
+      m->c2v[t].resize((size_t)nCt[t] * kNV[t]);
+      for (size_t i = 0; i < m->c2v[t].size(); ++i) m->c2v[t][i] = c2v[t][i] - 1;
+    }
+    m->patch.assign(nPatches, Patch());
+    m->gridPatchKeys.resize(nPatches);
+    for (int ip = 0; ip < nPatches; ++ip) {
+      for (int q = 0; q < nBTris[ip]; ++q) {
+        std::array<int, 4> k{bTri2v[ip][3 * q] - 1, bTri2v[ip][3 * q + 1] - 1,
+                             bTri2v[ip][3 * q + 2] - 1, -1};
+        std::sort(k.begin(), k.begin() + 3);
+        m->gridPatchKeys[ip].push_back(k);
+      }
+      for (int q = 0; q < nBQuads[ip]; ++q) {
+        std::array<int, 4> k{bQuad2v[ip][4 * q] - 1, bQuad2v[ip][4 * q + 1] - 1,
+                             bQuad2v[ip][4 * q + 2] - 1, bQuad2v[ip][4 * q + 3] - 1};
+        std::sort(k.begin(), k.end());
+        m->gridPatchKeys[ip].push_back(k);
+      }
+    }
+    build(m, nThreads);
+  } catch (const std::bad_alloc &) {
+    rc = RFMESH_ERR_NOMEM;
+  } catch (...) {
+    rc = RFMESH_ERR_GEOM;
+  }
+#ifdef _OPENMP
+  omp_set_num_threads(saved);
+#endif
+  if (rc != RFMESH_OK) {
+    delete m;
+    return rc;
+  }
+  *out = m;
+  return RFMESH_OK;
+}
+
+const int *rfmesh_bf2v(rfmesh_t m, int ip) {
+  return (m && ip >= 0 && ip < (int)m->patch.size()) ? m->patch[ip].bf2v.data() : nullptr;
+}
+
+const int *rfmesh_cell_conn(rfmesh_t m, int type) {
+  return (m && type >= 0 && type < 4) ? m->c2v[type].data() : nullptr;
+}
+
 int rfmesh_destroy(rfmesh_t m) {
   delete m;
   return RFMESH_OK;
@@ -511,18 +635,18 @@ int rfmesh_sizes(rfmesh_t m, long long s[RFMESH_NSIZES]) {
   s[RFMESH_NVERT] = (long long)(m->xyz.size() / 3);
   s[RFMESH_NCELLS] = m->nCells;
   s[RFMESH_NFACES] = (long long)(m->f2c.size() / 2);
-  s[RFMESH_NPATCHES] = RFMESH_NPATCH;
+  s[RFMESH_NPATCHES] = (long long)m->patch.size();
   s[RFMESH_NMEMBS] = (long long)m->csMem1.size();
   for (int t = 0; t < 4; ++t) s[RFMESH_NTETS + t] = m->nOfType[t];
   long long nb = 0;
-  for (int ip = 0; ip < RFMESH_NPATCH; ++ip) nb += (long long)m->patch[ip].bf2c.size();
+  for (int ip = 0; ip < (int)m->patch.size(); ++ip) nb += (long long)m->patch[ip].bf2c.size();
   s[RFMESH_NBFACES] = nb;
   s[RFMESH_MAXMEMBS] = m->maxMembs;
   return RFMESH_OK;
 }
 
 int rfmesh_patch_nbfaces(rfmesh_t m, int ip) {
-  if (!m || ip < 0 || ip >= RFMESH_NPATCH) return -1;
+  if (!m || ip < 0 || ip >= (int)m->patch.size()) return -1;
   return (int)m->patch[ip].bf2c.size();
 }
 
@@ -571,13 +695,13 @@ int rfmesh_set_stencils(rfmesh_t m, const int *offsets, const int *members, cons
 }
 
 const int *rfmesh_bf2c(rfmesh_t m, int ip) {
-  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].bf2c1.data() : nullptr;
+  return (m && ip >= 0 && ip < (int)m->patch.size()) ? m->patch[ip].bf2c1.data() : nullptr;
 }
 const double *rfmesh_bfn(rfmesh_t m, int ip) {
-  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].fn.data() : nullptr;
+  return (m && ip >= 0 && ip < (int)m->patch.size()) ? m->patch[ip].fn.data() : nullptr;
 }
 const double *rfmesh_bfc(rfmesh_t m, int ip) {
-  return (m && ip >= 0 && ip < RFMESH_NPATCH) ? m->patch[ip].fc.data() : nullptr;
+  return (m && ip >= 0 && ip < (int)m->patch.size()) ? m->patch[ip].fc.data() : nullptr;
 }
 
 }  // extern "C"

@@ -9,13 +9,13 @@ from __future__ import annotations
 
 import ctypes as C
 from dataclasses import dataclass, field
-from typing import List
+from typing import List, Optional
 
 import numpy as np
 
 from . import _build
 
-HEX, TET, MIXED = 0, 1, 2
+HEX, TET, MIXED, GRID = 0, 1, 2, 3
 XLO, XHI, YLO, YHI, ZLO, ZHI = range(6)
 _NSIZES = 11
 
@@ -43,6 +43,16 @@ def _load():
         lib.rfmesh_cofg_view.restype = C.POINTER(C.c_double)
         lib.rfmesh_set_stencils.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
+        ipp = C.POINTER(C.POINTER(C.c_int))
+        lib.rfmesh_create_grid.argtypes = [C.c_int, C.POINTER(C.c_double),
+                                           C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int),
+                                           C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int),
+                                           C.c_int, C.POINTER(C.c_int), ipp, C.POINTER(C.c_int),
+                                           ipp, C.c_int, C.c_int, C.POINTER(vp)]
+        lib.rfmesh_cell_conn.argtypes = [vp, C.c_int]
+        lib.rfmesh_cell_conn.restype = C.POINTER(C.c_int)
+        lib.rfmesh_bf2v.argtypes = [vp, C.c_int]
+        lib.rfmesh_bf2v.restype = C.POINTER(C.c_int)
         lib.rfmesh_destroy.argtypes = [vp]
         lib.rfmesh_sizes.argtypes = [vp, C.POINTER(C.c_longlong)]
         lib.rfmesh_patch_nbfaces.argtypes = [vp, C.c_int]
@@ -72,10 +82,12 @@ def _copy(ptr, n, dtype, shape):
 
 @dataclass
 class Patch:
-    """One boundary patch: faces bf2c (1-based), fn (nB,4), fc (nB,3)."""
+    """One boundary patch: faces bf2c (1-based), fn (nB,4), fc (nB,3), and the
+    face vertices bf2v (nB,4), 1-based, 0 for the 4th vertex of a triangle."""
     bf2c: np.ndarray
     fn: np.ndarray
     fc: np.ndarray
+    bf2v: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:
@@ -100,6 +112,8 @@ class BoxMesh:
     cell_type: np.ndarray
     patches: List[Patch] = field(default_factory=list)
     n_of_type: tuple = (0, 0, 0, 0)
+    # cell-to-vertex lists per type (tet, hex, prism, pyramid), 1-based, (n, nv)
+    conn: List[np.ndarray] = field(default_factory=list)
 
     @property
     def nBFaces(self) -> int:
@@ -131,44 +145,95 @@ def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 
     if rc != 0:
         raise RuntimeError(f"rfmesh_create_box failed with code {rc}")
     try:
-        if stencils == "device":
-            from . import engine
-            s = (C.c_longlong * _NSIZES)()
-            lib.rfmesh_sizes(h, s)
-            nV, nC = s[0], s[1]
-            view = lambda p, n: np.ctypeslib.as_array(p, shape=(n,))
-            vo = view(lib.rfmesh_v2c_offsets(h), nV + 1)
-            off, mem, mom = engine.mesh_stencils(
-                nC, nV, view(lib.rfmesh_cell_verts(h), 8 * nC), view(lib.rfmesh_cell_nverts(h), nC),
-                vo, view(lib.rfmesh_v2c(h), int(vo[-1])), view(lib.rfmesh_cofg_view(h), 3 * nC))
-            rc = lib.rfmesh_set_stencils(h, off.ctypes.data_as(C.POINTER(C.c_int)),
-                                         mem.ctypes.data_as(C.POINTER(C.c_int)),
-                                         mom.ctypes.data_as(C.POINTER(C.c_double)))
-            if rc != 0:
-                raise RuntimeError(f"rfmesh_set_stencils failed with code {rc}")
+        return _extract(lib, h, kind, (nx, ny, nz), stencils)
+    finally:
+        lib.rfmesh_destroy(h)
+
+
+_NV = (4, 8, 6, 5)
+
+
+def _extract(lib, h, kind, dims, stencils) -> BoxMesh:
+    """Region arrays of a built rfmesh handle (stencils built on the GPU first
+    when they were deferred)."""
+    if stencils == "device":
+        from . import engine
         s = (C.c_longlong * _NSIZES)()
         lib.rfmesh_sizes(h, s)
-        nV, nC, nF, nP, nM = s[0], s[1], s[2], s[3], s[4]
-        m = BoxMesh(
-            kind=kind, dims=(nx, ny, nz), nCells=nC, nFaces=nF,
-            xyz=_copy(lib.rfmesh_xyz(h), 3 * nV, np.float64, (nV, 3)),
-            vol=_copy(lib.rfmesh_vol(h), nC, np.float64, (nC,)),
-            cofg=_copy(lib.rfmesh_cofg(h), 3 * nC, np.float64, (nC, 3)),
-            f2c=_copy(lib.rfmesh_f2c(h), 2 * nF, np.int32, (nF, 2)),
-            fn=_copy(lib.rfmesh_fn(h), 4 * nF, np.float64, (nF, 4)),
-            fc=_copy(lib.rfmesh_fc(h), 3 * nF, np.float64, (nF, 3)),
-            c2cs_off=_copy(lib.rfmesh_c2cs_offsets(h), nC + 1, np.int32, (nC + 1,)),
-            c2cs_mem=_copy(lib.rfmesh_c2cs_members(h), nM, np.int32, (nM,)),
-            xyzmoms=_copy(lib.rfmesh_xyzmoms(h), 10 * nC, np.float64, (nC, 10)),
-            cell_type=_copy(lib.rfmesh_cell_type(h), nC, np.int32, (nC,)),
-            n_of_type=(s[5], s[6], s[7], s[8]),
-        )
-        for ip in range(nP):
-            nb = lib.rfmesh_patch_nbfaces(h, ip)
-            m.patches.append(Patch(
-                bf2c=_copy(lib.rfmesh_bf2c(h, ip), nb, np.int32, (nb,)),
-                fn=_copy(lib.rfmesh_bfn(h, ip), 4 * nb, np.float64, (nb, 4)),
-                fc=_copy(lib.rfmesh_bfc(h, ip), 3 * nb, np.float64, (nb, 3))))
-        return m
+        nV, nC = s[0], s[1]
+        view = lambda p, n: np.ctypeslib.as_array(p, shape=(n,))
+        vo = view(lib.rfmesh_v2c_offsets(h), nV + 1)
+        off, mem, mom = engine.mesh_stencils(
+            nC, nV, view(lib.rfmesh_cell_verts(h), 8 * nC), view(lib.rfmesh_cell_nverts(h), nC),
+            vo, view(lib.rfmesh_v2c(h), int(vo[-1])), view(lib.rfmesh_cofg_view(h), 3 * nC))
+        rc = lib.rfmesh_set_stencils(h, off.ctypes.data_as(C.POINTER(C.c_int)),
+                                     mem.ctypes.data_as(C.POINTER(C.c_int)),
+                                     mom.ctypes.data_as(C.POINTER(C.c_double)))
+        if rc != 0:
+            raise RuntimeError(f"rfmesh_set_stencils failed with code {rc}")
+    s = (C.c_longlong * _NSIZES)()
+    lib.rfmesh_sizes(h, s)
+    nV, nC, nF, nP, nM = s[0], s[1], s[2], s[3], s[4]
+    m = BoxMesh(
+        kind=kind, dims=dims, nCells=nC, nFaces=nF,
+        xyz=_copy(lib.rfmesh_xyz(h), 3 * nV, np.float64, (nV, 3)),
+        vol=_copy(lib.rfmesh_vol(h), nC, np.float64, (nC,)),
+        cofg=_copy(lib.rfmesh_cofg(h), 3 * nC, np.float64, (nC, 3)),
+        f2c=_copy(lib.rfmesh_f2c(h), 2 * nF, np.int32, (nF, 2)),
+        fn=_copy(lib.rfmesh_fn(h), 4 * nF, np.float64, (nF, 4)),
+        fc=_copy(lib.rfmesh_fc(h), 3 * nF, np.float64, (nF, 3)),
+        c2cs_off=_copy(lib.rfmesh_c2cs_offsets(h), nC + 1, np.int32, (nC + 1,)),
+        c2cs_mem=_copy(lib.rfmesh_c2cs_members(h), nM, np.int32, (nM,)),
+        xyzmoms=_copy(lib.rfmesh_xyzmoms(h), 10 * nC, np.float64, (nC, 10)),
+        cell_type=_copy(lib.rfmesh_cell_type(h), nC, np.int32, (nC,)),
+        n_of_type=(s[5], s[6], s[7], s[8]),
+    )
+    for ip in range(nP):
+        nb = lib.rfmesh_patch_nbfaces(h, ip)
+        m.patches.append(Patch(
+            bf2c=_copy(lib.rfmesh_bf2c(h, ip), nb, np.int32, (nb,)),
+            fn=_copy(lib.rfmesh_bfn(h, ip), 4 * nb, np.float64, (nb, 4)),
+            fc=_copy(lib.rfmesh_bfc(h, ip), 3 * nb, np.float64, (nb, 3)),
+            bf2v=_copy(lib.rfmesh_bf2v(h, ip), 4 * nb, np.int32, (nb, 4)) + 1))
+    m.conn = [_copy(lib.rfmesh_cell_conn(h, t), _NV[t] * int(s[5 + t]), np.int32,
+                    (int(s[5 + t]), _NV[t])) + 1 for t in range(4)]
+    return m
+
+
+def from_grid(xyz, tet2v=None, hex2v=None, pri2v=None, pyr2v=None, patches=(),
+              threads: int = 0, stencils: str = "host") -> BoxMesh:
+    """Region arrays of a grid in the reference's layout (rfmesh_create_grid):
+    xyz (nVert,3); tet2v (n,4), hex2v (n,8), pri2v (n,6), pyr2v (n,5), 1-based;
+    patches = [(tri2v (n,3), quad2v (n,4)), ...], 1-based."""
+    if stencils not in ("host", "device"):
+        raise ValueError(stencils)
+    lib = _load()
+    ip_t = C.POINTER(C.c_int)
+    keep = []
+
+    def arr(a, cols, dt=np.int32):
+        a = np.zeros((0, cols), dt) if a is None else np.ascontiguousarray(a, dt).reshape(-1, cols)
+        keep.append(a)
+        return a
+
+    xyz_a = arr(xyz, 3, np.float64)
+    conn = [arr(tet2v, 4), arr(hex2v, 8), arr(pri2v, 6), arr(pyr2v, 5)]
+    nP = len(patches)
+    tris = [arr(t, 3) for t, _ in patches]
+    quads = [arr(q, 4) for _, q in patches]
+    nT = (C.c_int * max(1, nP))(*[t.shape[0] for t in tris])
+    nQ = (C.c_int * max(1, nP))(*[q.shape[0] for q in quads])
+    pT = (ip_t * max(1, nP))(*[t.ctypes.data_as(ip_t) for t in tris])
+    pQ = (ip_t * max(1, nP))(*[q.ctypes.data_as(ip_t) for q in quads])
+    h = C.c_void_p()
+    flags = RFMESH_DEFER_STENCILS if stencils == "device" else 0
+    rc = lib.rfmesh_create_grid(
+        xyz_a.shape[0], xyz_a.ctypes.data_as(C.POINTER(C.c_double)),
+        *[v for c in conn for v in (c.shape[0], c.ctypes.data_as(ip_t))],
+        nP, nT, pT, nQ, pQ, int(threads), flags, C.byref(h))
+    if rc != 0:
+        raise RuntimeError(f"rfmesh_create_grid failed with code {rc}")
+    try:
+        return _extract(lib, h, GRID, (0, 0, 0), stencils)
     finally:
         lib.rfmesh_destroy(h)
