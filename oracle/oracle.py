@@ -39,7 +39,7 @@ class OrcPatch(C.Structure):
     _fields_ = [("bcType", C.c_int), ("spaceOrder", C.c_int), ("bcOptType", C.c_int),
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
-                ("distrib", C.c_int)]
+                ("distrib", C.c_int), ("nData", C.c_int)]
 
 
 class OrcRegion(C.Structure):
@@ -114,9 +114,9 @@ class Oracle:
             P.bf2c = _ip(keep(p.bf2c, np.int32))
             P.fn = _dp(keep(p.fn, np.float64))
             P.fc = _dp(keep(p.fc, np.float64))
-            vals = np.zeros(1) if bc.pout is None else np.atleast_1d(np.asarray(bc.pout, np.float64))
+            vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(keep(vals, np.float64))
-            P.distrib = 1 if vals.shape[0] > 1 else 0
+            P.distrib, P.nData = dist, nd
             np_ += 1
         reg.nPatches = np_
         reg.spaceDiscr, reg.spaceOrder, reg.reconst, reg.rkScheme = (

@@ -21,7 +21,7 @@
 namespace {
 
 // modfloflu/ModParameters.F90
-const int BC_OUTFLOW = 20, BC_SLIPWALL = 60;
+const int BC_OUTFLOW = 20, BC_SLIPWALL = 60, BC_FARFIELD = 80, BC_INJECTION = 90;
 const int BCOPT_SUPERSONIC = 0, BCOPT_SUBSONIC = 1, BCOPT_MIXED = 2;
 const int DISCR_UPW_ROE = 1, DISCR_UPW_HLLC = 3, DISCR_UPW_AUSMPLUS = 4;
 const int RECONST_LIM_VENKAT = 11;
@@ -302,10 +302,69 @@ void bcond_outflow_perf(int bcOpt, double pout, double sxn, double syn, double s
   }
 }
 
-// Boundary face flux: rocflu/RFLU_CentralSecondPatch.F90:638-1013 (ORDER 2)
-// and rocflu/RFLU_CentralFirstPatch.F90:575-946 (ORDER 1), slip wall and
-// outflow.  Slip walls leave the mass residual untouched (flx[0] unused,
-// returns false for it).
+// RFLU_SetRindStateFarfieldPerf (modflu/RFLU_ModRindStates.F90:249-421),
+// TCPERF, no lift correction (corrFlag false), ksg = 0.
+void rind_farfield_perf(double cpGas, double mmGas, double nx, double ny, double nz,
+                        double machInf, double pInf, double tInf, double alphaInf,
+                        double betaInf, double rl, double rul, double rvl, double rwl, double rel,
+                        double *rr, double *rur, double *rvr, double *rwr, double *rer,
+                        double *pr) {
+  double rGas = R_M(mmGas);
+  double gGas = G_CpR(cpGas, rGas);
+  double ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+  double ql = ul * nx + vl * ny + wl * nz;
+  double el = rel / rl;
+  double sl2 = ul * ul + vl * vl + wl * wl;
+  double pl = (gGas - 1.0) * rl * (el - 0.5 * sl2 - KSG);  // MixtPerf_P_DEoGVm2
+  double ri = pInf / (rGas * tInf);                        // MixtPerf_D_PRT
+  double pi = pInf;
+  double qi = machInf * std::sqrt(gGas * rGas * tInf);     // MixtPerf_C_GRT
+  double ui = qi * std::cos(alphaInf) * std::cos(betaInf);
+  double vi = qi * std::sin(alphaInf) * std::cos(betaInf);
+  double wi = qi * std::sin(betaInf);
+  if (machInf < 1.0) {
+    double al = C_DGP(rl, gGas, pl);
+    double pb, rb, ub, vb, wb;
+    if (ql < 0.0) {
+      pb = 0.5 * (pi + pl - rl * al * ((ui - ul) * nx + (vi - vl) * ny + (wi - wl) * nz));
+      rb = ri - (pi - pb) / (al * al);
+      ub = ui - nx * (pi - pb) / (rl * al);
+      vb = vi - ny * (pi - pb) / (rl * al);
+      wb = wi - nz * (pi - pb) / (rl * al);
+    } else {
+      pb = pi;
+      rb = rl - (pl - pi) / (al * al);
+      ub = ul + nx * (pl - pi) / (rl * al);
+      vb = vl + ny * (pl - pi) / (rl * al);
+      wb = wl + nz * (pl - pi) / (rl * al);
+    }
+    *rr = rb;
+    *rur = rb * ub;
+    *rvr = rb * vb;
+    *rwr = rb * wb;
+    *rer = rb * Eo_DGPUVW(rb, gGas, pb, ub, vb, wb, KSG);
+    *pr = pb;
+  } else if (ql < 0.0) {
+    *rr = ri;
+    *rur = ri * ui;
+    *rvr = ri * vi;
+    *rwr = ri * wi;
+    *rer = ri * (pi / (ri * (gGas - 1.0)) + 0.5 * qi * qi + KSG);  // MixtPerf_Eo_DGPVm
+    *pr = pi;
+  } else {
+    *rr = rl;
+    *rur = rul;
+    *rvr = rvl;
+    *rwr = rwl;
+    *rer = rel;
+    *pr = pl;
+  }
+}
+
+// Boundary face flux: rocflu/RFLU_CentralSecondPatch.F90:638-1351 (ORDER 2)
+// and rocflu/RFLU_CentralFirstPatch.F90:575-1133 (ORDER 1): slip wall,
+// outflow, farfield and injection.  Slip walls leave the mass residual
+// untouched (flx[0] unused, returns false for it).
 void patch_flux(const Ctx &c, const orc_patch_t &p, int ifl, double flx[5], bool *hasMass) {
   const orc_region_t *r = c.r;
   int c1 = p.bf2c[ifl];
@@ -332,8 +391,34 @@ void patch_flux(const Ctx &c, const orc_patch_t &p, int ifl, double flx[5], bool
     *hasMass = false;
     return;
   }
-  // BC_OUTFLOW
+  const int nData = p.nData > 0 ? p.nData : 1;
+  const double *vals = p.vals ? p.vals + (size_t)nData * (p.distrib ? ifl : 0) : nullptr;
   double cp = r->gvCp, mm = r->gvMol;
+  if (p.bcType == BC_INJECTION && vals[0] > 0.0) {
+    // burning surface: RFLU_SetRindStateInjectPerf (RFLU_ModRindStates.F90:460-505)
+    double pl;
+    if (p.spaceOrder == 2) {
+      double S[5], ir;
+      recon(c, c1, fcx, S, &ir, true);
+      pl = S[4];
+    } else {
+      pl = pdv;
+    }
+    double minj = vals[0], tinj = vals[1];
+    double rGas = R_M(mm);
+    double rl = pl / (rGas * tinj);                              // MixtPerf_D_PRT
+    double ql = -minj / rl + fs;
+    double ul = ql * nx, vl = ql * ny, wl = ql * nz;
+    double Hl = cp * tinj + 0.5 * (ul * ul + vl * vl + wl * wl) + 0.0;  // MixtPerf_Ho_CpTUVW
+    flx[0] = -minj * nm;
+    flx[1] = (-minj * ul + pl * nx) * nm;
+    flx[2] = (-minj * vl + pl * ny) * nm;
+    flx[3] = (-minj * wl + pl * nz) * nm;
+    flx[4] = (-minj * Hl + pl * fs) * nm;
+    *hasMass = true;
+    return;
+  }
+  // outflow, farfield, injection surface not burning
   double rl, rul, rvl, rwl, rel, pl;
   if (p.spaceOrder == 2) {
     double S[5], ir;
@@ -354,11 +439,39 @@ void patch_flux(const Ctx &c, const orc_patch_t &p, int ifl, double flx[5], bool
     rel = cv[4];
     pl = pdv;
   }
+  if (p.bcType == BC_INJECTION) {
+    // RFLU_SetRindStateSlipWallPerf (RFLU_ModRindStates.F90:539-588)
+    double rGas = R_M(mm);
+    double gGas = G_CpR(cp, rGas);
+    double irl = 1.0 / rl;
+    double ul = irl * rul, vl = irl * rvl, wl = irl * rwl;
+    double ql = ul * nx + vl * ny + wl * nz - fs;
+    double al = C_DGP(rl, gGas, pl);
+    if (ql < 0.0) {
+      double term = 1.0 + 0.5 * (gGas - 1.0) * ql / al;
+      pl = pl * std::pow(term, 2.0 * gGas / (gGas - 1.0));
+    } else {
+      double term = (gGas + 1.0) / 4.0;
+      pl = pl + term * rl * ql * (ql + std::sqrt(al * al + term * term * ql * ql) / term);
+    }
+    flx[0] = 0.0;
+    flx[1] = pl * nx * nm;
+    flx[2] = pl * ny * nm;
+    flx[3] = pl * nz * nm;
+    flx[4] = pl * fs * nm;
+    *hasMass = true;
+    return;
+  }
   double pr = pl;
-  if (p.bcOptType != BCOPT_SUPERSONIC) pr = p.vals[p.distrib ? ifl : 0];
   double rr, rur, rvr, rwr, rer;
-  bcond_outflow_perf(p.bcOptType, pr, nx, ny, nz, cp, mm, rl, rul, rvl, rwl, rel, pl, &rr, &rur,
-                     &rvr, &rwr, &rer);
+  if (p.bcType == BC_FARFIELD) {
+    rind_farfield_perf(cp, mm, nx, ny, nz, vals[0], vals[3], vals[4], vals[1], vals[2], rl, rul,
+                       rvl, rwl, rel, &rr, &rur, &rvr, &rwr, &rer, &pr);
+  } else {
+    if (p.bcOptType != BCOPT_SUPERSONIC) pr = vals[0];
+    bcond_outflow_perf(p.bcOptType, pr, nx, ny, nz, cp, mm, rl, rul, rvl, rwl, rel, pl, &rr,
+                       &rur, &rvr, &rwr, &rer);
+  }
   double ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
   double qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
   flx[0] = 0.5 * (ql * rl + qr * rr) * nm;

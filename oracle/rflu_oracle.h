@@ -25,15 +25,18 @@ extern "C" {
 #define ORC_MAX_PATCHES 16
 
 typedef struct {
-  int bcType;      /* BC_SLIPWALL=60, BC_OUTFLOW=20 (modfloflu/ModParameters.F90:401,413) */
+  int bcType;      /* BC_OUTFLOW=20, BC_SLIPWALL=60, BC_FARFIELD=80, BC_INJECTION=90
+                      (modfloflu/ModParameters.F90:398-434) */
   int spaceOrder;  /* 1 or 2 */
   int bcOptType;   /* outflow: BCOPT_SUPERSONIC=0, SUBSONIC=1, MIXED=2 */
   int nBFaces;
   const int *bf2c;      /* (nBFaces) 1-based */
   const double *fn;     /* (4,nBFaces) */
   const double *fc;     /* (3,nBFaces) */
-  const double *vals;   /* outflow static pressure, (nBFaces) if distrib else (1) */
+  const double *vals;   /* vals(nData,nBFaces) if distrib else vals(nData,1): outflow PRESS;
+                           farfield MACH, ATTACK, SLIP, PRESS, TEMP; injection MFRATE, TEMP */
   int distrib;
+  int nData;            /* leading dimension of vals (0 read as 1) */
 } orc_patch_t;
 
 typedef struct {

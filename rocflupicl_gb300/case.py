@@ -19,7 +19,7 @@ from . import mesh as _mesh
 DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS = 1, 3, 4
 RECONST_NONE, RECONST_LIM_VENKAT = 0, 11
 RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
-BC_OUTFLOW, BC_SLIPWALL = 20, 60
+BC_OUTFLOW, BC_SLIPWALL, BC_FARFIELD, BC_INJECTION = 20, 60, 80, 90
 BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 
@@ -64,6 +64,23 @@ class PatchBC:
     spaceOrder: int = 1          # .bc ORDER; defaults to spaceOrderBFaces = 1
     bcOptType: int = BCOPT_SUPERSONIC
     pout: Optional[np.ndarray] = None  # outflow static pressure (1,) or (nBFaces,)
+    # patch data (pPatch%mixt%vals): (nData,) for the whole patch or (nBFaces, nData);
+    # farfield (MACH, ATTACK, SLIP, PRESS, TEMP), injection (MFRATE, TEMP)
+    vals: Optional[np.ndarray] = None
+
+    def vals_array(self, n_bfaces: int):
+        """(vals (rows, nData) contiguous, nData, distrib) as the C ABI takes them."""
+        if self.vals is not None:
+            v = np.asarray(self.vals, np.float64)
+            if v.ndim == 1:
+                return np.ascontiguousarray(v.reshape(1, -1)), v.shape[0], 0
+            if v.shape[0] != n_bfaces:
+                raise ValueError("per-face patch values need one row per boundary face")
+            return np.ascontiguousarray(v), v.shape[1], 1
+        if self.pout is None:
+            return np.zeros((1, 1)), 1, 0
+        p = np.atleast_1d(np.asarray(self.pout, np.float64))
+        return np.ascontiguousarray(p.reshape(-1, 1)), 1, 1 if p.shape[0] > 1 else 0
 
 
 @dataclass

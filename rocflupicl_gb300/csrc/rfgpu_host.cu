@@ -194,12 +194,21 @@ int check_desc(const rfgpu_region_desc_t *d) {
   for (int ip = 0; ip < d->nPatches; ++ip) {
     const rfgpu_patch_t &p = d->patches[ip];
     if (p.nBFaces < 0 || (p.nBFaces > 0 && (!p.bf2c || !p.fn || !p.fc))) return RFGPU_ERR_ARG;
-    if (p.bcType != RFGPU_BC_SLIPWALL && p.bcType != RFGPU_BC_OUTFLOW) return RFGPU_ERR_UNSUPPORTED;
+    if (p.bcType != RFGPU_BC_SLIPWALL && p.bcType != RFGPU_BC_OUTFLOW &&
+        p.bcType != RFGPU_BC_FARFIELD && p.bcType != RFGPU_BC_INJECTION)
+      return RFGPU_ERR_UNSUPPORTED;
     if (p.spaceOrder != 1 && p.spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
+    if (p.nData < 0) return RFGPU_ERR_ARG;
+    const int nData = p.nData > 0 ? p.nData : 1;
     if (p.bcType == RFGPU_BC_OUTFLOW) {
       if (p.bcOptType < 0 || p.bcOptType > 2) return RFGPU_ERR_UNSUPPORTED;
       if (p.bcOptType != RFGPU_BCOPT_SUPERSONIC && !p.vals) return RFGPU_ERR_ARG;
     }
+    if (p.bcType == RFGPU_BC_FARFIELD) {
+      if (p.bcOptType != 0) return RFGPU_ERR_UNSUPPORTED;  // lift correction (airfoil-specific)
+      if (!p.vals || nData < 5) return RFGPU_ERR_ARG;
+    }
+    if (p.bcType == RFGPU_BC_INJECTION && (!p.vals || nData < 2)) return RFGPU_ERR_ARG;
   }
   const long long N = d->nCells;
   for (int f = 0; f < d->nFaces; ++f)
@@ -233,6 +242,25 @@ template <>
 RegionDev<double> &rd<double>(rfgpu_region_s *h) { return h->rd64; }
 template <>
 RegionDev<float> &rd<float>(rfgpu_region_s *h) { return h->rd32; }
+
+// Free-stream state of a farfield face (RFLU_SetRindStateFarfieldPerf,
+// modflu/RFLU_ModRindStates.F90:249-421, the part that depends only on the
+// patch values): ri = p/(R T), pi = p, qi = M sqrt(g R T) and its components
+// along the angles of attack and sideslip, in this order of operations.
+void farfield_state(const Phys &ph, const double *v, double dat[8]) {
+  const double machInf = v[0], alphaInf = v[1], betaInf = v[2], pInf = v[3], tInf = v[4];
+  const double rGas = ph.gvR, gGas = ph.gvG;
+  const double ri = pInf / (rGas * tInf);
+  const double qi = machInf * std::sqrt(gGas * rGas * tInf);
+  dat[0] = ri;
+  dat[1] = pInf;
+  dat[2] = qi;
+  dat[3] = qi * std::cos(alphaInf) * std::cos(betaInf);
+  dat[4] = qi * std::sin(alphaInf) * std::cos(betaInf);
+  dat[5] = qi * std::sin(betaInf);
+  dat[6] = machInf;
+  dat[7] = 0.0;
+}
 
 // Device numbering of cells and interior faces.  Empty maps: the host's.
 struct Order {
@@ -440,17 +468,29 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.flux = M.alloc<R>(8 * (size_t)F);
   // ---- boundary faces, patches in order
   std::vector<int> bf2c, bkind;
-  std::vector<double> bfnA, bfdA, bpout;
+  std::vector<double> bfnA, bfdA, bpout, bdat;
   for (int ip = 0; ip < d->nPatches; ++ip) {
     const rfgpu_patch_t &p = d->patches[ip];
-    int type = p.bcType == RFGPU_BC_SLIPWALL ? BK_SLIP : BK_OUTFLOW;
+    const int type = p.bcType == RFGPU_BC_SLIPWALL   ? BK_SLIP
+                     : p.bcType == RFGPU_BC_OUTFLOW  ? BK_OUTFLOW
+                     : p.bcType == RFGPU_BC_FARFIELD ? BK_FARFIELD
+                                                     : BK_INJECTION;
+    const int nData = p.nData > 0 ? p.nData : 1;
     for (int b = 0; b < p.nBFaces; ++b) {
       int c = o.nc(p.bf2c[b] - 1);
       bf2c.push_back(c);
       bkind.push_back(bk_pack(type, p.spaceOrder, type == BK_OUTFLOW ? p.bcOptType : 0));
       double pout = 0.0;
-      if (type == BK_OUTFLOW && p.bcOptType != RFGPU_BCOPT_SUPERSONIC) pout = p.vals[p.distrib ? b : 0];
+      const double *v = p.vals ? p.vals + (size_t)nData * (p.distrib ? b : 0) : nullptr;
+      if (type == BK_OUTFLOW && p.bcOptType != RFGPU_BCOPT_SUPERSONIC) pout = v[0];
       bpout.push_back(pout);
+      double dat[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      if (type == BK_FARFIELD) farfield_state(ph, v, dat);
+      if (type == BK_INJECTION) {
+        dat[0] = v[0];  // MFRATE
+        dat[1] = v[1];  // TEMP
+      }
+      bdat.insert(bdat.end(), dat, dat + 8);
       for (int k = 0; k < 4; ++k) bfnA.push_back(p.fn[4 * (size_t)b + k]);
       for (int k = 0; k < 3; ++k) bfdA.push_back(p.fc[3 * (size_t)b + k] - cofg[(size_t)k * N + c]);
     }
@@ -463,6 +503,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.bf2c = M.upload(bf2c, s);
   g.bkind = M.upload(bkind, s);
   g.bpout = M.upload(bpout, s);
+  g.bdat = M.upload(cast<R>(bdat), s);
   g.bfnA = M.upload(cast<R>(bfnA), s);
   g.bfd = M.upload(cast<R>(bfd), s);
   g.bflux = M.alloc<R>(8 * (size_t)B);

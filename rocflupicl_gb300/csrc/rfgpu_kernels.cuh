@@ -737,6 +737,60 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
   }
 }
 
+// Farfield rind state, RFLU_SetRindStateFarfieldPerf
+// (modflu/RFLU_ModRindStates.F90:249-421) without the airfoil lift
+// correction; fd = (ri, pi, qi, ui, vi, wi, machInf) of the face, evaluated
+// on the host.  Subsonic: characteristic combination of the interior and
+// free-stream states; supersonic: free stream in, interior out.
+template <typename R>
+__device__ __forceinline__ void farfield_rind(const R *fd, R gGas, R nx, R ny, R nz, R rl, R rul,
+                                              R rvl, R rwl, R rel, R &rr, R &rur, R &rvr, R &rwr,
+                                              R &rer, R &pr) {
+  const R ri = fd[0], pi = fd[1], qi = fd[2], ui = fd[3], vi = fd[4], wi = fd[5], machInf = fd[6];
+  const R ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+  const R ql = ul * nx + vl * ny + wl * nz;
+  const R el = rel / rl;
+  const R sl2 = ul * ul + vl * vl + wl * wl;
+  const R pl = (gGas - R(1)) * rl * (el - R(0.5) * sl2 - R(0));
+  if (machInf < R(1)) {
+    const R al = sqrt(gGas * pl / rl);
+    R pb, rb, ub, vb, wb;
+    if (ql < R(0)) {
+      pb = R(0.5) * (pi + pl - rl * al * ((ui - ul) * nx + (vi - vl) * ny + (wi - wl) * nz));
+      rb = ri - (pi - pb) / (al * al);
+      ub = ui - nx * (pi - pb) / (rl * al);
+      vb = vi - ny * (pi - pb) / (rl * al);
+      wb = wi - nz * (pi - pb) / (rl * al);
+    } else {
+      pb = pi;
+      rb = rl - (pl - pi) / (al * al);
+      ub = ul + nx * (pl - pi) / (rl * al);
+      vb = vl + ny * (pl - pi) / (rl * al);
+      wb = wl + nz * (pl - pi) / (rl * al);
+    }
+    rr = rb;
+    rur = rb * ub;
+    rvr = rb * vb;
+    rwr = rb * wb;
+    rer = rb * eo_dgpuvw(rb, gGas, pb, ub, vb, wb);
+    pr = pb;
+  } else if (ql < R(0)) {
+    rr = ri;
+    rur = ri * ui;
+    rvr = ri * vi;
+    rwr = ri * wi;
+    rer = ri * (pi / (ri * (gGas - R(1))) + R(0.5) * qi * qi + R(0));  // MixtPerf_Eo_DGPVm
+    pr = pi;
+  } else {
+    rr = rl;
+    rur = rul;
+    rvr = rvl;
+    rwr = rwl;
+    rer = rel;
+    pr = pl;
+  }
+}
+
 // Outflow boundary state, libfloflu/BcondOutflowPerf.F90:88-160 (ksg = 0).
 template <typename R>
 __device__ __forceinline__ void bcond_outflow(int bcOpt, R pout, R sxn, R syn, R szn, R gamma,
@@ -803,6 +857,7 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       ld16(g.grad + 16 * (size_t)c, G);
       reconstruct(G, g.bfd[b], g.bfd[B + b], g.bfd[2 * B + b], S);
     }
+    const R gvG = PC<R>{g.ph}.gvG();
     if (type == BK_SLIP) {
       R pl = S[4];
       flx[0] = R(-0.0);
@@ -810,8 +865,22 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       flx[2] = pl * ny * nm;
       flx[3] = pl * nz * nm;
       flx[4] = pl * fs * nm;
+    } else if (type == BK_INJECTION && g.bdat[8 * (size_t)b] > R(0)) {
+      // burning surface (RFLU_CentralSecondPatch.F90:1237-1351 / FirstPatch
+      // :1049-1133 with RFLU_SetRindStateInjectPerf, RFLU_ModRindStates.F90:460-505)
+      const R minj = g.bdat[8 * (size_t)b], tinj = g.bdat[8 * (size_t)b + 1];
+      const R rGas = R(g.ph.gvR), cpGas = R(g.ph.gvCp);
+      const R pl = S[4];
+      const R rl = pl / (rGas * tinj);
+      const R ql = -minj / rl + fs;
+      const R ul = ql * nx, vl = ql * ny, wl = ql * nz;
+      const R Hl = cpGas * tinj + R(0.5) * (ul * ul + vl * vl + wl * wl) + R(0);
+      flx[0] = -minj * nm;
+      flx[1] = (-minj * ul + pl * nx) * nm;
+      flx[2] = (-minj * vl + pl * ny) * nm;
+      flx[3] = (-minj * wl + pl * nz) * nm;
+      flx[4] = (-minj * Hl + pl * fs) * nm;
     } else {
-      const R gvG = PC<R>{g.ph}.gvG();
       R rl, rul, rvl, rwl, rel, pl;
       if (order == 2) {
         rl = S[0];
@@ -836,16 +905,43 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
           rel = rl * eo_dgpuvw(rl, gvG, pl, u, v, w);
         }
       }
-      R pr = (opt != 0) ? R(g.bpout[b]) : pl;
-      R rr, rur, rvr, rwr, rer;
-      bcond_outflow(opt, pr, nx, ny, nz, gvG, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr, rer);
-      R ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
-      R qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
-      flx[0] = R(0.5) * (ql * rl + qr * rr) * nm;
-      flx[1] = R(0.5) * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
-      flx[2] = R(0.5) * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
-      flx[3] = R(0.5) * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
-      flx[4] = R(0.5) * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+      if (type == BK_INJECTION) {
+        // surface not burning: slip-wall rind pressure (RFLU_SetRindStateSlipWallPerf,
+        // RFLU_ModRindStates.F90:539-588); the mass flux is a +0 contribution
+        const R irl = R(1) / rl;
+        const R ul = irl * rul, vl = irl * rvl, wl = irl * rwl;
+        const R ql = ul * nx + vl * ny + wl * nz - fs;
+        const R al = sqrt(gvG * pl / rl);
+        if (ql < R(0)) {
+          const R term = R(1) + R(0.5) * (gvG - R(1)) * ql / al;
+          pl = pl * pow(term, R(2) * gvG / (gvG - R(1)));
+        } else {
+          const R term = (gvG + R(1)) / R(4);
+          pl = pl + term * rl * ql * (ql + sqrt(al * al + term * term * ql * ql) / term);
+        }
+        flx[0] = R(0);
+        flx[1] = pl * nx * nm;
+        flx[2] = pl * ny * nm;
+        flx[3] = pl * nz * nm;
+        flx[4] = pl * fs * nm;
+      } else {
+        R pr, rr, rur, rvr, rwr, rer;
+        if (type == BK_FARFIELD) {
+          farfield_rind(g.bdat + 8 * (size_t)b, gvG, nx, ny, nz, rl, rul, rvl, rwl, rel, rr, rur,
+                        rvr, rwr, rer, pr);
+        } else {
+          pr = (opt != 0) ? R(g.bpout[b]) : pl;
+          bcond_outflow(opt, pr, nx, ny, nz, gvG, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr,
+                        rer);
+        }
+        R ql = (rul * nx + rvl * ny + rwl * nz) / rl - fs;
+        R qr = (rur * nx + rvr * ny + rwr * nz) / rr - fs;
+        flx[0] = R(0.5) * (ql * rl + qr * rr) * nm;
+        flx[1] = R(0.5) * (ql * rul + pl * nx + qr * rur + pr * nx) * nm;
+        flx[2] = R(0.5) * (ql * rvl + pl * ny + qr * rvr + pr * ny) * nm;
+        flx[3] = R(0.5) * (ql * rwl + pl * nz + qr * rwr + pr * nz) * nm;
+        flx[4] = R(0.5) * (ql * (rel + pl) + pl * fs + qr * (rer + pr) + pr * fs) * nm;
+      }
     }
     flx[5] = flx[6] = flx[7] = R(0);
     st8(g.bflux + 8 * (size_t)b, flx);

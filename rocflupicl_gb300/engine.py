@@ -40,7 +40,7 @@ class PatchT(C.Structure):
     _fields_ = [("bcType", C.c_int), ("spaceOrder", C.c_int), ("bcOptType", C.c_int),
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
-                ("distrib", C.c_int)]
+                ("distrib", C.c_int), ("nData", C.c_int)]
 
 
 class RegionDescT(C.Structure):
@@ -243,9 +243,9 @@ class Region:
             P.bf2c = _ip(k(p.bf2c, np.int32))
             P.fn = _dp(k(p.fn, np.float64))
             P.fc = _dp(k(p.fc, np.float64))
-            vals = np.zeros(1) if bc.pout is None else np.atleast_1d(np.asarray(bc.pout, np.float64))
+            vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(k(vals, np.float64))
-            P.distrib = 1 if vals.shape[0] > 1 else 0
+            P.distrib, P.nData = dist, nd
         d = RegionDescT()
         d.nCells, d.nFaces, d.f2cLd = m.nCells, m.nFaces, 2
         d.f2c = _ip(k(m.f2c, np.int32))

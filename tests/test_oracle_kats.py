@@ -141,3 +141,50 @@ def test_first_step_uses_imposed_dt():
     assert o.dt(c.cv, c.dv, 0.5, 1.234e-4, 0.0, 0.0) == 1.0 / (1.0 / 1.234e-4)
     assert abs(o.dt(c.cv, c.dv, 0.5, 1.234e-4, 0.0, 1e-3) - d_cfl) <= 1e-18
     assert o.dt(c.cv, c.dv, 0.5, 1.0, 1.0, 1.0) == 1.0   # dtMinLimit floor
+
+
+def _farfield_state(num, mach, alpha, beta, p, T):
+    """Free-stream primitive state of the farfield values (reference units)."""
+    R = 8314.3 / num.gv[1]
+    g = num.gv[0] / (num.gv[0] - R)
+    r = p / (R * T)
+    q = mach * np.sqrt(g * R * T)
+    return r, q * np.cos(alpha) * np.cos(beta), q * np.sin(alpha) * np.cos(beta), q * np.sin(beta)
+
+
+@pytest.mark.parametrize("mach", [0.5, 2.0])
+@pytest.mark.parametrize("order", [1, 2])
+def test_farfield_preserves_its_free_stream(mach, order):
+    """With the interior at the farfield's own free-stream state every face
+    (interior: consistency of the Riemann flux; farfield: the rind state is the
+    free stream, subsonic and supersonic branches) carries the physical flux
+    of one uniform state, so every closed cell's residual vanishes."""
+    c = K.tet_shock_box(3, seed=2, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_ROE))
+    alpha, beta, p, T = 0.3, 0.1, 9.0e4, 280.0
+    vals = np.array([mach, alpha, beta, p, T])
+    c.bcs = [K.PatchBC(K.BC_FARFIELD, order, 0, vals=vals) for _ in range(6)]
+    n = c.mesh.nCells
+    r, u, v, w = _farfield_state(c.numerics, mach, alpha, beta, p, T)
+    cv = K.prim_to_cv(c.numerics, np.full(n, r), np.full(n, u), np.full(n, v), np.full(n, w),
+                      np.full(n, p))
+    rhs, _ = Oracle(c).residual(cv, K.eos_dv(c.numerics, cv))
+    scale = (p + r * (u * u + v * v + w * w)) * c.mesh.fn[:, 3].max()
+    assert np.abs(rhs).max() < 1e-9 * scale
+
+
+@pytest.mark.parametrize("order", [1, 2])
+def test_injection_mass_inflow(order):
+    """A burning injection patch (mass flux mInj per unit area) adds exactly
+    -mInj times its area to the domain's mass residual; every other face is a
+    slip wall or interior (no net mass).  A non-burning injection patch adds
+    none."""
+    c = K.tet_shock_box(3, seed=4, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_HLLC))
+    minj = 3.5
+    for burning in (True, False):
+        c.bcs = [K.PatchBC(K.BC_SLIPWALL, order) for _ in range(6)]
+        c.bcs[0] = K.PatchBC(K.BC_INJECTION, order, 0,
+                             vals=np.array([minj if burning else 0.0, 300.0]))
+        rhs, _ = Oracle(c).residual(c.cv, c.dv)
+        area = c.mesh.patches[0].fn[:, 3].sum()
+        expect = -minj * area if burning else 0.0
+        assert abs(rhs[:, 0].sum() - expect) < 1e-12 * np.abs(rhs[:, 0]).sum() + 1e-14 * abs(expect)
