@@ -53,6 +53,7 @@ enum {
   RFGPU_DISCR_UPW_ROE = 1, RFGPU_DISCR_UPW_HLLC = 3, RFGPU_DISCR_UPW_AUSMPLUS = 4,
   RFGPU_RECONST_NONE = 0, RFGPU_RECONST_LIM_VENKAT = 11,
   RFGPU_RK_SCHEME_4_CLASSICAL = 1, RFGPU_RK_SCHEME_3_WRAY = 2, RFGPU_RK_SCHEME_1_EULER = 3,
+  RFGPU_BC_INFLOW_TOTANG = 10, RFGPU_BC_INFLOW_VELTEMP = 11,
   RFGPU_BC_OUTFLOW = 20, RFGPU_BC_SLIPWALL = 60, RFGPU_BC_FARFIELD = 80,
   RFGPU_BC_INJECTION = 90,
   RFGPU_BCOPT_SUPERSONIC = 0, RFGPU_BCOPT_SUBSONIC = 1, RFGPU_BCOPT_MIXED = 2,
@@ -75,7 +76,7 @@ enum {
 typedef struct {
   int bcType;            /* RFGPU_BC_SLIPWALL or RFGPU_BC_OUTFLOW */
   int spaceOrder;        /* .bc ORDER: 1 or 2 */
-  int bcOptType;         /* outflow TYPE: BCOPT_*; farfield: the CORR switch (0 only) */
+  int bcOptType;         /* outflow, inflow TYPE: BCOPT_*; farfield: the CORR switch (0 only) */
   int nBFaces;
   const int *bf2c;       /* bf2c(nBFaces), 1-based */
   const double *fn;      /* fn(4,nBFaces): unit normal, area */
@@ -83,9 +84,12 @@ typedef struct {
   const double *vals;    /* pPatch%mixt%vals from its first used column: vals(nData,nBFaces)
                             if distrib, else vals(nData,1); outflow: PRESS; farfield: MACH,
                             ATTACK, SLIP, PRESS, TEMP (angles in radians); injection:
-                            MFRATE, TEMP (modfloflu/ModParameters.F90:479-493) */
+                            MFRATE, TEMP; inflow TOTANG: PTOT, TTOT, BETAH, BETAV, MACH;
+                            inflow VELTEMP: U, V, W, T, P (modfloflu/ModParameters.F90:
+                            452-493) */
   int distrib;
   int nData;             /* leading dimension of vals; 0 is read as 1 */
+  int bcOptFixed;        /* inflow TOTANG FIXED switch (BCOPT_FIXED_NO 0 / YES 1) */
 } rfgpu_patch_t;
 
 /* Everything RFLU_InitFlowSolver has built for one region, plus the numerics

@@ -39,7 +39,8 @@ class OrcPatch(C.Structure):
     _fields_ = [("bcType", C.c_int), ("spaceOrder", C.c_int), ("bcOptType", C.c_int),
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
-                ("distrib", C.c_int), ("nData", C.c_int)]
+                ("distrib", C.c_int), ("nData", C.c_int),
+                ("bcOptFixed", C.c_int)]
 
 
 class OrcRegion(C.Structure):
@@ -117,6 +118,7 @@ class Oracle:
             vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(keep(vals, np.float64))
             P.distrib, P.nData = dist, nd
+            P.bcOptFixed = bc.bcOptFixed
             np_ += 1
         reg.nPatches = np_
         reg.spaceDiscr, reg.spaceOrder, reg.reconst, reg.rkScheme = (

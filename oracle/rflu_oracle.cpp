@@ -21,7 +21,9 @@
 namespace {
 
 // modfloflu/ModParameters.F90
-const int BC_OUTFLOW = 20, BC_SLIPWALL = 60, BC_FARFIELD = 80, BC_INJECTION = 90;
+const int BC_INFLOW_TOTANG = 10, BC_INFLOW_VELTEMP = 11, BC_OUTFLOW = 20, BC_SLIPWALL = 60,
+          BC_FARFIELD = 80, BC_INJECTION = 90;
+const int BCOPT_FIXED_NO = 0;
 const int BCOPT_SUPERSONIC = 0, BCOPT_SUBSONIC = 1, BCOPT_MIXED = 2;
 const int DISCR_UPW_ROE = 1, DISCR_UPW_HLLC = 3, DISCR_UPW_AUSMPLUS = 4;
 const int RECONST_LIM_VENKAT = 11;
@@ -361,6 +363,79 @@ void rind_farfield_perf(double cpGas, double mmGas, double nx, double ny, double
   }
 }
 
+// libfloflu/BcondInflowPerf.F90:93-272, TCPERF.  The reference leaves ksg
+// unset on the supersonic branch, and all outputs unset for a SUBSONIC patch
+// whose interior normal velocity is supersonic; ksg = 0 here, and the
+// interior state in the latter case.
+void bcond_inflow_perf(int bcOptType, int bcOptFixed, double ptot, double ttot, double betah,
+                       double betav, double mach, double sxn, double syn, double szn,
+                       double cpgas, double mm, double rl, double rul, double rvl, double rwl,
+                       double rel, double pl, double *rr, double *rur, double *rvr, double *rwr,
+                       double *rer, double *pr) {
+  double rgas = R_M(mm);
+  double g = G_CpR(cpgas, rgas);
+  bool prescribed = bcOptType == BCOPT_SUPERSONIC;
+  if (!prescribed) {
+    double gm1 = g - 1.0;
+    double ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+    double a02 = g * rgas * ttot;                                                 // C2_GRT
+    double al = std::sqrt(a02 - 0.5 * (g - 1.0) * (ul * ul + vl * vl + wl * wl));  // C_Co2GUVW
+    double ql = ul * sxn + vl * syn + wl * szn;
+    if (std::fabs(ql) < al) {
+      double sl = std::sqrt(ul * ul + vl * vl + wl * wl);
+      double eta = -1.0;
+      if (bcOptFixed == BCOPT_FIXED_NO && sl > 1.0e-6) eta = ql / sl;
+      double Rm = al - 0.5 * gm1 * ql;
+      double disc = 0.5 * gm1 * (eta * eta) * (a02 / (Rm * Rm) * (1.0 + 0.5 * gm1 * (eta * eta)) - 1.0);
+      double ar, tr, sr;
+      if (disc < 0.0) {
+        ar = std::sqrt(a02);
+        tr = ttot;
+        *pr = ptot;
+        sr = 0.0;
+      } else {
+        ar = Rm / (1.0 + 0.5 * gm1 * eta * eta) * (1.0 + std::sqrt(disc));
+        tr = ar * ar / (g * rgas);                                  // T_CGR
+        *pr = ptot * std::pow(tr / ttot, g / (g - 1.0));            // P_GPoTTo
+        double c2 = ar * ar;
+        sr = a02 > c2 ? std::sqrt(2.0 / (g - 1.0) * (a02 - c2)) : 0.0;  // Vm_C2Co2G
+      }
+      *rr = *pr / (rgas * tr);
+      double ur = sr * std::cos(betah) * std::cos(betav);
+      double vr = sr * std::sin(betah);
+      double wr = sr * std::cos(betah) * std::sin(betav);
+      *rer = *rr * (*pr / (*rr * (g - 1.0)) + 0.5 * sr * sr + KSG);  // Eo_DGPVm
+      *rur = *rr * ur;
+      *rvr = *rr * vr;
+      *rwr = *rr * wr;
+      return;
+    }
+    prescribed = bcOptType == BCOPT_MIXED;
+  }
+  if (prescribed) {
+    double p = ptot / (std::pow(1.0 + 0.5 * (g - 1.0) * mach * mach, g / (g - 1.0)));  // P_GMaPo
+    double t = ttot / (1.0 + 0.5 * (g - 1.0) * mach * mach);                          // T_GMaTo
+    double r = p / (rgas * t);
+    double ar = std::sqrt(g * rgas * t);
+    double ur = mach * ar * std::cos(betah) * std::cos(betav);
+    double vr = mach * ar * std::sin(betah);
+    double wr = mach * ar * std::cos(betah) * std::sin(betav);
+    *rr = r;
+    *rur = r * ur;
+    *rvr = r * vr;
+    *rwr = r * wr;
+    *rer = r * Eo_DGPUVW(r, g, p, ur, vr, wr, KSG);
+    *pr = p;
+  } else {
+    *rr = rl;
+    *rur = rul;
+    *rvr = rvl;
+    *rwr = rwl;
+    *rer = rel;
+    *pr = pl;
+  }
+}
+
 // Boundary face flux: rocflu/RFLU_CentralSecondPatch.F90:638-1351 (ORDER 2)
 // and rocflu/RFLU_CentralFirstPatch.F90:575-1133 (ORDER 1): slip wall,
 // outflow, farfield and injection.  Slip walls leave the mass residual
@@ -467,6 +542,25 @@ void patch_flux(const Ctx &c, const orc_patch_t &p, int ifl, double flx[5], bool
   if (p.bcType == BC_FARFIELD) {
     rind_farfield_perf(cp, mm, nx, ny, nz, vals[0], vals[3], vals[4], vals[1], vals[2], rl, rul,
                        rvl, rwl, rel, &rr, &rur, &rvr, &rwr, &rer, &pr);
+  } else if (p.bcType == BC_INFLOW_TOTANG) {
+    double mach = p.bcOptType != BCOPT_SUBSONIC ? vals[4] : 0.0;
+    bcond_inflow_perf(p.bcOptType, p.bcOptFixed, vals[0], vals[1], vals[2], vals[3], mach, nx, ny,
+                      nz, cp, mm, rl, rul, rvl, rwl, rel, pl, &rr, &rur, &rvr, &rwr, &rer, &pr);
+  } else if (p.bcType == BC_INFLOW_VELTEMP) {
+    double rgas = R_M(mm);
+    double g = G_CpR(cp, rgas);
+    double ur = vals[0], vr = vals[1], wr = vals[2], tr = vals[3];
+    if (p.bcOptType != BCOPT_SUBSONIC) {
+      pr = vals[4];
+      rr = pr / (rgas * tr);  // D_PRT
+    } else {
+      rr = rl;
+      pr = rr * rgas * tr;    // P_DRT
+    }
+    rer = rr * Eo_DGPUVW(rr, g, pr, ur, vr, wr, KSG);
+    rur = rr * ur;
+    rvr = rr * vr;
+    rwr = rr * wr;
   } else {
     if (p.bcOptType != BCOPT_SUPERSONIC) pr = vals[0];
     bcond_outflow_perf(p.bcOptType, pr, nx, ny, nz, cp, mm, rl, rul, rvl, rwl, rel, pl, &rr,

@@ -25,7 +25,8 @@ extern "C" {
 #define ORC_MAX_PATCHES 16
 
 typedef struct {
-  int bcType;      /* BC_OUTFLOW=20, BC_SLIPWALL=60, BC_FARFIELD=80, BC_INJECTION=90
+  int bcType;      /* BC_INFLOW_TOTANG=10, BC_INFLOW_VELTEMP=11, BC_OUTFLOW=20,
+                      BC_SLIPWALL=60, BC_FARFIELD=80, BC_INJECTION=90
                       (modfloflu/ModParameters.F90:398-434) */
   int spaceOrder;  /* 1 or 2 */
   int bcOptType;   /* outflow: BCOPT_SUPERSONIC=0, SUBSONIC=1, MIXED=2 */
@@ -37,6 +38,7 @@ typedef struct {
                            farfield MACH, ATTACK, SLIP, PRESS, TEMP; injection MFRATE, TEMP */
   int distrib;
   int nData;            /* leading dimension of vals (0 read as 1) */
+  int bcOptFixed;       /* inflow TOTANG FIXED switch */
 } orc_patch_t;
 
 typedef struct {

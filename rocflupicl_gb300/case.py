@@ -20,6 +20,7 @@ DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS = 1, 3, 4
 RECONST_NONE, RECONST_LIM_VENKAT = 0, 11
 RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
 BC_OUTFLOW, BC_SLIPWALL, BC_FARFIELD, BC_INJECTION = 20, 60, 80, 90
+BC_INFLOW_TOTANG, BC_INFLOW_VELTEMP = 10, 11
 BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 
@@ -67,6 +68,7 @@ class PatchBC:
     # patch data (pPatch%mixt%vals): (nData,) for the whole patch or (nBFaces, nData);
     # farfield (MACH, ATTACK, SLIP, PRESS, TEMP), injection (MFRATE, TEMP)
     vals: Optional[np.ndarray] = None
+    bcOptFixed: int = 0          # inflow TOTANG FIXED switch
 
     def vals_array(self, n_bfaces: int):
         """(vals (rows, nData) contiguous, nData, distrib) as the C ABI takes them."""

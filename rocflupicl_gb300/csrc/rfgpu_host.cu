@@ -195,7 +195,8 @@ int check_desc(const rfgpu_region_desc_t *d) {
     const rfgpu_patch_t &p = d->patches[ip];
     if (p.nBFaces < 0 || (p.nBFaces > 0 && (!p.bf2c || !p.fn || !p.fc))) return RFGPU_ERR_ARG;
     if (p.bcType != RFGPU_BC_SLIPWALL && p.bcType != RFGPU_BC_OUTFLOW &&
-        p.bcType != RFGPU_BC_FARFIELD && p.bcType != RFGPU_BC_INJECTION)
+        p.bcType != RFGPU_BC_FARFIELD && p.bcType != RFGPU_BC_INJECTION &&
+        p.bcType != RFGPU_BC_INFLOW_TOTANG && p.bcType != RFGPU_BC_INFLOW_VELTEMP)
       return RFGPU_ERR_UNSUPPORTED;
     if (p.spaceOrder != 1 && p.spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
     if (p.nData < 0) return RFGPU_ERR_ARG;
@@ -209,6 +210,11 @@ int check_desc(const rfgpu_region_desc_t *d) {
       if (!p.vals || nData < 5) return RFGPU_ERR_ARG;
     }
     if (p.bcType == RFGPU_BC_INJECTION && (!p.vals || nData < 2)) return RFGPU_ERR_ARG;
+    if (p.bcType == RFGPU_BC_INFLOW_TOTANG || p.bcType == RFGPU_BC_INFLOW_VELTEMP) {
+      if (p.bcOptType < 0 || p.bcOptType > 2) return RFGPU_ERR_UNSUPPORTED;
+      if (p.bcOptFixed < 0 || p.bcOptFixed > 1) return RFGPU_ERR_UNSUPPORTED;
+      if (!p.vals || nData < 5) return RFGPU_ERR_ARG;
+    }
   }
   const long long N = d->nCells;
   for (int f = 0; f < d->nFaces; ++f)
@@ -247,7 +253,7 @@ RegionDev<float> &rd<float>(rfgpu_region_s *h) { return h->rd32; }
 // modflu/RFLU_ModRindStates.F90:249-421, the part that depends only on the
 // patch values): ri = p/(R T), pi = p, qi = M sqrt(g R T) and its components
 // along the angles of attack and sideslip, in this order of operations.
-void farfield_state(const Phys &ph, const double *v, double dat[8]) {
+void farfield_state(const Phys &ph, const double *v, double dat[16]) {
   const double machInf = v[0], alphaInf = v[1], betaInf = v[2], pInf = v[3], tInf = v[4];
   const double rGas = ph.gvR, gGas = ph.gvG;
   const double ri = pInf / (rGas * tInf);
@@ -260,6 +266,40 @@ void farfield_state(const Phys &ph, const double *v, double dat[8]) {
   dat[5] = qi * std::sin(betaInf);
   dat[6] = machInf;
   dat[7] = 0.0;
+}
+
+// Total-pressure / total-temperature inflow (libfloflu/BcondInflowPerf.F90:
+// 93-272), the parts that depend only on the patch values: a02 = g R ttot,
+// the flow-angle cosines and sines, and the prescribed state of the
+// supersonic branch (Mach from the patch; also the MIXED type's state when the
+// interior normal velocity is supersonic), MixtPerf_P_GMaPo, _T_GMaTo, _D_PRT,
+// _C_GRT, _Eo_DGPUVW in their order of operations.  The reference leaves ksg
+// unset on the supersonic branch; it is 0 here.
+void inflow_totang_state(const Phys &ph, const double *v, int opt, int fixed, double dat[16]) {
+  const double ptot = v[0], ttot = v[1], betah = v[2], betav = v[3];
+  const double mach = opt != RFGPU_BCOPT_SUBSONIC ? v[4] : 0.0;
+  const double rgas = ph.gvR, g = ph.gvG;
+  dat[0] = ptot;
+  dat[1] = ttot;
+  dat[2] = g * rgas * ttot;  // MixtPerf_C2_GRT
+  dat[3] = std::cos(betah);
+  dat[4] = std::sin(betah);
+  dat[5] = std::cos(betav);
+  dat[6] = std::sin(betav);
+  dat[7] = fixed;
+  const double pr = ptot / (std::pow(1.0 + 0.5 * (g - 1.0) * mach * mach, g / (g - 1.0)));
+  const double tr = ttot / (1.0 + 0.5 * (g - 1.0) * mach * mach);
+  const double rr = pr / (rgas * tr);
+  const double ar = std::sqrt(g * rgas * tr);
+  const double ur = mach * ar * std::cos(betah) * std::cos(betav);
+  const double vr = mach * ar * std::sin(betah);
+  const double wr = mach * ar * std::cos(betah) * std::sin(betav);
+  dat[8] = rr;
+  dat[9] = rr * ur;
+  dat[10] = rr * vr;
+  dat[11] = rr * wr;
+  dat[12] = rr * (pr / (rr * (g - 1.0)) + 0.5 * (ur * ur + vr * vr + wr * wr) + 0.0);
+  dat[13] = pr;
 }
 
 // Device numbering of cells and interior faces.  Empty maps: the host's.
@@ -471,26 +511,32 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   std::vector<double> bfnA, bfdA, bpout, bdat;
   for (int ip = 0; ip < d->nPatches; ++ip) {
     const rfgpu_patch_t &p = d->patches[ip];
-    const int type = p.bcType == RFGPU_BC_SLIPWALL   ? BK_SLIP
-                     : p.bcType == RFGPU_BC_OUTFLOW  ? BK_OUTFLOW
-                     : p.bcType == RFGPU_BC_FARFIELD ? BK_FARFIELD
-                                                     : BK_INJECTION;
+    const int type = p.bcType == RFGPU_BC_SLIPWALL         ? BK_SLIP
+                     : p.bcType == RFGPU_BC_OUTFLOW        ? BK_OUTFLOW
+                     : p.bcType == RFGPU_BC_FARFIELD       ? BK_FARFIELD
+                     : p.bcType == RFGPU_BC_INFLOW_TOTANG  ? BK_INFLOW_TA
+                     : p.bcType == RFGPU_BC_INFLOW_VELTEMP ? BK_INFLOW_VT
+                                                           : BK_INJECTION;
     const int nData = p.nData > 0 ? p.nData : 1;
     for (int b = 0; b < p.nBFaces; ++b) {
       int c = o.nc(p.bf2c[b] - 1);
       bf2c.push_back(c);
-      bkind.push_back(bk_pack(type, p.spaceOrder, type == BK_OUTFLOW ? p.bcOptType : 0));
+      const bool withOpt = type == BK_OUTFLOW || type == BK_INFLOW_TA || type == BK_INFLOW_VT;
+      bkind.push_back(bk_pack(type, p.spaceOrder, withOpt ? p.bcOptType : 0));
       double pout = 0.0;
       const double *v = p.vals ? p.vals + (size_t)nData * (p.distrib ? b : 0) : nullptr;
       if (type == BK_OUTFLOW && p.bcOptType != RFGPU_BCOPT_SUPERSONIC) pout = v[0];
       bpout.push_back(pout);
-      double dat[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+      double dat[kBData] = {0};
       if (type == BK_FARFIELD) farfield_state(ph, v, dat);
       if (type == BK_INJECTION) {
         dat[0] = v[0];  // MFRATE
         dat[1] = v[1];  // TEMP
       }
-      bdat.insert(bdat.end(), dat, dat + 8);
+      if (type == BK_INFLOW_TA) inflow_totang_state(ph, v, p.bcOptType, p.bcOptFixed, dat);
+      if (type == BK_INFLOW_VT)
+        for (int k = 0; k < 5; ++k) dat[k] = v[k];  // U, V, W, T, P
+      bdat.insert(bdat.end(), dat, dat + kBData);
       for (int k = 0; k < 4; ++k) bfnA.push_back(p.fn[4 * (size_t)b + k]);
       for (int k = 0; k < 3; ++k) bfdA.push_back(p.fc[3 * (size_t)b + k] - cofg[(size_t)k * N + c]);
     }

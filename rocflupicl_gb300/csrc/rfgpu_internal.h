@@ -17,7 +17,7 @@
 //                2*face + side, code < 0: -(bface+1); cfNb = other cell,
 //                cfD[3] = cofg - fc (limiter vector)
 //   faces        f2c[2][F], fnA[F][4] (normal, area), fdl/fdr[3][F] = fc - cofg(c1/c2)
-//   boundary     bf2c[B], bfnA[B][4], bfd[3][B], bkind[B], bpout[B], bdat[B][8]
+//   boundary     bf2c[B], bfnA[B][4], bfd[3][B], bkind[B], bpout[B], bdat[B][16]
 //   scratch      flux[F][8], bflux[B][8] (R, 5 used)
 // Cells and faces are in the device numbering (the host's, or a locality
 // order chosen at registration, cellNew/cellOld); the face indices stored in
@@ -33,7 +33,9 @@ namespace rfgpu {
 constexpr int kSlice = 32;
 
 // boundary kind bits
-enum { BK_SLIP = 0, BK_OUTFLOW = 1, BK_FARFIELD = 2, BK_INJECTION = 3 };
+enum { BK_SLIP = 0, BK_OUTFLOW = 1, BK_FARFIELD = 2, BK_INJECTION = 3, BK_INFLOW_TA = 4,
+       BK_INFLOW_VT = 5 };
+constexpr int kBData = 16;  // per boundary face data slots (bdat)
 __host__ __device__ inline int bk_pack(int type, int order, int opt) {
   return type | (order << 4) | (opt << 8);
 }
@@ -88,8 +90,13 @@ struct RegionDev {
   const R *bfd;        // [3][B]
   const int *bkind;
   const double *bpout;
-  // per boundary face data [B][8]: farfield (ri, pi, qi, ui, vi, wi, machInf, 0),
-  // free-stream state evaluated once on the host; injection (mInj, tInj, 0, ...)
+  // per boundary face data [B][kBData], evaluated once on the host:
+  //   farfield   ri, pi, qi, ui, vi, wi, machInf
+  //   injection  mInj, tInj
+  //   inflow TOTANG   ptot, ttot, a02 = g R ttot, cos/sin betah, cos/sin betav,
+  //                   fixed, then the prescribed state of the supersonic / mixed
+  //                   branch rr, rur, rvr, rwr, rer, pr (slots 8..13)
+  //   inflow VELTEMP  ur, vr, wr, tr, pr
   const R *bdat;
   R *bflux;            // [B][8]
   // time step

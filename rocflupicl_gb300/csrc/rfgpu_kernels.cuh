@@ -791,6 +791,70 @@ __device__ __forceinline__ void farfield_rind(const R *fd, R gGas, R nx, R ny, R
   }
 }
 
+// Total-pressure / total-temperature inflow state, libfloflu/BcondInflowPerf.F90:
+// 93-272 (ksg = 0).  d = (ptot, ttot, a02, cos betah, sin betah, cos betav,
+// sin betav, fixed, supersonic-branch state rr, rur, rvr, rwr, rer, pr).  A
+// SUBSONIC patch whose interior normal velocity is supersonic leaves the
+// reference's outputs unset; the interior state is used here.
+template <typename R>
+__device__ __forceinline__ void inflow_totang(const R *d, int opt, R g, R rgas, R nx, R ny, R nz,
+                                              R rl, R rul, R rvl, R rwl, R rel, R pl, R &rr,
+                                              R &rur, R &rvr, R &rwr, R &rer, R &pr) {
+  const R ptot = d[0], ttot = d[1], a02 = d[2], cbh = d[3], sbh = d[4], cbv = d[5], sbv = d[6];
+  const bool fixed = d[7] != R(0);
+  bool prescribed = opt == 0;  // BCOPT_SUPERSONIC
+  if (!prescribed) {
+    const R gm1 = g - R(1);
+    const R ul = rul / rl, vl = rvl / rl, wl = rwl / rl;
+    const R al = sqrt(a02 - R(0.5) * (g - R(1)) * (ul * ul + vl * vl + wl * wl));  // C_Co2GUVW
+    const R ql = ul * nx + vl * ny + wl * nz;
+    if (fabs(ql) < al) {
+      const R sl = sqrt(ul * ul + vl * vl + wl * wl);
+      R eta = R(-1);
+      if (!fixed && sl > R(1.0e-6)) eta = ql / sl;
+      const R Rm = al - R(0.5) * gm1 * ql;
+      const R disc =
+          R(0.5) * gm1 * (eta * eta) * (a02 / (Rm * Rm) * (R(1) + R(0.5) * gm1 * (eta * eta)) - R(1));
+      R ar, tr, sr;
+      if (disc < R(0)) {
+        ar = sqrt(a02);
+        tr = ttot;
+        pr = ptot;
+        sr = R(0);
+      } else {
+        ar = Rm / (R(1) + R(0.5) * gm1 * eta * eta) * (R(1) + sqrt(disc));
+        tr = ar * ar / (g * rgas);                          // MixtPerf_T_CGR
+        pr = ptot * pow(tr / ttot, g / (g - R(1)));         // MixtPerf_P_GPoTTo
+        const R c2 = ar * ar;
+        sr = a02 > c2 ? sqrt(R(2) / (g - R(1)) * (a02 - c2)) : R(0);  // MixtPerf_Vm_C2Co2G
+      }
+      rr = pr / (rgas * tr);
+      const R ur = sr * cbh * cbv, vr = sr * sbh, wr = sr * cbh * sbv;
+      rer = rr * (pr / (rr * (g - R(1))) + R(0.5) * sr * sr + R(0));  // MixtPerf_Eo_DGPVm
+      rur = rr * ur;
+      rvr = rr * vr;
+      rwr = rr * wr;
+      return;
+    }
+    prescribed = opt == 2;  // BCOPT_MIXED
+  }
+  if (prescribed) {
+    rr = d[8];
+    rur = d[9];
+    rvr = d[10];
+    rwr = d[11];
+    rer = d[12];
+    pr = d[13];
+  } else {
+    rr = rl;
+    rur = rul;
+    rvr = rvl;
+    rwr = rwl;
+    rer = rel;
+    pr = pl;
+  }
+}
+
 // Outflow boundary state, libfloflu/BcondOutflowPerf.F90:88-160 (ksg = 0).
 template <typename R>
 __device__ __forceinline__ void bcond_outflow(int bcOpt, R pout, R sxn, R syn, R szn, R gamma,
@@ -865,10 +929,10 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       flx[2] = pl * ny * nm;
       flx[3] = pl * nz * nm;
       flx[4] = pl * fs * nm;
-    } else if (type == BK_INJECTION && g.bdat[8 * (size_t)b] > R(0)) {
+    } else if (type == BK_INJECTION && g.bdat[kBData * (size_t)b] > R(0)) {
       // burning surface (RFLU_CentralSecondPatch.F90:1237-1351 / FirstPatch
       // :1049-1133 with RFLU_SetRindStateInjectPerf, RFLU_ModRindStates.F90:460-505)
-      const R minj = g.bdat[8 * (size_t)b], tinj = g.bdat[8 * (size_t)b + 1];
+      const R minj = g.bdat[kBData * (size_t)b], tinj = g.bdat[kBData * (size_t)b + 1];
       const R rGas = R(g.ph.gvR), cpGas = R(g.ph.gvCp);
       const R pl = S[4];
       const R rl = pl / (rGas * tinj);
@@ -927,8 +991,25 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
       } else {
         R pr, rr, rur, rvr, rwr, rer;
         if (type == BK_FARFIELD) {
-          farfield_rind(g.bdat + 8 * (size_t)b, gvG, nx, ny, nz, rl, rul, rvl, rwl, rel, rr, rur,
+          farfield_rind(g.bdat + kBData * (size_t)b, gvG, nx, ny, nz, rl, rul, rvl, rwl, rel, rr, rur,
                         rvr, rwr, rer, pr);
+        } else if (type == BK_INFLOW_TA) {
+          inflow_totang(g.bdat + kBData * (size_t)b, opt, gvG, R(g.ph.gvR), nx, ny, nz, rl, rul, rvl,
+                        rwl, rel, pl, rr, rur, rvr, rwr, rer, pr);
+        } else if (type == BK_INFLOW_VT) {
+          const R *d = g.bdat + kBData * (size_t)b;
+          const R ur = d[0], vr = d[1], wr = d[2], tr = d[3], rGas = R(g.ph.gvR);
+          if (opt != 1) {  // BCOPT_SUBSONIC
+            pr = d[4];
+            rr = pr / (rGas * tr);  // MixtPerf_D_PRT
+          } else {
+            rr = rl;
+            pr = rr * rGas * tr;    // MixtPerf_P_DRT
+          }
+          rer = rr * eo_dgpuvw(rr, gvG, pr, ur, vr, wr);
+          rur = rr * ur;
+          rvr = rr * vr;
+          rwr = rr * wr;
         } else {
           pr = (opt != 0) ? R(g.bpout[b]) : pl;
           bcond_outflow(opt, pr, nx, ny, nz, gvG, rl, rul, rvl, rwl, rel, pl, rr, rur, rvr, rwr,

@@ -40,7 +40,8 @@ class PatchT(C.Structure):
     _fields_ = [("bcType", C.c_int), ("spaceOrder", C.c_int), ("bcOptType", C.c_int),
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
-                ("distrib", C.c_int), ("nData", C.c_int)]
+                ("distrib", C.c_int), ("nData", C.c_int),
+                ("bcOptFixed", C.c_int)]
 
 
 class RegionDescT(C.Structure):
@@ -246,6 +247,7 @@ class Region:
             vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(k(vals, np.float64))
             P.distrib, P.nData = dist, nd
+            P.bcOptFixed = bc.bcOptFixed
         d = RegionDescT()
         d.nCells, d.nFaces, d.f2cLd = m.nCells, m.nFaces, 2
         d.f2c = _ip(k(m.f2c, np.int32))

@@ -188,3 +188,47 @@ def test_injection_mass_inflow(order):
         area = c.mesh.patches[0].fn[:, 3].sum()
         expect = -minj * area if burning else 0.0
         assert abs(rhs[:, 0].sum() - expect) < 1e-12 * np.abs(rhs[:, 0]).sum() + 1e-14 * abs(expect)
+
+
+def _uniform_inflow_case(bc_in, mach=0.5, order=2):
+    """Uniform flow along +x at `mach` through a tet box: the given inflow patch
+    at x = 0, subsonic outflow at the ambient pressure at x = 1, slip walls on
+    y and z (the flow is parallel to them)."""
+    c = K.tet_shock_box(3, seed=6, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_AUSMPLUS))
+    num = c.numerics
+    g = num.gamma_gv
+    R = 8314.3 / num.gv[1]
+    rho, p = 1.1, 1.0e5
+    T = p / (rho * R)
+    u = mach * np.sqrt(g * R * T)
+    n = c.mesh.nCells
+    cv = K.prim_to_cv(num, np.full(n, rho), np.full(n, u), np.zeros(n), np.zeros(n), np.full(n, p))
+    c.cv, c.dv = cv, K.eos_dv(num, cv)
+    c.bcs = [bc_in(rho, u, p, T, g), K.PatchBC(K.BC_OUTFLOW, order, K.BCOPT_SUBSONIC, pout=np.array([p]))]
+    c.bcs += [K.PatchBC(K.BC_SLIPWALL, order) for _ in range(4)]
+    return c, p * c.mesh.fn[:, 3].max()
+
+
+@pytest.mark.parametrize("opt", [0, 1, 2])
+@pytest.mark.parametrize("order", [1, 2])
+def test_inflow_totang_preserves_consistent_uniform_flow(opt, order):
+    """Total pressure and temperature, flow angles and (supersonic / mixed) Mach
+    number of the interior's own uniform state: every inflow branch returns
+    that state, so the residual vanishes."""
+    def bc(rho, u, p, T, g):
+        m2 = 0.5 if opt != 0 else 0.5   # the prescribed branch uses the patch Mach
+        f = 1.0 + 0.5 * (g - 1.0) * m2 * m2
+        return K.PatchBC(K.BC_INFLOW_TOTANG, order, opt,
+                         vals=np.array([p * f ** (g / (g - 1.0)), T * f, 0.0, 0.0, m2]))
+    c, scale = _uniform_inflow_case(bc, order=order)
+    rhs, _ = Oracle(c).residual(c.cv, c.dv)
+    assert np.abs(rhs).max() < 1e-9 * scale
+
+
+@pytest.mark.parametrize("opt", [0, 1])
+def test_inflow_veltemp_preserves_consistent_uniform_flow(opt):
+    def bc(rho, u, p, T, g):
+        return K.PatchBC(K.BC_INFLOW_VELTEMP, 2, opt, vals=np.array([u, 0.0, 0.0, T, p]))
+    c, scale = _uniform_inflow_case(bc)
+    rhs, _ = Oracle(c).residual(c.cv, c.dv)
+    assert np.abs(rhs).max() < 1e-9 * scale

@@ -298,3 +298,74 @@ def test_farfield_lift_correction_refused():
     with pytest.raises(E.EngineError) as ei:
         E.Region(c)
     assert ei.value.code == E.ERR_UNSUPPORTED
+
+
+def _inflow_case(variant, order, prec=K.PREC_FP64):
+    """Tet shock box with an inflow patch at x = 0 holding (or, supersonic,
+    overdriving) the post-shock state that arrives there."""
+    c = make("tet", K.DISCR_UPW_AUSMPLUS, precision=prec)
+    g = c.numerics.gamma_gv
+    R = 8314.3 / c.numerics.gv[1]
+    r2, u2, p2 = K.rankine_hugoniot(2.0, g, 1.2, 1.0e5)
+    T2 = p2 / (r2 * R)
+    m2 = u2 / np.sqrt(g * R * T2)
+    f = 1.0 + 0.5 * (g - 1.0) * m2 * m2
+    pt, Tt = p2 * f ** (g / (g - 1.0)), T2 * f
+    if variant.startswith("totang"):
+        opt = {"totang_sub": K.BCOPT_SUBSONIC, "totang_sup": K.BCOPT_SUPERSONIC,
+               "totang_mixed": K.BCOPT_MIXED}[variant]
+        mach = 1.5 if opt == K.BCOPT_SUPERSONIC else m2
+        c.bcs[0] = K.PatchBC(K.BC_INFLOW_TOTANG, order, opt,
+                             vals=np.array([pt, Tt, 0.1, 0.05, mach]), bcOptFixed=0)
+    else:
+        opt = K.BCOPT_SUBSONIC if variant == "veltemp_sub" else K.BCOPT_SUPERSONIC
+        c.bcs[0] = K.PatchBC(K.BC_INFLOW_VELTEMP, order, opt,
+                             vals=np.array([u2, 5.0, -3.0, T2, p2]))
+    return c
+
+
+INFLOW = ["totang_sub", "totang_sup", "totang_mixed", "veltemp_sub", "veltemp_sup"]
+
+
+@pytest.mark.parametrize("order", [1, 2])
+@pytest.mark.parametrize("variant", INFLOW)
+def test_inflow_patches(variant, order):
+    """FP64 path against the oracle: bit-identical, except where the subsonic
+    total-condition inflow takes a power at run time (a few ulp allowed)."""
+    c = _inflow_case(variant, order)
+    o = _oracle(c)
+    rhs_o, _ = o.residual(c.cv, c.dv)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    o.run(cv, dv, n_steps=3)
+    r = E.Region(c)
+    rhs_g = r.residual()
+    r.solve(n_steps=3)
+    cvg, dvg = r.download()
+    if variant in ("totang_sub", "totang_mixed"):
+        assert np.abs(rhs_g - rhs_o).max() <= 1e-13 * np.abs(rhs_o).max()
+        assert np.allclose(cvg, cv, rtol=1e-12, atol=0) and np.allclose(dvg, dv, rtol=1e-12, atol=0)
+    else:
+        assert_same(rhs_g, rhs_o, "residual")
+        assert_same(cvg, cv, "cv")
+        assert_same(dvg, dv, "dv")
+    r.close()
+
+
+@pytest.mark.parametrize("variant", INFLOW)
+def test_inflow_patches_mixed(variant):
+    c = _inflow_case(variant, 2, prec=K.PREC_MIXED)
+    o = _oracle(c)
+    rhs_o, _ = o.residual(c.cv, c.dv)
+    r = E.Region(c)
+    rhs_g = r.residual()
+    scale = np.abs(rhs_o).max(axis=0)
+    assert np.all(np.abs(rhs_g - rhs_o).max(axis=0) <= 1e-5 * scale)
+    if variant != "totang_sup":
+        cv, dv = c.cv.copy(), c.dv.copy()
+        dti = o.dt(cv, dv, c.numerics.cfl, 1.0, 0.0, 1.0)
+        o.run(cv, dv, n_steps=5, dt_imposed=dti)
+        r.solve(n_steps=5, dt_imposed=dti)
+        cvg, dvg = r.download()
+        assert np.mean(np.abs(cvg[:, 0] / cv[:, 0] - 1.0)) <= 1e-5
+        assert np.mean(np.abs(dvg[:, 0] / dv[:, 0] - 1.0)) <= 1e-5
+    r.close()
