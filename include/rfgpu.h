@@ -51,6 +51,7 @@ enum {
 /* values of the keys below (modfloflu/ModParameters.F90) */
 enum {
   RFGPU_DISCR_UPW_ROE = 1, RFGPU_DISCR_UPW_HLLC = 3, RFGPU_DISCR_UPW_AUSMPLUS = 4,
+  RFGPU_DISCR_UPW_AUSMPLUSUP = 5,
   RFGPU_RECONST_NONE = 0, RFGPU_RECONST_LIM_VENKAT = 11,
   RFGPU_RK_SCHEME_4_CLASSICAL = 1, RFGPU_RK_SCHEME_3_WRAY = 2, RFGPU_RK_SCHEME_1_EULER = 3,
   RFGPU_BC_INFLOW_TOTANG = 10, RFGPU_BC_INFLOW_VELTEMP = 11,
@@ -122,6 +123,8 @@ typedef struct {
   int venkatGuard;         /* 0: limiter term exactly as the reference;
                               1: guard added with the sign of the denominator */
   int cellOrder;           /* RFGPU_ORDER_*: device numbering of cells and faces */
+  double ausmSigma, ausmKp, ausmKu, ausmMInf; /* AUSM+up (DISCR 5) SIGMA, KP, KU, MINF
+                              (libfloflu/ReadNumericsSection.F90:239-276) */
 } rfgpu_region_desc_t;
 
 /* Register a region: copies and reorders the arrays to device-resident SoA.

@@ -53,7 +53,9 @@ class OrcRegion(C.Structure):
                 ("spaceDiscr", C.c_int), ("spaceOrder", C.c_int), ("reconst", C.c_int),
                 ("rkScheme", C.c_int), ("refCp", C.c_double), ("refGamma", C.c_double),
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
-                ("dissFact", C.c_double), ("venkatGuard", C.c_int)]
+                ("dissFact", C.c_double), ("venkatGuard", C.c_int),
+                ("ausmSigma", C.c_double), ("ausmKp", C.c_double), ("ausmKu", C.c_double),
+                ("ausmMInf", C.c_double)]
 
 
 def _load():
@@ -127,6 +129,8 @@ class Oracle:
         reg.gvCp, reg.gvMol = num.gv
         reg.epsentr, reg.dissFact = num.epsentr, num.dissFact
         reg.venkatGuard = num.venkatGuard
+        reg.ausmSigma, reg.ausmKp, reg.ausmKu, reg.ausmMInf = (
+            num.ausmSigma, num.ausmKp, num.ausmKu, num.ausmMInf)
         self.reg = reg
         self.nCells = m.nCells
         self.num = num

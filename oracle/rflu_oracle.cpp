@@ -25,7 +25,7 @@ const int BC_INFLOW_TOTANG = 10, BC_INFLOW_VELTEMP = 11, BC_OUTFLOW = 20, BC_SLI
           BC_FARFIELD = 80, BC_INJECTION = 90;
 const int BCOPT_FIXED_NO = 0;
 const int BCOPT_SUPERSONIC = 0, BCOPT_SUBSONIC = 1, BCOPT_MIXED = 2;
-const int DISCR_UPW_ROE = 1, DISCR_UPW_HLLC = 3, DISCR_UPW_AUSMPLUS = 4;
+const int DISCR_UPW_ROE = 1, DISCR_UPW_HLLC = 3, DISCR_UPW_AUSMPLUS = 4, DISCR_UPW_AUSMPLUSUP = 5;
 const int RECONST_LIM_VENKAT = 11;
 const int RK_SCHEME_4_CLASSICAL = 1, RK_SCHEME_3_WRAY = 2, RK_SCHEME_1_EULER = 3;
 const double KSG = 0.0;
@@ -222,6 +222,53 @@ void hllc_states(const orc_region_t *r, const double L[5], const double R[5], do
   }
 }
 
+// RFLU_AUSMPlusUp_FluxFunction2 (modflu/RFLU_ModAUSMPlusUpFlux.F90:469-588)
+// on given states with their total enthalpies and sound speeds; vFracF = 1
+// (no particles).  The routine computes a blending factor from the mean Mach
+// number and then overwrites it with 1, so alpha = 3/16 as in AUSM+.
+void ausmup_flux(double sigma, double kp, double ku, double nx, double ny, double nz, double nm,
+                 double fs, double rl, double ul, double vl, double wl, double pl, double Hl,
+                 double al, double rr, double ur, double vr, double wr, double pr, double Hr,
+                 double ar, double flx[5]) {
+  double ql = ul * nx + vl * ny + wl * nz - fs;
+  double qr = ur * nx + vr * ny + wr * nz - fs;
+  double af = 0.5 * (al + ar);
+  double ml = ql / af, mla = std::fabs(ml);
+  double mr = qr / af, mra = std::fabs(mr);
+  double mbarsq = 0.5 * (ml * ml + mr * mr);
+  double fa = 1.0;
+  double alpha = 0.1875 * (5 * fa * fa - 4);
+  double mlp, wtl, mrm, wtr;
+  if (mla <= 1.0) {
+    mlp = 0.25 * (ml + 1.0) * (ml + 1.0) + 0.125 * (ml * ml - 1.0) * (ml * ml - 1.0);
+    wtl = 0.25 * (ml + 1.0) * (ml + 1.0) * (2.0 - ml) + alpha * ml * (ml * ml - 1.0) * (ml * ml - 1.0);
+  } else {
+    mlp = 0.5 * (ml + mla);
+    wtl = 0.5 * (1.0 + ml / mla);
+  }
+  if (mra <= 1.0) {
+    mrm = -0.25 * (mr - 1.0) * (mr - 1.0) - 0.125 * (mr * mr - 1.0) * (mr * mr - 1.0);
+    wtr = 0.25 * (mr - 1.0) * (mr - 1.0) * (2.0 + mr) - alpha * mr * (mr * mr - 1.0) * (mr * mr - 1.0);
+  } else {
+    mrm = 0.5 * (mr - mra);
+    wtr = 0.5 * (1.0 - mr / mra);
+  }
+  double rf = 0.5 * (rl + rr);
+  double sigmabar = 1.0 - sigma * mbarsq;
+  double mp = (-(kp * fmax_f(sigmabar, 0.0) * (pr - pl))) / (fa * rf * af * af);
+  double pu = -(ku * wtl * wtr * fa * af * (rl + rr) * (qr - ql));
+  double mf = mlp + mrm + mp;
+  double mfa = std::fabs(mf);
+  double mfp = 0.5 * (mf + mfa), mfm = 0.5 * (mf - mfa);
+  double pf = wtl * pl + wtr * pr + pu;
+  const double vFracF = 1.0;
+  flx[0] = (af * vFracF * (mfp * rl + mfm * rr)) * nm;
+  flx[1] = (af * vFracF * (mfp * rl * ul + mfm * rr * ur) + pf * nx) * nm;
+  flx[2] = (af * vFracF * (mfp * rl * vl + mfm * rr * vr) + pf * ny) * nm;
+  flx[3] = (af * vFracF * (mfp * rl * wl + mfm * rr * wr) + pf * nz) * nm;
+  flx[4] = (af * vFracF * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
+}
+
 // ---- per-face fluxes on the region ----------------------------------------
 
 struct Ctx {
@@ -260,6 +307,26 @@ void interior_flux(const Ctx &c, int ifg, double flx[5]) {
   double L[5], R[5], irl, irr;
   recon(c, c1, fcx, L, &irl, second);
   recon(c, c2, fcx, R, &irr, second);
+  if (r->spaceDiscr == DISCR_UPW_AUSMPLUSUP) {
+    double Hl, al, Hr, ar;
+    if (second) {  // RFLU_AUSMPlusUp_ComputeFlux2_TCP (:3255-3632)
+      double cp = r->refCp, g = r->refGamma, gc = cp - cp / g;  // MixtPerf_R_CpG
+      double tl = L[4] / (L[0] * gc), tr = R[4] / (R[0] * gc);  // MixtPerf_T_DPR
+      al = std::sqrt(g * gc * tl);
+      Hl = cp * tl + 0.5 * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]) + KSG;
+      ar = std::sqrt(g * gc * tr);
+      Hr = cp * tr + 0.5 * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]) + KSG;
+    } else {       // RFLU_AUSMPlusUp_ComputeFlux1 (:894-1366): E/rho + p/rho, dv(SOUN)
+      const double *cv1 = c.cv + 5 * (size_t)(c1 - 1), *cv2 = c.cv + 5 * (size_t)(c2 - 1);
+      al = c.dv[3 * (size_t)(c1 - 1) + 2];
+      Hl = cv1[4] * irl + L[4] / L[0];
+      ar = c.dv[3 * (size_t)(c2 - 1) + 2];
+      Hr = cv2[4] * irr + R[4] / R[0];
+    }
+    ausmup_flux(r->ausmSigma, r->ausmKp, r->ausmKu, n[0], n[1], n[2], n[3], fs, L[0], L[1],
+                L[2], L[3], L[4], Hl, al, R[0], R[1], R[2], R[3], R[4], Hr, ar, flx);
+    return;
+  }
   switch (r->spaceDiscr) {
     case DISCR_UPW_AUSMPLUS: ausm_states(r, L, R, n, fs, flx); break;
     case DISCR_UPW_ROE: roe_states(r, L, R, n, fs, flx); break;
@@ -1080,6 +1147,16 @@ void orc_face_flux(const orc_region_t *r, const double *left, const double *righ
   switch (r->spaceDiscr) {
     case DISCR_UPW_AUSMPLUS: ausm_states(r, L, R, n, 0.0, flux); break;
     case DISCR_UPW_ROE: roe_states(r, L, R, n, 0.0, flux); break;
+    case DISCR_UPW_AUSMPLUSUP: {  // second-order state set-up
+      double cp = r->refCp, g = r->refGamma, gc = cp - cp / g;
+      double tl = L[4] / (L[0] * gc), tr = R[4] / (R[0] * gc);
+      double al = std::sqrt(g * gc * tl), ar = std::sqrt(g * gc * tr);
+      double Hl = cp * tl + 0.5 * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]) + KSG;
+      double Hr = cp * tr + 0.5 * (R[1] * R[1] + R[2] * R[2] + R[3] * R[3]) + KSG;
+      ausmup_flux(r->ausmSigma, r->ausmKp, r->ausmKu, n[0], n[1], n[2], n[3], 0.0, L[0], L[1],
+                  L[2], L[3], L[4], Hl, al, R[0], R[1], R[2], R[3], R[4], Hr, ar, flux);
+      break;
+    }
     default: hllc_states(r, L, R, 1.0 / L[0], 1.0 / R[0], n, 0.0, flux); break;
   }
 }

@@ -53,7 +53,7 @@ typedef struct {
   const double *xyzMoms;/* (10,nCells) */
   orc_patch_t patches[ORC_MAX_PATCHES];
   /* numerics (libflu/RFLU_InitInputValues.F90 keys) */
-  int spaceDiscr;   /* DISCR_UPW_ROE=1, HLLC=3, AUSMPLUS=4 */
+  int spaceDiscr;   /* DISCR_UPW_ROE=1, HLLC=3, AUSMPLUS=4, AUSMPLUSUP=5 */
   int spaceOrder;   /* 1 or 2 */
   int reconst;      /* RECONST_NONE=0, RECONST_LIM_VENKAT=11 */
   int rkScheme;     /* RK_SCHEME_4_CLASSICAL=1, RK_SCHEME_3_WRAY=2, RK_SCHEME_1_EULER=3 */
@@ -64,6 +64,9 @@ typedef struct {
    * labelled extension numer/(denom+copysign(1e-12,denom)), which keeps the
    * guard from cancelling a negative denominator (see venkat_term) */
   int venkatGuard;
+  /* AUSM+up (DISCR_UPW_AUSMPLUSUP=5) parameters sigma, kp, ku, mInf
+   * (libfloflu/ReadNumericsSection.F90:239-276; defaults 1, 0.25, 0.75, 0.1) */
+  double ausmSigma, ausmKp, ausmKu, ausmMInf;
 } orc_region_t;
 
 /* status bits, shared with the engine */

@@ -16,7 +16,7 @@ import numpy as np
 from . import mesh as _mesh
 
 # modfloflu/ModParameters.F90
-DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS = 1, 3, 4
+DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS, DISCR_UPW_AUSMPLUSUP = 1, 3, 4, 5
 RECONST_NONE, RECONST_LIM_VENKAT = 0, 11
 RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
 BC_OUTFLOW, BC_SLIPWALL, BC_FARFIELD, BC_INJECTION = 20, 60, 80, 90
@@ -24,7 +24,8 @@ BC_INFLOW_TOTANG, BC_INFLOW_VELTEMP = 10, 11
 BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
 PREC_FP64, PREC_MIXED = 0, 1
 
-SCHEME_NAMES = {DISCR_UPW_ROE: "roe", DISCR_UPW_HLLC: "hllc", DISCR_UPW_AUSMPLUS: "ausm+"}
+SCHEME_NAMES = {DISCR_UPW_ROE: "roe", DISCR_UPW_HLLC: "hllc", DISCR_UPW_AUSMPLUS: "ausm+",
+                DISCR_UPW_AUSMPLUSUP: "ausm+up"}
 
 
 @dataclass
@@ -43,6 +44,12 @@ class Numerics:
     # 0: Venkatakrishnan term numer/(denom+1e-12) exactly as the reference;
     # 1: labelled extension adding 1e-12 with the sign of denom (d2 < 0 case)
     venkatGuard: int = 0
+    # AUSM+up (DISCR 5): SIGMA, KP, KU, MINF of the NUMERICS section
+    # (libfloflu/ReadNumericsSection.F90:239-276 defaults)
+    ausmSigma: float = 1.0
+    ausmKp: float = 0.25
+    ausmKu: float = 0.75
+    ausmMInf: float = 0.1
 
     @property
     def gv(self):

@@ -182,7 +182,7 @@ int check_desc(const rfgpu_region_desc_t *d) {
   if (d->gasModel != RFGPU_GAS_MODEL_TCPERF || d->flowModel != RFGPU_FLOW_EULER)
     return RFGPU_ERR_UNSUPPORTED;
   if (d->spaceDiscr != RFGPU_DISCR_UPW_ROE && d->spaceDiscr != RFGPU_DISCR_UPW_HLLC &&
-      d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUS)
+      d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUS && d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUSUP)
     return RFGPU_ERR_UNSUPPORTED;
   if (d->spaceOrder != 1 && d->spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
   if (d->reconst != RFGPU_RECONST_NONE && d->reconst != RFGPU_RECONST_LIM_VENKAT)
@@ -734,6 +734,13 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   ph.gvGF = (float)ph.gvG;
   ph.epsentrF = (float)ph.epsentr;
   ph.dissFactF = (float)ph.dissFact;
+  ph.ausmSigma = d->ausmSigma;
+  ph.ausmKp = d->ausmKp;
+  ph.ausmKu = d->ausmKu;
+  ph.ausmMInf = d->ausmMInf;
+  ph.ausmSigmaF = (float)ph.ausmSigma;
+  ph.ausmKpF = (float)ph.ausmKp;
+  ph.ausmKuF = (float)ph.ausmKu;
   for (int i = 0; i < 5; ++i) ph.grkF[i] = (float)ph.grk[i];
   h->nSteps = ph.nSteps;
   try {

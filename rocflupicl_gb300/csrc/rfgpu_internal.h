@@ -48,6 +48,10 @@ struct Phys {
   int nSteps, rkScheme, spaceDiscr, spaceOrder, reconst, venkatGuard;
   // FP32 copies for the mixed-path kernels (no per-thread FP64 conversions)
   float refCpF, refGammaF, gcRefF, gvGF, epsentrF, dissFactF, grkF[5];
+  // AUSM+up parameters (sigma, kp, ku; mInf is read by the reference but its
+  // flux function 2 overwrites the factor that uses it)
+  double ausmSigma, ausmKp, ausmKu, ausmMInf;
+  float ausmSigmaF, ausmKpF, ausmKuF;
 };
 
 template <typename R>

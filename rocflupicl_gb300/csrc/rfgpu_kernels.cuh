@@ -94,6 +94,59 @@ __device__ __forceinline__ void ausm_flux(const Phys &ph, const R L[5], const R 
   flx[4] = (af * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
 }
 
+// AUSM+up, RFLU_AUSMPlusUp_FluxFunction2 (modflu/RFLU_ModAUSMPlusUpFlux.F90:
+// 469-588) with vFracF = 1 (no particles): AUSM+ split Mach numbers and
+// pressures plus the pressure-diffusion (kp, sigma) and velocity-diffusion
+// (ku) terms; the routine's blending factor is overwritten with 1, so
+// alpha = 3/16.  H and a of both sides come from the caller (they are set up
+// differently at first and second order).
+template <typename R>
+__device__ __forceinline__ void ausmup_flux(R sigma, R kp, R ku, const R L[5], const R Rt[5],
+                                            R Hl, R al, R Hr, R ar, R nx, R ny, R nz, R nm,
+                                            R flx[5]) {
+  const R fs = R(0);
+  const R rl = L[0], ul = L[1], vl = L[2], wl = L[3], pl = L[4];
+  const R rr = Rt[0], ur = Rt[1], vr = Rt[2], wr = Rt[3], pr = Rt[4];
+  R ql = ul * nx + vl * ny + wl * nz - fs;
+  R qr = ur * nx + vr * ny + wr * nz - fs;
+  R af = R(0.5) * (al + ar);
+  R ml = ql / af, mla = fabs(ml);
+  R mr = qr / af, mra = fabs(mr);
+  R mbarsq = R(0.5) * (ml * ml + mr * mr);
+  const R fa = R(1);
+  const R alpha = R(0.1875) * (R(5) * fa * fa - R(4));
+  R mlp, wtl, mrm, wtr;
+  if (mla <= R(1)) {
+    mlp = R(0.25) * (ml + R(1)) * (ml + R(1)) + R(0.125) * (ml * ml - R(1)) * (ml * ml - R(1));
+    wtl = R(0.25) * (ml + R(1)) * (ml + R(1)) * (R(2) - ml) +
+          alpha * ml * (ml * ml - R(1)) * (ml * ml - R(1));
+  } else {
+    mlp = R(0.5) * (ml + mla);
+    wtl = R(0.5) * (R(1) + ml / mla);
+  }
+  if (mra <= R(1)) {
+    mrm = -(R(0.25) * (mr - R(1)) * (mr - R(1))) - R(0.125) * (mr * mr - R(1)) * (mr * mr - R(1));
+    wtr = R(0.25) * (mr - R(1)) * (mr - R(1)) * (R(2) + mr) -
+          alpha * mr * (mr * mr - R(1)) * (mr * mr - R(1));
+  } else {
+    mrm = R(0.5) * (mr - mra);
+    wtr = R(0.5) * (R(1) - mr / mra);
+  }
+  R rf = R(0.5) * (rl + rr);
+  R sigmabar = R(1) - sigma * mbarsq;
+  R mp = (-(kp * (sigmabar > R(0) ? sigmabar : R(0)) * (pr - pl))) / (fa * rf * af * af);
+  R pu = -(ku * wtl * wtr * fa * af * (rl + rr) * (qr - ql));
+  R mf = mlp + mrm + mp, mfa = fabs(mf);
+  R mfp = R(0.5) * (mf + mfa), mfm = R(0.5) * (mf - mfa);
+  R pf = wtl * pl + wtr * pr + pu;
+  const R vFracF = R(1);
+  flx[0] = (af * vFracF * (mfp * rl + mfm * rr)) * nm;
+  flx[1] = (af * vFracF * (mfp * rl * ul + mfm * rr * ur) + pf * nx) * nm;
+  flx[2] = (af * vFracF * (mfp * rl * vl + mfm * rr * vr) + pf * ny) * nm;
+  flx[3] = (af * vFracF * (mfp * rl * wl + mfm * rr * wr) + pf * nz) * nm;
+  flx[4] = (af * vFracF * (mfp * rl * Hl + mfm * rr * Hr) + pf * fs) * nm;
+}
+
 template <typename R>
 __device__ __forceinline__ R entropy_fix(R l, R d) {  // RFLU_ModEntropyFixes.F90:95-106
   return (l > d) ? l : (l * l + d * d) / (R(2) * d);
@@ -691,6 +744,53 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
   }
 }
 
+// Riemann flux of one interior face on its (reconstructed) states, by DISCR.
+// AUSM+up sets up H and a as its face loops do: at second order from the
+// reconstructed state with refCp/refGamma (T = p/(rho R), a = sqrt(g R T),
+// H = cp T + |v|^2/2; RFLU_AUSMPlusUp_ComputeFlux2_TCP :3255-3632), at first
+// order from the cells (H = E/rho + p/rho, a = dv(SOUN); ComputeFlux1
+// :894-1366, FP32 sound speed sqrt(g p/rho) on the mixed path).
+template <typename R>
+__device__ __forceinline__ void face_riemann(const RegionDev<R> &g, int c1, int c2, const R L[5],
+                                             const R Rt[5], R irl, R irr, const R nrm[4],
+                                             R flx[8]) {
+  const int sd = g.ph.spaceDiscr;
+  if (sd == 4) {
+    ausm_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  } else if (sd == 1) {
+    roe_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  } else if (sd == 5) {
+    const PC<R> k{g.ph};
+    R Hl, al, Hr, ar;
+    if (g.ph.spaceOrder > 1) {
+      const R cp = k.cp(), gm = k.g(), gc = k.gc();
+      const R tl = L[4] / (L[0] * gc), tr = Rt[4] / (Rt[0] * gc);
+      al = sqrt(gm * gc * tl);
+      Hl = cp * tl + R(0.5) * (L[1] * L[1] + L[2] * L[2] + L[3] * L[3]) + R(0);
+      ar = sqrt(gm * gc * tr);
+      Hr = cp * tr + R(0.5) * (Rt[1] * Rt[1] + Rt[2] * Rt[2] + Rt[3] * Rt[3]) + R(0);
+    } else if (sizeof(R) == 8) {
+      const int N = g.nCells;
+      al = R(g.dv[2 * N + c1]);
+      Hl = R(g.cv[4 * N + c1]) * irl + L[4] / L[0];
+      ar = R(g.dv[2 * N + c2]);
+      Hr = R(g.cv[4 * N + c2]) * irr + Rt[4] / Rt[0];
+    } else {
+      const R gv = k.gvG();
+      al = sqrt(gv * L[4] / L[0]);
+      Hl = eo_dgpuvw(L[0], gv, L[4], L[1], L[2], L[3]) + L[4] / L[0];
+      ar = sqrt(gv * Rt[4] / Rt[0]);
+      Hr = eo_dgpuvw(Rt[0], gv, Rt[4], Rt[1], Rt[2], Rt[3]) + Rt[4] / Rt[0];
+    }
+    const R sig = sizeof(R) == 8 ? R(g.ph.ausmSigma) : R(g.ph.ausmSigmaF);
+    const R kp = sizeof(R) == 8 ? R(g.ph.ausmKp) : R(g.ph.ausmKpF);
+    const R ku = sizeof(R) == 8 ? R(g.ph.ausmKu) : R(g.ph.ausmKuF);
+    ausmup_flux(sig, kp, ku, L, Rt, Hl, al, Hr, ar, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  } else {
+    hllc_flux(g.ph, L, Rt, irl, irr, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  }
+}
+
 // Interior face fluxes, *_ComputeFlux2_TCP face loops (AUSM+ :2726-2846,
 // Roe :2646-2855, HLLC :2239-2409), written to the face flux buffer.
 template <typename R>
@@ -725,13 +825,7 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
       reconstruct(G, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
     }
     R flx[8];
-    const int sd = g.ph.spaceDiscr;
-    if (sd == 4)
-      ausm_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
-    else if (sd == 1)
-      roe_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
-    else
-      hllc_flux(g.ph, L, Rt, irl, irr, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+    face_riemann(g, c1, c2, L, Rt, irl, irr, nrm, flx);
     flx[5] = flx[6] = flx[7] = R(0);
     st8(g.flux + 8 * (size_t)f, flx);
   }
@@ -1663,13 +1757,7 @@ __global__ void __launch_bounds__(128) k_face_flux_scratch(const RegionDev<R> g,
     reconstruct(G, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
   }
   R flx[8];
-  const int sd = g.ph.spaceDiscr;
-  if (sd == 4)
-    ausm_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
-  else if (sd == 1)
-    roe_flux(g.ph, L, Rt, nrm[0], nrm[1], nrm[2], nrm[3], flx);
-  else
-    hllc_flux(g.ph, L, Rt, irl, irr, nrm[0], nrm[1], nrm[2], nrm[3], flx);
+  face_riemann(g, c1, c2, L, Rt, irl, irr, nrm, flx);
   flx[5] = flx[6] = flx[7] = R(0);
   st8(flux + 8 * (size_t)f, flx);
 }

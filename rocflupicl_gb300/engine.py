@@ -57,7 +57,8 @@ class RegionDescT(C.Structure):
                 ("rkScheme", C.c_int), ("refCp", C.c_double), ("refGamma", C.c_double),
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
                 ("dissFact", C.c_double), ("precision", C.c_int), ("venkatGuard", C.c_int),
-                ("cellOrder", C.c_int)]
+                ("cellOrder", C.c_int), ("ausmSigma", C.c_double), ("ausmKp", C.c_double),
+                ("ausmKu", C.c_double), ("ausmMInf", C.c_double)]
 
 
 # device numbering of cells and faces (rfgpu.h RFGPU_ORDER_*)
@@ -271,6 +272,8 @@ class Region:
         d.precision = self.precision
         d.venkatGuard = num.venkatGuard
         d.cellOrder = cell_order
+        d.ausmSigma, d.ausmKp, d.ausmKu, d.ausmMInf = (
+            num.ausmSigma, num.ausmKp, num.ausmKu, num.ausmMInf)
         h = C.c_void_p()
         _check(self.lib.rfgpu_region_create(C.byref(d), C.byref(h)), "rfgpu_region_create")
         self.h = h

@@ -67,7 +67,7 @@ def _desc(c, **over):
     return lib, d, keep
 
 
-@pytest.mark.parametrize("field,value", [("spaceDiscr", 5), ("spaceOrder", 3), ("reconst", 1),
+@pytest.mark.parametrize("field,value", [("spaceDiscr", 2), ("spaceOrder", 3), ("reconst", 1),
                                          ("rkScheme", 7), ("gasModel", 2), ("flowModel", 1),
                                          ("precision", 9)])
 def test_unsupported_options_refused_before_any_cuda_call(field, value):

@@ -44,7 +44,8 @@ def test_gtlin_gradients_exact(kind):
         assert np.allclose(grad[:, var, :], a[var, 1:], rtol=0, atol=1e-10), var
 
 
-@pytest.mark.parametrize("scheme", [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC])
+@pytest.mark.parametrize("scheme", [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC,
+                                    K.DISCR_UPW_AUSMPLUSUP])
 def test_flux_consistency(scheme):
     c = K.shock_tube(4, numerics=K.Numerics(spaceDiscr=scheme))
     o = Oracle(c)

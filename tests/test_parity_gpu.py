@@ -18,7 +18,7 @@ from rocflupicl_gb300 import engine as E
 
 pytestmark = pytest.mark.gpu
 
-SCHEMES = [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC]
+SCHEMES = [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC, K.DISCR_UPW_AUSMPLUSUP]
 
 
 def _oracle(c):
@@ -108,11 +108,16 @@ def test_host_driven_stages(rk):
     r.close()
 
 
-@pytest.mark.parametrize("variant", ["order1", "nolimiter", "refguard", "subsonic", "order1bc"])
+@pytest.mark.parametrize("variant", ["order1", "nolimiter", "refguard", "subsonic", "order1bc",
+                                     "order1_ausmup", "ausmup_params"])
 def test_option_envelope_bitwise(variant):
     scheme = K.DISCR_UPW_AUSMPLUS
     if variant == "order1":
         c = make("tet", scheme, spaceOrder=1)
+    elif variant == "order1_ausmup":
+        c = make("mixed", K.DISCR_UPW_AUSMPLUSUP, spaceOrder=1)
+    elif variant == "ausmup_params":
+        c = make("tet", K.DISCR_UPW_AUSMPLUSUP, ausmSigma=0.5, ausmKp=0.1, ausmKu=1.0)
     elif variant == "nolimiter":
         c = make("tet", K.DISCR_UPW_HLLC, reconst=K.RECONST_NONE)
     elif variant == "refguard":
@@ -189,7 +194,7 @@ def test_status_flags_on_host_injected_nan():
 
 def test_unsupported_option_refused():
     c = make("tube", K.DISCR_UPW_AUSMPLUS)
-    c.numerics.spaceDiscr = 5  # AUSM+up is not in the envelope
+    c.numerics.spaceDiscr = 2  # central scheme (DISCR_CEN_SCAL) is not in the envelope
     with pytest.raises(E.EngineError) as ei:
         E.Region(c)
     assert ei.value.code == E.ERR_UNSUPPORTED
