@@ -48,7 +48,8 @@ def parse():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--workload", default="tet", choices=["tet", "sod", "mixed", "tubes", "serving"],
                     help="tet: the headline line; the others print their own measurement")
-    ap.add_argument("--n", type=int, default=128, help="base hexes per direction")
+    ap.add_argument("--n", "--hexes", dest="n", type=int, default=128,
+                    help="base hexes per direction")
     ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
     ap.add_argument("--cell-order", default="locality", choices=["locality", "host"],
                     help="device numbering of cells and faces (results are identical)")
