@@ -178,7 +178,8 @@ def workload_config(c, a):
     return {"workload": f"tet_shock_box {a.n}^3x6 Kuhn tets, jitter 0.1h, Ms=2, lognormal rho sigma 0.1; "
                         f"{a.scheme} flux, WLSQ+Venkatakrishnan, Wray RK3",
             "cells": m.nCells, "faces": m.nFaces, "bfaces": m.nBFaces, "stencil_members": m.nMembs,
-            "precision": "mixed: FP32 reconstruction/limiter/flux, FP64 geometry/accumulate/update/EOS",
+            "precision": "mixed: FP32 gradient/limiter/reconstruction/flux/EOS, compensated FP32 residual sums, "
+                         "float-float conserved state; FP64 geometry masters and FP64 cv/dv on download",
             "l2": "inputs larger than L2 (working set >10 GB vs 129 MB L2)",
             "cell_order": getattr(a, "cell_order", "locality"),
             "parallelism": "replicas (one independent region per GPU)"}
@@ -336,6 +337,10 @@ def main():
             "algorithmic_bytes_per_launch": kb[dom],
             "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
             "step_gbs": step_gbs, "step_frac": step_gbs / peak}
+    if dom == "gradient":
+        roof["note"] = ("the gradient pass gathers every stencil member's record (~40 per tet) through "
+                        "L1/L2; its limit is the L1TEX data pipe (one wavefront per gathered record per "
+                        "lane), DRAM traffic is below the algorithmic bytes")
 
     # ---- e2e through the C ABI with host buffers --------------------------------
     e2e = None
@@ -429,7 +434,7 @@ def main():
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
                 "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 flux / f64 accumulate", "data": "synthetic (seeded)",
+                "dtype": "f32 (float-float state)", "data": "synthetic (seeded)",
                 "config": workload_config(c, a), "roofline": roof, "cpu_baseline": cpu,
                 "e2e": e2e, "gpu_launches": launches, "clocks": clk, "status": status,
                 "kernels": per, "fp64": fp64, "device_bytes": dev_bytes, "serving": serving}

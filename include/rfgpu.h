@@ -93,12 +93,25 @@ typedef struct {
   int bcOptFixed;        /* inflow TOTANG FIXED switch (BCOPT_FIXED_NO 0 / YES 1) */
 } rfgpu_patch_t;
 
+/* One border of a partitioned region: the cells it sends to one neighbour
+ * region and the virtual cells it receives from it (t_border,
+ * modfloflu/ModBorder.F90:87-99).  Send cell k of this border pairs with
+ * receive cell k of the neighbour's matching border. */
+typedef struct {
+  int iRegionGlobal;     /* border%iRegionGlobal: the neighbour region */
+  int iBorder;           /* border%iBorder: 1-based index of the matching border in the neighbour */
+  int nCellsSend;        /* border%nCellsSend */
+  const int *icgSend;    /* border%icgSend(nCellsSend): actual cells of this region, 1-based */
+  int nCellsRecv;        /* border%nCellsRecv */
+  const int *icgRecv;    /* border%icgRecv(nCellsRecv): virtual cells of this region, 1-based */
+} rfgpu_border_t;
+
 /* Everything RFLU_InitFlowSolver has built for one region, plus the numerics
  * keys.  Mirrors t_region / t_grid / t_mixt_input fields
  * (modfloflu/ModDataStruct.F90:100-167, ModGrid.F90:84-317,
  * ModMixture.F90:76-195). */
 typedef struct {
-  int nCells;            /* nCells == nCellsTot: one region, no virtual cells */
+  int nCells;            /* actual cells (grid%nCells); see nCellsTot for virtual cells */
   int nFaces;            /* interior faces (nFaces); f2c may have a larger leading dim */
   int f2cLd;             /* leading dimension of f2c (>= 2) */
   const int *f2c;        /* f2c(f2cLd,nFaces), 1-based */
@@ -125,6 +138,21 @@ typedef struct {
   int cellOrder;           /* RFGPU_ORDER_*: device numbering of cells and faces */
   double ausmSigma, ausmKp, ausmKu, ausmMInf; /* AUSM+up (DISCR 5) SIGMA, KP, KU, MINF
                               (libfloflu/ReadNumericsSection.F90:239-276) */
+  /* Partitioned regions.  nCellsTot (grid%nCellsTot) counts the actual cells
+   * 1..nCells followed by the virtual cells nCells+1..nCellsTot; 0 means
+   * nCells (no virtual cells).  With virtual cells, cofg, vol, c2csOffsets,
+   * xyzMoms, cv and dv cover nCellsTot cells, stencil members and f2c may
+   * name virtual cells (nFaces holds the actual-actual and actual-virtual
+   * faces), and every per-cell array crossing this ABI (cv, dv, rhs, grad)
+   * has nCellsTot columns.  As in the reference, gradients and limiter cover
+   * all nCellsTot cells (CellGradientsMP), residuals of virtual cells are
+   * zero (ZeroDummyCellsMP) and the update, EOS, checks and time step cover
+   * the actual cells; virtual cells change only through the border calls
+   * below or a coupled batch. */
+  int nCellsTot;
+  int iRegionGlobal;       /* pRegion%iRegionGlobal: matches borders between regions */
+  int nBorders;            /* grid%nBorders */
+  const rfgpu_border_t *borders;
 } rfgpu_region_desc_t;
 
 /* Register a region: copies and reorders the arrays to device-resident SoA.
@@ -148,7 +176,10 @@ int rfgpu_dt(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
 /* One full time step on the device without host round trips: dt as above
  * using the device-resident current time, clipped so time does not pass
  * endTime (rocflu/RFLU_TimeStepping.F90:490-493; endTime <= 0 disables the
- * clip), then nrkSteps stages, then time += dtMin. */
+ * clip), then nrkSteps stages, then time += dtMin.  A region with borders
+ * needs its neighbours between stages: it is stepped through a coupled batch
+ * (rfgpu_batch_create_ex) or rfgpu_stage plus the border calls, and gets
+ * RFGPU_ERR_UNSUPPORTED here and from rfgpu_steps_graph. */
 int rfgpu_step(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
                double endTime);
 
@@ -157,16 +188,16 @@ int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed
                       double dtMinLimit, double endTime);
 
 /* Residual only: CellGradientsMP + ConvectiveFluxesMP (libfloflu/RungeKuttaMP.F90:223-233)
- * on the resident state, which it does not modify.  rhs (5,nCells) host
- * output or NULL (result stays on the device). */
+ * on the resident state, which it does not modify.  rhs (5,nCellsTot) host
+ * output (zero for virtual cells) or NULL (result stays on the device). */
 int rfgpu_residual(rfgpu_region_t h, double *rhs);
 
-/* Host copies: cv(5,nCells), dv(3,nCells); either may be NULL. */
+/* Host copies: cv(5,nCellsTot), dv(3,nCellsTot); either may be NULL. */
 int rfgpu_download(rfgpu_region_t h, double *cv, double *dv);
-/* Restart / host edits: cv(5,nCells); dv NULL recomputes dv from cv. */
+/* Restart / host edits: cv(5,nCellsTot); dv NULL recomputes dv from cv. */
 int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv);
 
-/* Limited gradients of the last residual/stage: grad(3,5,nCells). */
+/* Limited gradients of the last residual/stage: grad(3,5,nCellsTot). */
 int rfgpu_download_grad(rfgpu_region_t h, double *grad);
 
 /* Time state: current time and last dtMin. */
@@ -190,9 +221,9 @@ int rfgpu_set_tuning(rfgpu_region_t h, int blockCells, int blockFaces);
  * the handle's stream around every kernel; rfgpu_profile_read synchronises and
  * returns, per kernel class, the summed milliseconds and launch counts, then
  * resets.  Classes: 0 gradient, 1 limiter, 2 face flux, 3 boundary-face flux,
- * 4 gather+update, 5 dt faces, 6 dt boundary faces, 7 dt cells, 8 dt finalize.
- * Graph replays are not profiled. */
-#define RFGPU_NPROF 9
+ * 4 gather+update, 5 dt faces, 6 dt boundary faces, 7 dt cells, 8 dt finalize,
+ * 9 halo exchange.  Graph replays are not profiled. */
+#define RFGPU_NPROF 10
 int rfgpu_profile(rfgpu_region_t h, int enable);
 int rfgpu_profile_read(rfgpu_region_t h, double *ms, long long *count, int n);
 
@@ -209,9 +240,46 @@ int rfgpu_mem_info(long long *freeBytes, long long *totalBytes);
 void *rfgpu_host_alloc(long long bytes);
 int rfgpu_host_free(void *p);
 
-/* Batches: many independent regions advanced together, one launch per pass
- * over all regions (a persistent grid walking a tile work list). */
+/* Halo exchange between partitioned regions (iBorder is 1-based).
+ *
+ * rfgpu_border_copy: RFLU_MPI_CopyWrapper for one border of src
+ * (modflu/RFLU_ModMPI.F90:564-666, RFLU_MPI_CopyCellData :332-390) followed by
+ * RFLU_SetVarsContWrapper of the received virtual cells
+ * (libfloflu/RungeKuttaMP.F90:381-396): cv of the border's send cells in src
+ * goes to the receive cells of the matching border in dst (the border's
+ * iRegionGlobal / iBorder), whose dv and cell records are recomputed.  Both
+ * handles must live on the same device; the copy is ordered after the work
+ * already queued on both handles' streams, and later work on either waits
+ * for it.
+ *
+ * rfgpu_border_pack / rfgpu_border_unpack: the buffer sides of
+ * RFLU_MPI_ISendWrapper / RFLU_MPI_RecvWrapper (RFLU_ModMPI.F90:2469-2555,
+ * 2856-2940) for a neighbour in another process: sendBuff(5,nCellsSend) =
+ * cv(:,icgSend) and cv(:,icgRecv) = recvBuff(5,nCellsRecv) plus the virtual
+ * cells' dv.  The buffers may be host or device memory (a CUDA-aware MPI can
+ * take device buffers directly).  Synchronous.  The engine's stage applies
+ * the update and AfterUpdateMP in one pass, so a pack after rfgpu_stage sees
+ * the state after AfterUpdateMP; the reference's ISendWrapper packs before
+ * it, which differs only where AfterUpdateMP changed a border cell
+ * (RFGPU_ST_PFLOOR / RFGPU_ST_PCLAMP). */
+int rfgpu_border_copy(rfgpu_region_t src, int iBorder, rfgpu_region_t dst);
+int rfgpu_border_pack(rfgpu_region_t h, int iBorder, double *sendBuff);
+int rfgpu_border_unpack(rfgpu_region_t h, int iBorder, const double *recvBuff);
+
+/* Batches: many regions advanced together, one launch per pass over all
+ * regions (a persistent grid walking a tile work list).  Regions of a plain
+ * batch are independent solves (each its own time step) and may not have
+ * borders.  RFGPU_BATCH_COUPLED makes the batch the regions of one
+ * partitioned case on this device (global%nRegionsLocal): one time step, the
+ * minimum over the batch (rocflu/RFLU_MinimumTimeStep.F90:131-208, the
+ * MPI_Allreduce over local regions), and after every stage's update the halo
+ * exchange of every border (RFLU_MPI_CopyWrapper + RFLU_SetVarsContWrapper of
+ * the virtual cells) in one launch.  Every border's neighbour must be in the
+ * batch (RFGPU_ERR_ARG otherwise) and the regions must share the gas
+ * constants (RFGPU_ERR_UNSUPPORTED). */
+enum { RFGPU_BATCH_COUPLED = 1 };
 int rfgpu_batch_create(rfgpu_region_t *regions, int nRegions, rfgpu_batch_t *out);
+int rfgpu_batch_create_ex(rfgpu_region_t *regions, int nRegions, int flags, rfgpu_batch_t *out);
 int rfgpu_batch_destroy(rfgpu_batch_t b);
 int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMinLimit,
                      double endTime);

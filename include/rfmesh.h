@@ -132,6 +132,16 @@ const double *rfmesh_cofg_view(rfmesh_t m);
  * most 40 per cell) and moments (10,nCells) built elsewhere. */
 int rfmesh_set_stencils(rfmesh_t m, const int *offsets, const int *members, const double *moms);
 
+/* The host stencil builder on connectivity given as arrays (the inputs of
+ * rfgpu_mesh_stencils, same outputs): e.g. the cells of one partitioned
+ * region, actual and virtual, whose stencils the reference builds from the
+ * region's own cells (RFLU_BuildC2CStencilWrapper over nCellsTot).
+ * c2csMembers needs room for 40 per cell.  RFMESH_ERR_ARG for a bad index,
+ * RFMESH_ERR_GEOM when a cell has more than 256 vertex-neighbour entries. */
+int rfmesh_build_stencils(int nCells, int nVerts, const int *cellVerts, const int *cellNVerts,
+                          const int *v2cOffsets, const int *v2c, const double *cofg, int nThreads,
+                          int *c2csOffsets, int *c2csMembers, double *xyzMoms);
+
 #ifdef __cplusplus
 }
 #endif

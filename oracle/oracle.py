@@ -55,7 +55,7 @@ class OrcRegion(C.Structure):
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
                 ("dissFact", C.c_double), ("venkatGuard", C.c_int),
                 ("ausmSigma", C.c_double), ("ausmKp", C.c_double), ("ausmKu", C.c_double),
-                ("ausmMInf", C.c_double)]
+                ("ausmMInf", C.c_double), ("nCellsTot", C.c_int)]
 
 
 def _load():
@@ -72,6 +72,7 @@ def _load():
         lib.orc_dt.argtypes = [R, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double]
         lib.orc_dt.restype = C.c_double
         lib.orc_set_dv.argtypes = [R, dp, dp]
+        lib.orc_set_dv_range.argtypes = [R, dp, dp, C.c_long, C.c_long]
         lib.orc_face_flux.argtypes = [R, dp, dp, dp, dp]
         _lib = lib
     return _lib
@@ -100,6 +101,7 @@ class Oracle:
 
         reg = OrcRegion()
         reg.nCells, reg.nFaces = m.nCells, m.nFaces
+        reg.nCellsTot = m.nTot
         reg.f2c = _ip(keep(m.f2c, np.int32))
         reg.fn = _dp(keep(m.fn, np.float64))
         reg.fc = _dp(keep(m.fc, np.float64))
@@ -132,9 +134,10 @@ class Oracle:
         reg.ausmSigma, reg.ausmKp, reg.ausmKu, reg.ausmMInf = (
             num.ausmSigma, num.ausmKp, num.ausmKu, num.ausmMInf)
         self.reg = reg
-        self.nCells = m.nCells
+        self.nCells = m.nTot      # rows of every per-cell array (actual + virtual)
+        self.nAct = m.nCells
         self.num = num
-        n = m.nCells
+        n = m.nTot
         self.cvOld = np.zeros((n, 5))
         self.rhs = np.zeros((n, 5))
         self.rhsSum = np.zeros((n, 5))
@@ -164,6 +167,10 @@ class Oracle:
         self.lib.orc_set_dv(C.byref(self.reg), _dp(np.ascontiguousarray(cv)), _dp(dv))
         return dv
 
+    def set_dv_range(self, cv, dv, first, last):
+        """dv(first:last) from cv in place (RFLU_SetVarsContWrapper over a range)."""
+        self.lib.orc_set_dv_range(C.byref(self.reg), _dp(cv), _dp(dv), first, last)
+
     def face_flux(self, left, right, n):
         f = np.zeros(5)
         self.lib.orc_face_flux(C.byref(self.reg), _dp(np.asarray(left, np.float64)),
@@ -191,6 +198,67 @@ class Oracle:
                 finished = True
             for s in range(1, nst + 1):
                 st |= self.stage(cv, dv, s, dtm, threads)
+            t += dtm
+            k += 1
+            if finished:
+                break
+        return t, k, st
+
+
+class MultiOracle:
+    """The oracle over the regions of one partitioned case
+    (libfloflu/RungeKuttaMP.F90:190-396 with nRegionsLocal regions): every
+    region's stage, then the halo exchange of every border
+    (RFLU_MPI_CopyWrapper: cv of the send cells into the neighbour's receive
+    cells) and the dependent variables of the received virtual cells
+    (RFLU_SetVarsContWrapper(nCells+1,nCellsTot)); one time step, the minimum
+    over the regions (RFLU_MinimumTimeStep)."""
+
+    def __init__(self, cases):
+        self.cases = list(cases)
+        self.orcs = [Oracle(c) for c in self.cases]
+        self.num = self.cases[0].numerics
+        ids = [c.mesh.iRegionGlobal for c in self.cases]
+        self.index = {g: i for i, g in enumerate(ids)}
+
+    def exchange(self, cvs, dvs):
+        for r, c in enumerate(self.cases):
+            for b in c.mesh.borders:
+                s = self.index[b.iRegionGlobal]
+                b2 = self.cases[s].mesh.borders[b.iBorder - 1]
+                cvs[s][b2.icgRecv - 1] = cvs[r][b.icgSend - 1]
+        for s, o in enumerate(self.orcs):
+            o.set_dv_range(cvs[s], dvs[s], o.nAct, o.nCells)
+
+    def dt(self, cvs, dvs, cfl, dtImposed, dtMinLimit=0.0, currentTime=1.0):
+        return min(o.dt(cv, dv, cfl, dtImposed, dtMinLimit, currentTime)
+                   for o, cv, dv in zip(self.orcs, cvs, dvs))
+
+    def stage(self, cvs, dvs, istage, dtMin) -> int:
+        st = 0
+        for o, cv, dv in zip(self.orcs, cvs, dvs):
+            st |= o.stage(cv, dv, istage, dtMin)
+        self.exchange(cvs, dvs)
+        return st
+
+    def run(self, cvs, dvs, n_steps=None, t_end=None, dt_imposed=None):
+        """Time loop as Oracle.run over all regions.  Returns (time, steps, status)."""
+        nst = {1: 4, 2: 3, 3: 1}[self.num.rkScheme]
+        t, k, st = 0.0, 0, 0
+        if dt_imposed is None:
+            dt_imposed = self.dt(cvs, dvs, self.num.cfl, 1.0, 0.0, 1.0)
+        while True:
+            if n_steps is not None and k >= n_steps:
+                break
+            if t_end is not None and t >= t_end:
+                break
+            dtm = self.dt(cvs, dvs, self.num.cfl, dt_imposed, 0.0, t)
+            finished = False
+            if t_end is not None and t + dtm > t_end:
+                dtm = t_end - t
+                finished = True
+            for s in range(1, nst + 1):
+                st |= self.stage(cvs, dvs, s, dtm)
             t += dtm
             k += 1
             if finished:

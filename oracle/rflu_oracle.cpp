@@ -732,8 +732,10 @@ inline void venkat_term(double d2, double dmax, double dmin, double epsq, double
 }
 
 // RFLU_ComputeLimiterVenkat + RFLU_LimitGradCells (modflu/RFLU_ModLimiters.F90:339-532,707-760)
+inline long n_tot(const orc_region_t *r) { return r->nCellsTot > 0 ? r->nCellsTot : r->nCells; }
+
 void venkat(const orc_region_t *r, const double *var, double *grad) {
-  const long nC = r->nCells;
+  const long nC = n_tot(r);
   const double THRD = 1.0 / 3.0;
   std::vector<double> vmin(var, var + 5 * nC), vmax(var, var + 5 * nC), lim(5 * nC, 1.0);
   for (long f = 0; f < r->nFaces; ++f) {
@@ -774,17 +776,17 @@ void venkat(const orc_region_t *r, const double *var, double *grad) {
 // CellGradientsMP (libfloflu/CellGradientsMP.F90:158-253), in place on cv
 void cell_gradients(const orc_region_t *r, double *cv, const double *dv, double *grad) {
   if (r->spaceOrder <= 1) return;
-  cons2prim(r, cv, dv, 0, r->nCells);
-  gradients(r, cv, grad, 0, r->nCells);
+  cons2prim(r, cv, dv, 0, n_tot(r));
+  gradients(r, cv, grad, 0, n_tot(r));
   if (r->reconst == RECONST_LIM_VENKAT) venkat(r, cv, grad);
-  prim2cons(r, cv, dv, 0, r->nCells);
+  prim2cons(r, cv, dv, 0, n_tot(r));
 }
 
 // ConvectiveFluxes (libfloflu/ConvectiveFluxes.F90:133-159) with diss = 0:
 // rhs = -diss, interior faces in order, then patches in order.
 void convective_fluxes(const orc_region_t *r, const double *cv, const double *dv,
                        const double *grad, double *rhs) {
-  for (long i = 0; i < 5L * r->nCells; ++i) rhs[i] = -0.0;
+  for (long i = 0; i < 5L * n_tot(r); ++i) rhs[i] = -0.0;
   Ctx c{r, cv, dv, grad};
   double flx[5];
   for (long f = 0; f < r->nFaces; ++f) {
@@ -802,6 +804,8 @@ void convective_fluxes(const orc_region_t *r, const double *cv, const double *dv
       for (int k = hasMass ? 0 : 1; k < 5; ++k) rhs[5 * c1 + k] = rhs[5 * c1 + k] + flx[k];
     }
   }
+  // ZeroDummyCellsMP (libfloflu/RungeKuttaMP.F90:232): virtual cells carry no residual
+  for (long i = 5L * r->nCells; i < 5L * n_tot(r); ++i) rhs[i] = 0.0;
 }
 
 // RkUpdateGeneric, static grid (libfloflu/RkUpdateGeneric.F90:229-314),
@@ -912,7 +916,12 @@ extern "C" {
 
 void orc_set_dv(const orc_region_t *r, const double *cv, double *dv) {
   double gc = R_M(r->gvMol), g = G_CpR(r->gvCp, gc);
-  for (long i = 0; i < r->nCells; ++i) set_dv_cell(gc, g, cv + 5 * i, dv + 3 * i);
+  for (long i = 0; i < n_tot(r); ++i) set_dv_cell(gc, g, cv + 5 * i, dv + 3 * i);
+}
+
+void orc_set_dv_range(const orc_region_t *r, const double *cv, double *dv, long first, long last) {
+  double gc = R_M(r->gvMol), g = G_CpR(r->gvCp, gc);
+  for (long i = first; i < last; ++i) set_dv_cell(gc, g, cv + 5 * i, dv + 3 * i);
 }
 
 int orc_rk_stage(const orc_region_t *r, int istage, double dtMin, double *cv, double *dv,
@@ -925,9 +934,9 @@ int orc_rk_stage(const orc_region_t *r, int istage, double dtMin, double *cv, do
   if (r->rkScheme != RK_SCHEME_4_CLASSICAL || istage == 1) std::memcpy(cvOld, cv, sizeof(double) * 5 * nC);
   cell_gradients(r, cv, dv, grad);
   convective_fluxes(r, cv, dv, grad, rhs);
-  // SourceTermsMP round trip (libfloflu/SourceTermsMP.F90:138,182)
-  cons2prim(r, cv, dv, 0, nC);
-  prim2cons(r, cv, dv, 0, nC);
+  // SourceTermsMP round trip (libfloflu/SourceTermsMP.F90:138,182), all cells
+  cons2prim(r, cv, dv, 0, n_tot(r));
+  prim2cons(r, cv, dv, 0, n_tot(r));
   // RKUpdateMP
   double fac = ark[istage - 1] * dtMin;
   for (long i = 0; i < nC; ++i)
@@ -943,10 +952,10 @@ int orc_rk_stage(const orc_region_t *r, int istage, double dtMin, double *cv, do
 
 void orc_residual(const orc_region_t *r, const double *cv, const double *dv, double *rhs,
                   double *grad) {
-  std::vector<double> q(cv, cv + 5 * (size_t)r->nCells);
+  std::vector<double> q(cv, cv + 5 * (size_t)n_tot(r));
   std::vector<double> g;
   if (!grad) {
-    g.assign(15 * (size_t)r->nCells, 0.0);
+    g.assign(15 * (size_t)n_tot(r), 0.0);
     grad = g.data();
   }
   cell_gradients(r, q.data(), dv, grad);
@@ -960,7 +969,7 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
 #else
   (void)nThreads;
 #endif
-  const long nC = r->nCells, nF = r->nFaces;
+  const long nC = r->nCells, nF = r->nFaces, nT = n_tot(r);
   double ark[5], grk[5];
   int nSteps;
   rk_coeffs(r->rkScheme, ark, grk, &nSteps);
@@ -970,27 +979,27 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
   }
   if (r->spaceOrder > 1) {
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < nC; ++i) cons2prim(r, cv, dv, i, i + 1);
+    for (long i = 0; i < nT; ++i) cons2prim(r, cv, dv, i, i + 1);
 #pragma omp parallel for schedule(static, 256)
-    for (long i = 0; i < nC; ++i) gradients(r, cv, grad, i, i + 1);
+    for (long i = 0; i < nT; ++i) gradients(r, cv, grad, i, i + 1);
     if (r->reconst == RECONST_LIM_VENKAT) {
       // per-cell gather form of the limiter: min/max and min over the cell's
       // interior faces are order independent, so this equals the face loop
-      std::vector<long> off(nC + 1, 0), lst(2 * nF);
+      std::vector<long> off(nT + 1, 0), lst(2 * nF);
       for (long f = 0; f < nF; ++f) {
         off[r->f2c[2 * f]]++;
         off[r->f2c[2 * f + 1]]++;
       }
-      for (long i = 0; i < nC; ++i) off[i + 1] += off[i];
+      for (long i = 0; i < nT; ++i) off[i + 1] += off[i];
       std::vector<long> fill(off.begin(), off.end() - 1);
       for (long f = 0; f < nF; ++f) {
         lst[fill[r->f2c[2 * f] - 1]++] = f;
         lst[fill[r->f2c[2 * f + 1] - 1]++] = f;
       }
       const double THRD = 1.0 / 3.0;
-      std::vector<double> lim(5 * nC);
+      std::vector<double> lim(5 * nT);
 #pragma omp parallel for schedule(static, 256)
-      for (long c = 0; c < nC; ++c) {
+      for (long c = 0; c < nT; ++c) {
         double vmin[5], vmax[5];
         for (int v = 0; v < 5; ++v) vmin[v] = vmax[v] = cv[5 * c + v];
         for (long e = off[c]; e < off[c + 1]; ++e) {
@@ -1018,12 +1027,12 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
         for (int v = 0; v < 5; ++v) lim[5 * c + v] = l[v];
       }
 #pragma omp parallel for schedule(static)
-      for (long c = 0; c < nC; ++c)
+      for (long c = 0; c < nT; ++c)
         for (int v = 0; v < 5; ++v)
           for (int d = 0; d < 3; ++d) grad[15 * c + 3 * v + d] = lim[5 * c + v] * grad[15 * c + 3 * v + d];
     }
 #pragma omp parallel for schedule(static)
-    for (long i = 0; i < nC; ++i) prim2cons(r, cv, dv, i, i + 1);
+    for (long i = 0; i < nT; ++i) prim2cons(r, cv, dv, i, i + 1);
   }
   // face fluxes, then per-cell gather in reference order
   std::vector<double> ff(5 * nF);
@@ -1044,15 +1053,15 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
   }
   // c2f in reference accumulation order: signed interior faces ascending,
   // then boundary faces by patch
-  std::vector<long> off(nC + 1, 0);
+  std::vector<long> off(nT + 1, 0);
   for (long f = 0; f < nF; ++f) {
     off[r->f2c[2 * f]]++;
     off[r->f2c[2 * f + 1]]++;
   }
   for (int ip = 0; ip < r->nPatches; ++ip)
     for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl) off[r->patches[ip].bf2c[ifl]]++;
-  for (long i = 0; i < nC; ++i) off[i + 1] += off[i];
-  std::vector<long> lst(off[nC]);
+  for (long i = 0; i < nT; ++i) off[i + 1] += off[i];
+  std::vector<long> lst(off[nT]);
   {
     std::vector<long> fill(off.begin(), off.end() - 1);
     for (long f = 0; f < nF; ++f) {
@@ -1087,13 +1096,20 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
     set_dv_cell(gc, g, cv + 5 * c, dv + 3 * c);
     st |= after_update_cell(gc, g, cv + 5 * c, dv + 3 * c);
   }
+  // virtual cells: ZeroDummyCellsMP, and the SourceTermsMP round trip the
+  // serial stage applies to every cell (the update overwrites it elsewhere)
+  for (long c = nC; c < nT; ++c) {
+    for (int k = 0; k < 5; ++k) rhs[5 * c + k] = 0.0;
+    cons2prim(r, cv, dv, c, c + 1);
+    prim2cons(r, cv, dv, c, c + 1);
+  }
   return st;
 }
 
 double orc_dt(const orc_region_t *r, const double *cv, const double *dv, double cfl,
               double dtImposed, double dtMinLimit, double currentTime) {
-  const long nC = r->nCells;
-  std::vector<double> dt(nC, 0.0);
+  const long nC = r->nCells;  // RFLU_TimeStepInviscid: minimum over the actual cells
+  std::vector<double> dt(n_tot(r), 0.0);
   const double fsu = 0.0;
   for (long f = 0; f < r->nFaces; ++f) {
     long c1 = r->f2c[2 * f] - 1, c2 = r->f2c[2 * f + 1] - 1;

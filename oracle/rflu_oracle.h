@@ -67,6 +67,13 @@ typedef struct {
   /* AUSM+up (DISCR_UPW_AUSMPLUSUP=5) parameters sigma, kp, ku, mInf
    * (libfloflu/ReadNumericsSection.F90:239-276; defaults 1, 0.25, 0.75, 0.1) */
   double ausmSigma, ausmKp, ausmKu, ausmMInf;
+  /* grid%nCellsTot: actual cells 1..nCells then virtual cells (0: nCells).
+   * Conversions, gradients and limiter cover all nCellsTot cells
+   * (CellGradientsMP, RFLU_ModLimiters.F90:393-412, RFLU_ModConvertCv.F90:845),
+   * residuals of virtual cells are zeroed (ZeroDummyCellsMP), the update, EOS,
+   * checks and time step cover 1..nCells; every per-cell array is sized
+   * nCellsTot. */
+  int nCellsTot;
 } orc_region_t;
 
 /* status bits, shared with the engine */
@@ -101,6 +108,9 @@ double orc_dt(const orc_region_t *r, const double *cv, const double *dv, double 
 
 /* RFLU_SetDependentVars (TCPERF) over all cells: dv from cv. */
 void orc_set_dv(const orc_region_t *r, const double *cv, double *dv);
+/* The same over cells first..last-1 (0-based), e.g. the virtual cells after a
+ * halo exchange (RFLU_SetVarsContWrapper(nCells+1,nCellsTot)). */
+void orc_set_dv_range(const orc_region_t *r, const double *cv, double *dv, long first, long last);
 
 /* Flux functions on one face for known-answer tests.  left/right = (r,u,v,w,p);
  * n = (nx,ny,nz,nm); returns flux(5). */

@@ -173,14 +173,18 @@ def rankine_hugoniot(Ms: float, gamma: float, rho1: float, p1: float):
 
 def tet_shock_box(n: int = 128, seed: int = 2024, jitter: float = 0.1, Ms: float = 2.0,
                   sigma: float = 0.1, x_shock: float = 0.2, numerics: Optional[Numerics] = None,
-                  n_steps: int = 100, threads: int = 0, stencils: str = "host") -> Case:
-    """Planar Ms shock over a perturbed tetrahedral box: n^3 hexes x 6 Kuhn tets,
-    interior vertices jittered by U(+-jitter*h); quiescent air rho=1.2, p=1e5
-    times a per-cell lognormal density factor exp(sigma*Z); Rankine-Hugoniot
-    post-shock state for x < x_shock.  Slip walls on y/z, supersonic outflow
-    (extrapolation) on the x ends."""
+                  n_steps: int = 100, threads: int = 0, stencils: str = "host",
+                  ny: Optional[int] = None, nz: Optional[int] = None,
+                  length=(1.0, 1.0, 1.0)) -> Case:
+    """Planar Ms shock over a perturbed tetrahedral box: n*ny*nz hexes (ny, nz
+    default n) x 6 Kuhn tets over [0,length], interior vertices jittered by
+    U(+-jitter*h); quiescent air rho=1.2, p=1e5 times a per-cell lognormal
+    density factor exp(sigma*Z); Rankine-Hugoniot post-shock state for
+    x < x_shock.  Slip walls on y/z, supersonic outflow (extrapolation) on the
+    x ends."""
     num = numerics or Numerics(spaceDiscr=DISCR_UPW_ROE)
-    m = _mesh.box(_mesh.TET, n, n, n, jitter=jitter, seed=seed, threads=threads, stencils=stencils)
+    m = _mesh.box(_mesh.TET, n, ny or n, nz or n, hi=tuple(length), jitter=jitter, seed=seed,
+                  threads=threads, stencils=stencils)
     rng = np.random.default_rng(seed)
     rho1, p1 = 1.2, 1.0e5
     r = rho1 * np.exp(sigma * rng.standard_normal(m.nCells))

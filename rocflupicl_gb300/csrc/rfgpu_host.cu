@@ -108,9 +108,24 @@ struct ProfState {
 
 }  // namespace
 
+// One border of a partitioned region: its send and receive cells in the
+// device numbering (host copies for matching borders into a coupled batch,
+// device copies for the border calls).
+struct BorderH {
+  int iRegionGlobal = 0, iBorder = 0;
+  std::vector<int> send, recv;
+  int *dSend = nullptr, *dRecv = nullptr;
+};
+
 struct rfgpu_region_s {
   int prec = 0;
-  int nCells = 0, nFaces = 0, nBFaces = 0;
+  int nCells = 0, nFaces = 0, nBFaces = 0;  // nCells: actual + virtual (nCellsTot)
+  int nAct = 0;                             // actual cells
+  int iRegionGlobal = 0;
+  double gvCp = 0.0, gvMol = 0.0;
+  std::vector<BorderH> borders;
+  double *bbuf = nullptr;                   // border buffer, 5 x the largest border
+  cudaEvent_t evA = nullptr, evB = nullptr; // ordering of border copies between streams
   int rkScheme = 2, nSteps = 3, spaceOrder = 2, reconst = 11;
   cudaStream_t stream = nullptr;
   DevAlloc mem;
@@ -216,7 +231,19 @@ int check_desc(const rfgpu_region_desc_t *d) {
       if (!p.vals || nData < 5) return RFGPU_ERR_ARG;
     }
   }
-  const long long N = d->nCells;
+  if (d->nCellsTot != 0 && d->nCellsTot < d->nCells) return RFGPU_ERR_ARG;
+  const long long N = d->nCellsTot > 0 ? d->nCellsTot : d->nCells;
+  if (d->nBorders < 0 || (d->nBorders > 0 && !d->borders)) return RFGPU_ERR_ARG;
+  for (int ib = 0; ib < d->nBorders; ++ib) {
+    const rfgpu_border_t &b = d->borders[ib];
+    if (b.nCellsSend < 0 || b.nCellsRecv < 0 || (b.nCellsSend > 0 && !b.icgSend) ||
+        (b.nCellsRecv > 0 && !b.icgRecv) || b.iBorder < 1)
+      return RFGPU_ERR_ARG;
+    for (int k = 0; k < b.nCellsSend; ++k)  // actual cells
+      if (b.icgSend[k] < 1 || b.icgSend[k] > d->nCells) return RFGPU_ERR_ARG;
+    for (int k = 0; k < b.nCellsRecv; ++k)  // virtual cells
+      if (b.icgRecv[k] <= d->nCells || b.icgRecv[k] > N) return RFGPU_ERR_ARG;
+  }
   for (int f = 0; f < d->nFaces; ++f)
     for (int k = 0; k < 2; ++k) {
       int c = d->f2c[(long long)f * d->f2cLd + k];
@@ -330,7 +357,8 @@ unsigned long long spread3(unsigned long long v) {
 // higher one (a counting sort on the lower cell, short runs sorted in place).
 Order locality_order(const rfgpu_region_desc_t *d) {
   Order o;
-  const int N = d->nCells, F = d->nFaces;
+  const int N = d->nCellsTot > 0 ? d->nCellsTot : d->nCells, F = d->nFaces;
+  const int nAct = d->nCells;
   double lo[3], hi[3];
   for (int k = 0; k < 3; ++k) lo[k] = hi[k] = d->cofg[k];
   for (int c = 0; c < N; ++c)
@@ -351,6 +379,8 @@ Order locality_order(const rfgpu_region_desc_t *d) {
       q = q < 0.0 ? 0.0 : (q > 2097151.0 ? 2097151.0 : q);
       m |= spread3((unsigned long long)q) << k;
     }
+    // virtual cells after the actual ones (bit 63 is above the 63-bit key)
+    if (c >= nAct) m |= 1ull << 63;
     key[c] = m;
     idx[c] = c;
   }
@@ -414,9 +444,10 @@ template <typename R>
 void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &ph, const Order &o) {
   cudaStream_t s = h->stream;
   DevAlloc &M = h->mem;
-  const int N = d->nCells, F = d->nFaces;
+  const int N = d->nCellsTot > 0 ? d->nCellsTot : d->nCells, F = d->nFaces;
   RegionDev<R> g{};
   g.nCells = N;
+  g.nAct = d->nCells;
   g.nFaces = F;
   g.ph = ph;
   // ---- cells
@@ -622,6 +653,21 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.cellNew = M.upload(o.cNew, s);
     g.cellOld = M.upload(o.cOld, s);
   }
+  // ---- borders (device numbering)
+  size_t maxB = 0;
+  h->borders.resize(d->nBorders);
+  for (int ib = 0; ib < d->nBorders; ++ib) {
+    const rfgpu_border_t &b = d->borders[ib];
+    BorderH &bh = h->borders[ib];
+    bh.iRegionGlobal = b.iRegionGlobal;
+    bh.iBorder = b.iBorder;
+    for (int k = 0; k < b.nCellsSend; ++k) bh.send.push_back(o.nc(b.icgSend[k] - 1));
+    for (int k = 0; k < b.nCellsRecv; ++k) bh.recv.push_back(o.nc(b.icgRecv[k] - 1));
+    bh.dSend = M.upload(bh.send, s);
+    bh.dRecv = M.upload(bh.recv, s);
+    maxB = std::max(maxB, std::max(bh.send.size(), bh.recv.size()));
+  }
+  if (d->nBorders > 0) h->bbuf = M.alloc<double>(5 * maxB);
   h->cellNew = g.cellNew;
   h->cellOld = g.cellOld;
   h->nBFaces = B;
@@ -703,7 +749,11 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   rfgpu_region_s *h = new (std::nothrow) rfgpu_region_s();
   if (!h) return RFGPU_ERR_NOMEM;
   h->prec = d->precision;
-  h->nCells = d->nCells;
+  h->nCells = d->nCellsTot > 0 ? d->nCellsTot : d->nCells;
+  h->nAct = d->nCells;
+  h->iRegionGlobal = d->iRegionGlobal;
+  h->gvCp = d->gvCp;
+  h->gvMol = d->gvMol;
   h->nFaces = d->nFaces;
   h->rkScheme = d->rkScheme;
   h->spaceOrder = d->spaceOrder;
@@ -786,6 +836,8 @@ int rfgpu_region_destroy(rfgpu_region_t h) {
   if (!h) return RFGPU_ERR_ARG;
   cudaStreamSynchronize(h->stream);
   if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->evA) cudaEventDestroy(h->evA);
+  if (h->evB) cudaEventDestroy(h->evB);
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
   h->prof.destroy();
@@ -815,6 +867,7 @@ int rfgpu_dt(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit,
 
 int rfgpu_step(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit, double endTime) {
   if (!h) return RFGPU_ERR_ARG;
+  if (!h->borders.empty()) return RFGPU_ERR_UNSUPPORTED;  // needs its neighbours between stages
   step_launch(h, cfl, dtImposed, dtMinLimit, endTime);
   return cuda_rc(cudaGetLastError());
 }
@@ -822,6 +875,7 @@ int rfgpu_step(rfgpu_region_t h, double cfl, double dtImposed, double dtMinLimit
 int rfgpu_steps_graph(rfgpu_region_t h, int nSteps, double cfl, double dtImposed,
                       double dtMinLimit, double endTime) {
   if (!h || nSteps < 0) return RFGPU_ERR_ARG;
+  if (!h->borders.empty()) return RFGPU_ERR_UNSUPPORTED;
   double key[4] = {cfl, dtImposed, dtMinLimit, endTime};
   if (!h->graph || std::memcmp(key, h->gkey, sizeof(key)) != 0) {
     if (h->graph) {
@@ -971,14 +1025,116 @@ int rfgpu_set_tuning(rfgpu_region_t h, int gridCap, int unused) {
   return RFGPU_OK;
 }
 
+// ---- borders --------------------------------------------------------------------
+
+int rfgpu_border_copy(rfgpu_region_t src, int iBorder, rfgpu_region_t dst) {
+  if (!src || !dst || src == dst || src->prec != dst->prec || iBorder < 1 ||
+      iBorder > (int)src->borders.size())
+    return RFGPU_ERR_ARG;
+  const BorderH &b = src->borders[iBorder - 1];
+  if (b.iRegionGlobal != dst->iRegionGlobal || b.iBorder > (int)dst->borders.size())
+    return RFGPU_ERR_ARG;
+  const BorderH &b2 = dst->borders[b.iBorder - 1];
+  if (b2.iRegionGlobal != src->iRegionGlobal || b2.recv.size() != b.send.size())
+    return RFGPU_ERR_ARG;
+  if (src->gvCp != dst->gvCp || src->gvMol != dst->gvMol) return RFGPU_ERR_UNSUPPORTED;
+  if (!src->evA && cudaEventCreateWithFlags(&src->evA, cudaEventDisableTiming) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  if (!dst->evB && cudaEventCreateWithFlags(&dst->evB, cudaEventDisableTiming) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  // dst waits for src's queued work (the state it reads), src's later work
+  // waits for the copy (the state it will overwrite)
+  if (cudaEventRecord(src->evA, src->stream) != cudaSuccess ||
+      cudaStreamWaitEvent(dst->stream, src->evA, 0) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  if (src->prec)
+    launch_halo_pair<float>(regs_of<float>(src), regs_of<float>(dst), b.dSend, b2.dRecv,
+                            (int)b.send.size(), dst->stream);
+  else
+    launch_halo_pair<double>(regs_of<double>(src), regs_of<double>(dst), b.dSend, b2.dRecv,
+                             (int)b.send.size(), dst->stream);
+  if (!b.send.empty()) dst->launches++;
+  if (cudaGetLastError() != cudaSuccess || cudaEventRecord(dst->evB, dst->stream) != cudaSuccess ||
+      cudaStreamWaitEvent(src->stream, dst->evB, 0) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return RFGPU_OK;
+}
+
+int rfgpu_border_pack(rfgpu_region_t h, int iBorder, double *sendBuff) {
+  if (!h || !sendBuff || iBorder < 1 || iBorder > (int)h->borders.size()) return RFGPU_ERR_ARG;
+  const BorderH &b = h->borders[iBorder - 1];
+  const int n = (int)b.send.size();
+  if (n == 0) return RFGPU_OK;
+  if (h->prec)
+    launch_border_pack<float>(regs_of<float>(h), b.dSend, n, h->bbuf, h->stream);
+  else
+    launch_border_pack<double>(regs_of<double>(h), b.dSend, n, h->bbuf, h->stream);
+  h->launches++;
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(sendBuff, h->bbuf, 5 * (size_t)n * 8, cudaMemcpyDefault, h->stream) !=
+          cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_border_unpack(rfgpu_region_t h, int iBorder, const double *recvBuff) {
+  if (!h || !recvBuff || iBorder < 1 || iBorder > (int)h->borders.size()) return RFGPU_ERR_ARG;
+  const BorderH &b = h->borders[iBorder - 1];
+  const int n = (int)b.recv.size();
+  if (n == 0) return RFGPU_OK;
+  if (cudaMemcpyAsync(h->bbuf, recvBuff, 5 * (size_t)n * 8, cudaMemcpyDefault, h->stream) !=
+      cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  if (h->prec)
+    launch_border_unpack<float>(regs_of<float>(h), b.dRecv, n, h->bbuf, h->stream);
+  else
+    launch_border_unpack<double>(regs_of<double>(h), b.dRecv, n, h->bbuf, h->stream);
+  h->launches++;
+  if (cudaGetLastError() != cudaSuccess) return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
 // ---- batches ------------------------------------------------------------------
 
 int rfgpu_batch_create(rfgpu_region_t *regions, int n, rfgpu_batch_t *out) {
-  if (!regions || n <= 0 || !out) return RFGPU_ERR_ARG;
+  return rfgpu_batch_create_ex(regions, n, 0, out);
+}
+
+int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch_t *out) {
+  if (!regions || n <= 0 || !out || (flags & ~RFGPU_BATCH_COUPLED)) return RFGPU_ERR_ARG;
   *out = nullptr;
   int prec = regions[0] ? regions[0]->prec : -1;
   for (int i = 0; i < n; ++i)
     if (!regions[i] || regions[i]->prec != prec) return RFGPU_ERR_ARG;
+  const bool coupled = (flags & RFGPU_BATCH_COUPLED) != 0;
+  // halo links: every border's send cells go to the receive cells of the
+  // neighbour's matching border (RFLU_MPI_CopyWrapper's pairing)
+  std::vector<HaloLink> links;
+  if (coupled) {
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < i; ++j)
+        if (regions[i]->iRegionGlobal == regions[j]->iRegionGlobal || regions[i] == regions[j])
+          return RFGPU_ERR_ARG;
+    for (int i = 0; i < n; ++i) {
+      const rfgpu_region_s *a = regions[i];
+      if (a->gvCp != regions[0]->gvCp || a->gvMol != regions[0]->gvMol)
+        return RFGPU_ERR_UNSUPPORTED;
+      for (const BorderH &b : a->borders) {
+        int j = -1;
+        for (int k = 0; k < n; ++k)
+          if (regions[k]->iRegionGlobal == b.iRegionGlobal) j = k;
+        if (j < 0 || b.iBorder > (int)regions[j]->borders.size()) return RFGPU_ERR_ARG;
+        const BorderH &b2 = regions[j]->borders[b.iBorder - 1];
+        if (b2.iRegionGlobal != a->iRegionGlobal || b2.recv.size() != b.send.size())
+          return RFGPU_ERR_ARG;
+        for (size_t k = 0; k < b.send.size(); ++k)
+          links.push_back(HaloLink{i, b.send[k], j, b2.recv[k]});
+      }
+    }
+  } else {
+    for (int i = 0; i < n; ++i)
+      if (!regions[i]->borders.empty()) return RFGPU_ERR_UNSUPPORTED;
+  }
   rfgpu_batch_s *b = new (std::nothrow) rfgpu_batch_s();
   if (!b) return RFGPU_ERR_NOMEM;
   b->prec = prec;
@@ -1016,6 +1172,11 @@ int rfgpu_batch_create(rfgpu_region_t *regions, int n, rfgpu_batch_t *out) {
     for (int i = 0; i < n; ++i) maxW = std::max(maxW, regions[i]->maxStW);
     b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n,
                    maxW};
+    if (coupled) {
+      b->work.coupled = 1;
+      b->work.halo = links.empty() ? nullptr : b->mem.upload(links, b->stream);
+      b->work.nHalo = (int)links.size();
+    }
     if (prec) {
       std::vector<RegionDev<float>> v;
       for (int i = 0; i < n; ++i) v.push_back(regions[i]->rd32);

@@ -56,7 +56,10 @@ struct Phys {
 
 template <typename R>
 struct RegionDev {
-  int nCells, nFaces, nBFaces, pad_;
+  // nCells: all cells of the region, actual then virtual (the extent and
+  // stride of every per-cell array); nAct: the actual cells, the ones the
+  // update, the checks and the time step cover
+  int nCells, nFaces, nBFaces, nAct;
   // state.  FP64 path: SoA cv, dv, rhsSum.  The mixed path advances its state
   // as float-float pairs, cvF[2][5][N] (hi rows, then lo rows; the pair's sum
   // carries about 48 significand bits) with the RK increment history in FP32
@@ -120,6 +123,12 @@ struct Tile {
   int first;
 };
 
+// One received virtual cell of a coupled batch: the state of cell srcCell of
+// region srcRegion goes to cell dstCell of region dstRegion (device numbering).
+struct HaloLink {
+  int srcRegion, srcCell, dstRegion, dstCell;
+};
+
 struct Work {
   const Tile *cellTiles, *faceTiles, *bfaceTiles;
   int nCellTiles, nFaceTiles, nBFaceTiles;
@@ -127,6 +136,11 @@ struct Work {
   int block;    // items per tile == threads per block
   int nRegions;
   int maxStW;   // widest stencil SELL slice over the regions (shared-memory staging)
+  // coupled batches: one time step for all regions, and the halo exchange
+  // after every stage's update
+  int coupled;
+  const HaloLink *halo;
+  int nHalo;
 };
 
 struct DtArgs {
@@ -149,7 +163,7 @@ struct StepArgs {
 
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
-       KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_COUNT };
+       KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_HALO, KP_COUNT };
 // KP_GRADIENT times the fused gradient + limiter kernel; KP_LIMITER, KP_DT_FACE
 // and KP_DT_BFACE are no longer launched separately (kept for the ABI's
 // class numbering).
@@ -176,6 +190,23 @@ void launch_download_direct(const RegionDev<R> *regs, const Work &w, double *cvH
                             cudaStream_t s);
 template <typename R>
 int configure_grad_smem(int maxW, int block);
+// Halo exchange: the links of a coupled batch (regs indexed by region), or
+// one border between two handles (send cells of src -> receive cells of dst,
+// device numbering).  Copies the conserved state and rebuilds the received
+// cells' dependent variables and records.
+template <typename R>
+void launch_halo(const RegionDev<R> *regs, const HaloLink *links, int n, cudaStream_t s);
+template <typename R>
+void launch_halo_pair(const RegionDev<R> *src, const RegionDev<R> *dst, const int *srcCells,
+                      const int *dstCells, int n, cudaStream_t s);
+// Border buffers in the Fortran layout buf(5,n): pack cv(:,cells) / unpack
+// into cv(:,cells) with the dependent variables and records of those cells.
+template <typename R>
+void launch_border_pack(const RegionDev<R> *g, const int *cells, int n, double *buf,
+                        cudaStream_t s);
+template <typename R>
+void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const double *buf,
+                          cudaStream_t s);
 // Residual with the face fluxes and the result in caller-supplied scratch
 // (used by rfgpu_residual_noalloc): rhs in the Fortran layout rhs(5,nCells), host numbering.
 template <typename R>

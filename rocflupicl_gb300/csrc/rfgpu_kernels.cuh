@@ -466,9 +466,83 @@ __device__ __forceinline__ void prefetch_ahead(int t, int nTiles, int dist, PF p
 #define RF_TILE_LOOP(tiles, nTiles)                                   \
   for (int t_ = blockIdx.x; t_ < (nTiles); t_ += gridDim.x)
 
-// Cons2Prim (modflu/RFLU_ModConvertCv.F90:221-231) of the uploaded state, and
-// optionally the EOS first (libflu/RFLU_SetDependentVars.F90:256-287).  The
-// record's centroid slots are kept.
+// Cons2Prim (modflu/RFLU_ModConvertCv.F90:221-231) of one cell's FP64 state
+// into its record, and optionally the EOS first (libflu/RFLU_SetDependentVars.F90:
+// 256-287).  The record's centroid slots are kept.  FP64 path.
+template <typename R>
+__device__ __forceinline__ void set_vars_cell(const RegionDev<R> &g, int c, int computeDv) {
+  const int N = g.nCells;
+  double q0 = g.cv[c], q1 = g.cv[N + c], q2 = g.cv[2 * N + c], q3 = g.cv[3 * N + c],
+         q4 = g.cv[4 * N + c];
+  double ir = 1.0 / q0;
+  if (computeDv) {
+    double gc = g.ph.gvR, gg = g.ph.gvG;
+    double Eo = ir * q4;
+    double Vm2 = ir * ir * (q1 * q1 + q2 * q2 + q3 * q3);
+    double p = (gg - 1.0) * q0 * (Eo - 0.5 * Vm2 - 0.0);
+    double T = p / (q0 * gc);
+    g.dv[c] = p;
+    g.dv[N + c] = T;
+    g.dv[2 * N + c] = sqrt(gg * gc * T);
+  }
+  R r[8];
+  ld8_rw(g.rec + 8 * (size_t)c, r);
+  r[0] = R(q0);
+  r[1] = R(ir * q1);
+  r[2] = R(ir * q2);
+  r[3] = R(ir * q3);
+  r[4] = R(g.dv[c]);
+  st8(g.rec + 8 * (size_t)c, r);
+}
+
+// Mixed path: a cell's state from an FP64 conserved vector (upload, border
+// receive): float-float split and the record, with p from dv when given, else
+// from the FP64 EOS.
+__device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c, const double q[5],
+                                                const double *pGiven) {
+  const int N = g.nCells;
+  const double ir = 1.0 / q[0];
+  double p;
+  if (pGiven) {
+    p = *pGiven;
+  } else {
+    const double gg = g.ph.gvG;
+    const double Eo = ir * q[4];
+    const double Vm2 = ir * ir * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+    p = (gg - 1.0) * q[0] * (Eo - 0.5 * Vm2 - 0.0);
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const float hi = (float)q[j];
+    g.cvF[(size_t)j * N + c] = hi;
+    g.cvF[(size_t)(5 + j) * N + c] = (float)(q[j] - (double)hi);
+  }
+  float r[8];
+  ld8_rw(g.rec + 8 * (size_t)c, r);
+  r[0] = float(q[0]);
+  r[1] = float(ir * q[1]);
+  r[2] = float(ir * q[2]);
+  r[3] = float(ir * q[3]);
+  r[4] = float(p);
+  st8(g.rec + 8 * (size_t)c, r);
+}
+
+// Conserved state of a cell as FP64 (the float-float pair joined on the
+// mixed path).
+template <typename R>
+__device__ __forceinline__ void cons_fp64(const RegionDev<R> &g, int c, double q[5]) {
+  const int N = g.nCells;
+  if constexpr (sizeof(R) == 4) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+  } else {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = g.cv[(size_t)j * N + c];
+  }
+}
+
+// Uploaded state -> records (and dv).
 template <typename R>
 __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
                        int nTiles, int computeDv) {
@@ -476,29 +550,86 @@ __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__rest
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
-    const int N = g.nCells;
-    if (c >= N) continue;
-    double q0 = g.cv[c], q1 = g.cv[N + c], q2 = g.cv[2 * N + c], q3 = g.cv[3 * N + c],
-           q4 = g.cv[4 * N + c];
-    double ir = 1.0 / q0;
-    if (computeDv) {
-      double gc = g.ph.gvR, gg = g.ph.gvG;
-      double Eo = ir * q4;
-      double Vm2 = ir * ir * (q1 * q1 + q2 * q2 + q3 * q3);
-      double p = (gg - 1.0) * q0 * (Eo - 0.5 * Vm2 - 0.0);
-      double T = p / (q0 * gc);
-      g.dv[c] = p;
-      g.dv[N + c] = T;
-      g.dv[2 * N + c] = sqrt(gg * gc * T);
-    }
-    R r[8];
-    ld8_rw(g.rec + 8 * (size_t)c, r);
-    r[0] = R(q0);
-    r[1] = R(ir * q1);
-    r[2] = R(ir * q2);
-    r[3] = R(ir * q3);
-    r[4] = R(g.dv[c]);
-    st8(g.rec + 8 * (size_t)c, r);
+    if (c >= g.nCells) continue;
+    set_vars_cell(g, c, computeDv);
+  }
+}
+
+// ---- halo exchange ---------------------------------------------------------------
+// One received virtual cell: RFLU_MPI_CopyCellData (modflu/RFLU_ModMPI.F90:
+// 332-390) of cv, then RFLU_SetVarsContWrapper of the cell
+// (libfloflu/RungeKuttaMP.F90:381-396): FP64 path, dv and the record rebuilt
+// from the copied cv with the EOS every cell uses; mixed path, the
+// float-float pair and the sender's record slots copied (the record is a
+// function of the pair and of the gas constants, which coupled regions share).
+template <typename R>
+__device__ __forceinline__ void halo_cell(const RegionDev<R> &gs, int cs, const RegionDev<R> &gd,
+                                          int cd) {
+  const int Ns = gs.nCells, Nd = gd.nCells;
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = gs.cv[(size_t)j * Ns + cs];
+    set_vars_cell(gd, cd, 1);
+  } else {
+#pragma unroll
+    for (int j = 0; j < 10; ++j) gd.cvF[(size_t)j * Nd + cd] = gs.cvF[(size_t)j * Ns + cs];
+    R a[8], b[8];
+    ld8_rw(gs.rec + 8 * (size_t)cs, a);
+    ld8_rw(gd.rec + 8 * (size_t)cd, b);
+#pragma unroll
+    for (int k = 0; k < 5; ++k) b[k] = a[k];
+    st8(gd.rec + 8 * (size_t)cd, b);
+  }
+}
+
+template <typename R>
+__global__ void k_halo(const RegionDev<R> *__restrict__ regs, const HaloLink *__restrict__ links,
+                       int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const HaloLink l = links[i];
+  halo_cell(regs[l.srcRegion], l.srcCell, regs[l.dstRegion], l.dstCell);
+}
+
+template <typename R>
+__global__ void k_halo_pair(const RegionDev<R> *__restrict__ src, const RegionDev<R> *__restrict__ dst,
+                            const int *__restrict__ srcCells, const int *__restrict__ dstCells,
+                            int n) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  halo_cell(*src, srcCells[i], *dst, dstCells[i]);
+}
+
+// sendBuff(5,n) = cv(:,cells) (RFLU_MPI_ISendWrapper's packing)
+template <typename R>
+__global__ void k_border_pack(const RegionDev<R> *__restrict__ gp, const int *__restrict__ cells,
+                              int n, double *__restrict__ buf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double q[5];
+  cons_fp64(*gp, cells[i], q);
+#pragma unroll
+  for (int j = 0; j < 5; ++j) buf[5 * (size_t)i + j] = q[j];
+}
+
+// cv(:,cells) = recvBuff(5,n), then the cells' dv and records
+// (RFLU_MPI_RecvWrapper + RFLU_SetVarsContWrapper(nCells+1,nCellsTot))
+template <typename R>
+__global__ void k_border_unpack(const RegionDev<R> *__restrict__ gp, const int *__restrict__ cells,
+                                int n, const double *__restrict__ buf) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const RegionDev<R> &g = *gp;
+  const int c = cells[i];
+  double q[5];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) q[j] = buf[5 * (size_t)i + j];
+  if constexpr (sizeof(R) == 8) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) g.cv[(size_t)j * g.nCells + c] = q[j];
+    set_vars_cell(g, c, 1);
+  } else {
+    state_from_fp64(g, c, q, nullptr);
   }
 }
 
@@ -738,7 +869,10 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
       for (int k = 0; k < 15; ++k) out[k] = acc[k];
       out[15] = R(0);
       st16(g.grad + 16 * (size_t)c, out);
-      if constexpr (fuseDt) dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
+      if constexpr (fuseDt) {
+        dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
+        if (c >= regs[tl.region].nAct) dtbits = 0x7FF0000000000000ull;  // actual cells only
+      }
     }
     if constexpr (fuseDt) dt_block_min<R>(dtbits, smin, g.dtBits);
   }
@@ -1364,6 +1498,13 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
     if (c >= N) continue;
+    if (c >= g.nAct) {  // virtual cell: ZeroDummyCellsMP, no update
+      if (a.writeRhs) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = 0.0;
+      }
+      continue;
+    }
     if constexpr (sizeof(R) == 4) {
       gather_update_mixed(g, c, a);
       continue;
@@ -1495,30 +1636,7 @@ __global__ void k_upload_direct(const RegionDev<R> *__restrict__ regs, const Til
     double q[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) q[j] = cvH[5 * (size_t)i + j];
-    const double ir = 1.0 / q[0];
-    double p;
-    if (dvH) {
-      p = dvH[3 * (size_t)i];
-    } else {
-      const double gg = g.ph.gvG;
-      const double Eo = ir * q[4];
-      const double Vm2 = ir * ir * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-      p = (gg - 1.0) * q[0] * (Eo - 0.5 * Vm2 - 0.0);
-    }
-#pragma unroll
-    for (int j = 0; j < 5; ++j) {
-      const float hi = (float)q[j];
-      g.cvF[(size_t)j * N + c] = hi;
-      g.cvF[(size_t)(5 + j) * N + c] = (float)(q[j] - (double)hi);
-    }
-    R r[8];
-    ld8_rw(g.rec + 8 * (size_t)c, r);
-    r[0] = R(q[0]);
-    r[1] = R(ir * q[1]);
-    r[2] = R(ir * q[2]);
-    r[3] = R(ir * q[3]);
-    r[4] = R(p);
-    st8(g.rec + 8 * (size_t)c, r);
+    if constexpr (sizeof(R) == 4) state_from_fp64(g, c, q, dvH ? dvH + 3 * (size_t)i : nullptr);
   }
 }
 
@@ -1565,7 +1683,7 @@ __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict_
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
     unsigned long long bits = 0x7FF0000000000000ull;  // +inf
-    if (c < g.nCells) {
+    if (c < g.nAct) {
       R r0[8];
       ld8(g.rec + 8 * (size_t)c, r0);
       bits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
@@ -1575,14 +1693,12 @@ __global__ void __launch_bounds__(128) k_dt_cell(const RegionDev<R> *__restrict_
 }
 
 // RFLU_MinimumTimeStep (rocflu/RFLU_MinimumTimeStep.F90:131-146,235-241) and the
-// end-time clip of rocflu/RFLU_TimeStepping.F90:490-493; one thread per region.
+// end-time clip of rocflu/RFLU_TimeStepping.F90:490-493 for one region, from
+// the minimum local time step `raw` (bit pattern).
 template <typename R>
-__global__ void k_dt_finalize(const RegionDev<R> *__restrict__ regs, int nRegions, DtArgs a) {
-  int r = blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= nRegions) return;
-  const RegionDev<R> &g = regs[r];
-  double dtMin = __longlong_as_double((long long)*g.dtBits);
-  *g.dtBits = 0x7FF0000000000000ull;
+__device__ __forceinline__ void dt_finalize_region(const RegionDev<R> &g, unsigned long long raw,
+                                                   const DtArgs &a) {
+  double dtMin = __longlong_as_double((long long)raw);
   const double t = a.useDeviceTime ? g.scal[1] : a.timeHost;
   dtMin = a.cfl * dtMin;
   double wI = 0.0, wC = 0.0;
@@ -1604,6 +1720,55 @@ __global__ void k_dt_finalize(const RegionDev<R> *__restrict__ regs, int nRegion
   g.scal[2] = dtMin;
   for (int i = 0; i < 5; ++i) g.scal[3 + i] = g.ph.ark[i] * dtMin;  // fac of RkUpdateGeneric
   if (a.useDeviceTime) g.scal[1] = tNew;
+}
+
+// One thread per independent region.
+template <typename R>
+__global__ void k_dt_finalize(const RegionDev<R> *__restrict__ regs, int nRegions, DtArgs a) {
+  int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nRegions) return;
+  const RegionDev<R> &g = regs[r];
+  const unsigned long long raw = *g.dtBits;
+  *g.dtBits = 0x7FF0000000000000ull;
+  dt_finalize_region(g, raw, a);
+}
+
+// Coupled regions (one block): the minimum over all regions first, as the
+// reference's MIN over local regions and MPI_Allreduce(MPI_MIN)
+// (RFLU_MinimumTimeStep.F90:148-208), then every region finalizes it.  The
+// per-region steps of RFLU_MinimumTimeStep (cfl scaling, imposed/computed
+// weighting, floor, dtMinLimit) are monotone non-decreasing, so applying them
+// to the minimum gives the reference's minimum of the per-region results.
+template <typename R>
+__global__ void k_dt_finalize_coupled(const RegionDev<R> *__restrict__ regs, int nRegions,
+                                      DtArgs a) {
+  __shared__ unsigned long long smin[32];
+  unsigned long long v = 0x7FF0000000000000ull;
+  for (int r = threadIdx.x; r < nRegions; r += blockDim.x) {
+    const unsigned long long x = *regs[r].dtBits;
+    v = x < v ? x : v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_down_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long raw = smin[0];
+  for (int w = 1; w < (int)(blockDim.x >> 5); ++w) raw = smin[w] < raw ? smin[w] : raw;
+  for (int r = threadIdx.x; r < nRegions; r += blockDim.x) {
+    *regs[r].dtBits = 0x7FF0000000000000ull;
+    dt_finalize_region(regs[r], raw, a);
+  }
+}
+
+template <typename R>
+void launch_dt_finalize(const RegionDev<R> *regs, const Work &w, const DtArgs &a,
+                        cudaStream_t s) {
+  if (w.coupled)
+    k_dt_finalize_coupled<R><<<1, 256, 0, s>>>(regs, w.nRegions, a);
+  else
+    launch_dt_finalize<R>(regs, w, a, s);
 }
 
 // ---- launchers ----------------------------------------------------------------
@@ -1648,7 +1813,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   }
   if (a.fuseDt && grad) {
     RF_MARK(KP_DT_FINAL, 0);
-    k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a.dt);
+    launch_dt_finalize<R>(regs, w, a.dt, s);
     RF_MARK(KP_DT_FINAL, 1);
     ++n;
   }
@@ -1671,6 +1836,12 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
     RF_MARK(KP_GATHER_UPDATE, 1);
     ++n;
   }
+  if (w.nHalo > 0 && a.update) {  // coupled regions: virtual cells from their owners
+    RF_MARK(KP_HALO, 0);
+    k_halo<R><<<(w.nHalo + 127) / 128, 128, 0, s>>>(regs, w.halo, w.nHalo);
+    RF_MARK(KP_HALO, 1);
+    ++n;
+  }
   if (launches) *launches += n;
 }
 
@@ -1686,7 +1857,7 @@ void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStr
     ++n;
   }
   RF_MARK(KP_DT_FINAL, 0);
-  k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a);
+  launch_dt_finalize<R>(regs, w, a, s);
   RF_MARK(KP_DT_FINAL, 1);
   ++n;
   if (launches) *launches += n;
@@ -1771,6 +1942,11 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
   const size_t hc = g.cellOld ? (size_t)g.cellOld[c] : (size_t)c;  // host numbering
+  if (c >= g.nAct) {  // virtual cell: ZeroDummyCellsMP
+#pragma unroll
+    for (int j = 0; j < 5; ++j) rhs[5 * hc + j] = 0.0;
+    return;
+  }
   if constexpr (sizeof(R) == 8) {
     double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
     for (int k = 0; k < n; ++k) {
@@ -1827,6 +2003,26 @@ void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, co
   k_gather_rhs_scratch<R><<<(g.nCells + 127) / 128, 128, 0, s>>>(g, flux, rhs);
 }
 
+template <typename R>
+void launch_halo(const RegionDev<R> *regs, const HaloLink *links, int n, cudaStream_t s) {
+  if (n > 0) k_halo<R><<<(n + 127) / 128, 128, 0, s>>>(regs, links, n);
+}
+template <typename R>
+void launch_halo_pair(const RegionDev<R> *src, const RegionDev<R> *dst, const int *srcCells,
+                      const int *dstCells, int n, cudaStream_t s) {
+  if (n > 0) k_halo_pair<R><<<(n + 127) / 128, 128, 0, s>>>(src, dst, srcCells, dstCells, n);
+}
+template <typename R>
+void launch_border_pack(const RegionDev<R> *g, const int *cells, int n, double *buf,
+                        cudaStream_t s) {
+  if (n > 0) k_border_pack<R><<<(n + 127) / 128, 128, 0, s>>>(g, cells, n, buf);
+}
+template <typename R>
+void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const double *buf,
+                          cudaStream_t s) {
+  if (n > 0) k_border_unpack<R><<<(n + 127) / 128, 128, 0, s>>>(g, cells, n, buf);
+}
+
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
   template void launch_upload_direct<R>(const RegionDev<R> *, const Work &, const double *,   \
@@ -1841,6 +2037,13 @@ void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, co
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
                              long long *, const Prof *);                                      \
   template void launch_step<R>(const RegionDev<R> *, const Work &, const DtArgs &, int,       \
-                               cudaStream_t, long long *, int, int, const Prof *);
+                               cudaStream_t, long long *, int, int, const Prof *);            \
+  template void launch_halo<R>(const RegionDev<R> *, const HaloLink *, int, cudaStream_t);    \
+  template void launch_halo_pair<R>(const RegionDev<R> *, const RegionDev<R> *, const int *,  \
+                                    const int *, int, cudaStream_t);                          \
+  template void launch_border_pack<R>(const RegionDev<R> *, const int *, int, double *,       \
+                                      cudaStream_t);                                          \
+  template void launch_border_unpack<R>(const RegionDev<R> *, const int *, int,               \
+                                        const double *, cudaStream_t);
 
 }  // namespace rfgpu

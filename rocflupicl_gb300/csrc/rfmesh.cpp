@@ -694,6 +694,49 @@ int rfmesh_set_stencils(rfmesh_t m, const int *offsets, const int *members, cons
   return RFMESH_OK;
 }
 
+int rfmesh_build_stencils(int nCells, int nVerts, const int *cellVerts, const int *cellNVerts,
+                          const int *v2cOffsets, const int *v2c, const double *cofg, int nThreads,
+                          int *c2csOffsets, int *c2csMembers, double *xyzMoms) {
+  if (nCells <= 0 || nVerts <= 0 || !cellVerts || !cellNVerts || !v2cOffsets || !v2c || !cofg ||
+      !c2csOffsets || !c2csMembers || !xyzMoms)
+    return RFMESH_ERR_ARG;
+  for (long long c = 0; c < nCells; ++c) {
+    if (cellNVerts[c] < 4 || cellNVerts[c] > 8) return RFMESH_ERR_ARG;
+    for (int a = 0; a < cellNVerts[c]; ++a)
+      if (cellVerts[8 * c + a] < 0 || cellVerts[8 * c + a] >= nVerts) return RFMESH_ERR_ARG;
+  }
+  if (v2cOffsets[0] != 0) return RFMESH_ERR_ARG;
+  for (long long v = 0; v < nVerts; ++v)
+    if (v2cOffsets[v + 1] < v2cOffsets[v]) return RFMESH_ERR_ARG;
+  for (long long e = 0; e < v2cOffsets[nVerts]; ++e)
+    if (v2c[e] < 0 || v2c[e] >= nCells) return RFMESH_ERR_ARG;
+  const rfm::CellView view{cofg, cellVerts, cellNVerts, v2cOffsets, v2c};
+  std::vector<int> cnt(nCells, 0), memb((size_t)nCells * rfm::kStencilMax);
+  int overflow = 0;
+  int saved = omp_get_max_threads();
+  if (nThreads > 0) omp_set_num_threads(nThreads);
+#pragma omp parallel reduction(| : overflow)
+  {
+    rfm::Scratch w;
+#pragma omp for schedule(dynamic, 1024)
+    for (long long icg = 0; icg < nCells; ++icg) {
+      const int degr = rfm::cell_stencil(view, (int)icg, &memb[(size_t)icg * rfm::kStencilMax],
+                                         &xyzMoms[10 * (size_t)icg], w);
+      if (degr < 0) overflow = 1;
+      cnt[icg] = degr < 0 ? 0 : degr;
+    }
+  }
+  omp_set_num_threads(saved);
+  if (overflow) return RFMESH_ERR_GEOM;
+  c2csOffsets[0] = 0;
+  for (long long c = 0; c < nCells; ++c) {
+    c2csOffsets[c + 1] = c2csOffsets[c] + cnt[c];
+    for (int k = 0; k < cnt[c]; ++k)
+      c2csMembers[c2csOffsets[c] + k] = memb[(size_t)c * rfm::kStencilMax + k] + 1;
+  }
+  return RFMESH_OK;
+}
+
 const int *rfmesh_bf2c(rfmesh_t m, int ip) {
   return (m && ip >= 0 && ip < (int)m->patch.size()) ? m->patch[ip].bf2c1.data() : nullptr;
 }

@@ -44,6 +44,12 @@ class PatchT(C.Structure):
                 ("bcOptFixed", C.c_int)]
 
 
+class BorderT(C.Structure):
+    _fields_ = [("iRegionGlobal", C.c_int), ("iBorder", C.c_int), ("nCellsSend", C.c_int),
+                ("icgSend", C.POINTER(C.c_int)), ("nCellsRecv", C.c_int),
+                ("icgRecv", C.POINTER(C.c_int))]
+
+
 class RegionDescT(C.Structure):
     _fields_ = [("nCells", C.c_int), ("nFaces", C.c_int), ("f2cLd", C.c_int),
                 ("f2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
@@ -58,7 +64,9 @@ class RegionDescT(C.Structure):
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
                 ("dissFact", C.c_double), ("precision", C.c_int), ("venkatGuard", C.c_int),
                 ("cellOrder", C.c_int), ("ausmSigma", C.c_double), ("ausmKp", C.c_double),
-                ("ausmKu", C.c_double), ("ausmMInf", C.c_double)]
+                ("ausmKu", C.c_double), ("ausmMInf", C.c_double), ("nCellsTot", C.c_int),
+                ("iRegionGlobal", C.c_int), ("nBorders", C.c_int),
+                ("borders", C.POINTER(BorderT))]
 
 
 # device numbering of cells and faces (rfgpu.h RFGPU_ORDER_*)
@@ -76,10 +84,13 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
            "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
-           "rfgpu_mesh_stencils"]
+           "rfgpu_mesh_stencils", "rfgpu_border_copy", "rfgpu_border_pack",
+           "rfgpu_border_unpack", "rfgpu_batch_create_ex"]
+
+BATCH_COUPLED = 1
 
 KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
-           "dt_bface", "dt_cell", "dt_finalize"]
+           "dt_bface", "dt_cell", "dt_finalize", "halo"]
 
 _lib = None
 
@@ -133,6 +144,10 @@ def load(path: Optional[str] = None):
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
         "rfgpu_batch_set_tuning": ([vp, C.c_int], C.c_int),
         "rfgpu_mesh_stencils": ([C.c_int, C.c_int, ip, ip, ip, ip, dp, ip, ip, dp], C.c_int),
+        "rfgpu_border_copy": ([vp, C.c_int, vp], C.c_int),
+        "rfgpu_border_pack": ([vp, C.c_int, dp], C.c_int),
+        "rfgpu_border_unpack": ([vp, C.c_int, dp], C.c_int),
+        "rfgpu_batch_create_ex": ([C.POINTER(vp), C.c_int, C.c_int, C.POINTER(vp)], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -228,7 +243,8 @@ class Region:
         m, num = case.mesh, case.numerics
         self.case = case
         self.num = num
-        self.nCells = m.nCells
+        self.nCells = m.nTot          # rows of every per-cell array crossing the ABI
+        self.nAct = m.nCells
         self.precision = num.precision if precision is None else precision
         keep = []
 
@@ -274,6 +290,18 @@ class Region:
         d.cellOrder = cell_order
         d.ausmSigma, d.ausmKp, d.ausmKu, d.ausmMInf = (
             num.ausmSigma, num.ausmKp, num.ausmKu, num.ausmMInf)
+        d.nCellsTot = m.nCellsTot
+        d.iRegionGlobal = m.iRegionGlobal
+        barr = (BorderT * max(1, len(m.borders)))()
+        for i, b in enumerate(m.borders):
+            B = barr[i]
+            B.iRegionGlobal, B.iBorder = b.iRegionGlobal, b.iBorder
+            B.nCellsSend, B.icgSend = len(b.icgSend), _ip(k(b.icgSend, np.int32))
+            B.nCellsRecv, B.icgRecv = len(b.icgRecv), _ip(k(b.icgRecv, np.int32))
+        d.nBorders = len(m.borders)
+        d.borders = barr
+        self.borders = m.borders
+        self.iRegionGlobal = m.iRegionGlobal
         h = C.c_void_p()
         _check(self.lib.rfgpu_region_create(C.byref(d), C.byref(h)), "rfgpu_region_create")
         self.h = h
@@ -347,6 +375,23 @@ class Region:
         g = np.empty((self.nCells, 5, 3))
         _check(self.lib.rfgpu_download_grad(self.h, _dp(g)), "rfgpu_download_grad")
         return g
+
+    # --- halo exchange (RFLU_MPI_CopyWrapper / ISendWrapper / RecvWrapper) -----
+    def border_copy(self, i_border: int, dst: "Region"):
+        """cv of this region's border i_border (1-based) send cells into the
+        receive cells of the matching border of dst, with their dv."""
+        _check(self.lib.rfgpu_border_copy(self.h, i_border, dst.h), "rfgpu_border_copy")
+
+    def border_pack(self, i_border: int) -> np.ndarray:
+        """sendBuff(5,nCellsSend) of border i_border as (nCellsSend, 5)."""
+        buf = np.empty((len(self.borders[i_border - 1].icgSend), 5))
+        _check(self.lib.rfgpu_border_pack(self.h, i_border, _dp(buf)), "rfgpu_border_pack")
+        return buf
+
+    def border_unpack(self, i_border: int, buf: np.ndarray):
+        """cv of border i_border's receive cells from recvBuff (nCellsRecv, 5)."""
+        buf = np.ascontiguousarray(buf, np.float64)
+        _check(self.lib.rfgpu_border_unpack(self.h, i_border, _dp(buf)), "rfgpu_border_unpack")
 
     def time(self):
         t, dt = C.c_double(), C.c_double()
@@ -435,12 +480,16 @@ class Region:
 class Batch:
     """Many regions advanced together: one launch per pass over all regions."""
 
-    def __init__(self, regions: Sequence[Region]):
+    def __init__(self, regions: Sequence[Region], coupled: bool = False):
+        """coupled=True: the regions of one partitioned case (one time step, the
+        minimum over them, and the halo exchange after every stage)."""
         self.lib = load()
         self.regions = list(regions)
         arr = (C.c_void_p * len(self.regions))(*[r.h for r in self.regions])
         h = C.c_void_p()
-        _check(self.lib.rfgpu_batch_create(arr, len(self.regions), C.byref(h)), "rfgpu_batch_create")
+        _check(self.lib.rfgpu_batch_create_ex(arr, len(self.regions),
+                                              BATCH_COUPLED if coupled else 0, C.byref(h)),
+               "rfgpu_batch_create_ex")
         self.h = h
 
     def step(self, cfl, dtImposed, dtMinLimit=0.0, endTime=0.0):

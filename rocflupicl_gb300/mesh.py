@@ -43,6 +43,10 @@ def _load():
         lib.rfmesh_cofg_view.restype = C.POINTER(C.c_double)
         lib.rfmesh_set_stencils.argtypes = [vp, C.POINTER(C.c_int), C.POINTER(C.c_int),
                                             C.POINTER(C.c_double)]
+        ip_ = C.POINTER(C.c_int)
+        lib.rfmesh_build_stencils.argtypes = [C.c_int, C.c_int, ip_, ip_, ip_, ip_,
+                                              C.POINTER(C.c_double), C.c_int, ip_, ip_,
+                                              C.POINTER(C.c_double)]
         ipp = C.POINTER(C.POINTER(C.c_int))
         lib.rfmesh_create_grid.argtypes = [C.c_int, C.POINTER(C.c_double),
                                            C.c_int, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_int),
@@ -95,10 +99,23 @@ class Patch:
 
 
 @dataclass
+class Border:
+    """One border of a partitioned region (t_border, modfloflu/ModBorder.F90:87-99):
+    the neighbour's global region id (1-based), the 1-based index of the
+    matching border in the neighbour, the actual cells sent (1-based local)
+    and the virtual cells received (1-based local).  Send cell k here pairs
+    with receive cell k of the matching border."""
+    iRegionGlobal: int
+    iBorder: int
+    icgSend: np.ndarray
+    icgRecv: np.ndarray
+
+
+@dataclass
 class BoxMesh:
     kind: int
     dims: tuple
-    nCells: int
+    nCells: int                 # actual cells
     nFaces: int
     xyz: np.ndarray
     vol: np.ndarray
@@ -114,6 +131,18 @@ class BoxMesh:
     n_of_type: tuple = (0, 0, 0, 0)
     # cell-to-vertex lists per type (tet, hex, prism, pyramid), 1-based, (n, nv)
     conn: List[np.ndarray] = field(default_factory=list)
+    # partitioned regions: actual + virtual cells (0: no virtual cells; the
+    # per-cell arrays vol, cofg, c2cs_off, xyzmoms, cell_type then have
+    # nCellsTot rows), the global region id and the borders
+    nCellsTot: int = 0
+    iRegionGlobal: int = 1
+    borders: List[Border] = field(default_factory=list)
+    # whole-mesh (0-based) ids of a partitioned region's cells, actual then virtual
+    global_cells: Optional[np.ndarray] = None
+
+    @property
+    def nTot(self) -> int:
+        return self.nCellsTot if self.nCellsTot > 0 else self.nCells
 
     @property
     def nBFaces(self) -> int:
@@ -198,6 +227,48 @@ def _extract(lib, h, kind, dims, stencils) -> BoxMesh:
     m.conn = [_copy(lib.rfmesh_cell_conn(h, t), _NV[t] * int(s[5 + t]), np.int32,
                     (int(s[5 + t]), _NV[t])) + 1 for t in range(4)]
     return m
+
+
+def build_stencils(cell_verts, cell_nverts, v2c_off, v2c, cofg, threads: int = 0):
+    """rfmesh_build_stencils: c2c stencils and WLSQ moments of every cell of
+    the given connectivity (0-based cell vertices padded to 8 with -1, vertex
+    counts, vertex-to-cell CSR in ascending cell order, centroids (n,3)) with
+    the host builder.  Returns (offsets (n+1, 0-based), members (1-based),
+    moments (n, 10))."""
+    lib = _load()
+    cv = np.ascontiguousarray(cell_verts, np.int32).reshape(-1)
+    nv = np.ascontiguousarray(cell_nverts, np.int32)
+    vo = np.ascontiguousarray(v2c_off, np.int32)
+    vc = np.ascontiguousarray(v2c, np.int32)
+    cg = np.ascontiguousarray(cofg, np.float64)
+    n = nv.shape[0]
+    off = np.empty(n + 1, np.int32)
+    mem = np.empty(40 * n, np.int32)
+    mom = np.empty((n, 10), np.float64)
+    ip = C.POINTER(C.c_int)
+    rc = lib.rfmesh_build_stencils(n, vo.shape[0] - 1, cv.ctypes.data_as(ip), nv.ctypes.data_as(ip),
+                                   vo.ctypes.data_as(ip), vc.ctypes.data_as(ip),
+                                   cg.ctypes.data_as(C.POINTER(C.c_double)), int(threads),
+                                   off.ctypes.data_as(ip), mem.ctypes.data_as(ip),
+                                   mom.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise RuntimeError(f"rfmesh_build_stencils failed with code {rc}")
+    return off, mem[:off[-1]].copy(), mom
+
+
+def cell_vertices(m: BoxMesh):
+    """Cell vertex lists of a mesh in its cell numbering (tets, hexes, prisms,
+    pyramids): (nCells, 8) 0-based padded with -1, and the counts."""
+    n = sum(int(c.shape[0]) for c in m.conn)
+    cv8 = np.full((n, 8), -1, np.int32)
+    nv = np.zeros(n, np.int32)
+    k = 0
+    for t, c in enumerate(m.conn):
+        nt = int(c.shape[0])
+        cv8[k:k + nt, :_NV[t]] = c - 1
+        nv[k:k + nt] = _NV[t]
+        k += nt
+    return cv8, nv
 
 
 def from_grid(xyz, tet2v=None, hex2v=None, pri2v=None, pyr2v=None, patches=(),

@@ -1,0 +1,166 @@
+"""Partitioned regions on the host: the partition's structure, the oracle's
+multi-region stage loop against the whole mesh, and the C ABI's validation
+of virtual cells and borders (no GPU)."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from rocflupicl_gb300 import case as K
+from rocflupicl_gb300 import engine as E
+from rocflupicl_gb300 import partition as P
+
+
+def tube(order=2, discr=K.DISCR_UPW_ROE, prec=K.PREC_FP64, n=24):
+    num = K.Numerics(spaceDiscr=discr, spaceOrder=order, venkatGuard=1, precision=prec)
+    return K.tet_shock_box(n, ny=4, nz=4, length=(6.0, 1.0, 1.0), x_shock=2.0, numerics=num)
+
+
+def test_partition_structure():
+    c = tube()
+    m = c.mesh
+    parts = P.partition_case(c, 3)
+    own = np.concatenate([p.mesh.global_cells[:p.mesh.nCells] for p in parts])
+    assert np.array_equal(np.sort(own), np.arange(m.nCells))  # every cell owned once
+    mem0 = m.c2cs_mem - 1
+    for p in parts:
+        g = p.mesh
+        loc = g.global_cells
+        assert g.nCellsTot == loc.shape[0] > g.nCells
+        act = set(loc[:g.nCells].tolist())
+        present = set(loc.tolist())
+        # the whole-mesh stencils and face neighbours of actual cells are present
+        for c0 in loc[:g.nCells]:
+            assert set(mem0[m.c2cs_off[c0]:m.c2cs_off[c0 + 1]].tolist()) <= present
+        # every face with an actual cell, in the whole mesh's order
+        fa = m.f2c - 1
+        sel = np.flatnonzero(np.isin(fa[:, 0], list(act)) | np.isin(fa[:, 1], list(act)))
+        assert g.nFaces == sel.shape[0]
+        assert np.array_equal(loc[g.f2c - 1], fa[sel])
+        # virtual cells in ascending whole-mesh id
+        assert np.all(np.diff(loc[g.nCells:]) > 0)
+        # every virtual cell is received exactly once
+        rec = np.concatenate([b.icgRecv for b in g.borders])
+        assert np.array_equal(np.sort(rec), np.arange(g.nCells + 1, g.nCellsTot + 1))
+        for b in g.borders:
+            nb = parts[b.iRegionGlobal - 1].mesh
+            b2 = nb.borders[b.iBorder - 1]
+            assert b2.iRegionGlobal == g.iRegionGlobal
+            assert np.all(b.icgSend <= g.nCells)
+            # send cell k here is receive cell k there: the same whole-mesh cell
+            assert np.array_equal(loc[b.icgSend - 1], nb.global_cells[b2.icgRecv - 1])
+
+
+def _run_multi(parts, n_steps):
+    from oracle.oracle import MultiOracle
+    mo = MultiOracle(parts)
+    cvs = [p.cv.copy() for p in parts]
+    dvs = [p.dv.copy() for p in parts]
+    t, k, st = mo.run(cvs, dvs, n_steps=n_steps)
+    return t, cvs, dvs, st
+
+
+def test_oracle_first_order_partition_equals_whole_mesh():
+    """First order: an actual cell's residual sums the same face fluxes in the
+    same order in its region as in the whole mesh (faces keep the whole mesh's
+    order, virtual cells carry their owners' state), and the global time step is
+    the whole mesh's, so the partitioned run is bit-identical."""
+    from oracle.oracle import Oracle
+    c = tube(order=1)
+    parts = P.partition_case(c, 3)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    t0, _, _ = Oracle(c).run(cv, dv, n_steps=6)
+    t1, cvs, dvs, st = _run_multi(parts, 6)
+    assert st == 0 and t1 == t0
+    for p, x, y in zip(parts, cvs, dvs):
+        p.cv[:], p.dv[:] = x, y
+    assert np.array_equal(P.gather(parts, "cv"), cv)
+    assert np.array_equal(P.gather(parts, "dv"), dv)
+
+
+def test_oracle_second_order_partition_close_to_whole_mesh():
+    """Second order: a virtual cell's limiter sees only the faces its region
+    holds (RFLU_ComputeLimiterVenkat runs over 1..nFaces) and its stencil is
+    the region's own, so the partitioned run differs from the whole-mesh one
+    near borders, as in the reference; it stays close."""
+    from oracle.oracle import Oracle
+    c = tube(order=2)
+    parts = P.partition_case(c, 3)
+    cv, dv = c.cv.copy(), c.dv.copy()
+    Oracle(c).run(cv, dv, n_steps=6)
+    _, cvs, _, st = _run_multi(parts, 6)
+    assert st == 0
+    for p, x in zip(parts, cvs):
+        p.cv[:] = x
+    g = P.gather(parts, "cv")
+    l1 = np.abs(g[:, 0] - cv[:, 0]).sum() / np.abs(cv[:, 0]).sum()
+    assert 0.0 < l1 < 2e-3
+
+
+def test_oracle_omp_stage_equals_serial_with_virtual_cells():
+    from oracle.oracle import Oracle
+    parts = P.partition_case(tube(order=2), 3)
+    p = parts[1]
+    oa, ob = Oracle(p), Oracle(p)
+    a_cv, a_dv, b_cv, b_dv = p.cv.copy(), p.dv.copy(), p.cv.copy(), p.dv.copy()
+    for s in (1, 2, 3):
+        oa.stage(a_cv, a_dv, s, 1e-7)
+        ob.stage(b_cv, b_dv, s, 1e-7, threads=4)
+    assert np.array_equal(a_cv, b_cv) and np.array_equal(a_dv, b_dv)
+    assert np.array_equal(oa.rhs, ob.rhs)
+    assert not np.any(oa.rhs[p.mesh.nCells:])  # ZeroDummyCellsMP
+
+
+def _desc_of(case, **over):
+    """A region descriptor through Region's field filling, without creating it."""
+    from test_abi import _desc
+    lib, d, keep = _desc(case)
+    m = case.mesh
+    d.nCellsTot = m.nTot
+    d.iRegionGlobal = m.iRegionGlobal
+    barr = (E.BorderT * max(1, len(m.borders)))()
+    for i, b in enumerate(m.borders):
+        s = np.ascontiguousarray(b.icgSend, np.int32)
+        r = np.ascontiguousarray(b.icgRecv, np.int32)
+        keep += [s, r]
+        barr[i].iRegionGlobal, barr[i].iBorder = b.iRegionGlobal, b.iBorder
+        barr[i].nCellsSend, barr[i].icgSend = s.shape[0], E._ip(s)
+        barr[i].nCellsRecv, barr[i].icgRecv = r.shape[0], E._ip(r)
+    d.nBorders = len(m.borders)
+    d.borders = barr
+    keep.append(barr)
+    for key, val in over.items():
+        setattr(d, key, val)
+    return lib, d, keep
+
+
+@pytest.mark.parametrize("bad", ["recv_actual", "send_virtual", "tot_small", "iborder"])
+def test_border_indices_refused_before_any_cuda_call(bad):
+    p = P.partition_case(tube(order=2, n=12), 2)[0]
+    lib, d, keep = _desc_of(p)
+    b = d.borders[0]
+    if bad == "recv_actual":
+        arr = np.array([1] * b.nCellsRecv, np.int32)
+        keep.append(arr)
+        b.icgRecv = E._ip(arr)
+    elif bad == "send_virtual":
+        arr = np.full(b.nCellsSend, p.mesh.nCells + 1, np.int32)
+        keep.append(arr)
+        b.icgSend = E._ip(arr)
+    elif bad == "tot_small":
+        d.nCellsTot = p.mesh.nCells - 1
+    else:
+        b.iBorder = 0
+    h = C.c_void_p()
+    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_ARG
+    assert not h.value
+
+
+def test_border_calls_reject_null_handles():
+    lib = E.load()
+    assert lib.rfgpu_border_copy(None, 1, None) == E.ERR_ARG
+    buf = np.zeros(5)
+    assert lib.rfgpu_border_pack(None, 1, E._dp(buf)) == E.ERR_ARG
+    assert lib.rfgpu_border_unpack(None, 1, E._dp(buf)) == E.ERR_ARG
+    out = C.c_void_p()
+    assert lib.rfgpu_batch_create_ex(None, 0, E.BATCH_COUPLED, C.byref(out)) == E.ERR_ARG
