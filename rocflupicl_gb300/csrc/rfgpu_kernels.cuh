@@ -1768,7 +1768,7 @@ void launch_dt_finalize(const RegionDev<R> *regs, const Work &w, const DtArgs &a
   if (w.coupled)
     k_dt_finalize_coupled<R><<<1, 256, 0, s>>>(regs, w.nRegions, a);
   else
-    launch_dt_finalize<R>(regs, w, a, s);
+    k_dt_finalize<R><<<(w.nRegions + 127) / 128, 128, 0, s>>>(regs, w.nRegions, a);
 }
 
 // ---- launchers ----------------------------------------------------------------
