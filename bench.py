@@ -46,7 +46,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="tet", choices=["tet", "sod", "mixed", "tubes", "serving"],
+    ap.add_argument("--workload", default="tet", choices=["tet", "sod", "mixed", "tubes", "serving", "partitioned"],
                     help="tet: the headline line; the others print their own measurement")
     ap.add_argument("--n", "--hexes", dest="n", type=int, default=128,
                     help="base hexes per direction")
@@ -264,6 +264,8 @@ def run_secondary(a, dist):
         out = W.run_mixed_residual(repeats=a.steps)
     elif a.workload == "tubes":
         out = W.run_tubes(steps=a.steps)
+    elif a.workload == "partitioned":
+        out = W.run_partitioned(n=a.n if a.n != 128 else 64, steps=a.steps)
     else:
         from rocflupicl_gb300 import serving as S
         out = {"workload": "serving sweep", "rates": {}}
