@@ -333,6 +333,39 @@ int rfgpu_mesh_stencils(int nCells, int nVerts, const int *cellVerts, const int 
                         const int *v2cOffsets, const int *v2c, const double *cofg,
                         int *c2csOffsets, int *c2csMembers, double *xyzMoms);
 
+/* Device-side mesh preprocessing of a whole box mesh: the face list, face
+ * and cell geometry, vertex-to-cell lists, c2c stencils and WLSQ moments
+ * (RFLU_BuildFaceList, modflu/RFLU_ModFaceList.F90:784-1609; RFLU_BuildGeometry,
+ * modflu/RFLU_ModGeometry.F90:307-672; the stencils and moments as
+ * rfgpu_mesh_stencils), the arrays rfmesh.h's host builder makes for the same
+ * cells, bit for bit: faces numbered by first encounter sweeping the cells,
+ * oriented outward from their first cell, interior faces then the six box
+ * patches (XLO, XHI, YLO, YHI, ZLO, ZHI) by the plane their centroid lies on.
+ * Inputs: xyz(3,nVerts); cell vertices (8,nCells) 0-based padded with -1, the
+ * vertex counts and the cell types (0 tet, 1 hex, 2 prism, 3 pyramid, vertex
+ * counts 4/8/6/5), cells numbered by type as rfmesh.h numbers them; the box
+ * bounds.  Every index is validated on the host (RFGPU_ERR_ARG); a face on
+ * three cells, a boundary face off the box or a non-positive volume gives
+ * RFGPU_ERR_ARG, a cell with more than 256 vertex-neighbour entries
+ * RFGPU_ERR_UNSUPPORTED.  Synchronous; the results are held by the handle.
+ * sizes: nFaces, nMembs, then the boundary faces of the six patches.
+ * Outputs in the layouts of rfmesh.h: f2c(2,nFaces) 1-based, fn(4,nFaces),
+ * fc(3,nFaces), vol(nCells), cofg(3,nCells), stencil offsets (nCells+1,
+ * 0-based) and members (1-based), xyzMoms(10,nCells), vertex-to-cell offsets
+ * (nVerts+1) and cells (0-based); per patch bf2c (1-based), fn(4,n), fc(3,n)
+ * and the face vertices (4,n) 0-based, -1 for a triangle's fourth.  Any output
+ * pointer may be NULL. */
+typedef struct rfgpu_mesh_s *rfgpu_mesh_t;
+int rfgpu_mesh_build(int nCells, int nVerts, const double *xyz, const int *cellVerts,
+                     const int *cellNVerts, const int *cellType, const double lo[3],
+                     const double hi[3], rfgpu_mesh_t *out);
+int rfgpu_mesh_sizes(rfgpu_mesh_t m, long long sizes[8]);
+int rfgpu_mesh_faces(rfgpu_mesh_t m, int *f2c, double *fn, double *fc);
+int rfgpu_mesh_cells(rfgpu_mesh_t m, double *vol, double *cofg, int *c2csOffsets,
+                     int *c2csMembers, double *xyzMoms, int *v2cOffsets, int *v2c);
+int rfgpu_mesh_patch(rfgpu_mesh_t m, int iPatch, int *bf2c, double *fn, double *fc, int *bf2v);
+int rfgpu_mesh_destroy(rfgpu_mesh_t m);
+
 #ifdef __cplusplus
 }
 #endif

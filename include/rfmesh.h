@@ -64,9 +64,14 @@ enum { RFMESH_OK = 0, RFMESH_ERR_ARG = 1, RFMESH_ERR_GEOM = 2, RFMESH_ERR_NOMEM 
 
 /* flags of rfmesh_create_box_ex */
 enum {
-  RFMESH_DEFER_STENCILS = 1  /* build everything but the c2c stencils and moments; supply
+  RFMESH_DEFER_STENCILS = 1, /* build everything but the c2c stencils and moments; supply
                                 them with rfmesh_set_stencils (e.g. from the GPU builder
                                 rfgpu_mesh_stencils, which runs the same per-cell routine) */
+  RFMESH_CELLS_ONLY = 2      /* generate the vertices and cells only (rfmesh_xyz,
+                                rfmesh_cell_verts, rfmesh_cell_nverts, rfmesh_cell_type,
+                                rfmesh_cell_conn); the face list, geometry, vertex-to-cell
+                                lists and stencils come from the device builder
+                                rfgpu_mesh_build, which reproduces this library's */
 };
 
 /* Build a box mesh over [lo,hi] with nx*ny*nz base hexes.  Interior vertices

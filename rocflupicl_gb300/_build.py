@@ -71,6 +71,7 @@ GPU_UNITS = [
     ("rfgpu_host.cu", []),
     ("rfgpu_fp64.cu", ["--fmad=false"]),
     ("rfgpu_mixed.cu", []),
+    ("rfgpu_meshbuild.cu", ["--fmad=false"]),
 ]
 
 

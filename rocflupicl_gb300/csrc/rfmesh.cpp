@@ -4,6 +4,7 @@
 // host (x86_64 here, aarch64 on the GPU nodes) and matches the unfused
 // Fortran arithmetic it restates.
 #include "rfmesh.h"
+#include "rfmesh_geom.h"
 #include "rfmesh_stencil.h"
 
 #include <algorithm>
@@ -23,15 +24,15 @@
 
 namespace {
 
-enum { T_TET = 0, T_HEX = 1, T_PRI = 2, T_PYR = 3 };
+using rfm::T_TET;
+using rfm::T_HEX;
+using rfm::T_PRI;
+using rfm::T_PYR;
 const int kNV[4] = {4, 8, 6, 5};
 const int kNF[4] = {4, 6, 5, 5};
-// local faces, cyclic vertex order, -1 padded (tri faces)
-const int kFaces[4][6][4] = {
-    {{0, 2, 1, -1}, {0, 1, 3, -1}, {1, 2, 3, -1}, {0, 3, 2, -1}},
-    {{0, 3, 2, 1}, {4, 5, 6, 7}, {0, 1, 5, 4}, {1, 2, 6, 5}, {2, 3, 7, 6}, {3, 0, 4, 7}},
-    {{0, 2, 1, -1}, {3, 4, 5, -1}, {0, 1, 4, 3}, {1, 2, 5, 4}, {2, 0, 3, 5}},
-    {{0, 3, 2, 1}, {0, 1, 4, -1}, {1, 2, 4, -1}, {2, 3, 4, -1}, {3, 0, 4, -1}}};
+// local faces, cyclic vertex order, -1 padded (tri faces); the table the
+// device builder uses too
+const int kFaces[4][6][4] = RFM_FACE_TABLE;
 
 struct Patch {
   std::vector<int> bf2c;    // 0-based internally
@@ -77,34 +78,7 @@ struct rfmesh_s {
 
 namespace {
 
-// FaceVectorTria / FaceVectorQuad (libfloflu/FaceVector.F90:79-136) and
-// FaceCentroidTria / FaceCentroidQuad (libfloflu/FaceCentroid.F90:77-122).
-void face_vec_cen(const double *xyz, const int *fv, double S[3], double C[3]) {
-  if (fv[3] < 0) {
-    const double *p1 = xyz + 3 * (size_t)fv[0], *p2 = xyz + 3 * (size_t)fv[1],
-                 *p3 = xyz + 3 * (size_t)fv[2];
-    double dxa = p1[0] - p2[0], dya = p1[1] - p2[1], dza = p1[2] - p2[2];
-    double dxb = p1[0] - p3[0], dyb = p1[1] - p3[1], dzb = p1[2] - p3[2];
-    S[0] = 0.5 * (dya * dzb - dyb * dza);
-    S[1] = -0.5 * (dxa * dzb - dxb * dza);
-    S[2] = 0.5 * (dxa * dyb - dxb * dya);
-    const double thrd = 1.0 / 3.0;
-    C[0] = thrd * (p1[0] + p2[0] + p3[0]);
-    C[1] = thrd * (p1[1] + p2[1] + p3[1]);
-    C[2] = thrd * (p1[2] + p2[2] + p3[2]);
-  } else {
-    const double *p1 = xyz + 3 * (size_t)fv[0], *p2 = xyz + 3 * (size_t)fv[1],
-                 *p3 = xyz + 3 * (size_t)fv[2], *p4 = xyz + 3 * (size_t)fv[3];
-    double dxa = p3[0] - p1[0], dya = p3[1] - p1[1], dza = p3[2] - p1[2];
-    double dxb = p2[0] - p4[0], dyb = p2[1] - p4[1], dzb = p2[2] - p4[2];
-    S[0] = 0.5 * (dza * dyb - dya * dzb);
-    S[1] = 0.5 * (dxa * dzb - dza * dxb);
-    S[2] = 0.5 * (dya * dxb - dxa * dyb);
-    C[0] = 0.25 * (p1[0] + p2[0] + p3[0] + p4[0]);
-    C[1] = 0.25 * (p1[1] + p2[1] + p3[1] + p4[1]);
-    C[2] = 0.25 * (p1[2] + p2[2] + p3[2] + p4[2]);
-  }
-}
+using rfm::face_vec_cen;  // FaceVector / FaceCentroid, shared with the device builder
 
 inline uint64_t vid(int i, int j, int k, int nx, int ny) {
   return (uint64_t)i + (uint64_t)(nx + 1) * ((uint64_t)j + (uint64_t)(ny + 1) * (uint64_t)k);
@@ -228,11 +202,11 @@ void generate(rfmesh_s *m, int nx, int ny, int nz, double jitter, unsigned long 
 
 void set_stencils(rfmesh_s *m, const std::vector<int> &cnt, const std::vector<int> &memb);
 
-void build(rfmesh_s *m, int nThreads) {
-  (void)nThreads;
+// Global cell numbering (tets, hexes, prisms, pyramids) and the connectivity
+// padded to 8 vertices that the stencil and device builders take.
+void cells(rfmesh_s *m) {
   m->nCells = m->nOfType[0] + m->nOfType[1] + m->nOfType[2] + m->nOfType[3];
   const long long nC = m->nCells;
-  const long long nV = (long long)(m->xyz.size() / 3);
   m->ctype.resize(nC);
   m->cloc.resize(nC);
   {
@@ -243,6 +217,20 @@ void build(rfmesh_s *m, int nThreads) {
         m->cloc[icg] = (int)l;
       }
   }
+  m->cv8.assign(8 * (size_t)nC, -1);
+  m->nv8.resize(nC);
+  for (long long c = 0; c < nC; ++c) {
+    m->nv8[c] = m->nv(c);
+    const int *v = m->verts(c);
+    for (int a = 0; a < m->nv(c); ++a) m->cv8[8 * (size_t)c + a] = v[a];
+  }
+}
+
+void build(rfmesh_s *m, int nThreads) {
+  (void)nThreads;
+  cells(m);
+  const long long nC = m->nCells;
+  const long long nV = (long long)(m->xyz.size() / 3);
   // approximate centroids: vertex averages (RFLU_ModGeometry.F90:1277-1460)
   m->cofgApp.assign(3 * (size_t)nC, 0.0);
   for (long long icg = 0; icg < nC; ++icg) {
@@ -365,14 +353,7 @@ void build(rfmesh_s *m, int nThreads) {
   m->fn.resize(4 * (size_t)nF);
   m->fc.resize(3 * (size_t)nF);
   auto contrib = [&](int c, const double S[3], const double C[3], double sgn) {
-    const double *ca = &m->cofgApp[3 * (size_t)c];
-    double term = (C[0] - ca[0]) * S[0] + (C[1] - ca[1]) * S[1] + (C[2] - ca[2]) * S[2];
-    if (sgn > 0) m->vol[c] = m->vol[c] + term; else m->vol[c] = m->vol[c] - term;
-    term = C[0] * S[0] + C[1] * S[1] + C[2] * S[2];
-    for (int d = 0; d < 3; ++d) {
-      if (sgn > 0) m->cofg[3 * (size_t)c + d] = m->cofg[3 * (size_t)c + d] + term * C[d];
-      else m->cofg[3 * (size_t)c + d] = m->cofg[3 * (size_t)c + d] - term * C[d];
-    }
+    rfm::face_contrib(S, C, &m->cofgApp[3 * (size_t)c], sgn, &m->vol[c], &m->cofg[3 * (size_t)c]);
   };
   for (int64_t f = 0; f < nF; ++f) {
     double S[3], C[3];
@@ -442,13 +423,6 @@ void build(rfmesh_s *m, int nThreads) {
   // c2c stencils (RFLU_ModStencilsCells.F90:750-1416) and moments
   // (RFLU_ModWeights.F90:1770-1894): the per-cell routine shared with the
   // device builder (rfmesh_stencil.h)
-  m->cv8.assign(8 * (size_t)nC, -1);
-  m->nv8.resize(nC);
-  for (long long c = 0; c < nC; ++c) {
-    m->nv8[c] = m->nv(c);
-    const int *v = m->verts(c);
-    for (int a = 0; a < m->nv(c); ++a) m->cv8[8 * (size_t)c + a] = v[a];
-  }
   if (m->skipStencils) return;
   const rfm::CellView view{m->cofg.data(), m->cv8.data(), m->nv8.data(), m->v2cOff.data(),
                            m->v2c.data()};
@@ -517,7 +491,10 @@ int rfmesh_create_box_ex(int kind, int nx, int ny, int nz, const double lo[3], c
   int rc = RFMESH_OK;
   try {
     generate(m, nx, ny, nz, jitter, seed);
-    build(m, nThreads);
+    if (flags & RFMESH_CELLS_ONLY)
+      cells(m);
+    else
+      build(m, nThreads);
   } catch (const std::bad_alloc &) {
     rc = RFMESH_ERR_NOMEM;
   } catch (...) {

@@ -85,7 +85,9 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
            "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
            "rfgpu_mesh_stencils", "rfgpu_border_copy", "rfgpu_border_pack",
-           "rfgpu_border_unpack", "rfgpu_batch_create_ex"]
+           "rfgpu_border_unpack", "rfgpu_batch_create_ex", "rfgpu_mesh_build",
+           "rfgpu_mesh_sizes", "rfgpu_mesh_faces", "rfgpu_mesh_cells", "rfgpu_mesh_patch",
+           "rfgpu_mesh_destroy"]
 
 BATCH_COUPLED = 1
 
@@ -148,6 +150,12 @@ def load(path: Optional[str] = None):
         "rfgpu_border_pack": ([vp, C.c_int, dp], C.c_int),
         "rfgpu_border_unpack": ([vp, C.c_int, dp], C.c_int),
         "rfgpu_batch_create_ex": ([C.POINTER(vp), C.c_int, C.c_int, C.POINTER(vp)], C.c_int),
+        "rfgpu_mesh_build": ([C.c_int, C.c_int, dp, ip, ip, ip, dp, dp, C.POINTER(vp)], C.c_int),
+        "rfgpu_mesh_sizes": ([vp, C.POINTER(C.c_longlong)], C.c_int),
+        "rfgpu_mesh_faces": ([vp, ip, dp, dp], C.c_int),
+        "rfgpu_mesh_cells": ([vp, dp, dp, ip, ip, dp, ip, ip], C.c_int),
+        "rfgpu_mesh_patch": ([vp, C.c_int, ip, dp, dp, ip], C.c_int),
+        "rfgpu_mesh_destroy": ([vp], C.c_int),
     }
     for name, (args, res) in sig.items():
         f = getattr(lib, name)
@@ -207,6 +215,50 @@ def mesh_stencils(n_cells: int, n_verts: int, cell_verts, cell_nverts, v2c_off, 
     _check(lib.rfgpu_mesh_stencils(n_cells, n_verts, _ip(cv), _ip(nv), _ip(vo), _ip(vc), _dp(cg),
                                    _ip(off), _ip(mem), _dp(mom)), "rfgpu_mesh_stencils")
     return off, mem[:off[-1]].copy(), mom
+
+
+def mesh_build(n_verts: int, xyz, cell_verts, cell_nverts, cell_type, lo, hi):
+    """rfgpu_mesh_build: face list, geometry, vertex-to-cell lists, stencils and
+    moments of a box mesh on the GPU (rfmesh.h's host builder, bit for bit).
+    Returns a dict of arrays in the host builder's layouts."""
+    lib = load()
+    xyz = np.ascontiguousarray(xyz, np.float64)
+    cv = np.ascontiguousarray(cell_verts, np.int32)
+    nv = np.ascontiguousarray(cell_nverts, np.int32)
+    ct = np.ascontiguousarray(cell_type, np.int32)
+    n = nv.shape[0]
+    lo_a = (C.c_double * 3)(*lo)
+    hi_a = (C.c_double * 3)(*hi)
+    h = C.c_void_p()
+    _check(lib.rfgpu_mesh_build(n, n_verts, _dp(xyz), _ip(cv), _ip(nv), _ip(ct), lo_a, hi_a,
+                                C.byref(h)), "rfgpu_mesh_build")
+    try:
+        sz = (C.c_longlong * 8)()
+        _check(lib.rfgpu_mesh_sizes(h, sz), "rfgpu_mesh_sizes")
+        nF, nM = sz[0], sz[1]
+        out = {"f2c": np.empty((nF, 2), np.int32), "fn": np.empty((nF, 4)),
+               "fc": np.empty((nF, 3)), "vol": np.empty(n), "cofg": np.empty((n, 3)),
+               "c2cs_off": np.empty(n + 1, np.int32), "c2cs_mem": np.empty(nM, np.int32),
+               "xyzmoms": np.empty((n, 10)), "v2c_off": np.empty(n_verts + 1, np.int32)}
+        _check(lib.rfgpu_mesh_faces(h, _ip(out["f2c"]), _dp(out["fn"]), _dp(out["fc"])),
+               "rfgpu_mesh_faces")
+        _check(lib.rfgpu_mesh_cells(h, _dp(out["vol"]), _dp(out["cofg"]), _ip(out["c2cs_off"]),
+                                    _ip(out["c2cs_mem"]), _dp(out["xyzmoms"]),
+                                    _ip(out["v2c_off"]), None), "rfgpu_mesh_cells")
+        out["v2c"] = np.empty(int(out["v2c_off"][-1]), np.int32)
+        _check(lib.rfgpu_mesh_cells(h, None, None, None, None, None, None, _ip(out["v2c"])),
+               "rfgpu_mesh_cells")
+        out["patches"] = []
+        for ipt in range(6):
+            nb = sz[2 + ipt]
+            pa = {"bf2c": np.empty(nb, np.int32), "fn": np.empty((nb, 4)), "fc": np.empty((nb, 3)),
+                  "bf2v": np.empty((nb, 4), np.int32)}
+            _check(lib.rfgpu_mesh_patch(h, ipt, _ip(pa["bf2c"]), _dp(pa["fn"]), _dp(pa["fc"]),
+                                        _ip(pa["bf2v"])), "rfgpu_mesh_patch")
+            out["patches"].append(pa)
+        return out
+    finally:
+        lib.rfgpu_mesh_destroy(h)
 
 
 class PinnedArray:

@@ -154,6 +154,7 @@ class BoxMesh:
 
 
 RFMESH_DEFER_STENCILS = 1
+RFMESH_CELLS_ONLY = 2
 
 
 def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 1.0),
@@ -161,13 +162,24 @@ def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 
     """Build a box mesh (HEX / Kuhn TET / MIXED) and return its region arrays.
     stencils="device" builds the c2c stencils and WLSQ moments on the GPU
     (rfgpu_mesh_stencils: the host builder's per-cell routine, identical
-    output) and the rest on the host."""
-    if stencils not in ("host", "device"):
+    output) and the rest on the host; stencils="all-device" builds everything
+    but the vertices and cells on the GPU (rfgpu_mesh_build: face list,
+    geometry, vertex-to-cell lists, stencils, moments; identical output)."""
+    if stencils not in ("host", "device", "all-device"):
         raise ValueError(stencils)
     lib = _load()
     h = C.c_void_p()
     lo_a = (C.c_double * 3)(*lo)
     hi_a = (C.c_double * 3)(*hi)
+    if stencils == "all-device":
+        rc = lib.rfmesh_create_box_ex(kind, nx, ny, nz, lo_a, hi_a, float(jitter), int(seed),
+                                      int(threads), RFMESH_CELLS_ONLY, C.byref(h))
+        if rc != 0:
+            raise RuntimeError(f"rfmesh_create_box failed with code {rc}")
+        try:
+            return _from_device(lib, h, kind, (nx, ny, nz), lo, hi)
+        finally:
+            lib.rfmesh_destroy(h)
     flags = RFMESH_DEFER_STENCILS if stencils == "device" else 0
     rc = lib.rfmesh_create_box_ex(kind, nx, ny, nz, lo_a, hi_a, float(jitter), int(seed),
                                   int(threads), flags, C.byref(h))
@@ -180,6 +192,28 @@ def box(kind: int, nx: int, ny: int, nz: int, lo=(0.0, 0.0, 0.0), hi=(1.0, 1.0, 
 
 
 _NV = (4, 8, 6, 5)
+
+
+def _from_device(lib, h, kind, dims, lo, hi) -> BoxMesh:
+    """Region arrays of a cells-only rfmesh handle, built by rfgpu_mesh_build."""
+    from . import engine
+    s = (C.c_longlong * _NSIZES)()
+    lib.rfmesh_sizes(h, s)
+    nV, nC = s[0], s[1]
+    xyz = _copy(lib.rfmesh_xyz(h), 3 * nV, np.float64, (nV, 3))
+    cv8 = _copy(lib.rfmesh_cell_verts(h), 8 * nC, np.int32, (nC, 8))
+    nv = _copy(lib.rfmesh_cell_nverts(h), nC, np.int32, (nC,))
+    ct = _copy(lib.rfmesh_cell_type(h), nC, np.int32, (nC,))
+    r = engine.mesh_build(nV, xyz, cv8, nv, ct, lo, hi)
+    m = BoxMesh(kind=kind, dims=dims, nCells=nC, nFaces=r["f2c"].shape[0], xyz=xyz, vol=r["vol"],
+                cofg=r["cofg"], f2c=r["f2c"], fn=r["fn"], fc=r["fc"], c2cs_off=r["c2cs_off"],
+                c2cs_mem=r["c2cs_mem"], xyzmoms=r["xyzmoms"], cell_type=ct,
+                n_of_type=(s[5], s[6], s[7], s[8]))
+    for pa in r["patches"]:
+        m.patches.append(Patch(bf2c=pa["bf2c"], fn=pa["fn"], fc=pa["fc"], bf2v=pa["bf2v"] + 1))
+    m.conn = [_copy(lib.rfmesh_cell_conn(h, t), _NV[t] * int(s[5 + t]), np.int32,
+                    (int(s[5 + t]), _NV[t])) + 1 for t in range(4)]
+    return m
 
 
 def _extract(lib, h, kind, dims, stencils) -> BoxMesh:

@@ -71,10 +71,12 @@ def poisson_requests(count: int, lam: float, seed: int, cells_min: int = 10_000,
 
 
 def build_case(req: Request, precision: int = K.PREC_MIXED, threads: int = 4,
-               stencils: str = "device") -> K.Case:
-    """The request's mesh and initial state.  stencils="device" builds the c2c
-    stencils and WLSQ moments on the GPU (identical to the host builder's),
-    the dominant part of the preparation on the host."""
+               stencils: str = "all-device") -> K.Case:
+    """The request's mesh and initial state.  stencils="all-device" builds the
+    face list, geometry, vertex-to-cell lists, c2c stencils and WLSQ moments
+    on the GPU (identical to the host builder's), leaving the vertex and cell
+    generation on the host; "device" builds only the stencils and moments
+    there."""
     num = K.Numerics(spaceDiscr=req.scheme, precision=precision, venkatGuard=1)
     return K.tet_shock_box(req.n, seed=req.seed, Ms=req.Ms, numerics=num, threads=threads,
                            stencils=stencils)
@@ -97,7 +99,7 @@ class Server:
                  precision: int = K.PREC_MIXED, prepare_workers: int = 4,
                  mesh_threads: int = 4, keep_state: bool = False,
                  bytes_per_cell: float = 800.0, max_steps: int = 100000,
-                 stencils: str = "device"):
+                 stencils: str = "all-device"):
         self.t_end = t_end
         self.stencils = stencils
         self.max_steps = max_steps
@@ -227,7 +229,7 @@ class Server:
 
 
 def solve_alone(req: Request, t_end: float, precision: int = K.PREC_MIXED,
-                max_steps: int = 100000, stencils: str = "device"):
+                max_steps: int = 100000, stencils: str = "all-device"):
     """The same request run by itself: first step with its own dtImposed, then
     device steps to the end time."""
     c = build_case(req, precision, stencils=stencils)

@@ -143,3 +143,29 @@ def test_mesh_stencils_validates_before_any_device_work():
         with pytest.raises(E.EngineError) as ei:
             E.mesh_stencils(nC, nV, cv2, nv2, vo, vc2, cg)
         assert ei.value.code == E.ERR_ARG
+
+
+def test_mesh_build_validates_before_any_device_work():
+    """rfgpu_mesh_build checks every index and cell type on the host first."""
+    lib = E.load()
+    xyz = np.zeros((5, 3))
+    cv = np.full((1, 8), -1, np.int32)
+    cv[0, :4] = [0, 1, 2, 3]
+    nv = np.array([4], np.int32)
+    ct = np.array([0], np.int32)
+    lo = (C.c_double * 3)(0.0, 0.0, 0.0)
+    hi = (C.c_double * 3)(1.0, 1.0, 1.0)
+    h = C.c_void_p()
+    for bad in ("vertex", "type", "count", "pad"):
+        cv2, nv2, ct2 = cv.copy(), nv.copy(), ct.copy()
+        if bad == "vertex":
+            cv2[0, 1] = 5
+        elif bad == "type":
+            ct2[0] = 4
+        elif bad == "count":
+            nv2[0] = 8
+        else:
+            cv2[0, 5] = 2
+        assert lib.rfgpu_mesh_build(1, 5, E._dp(xyz), E._ip(cv2), E._ip(nv2), E._ip(ct2), lo, hi,
+                                    C.byref(h)) == E.ERR_ARG
+        assert not h.value
