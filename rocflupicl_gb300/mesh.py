@@ -92,6 +92,8 @@ class Patch:
     fn: np.ndarray
     fc: np.ndarray
     bf2v: Optional[np.ndarray] = None
+    # partitioned regions: positions of these faces in the whole mesh's patch
+    global_faces: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:

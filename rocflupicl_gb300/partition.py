@@ -111,7 +111,8 @@ def partition(m: M.BoxMesh, n_regions: int, axis: int = 0, layers: int = 2,
             sel = np.flatnonzero(inA[p.bf2c - 1])
             patches.append(M.Patch(bf2c=(g2l[p.bf2c[sel] - 1] + 1).astype(np.int32),
                                    fn=p.fn[sel].copy(), fc=p.fc[sel].copy(),
-                                   bf2v=None if p.bf2v is None else p.bf2v[sel].copy()))
+                                   bf2v=None if p.bf2v is None else p.bf2v[sel].copy(),
+                                   global_faces=sel))
         # stencils over the region's own cells: vertex-to-cell lists of the
         # region's cells in ascending local id
         lcv = cv8[loc]
@@ -163,9 +164,20 @@ def partition_case(case, n_regions: int, axis: int = 0, layers: int = 2, threads
     the region's state rows cv, dv (actual then virtual cells) and the same
     boundary conditions and numerics."""
     parts = partition(case.mesh, n_regions, axis, layers, threads)
-    return [replace(case, name=f"{case.name}.r{p.iRegionGlobal}", mesh=p,
-                    cv=case.cv[p.global_cells].copy(), dv=case.dv[p.global_cells].copy())
-            for p in parts]
+    out = []
+    for p in parts:
+        bcs = []
+        for bc, pa, whole in zip(case.bcs, p.patches, case.mesh.patches):
+            # per-face patch values follow their faces
+            v, po = bc.vals, bc.pout
+            if v is not None and np.ndim(v) == 2 and np.shape(v)[0] == whole.n:
+                v = np.asarray(v)[pa.global_faces]
+            if po is not None and np.size(po) == whole.n and whole.n > 1:
+                po = np.asarray(po)[pa.global_faces]
+            bcs.append(replace(bc, vals=v, pout=po))
+        out.append(replace(case, name=f"{case.name}.r{p.iRegionGlobal}", mesh=p, bcs=bcs,
+                           cv=case.cv[p.global_cells].copy(), dv=case.dv[p.global_cells].copy()))
+    return out
 
 
 def gather(cases, field: str = "cv") -> np.ndarray:

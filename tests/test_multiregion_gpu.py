@@ -214,3 +214,49 @@ def test_halo_launches_profiled():
     b.close()
     for r in regs:
         r.close()
+
+
+def _variant(name):
+    if name == "mixed_elements":
+        c = K.mixed_box(8, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_HLLC, venkatGuard=1))
+        return c, 3
+    disc = K.DISCR_UPW_AUSMPLUSUP if name == "ausmup" else K.DISCR_UPW_ROE
+    rk = {"rk4": K.RK_SCHEME_4_CLASSICAL, "euler": K.RK_SCHEME_1_EULER}.get(name,
+                                                                          K.RK_SCHEME_3_WRAY)
+    num = K.Numerics(spaceDiscr=disc, venkatGuard=1, rkScheme=rk)
+    c = K.tet_shock_box(24, ny=4, nz=4, length=(6.0, 1.0, 1.0), x_shock=2.0, numerics=num)
+    if name == "farfield":
+        for ip in (0, 1):
+            c.bcs[ip] = K.PatchBC(K.BC_FARFIELD, 2, 0,
+                                  vals=np.array([0.6, 0.1, 0.05, 1.0e5, 300.0]))
+    elif name == "inject":
+        n0 = c.mesh.patches[2].n   # YLO wall, cut by every region
+        vals = np.stack([np.linspace(1.0, 3.0, n0), np.full(n0, 320.0)], axis=1)
+        c.bcs[2] = K.PatchBC(K.BC_INJECTION, 2, 0, vals=vals)
+    elif name == "inflow":
+        g = c.numerics.gamma_gv
+        R = 8314.3 / c.numerics.gv[1]
+        r2, u2, p2 = K.rankine_hugoniot(2.0, g, 1.2, 1.0e5)
+        T2 = p2 / (r2 * R)
+        m2 = u2 / np.sqrt(g * R * T2)
+        f = 1.0 + 0.5 * (g - 1.0) * m2 * m2
+        c.bcs[0] = K.PatchBC(K.BC_INFLOW_TOTANG, 2, K.BCOPT_MIXED,
+                             vals=np.array([p2 * f ** (g / (g - 1.0)), T2 * f, 0.1, 0.05, m2]))
+    elif name == "order1_patches":
+        for ip in range(6):
+            c.bcs[ip] = K.PatchBC(c.bcs[ip].bcType, 1, c.bcs[ip].bcOptType)
+    return c, 3
+
+
+@pytest.mark.parametrize("name", ["mixed_elements", "rk4", "euler", "ausmup", "farfield",
+                                  "inject", "inflow", "order1_patches"])
+def test_partition_variants_bitwise_oracle(name):
+    c, n = _variant(name)
+    parts = P.partition_case(c, n)
+    t, cvs, dvs, st = oracle_run(parts, n_steps=4)
+    out, times, sts = batch_run(parts, n_steps=4)
+    for (cv, dv), ocv, odv in zip(out, cvs, dvs):
+        assert np.array_equal(cv, ocv)
+        assert np.array_equal(dv, odv)
+    assert all(x == t for x in times)
+    assert st == 0 and sts == [0] * len(parts)

@@ -164,3 +164,18 @@ def test_border_calls_reject_null_handles():
     assert lib.rfgpu_border_unpack(None, 1, E._dp(buf)) == E.ERR_ARG
     out = C.c_void_p()
     assert lib.rfgpu_batch_create_ex(None, 0, E.BATCH_COUPLED, C.byref(out)) == E.ERR_ARG
+
+
+def test_partition_splits_per_face_patch_values():
+    c = tube(order=2)
+    n0 = c.mesh.patches[2].n
+    vals = np.stack([np.arange(n0, dtype=float), np.full(n0, 320.0)], axis=1)
+    c.bcs[2] = K.PatchBC(K.BC_INJECTION, 2, 0, vals=vals)
+    parts = P.partition_case(c, 3)
+    got = []
+    for p in parts:
+        pa = p.mesh.patches[2]
+        assert p.bcs[2].vals.shape == (pa.n, 2)
+        assert np.array_equal(p.bcs[2].vals[:, 0], pa.global_faces.astype(float))
+        got.append(pa.global_faces)
+    assert np.array_equal(np.sort(np.concatenate(got)), np.arange(n0))
