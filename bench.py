@@ -421,7 +421,8 @@ def main():
                         "max_active": srv.max_active, "batch_iterations": srv.iterations,
                         "cells": "6k^3, log-uniform 10k-4M", "precision": "mixed",
                         "latency": "arrival -> state read back, including mesh preparation "
-                                   "(host face list and geometry, GPU stencils) and queueing"})
+                                   "(vertices and cells on the host; face list, geometry and "
+                                   "stencils on the GPU), registration and queueing"})
 
     # ---- CPU baseline (rank 0) --------------------------------------------------
     cpu = None

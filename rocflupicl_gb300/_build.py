@@ -68,7 +68,7 @@ def build_mesh(force: bool = False) -> Path:
 
 GPU_UNITS = [
     # (source, extra nvcc flags)
-    ("rfgpu_host.cu", []),
+    ("rfgpu_host.cu", ["-Xcompiler", "-fopenmp"]),  # registration loops on host threads
     ("rfgpu_fp64.cu", ["--fmad=false"]),
     ("rfgpu_mixed.cu", []),
     ("rfgpu_meshbuild.cu", ["--fmad=false"]),
@@ -92,7 +92,7 @@ def build_gpu(force: bool = False) -> Path:
                      "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr",
                      f"-I{INCLUDE}", f"-I{CSRC}", *extra, "-c", str(CSRC / s), "-o", str(obj)])
     _run_all(cmds)
-    _run_all([[nvcc, GENCODE, "-shared", *map(str, objs), "-o", str(lib), "-lcudart"]])
+    _run_all([[nvcc, GENCODE, "-shared", *map(str, objs), "-o", str(lib), "-lcudart", "-lgomp"]])
     return lib
 
 

@@ -244,20 +244,30 @@ int check_desc(const rfgpu_region_desc_t *d) {
     for (int k = 0; k < b.nCellsRecv; ++k)  // virtual cells
       if (b.icgRecv[k] <= d->nCells || b.icgRecv[k] > N) return RFGPU_ERR_ARG;
   }
+  int bad = 0;
+#pragma omp parallel for schedule(static) reduction(| : bad)
   for (int f = 0; f < d->nFaces; ++f)
     for (int k = 0; k < 2; ++k) {
       int c = d->f2c[(long long)f * d->f2cLd + k];
-      if (c < 1 || c > N) return RFGPU_ERR_ARG;
+      if (c < 1 || c > N) bad = 1;
     }
+  if (bad) return RFGPU_ERR_ARG;
   if (d->c2csOffsets[0] != 0) return RFGPU_ERR_ARG;
+#pragma omp parallel for schedule(static) reduction(| : bad)
   for (long long c = 0; c < N; ++c)
-    if (d->c2csOffsets[c + 1] < d->c2csOffsets[c]) return RFGPU_ERR_ARG;
-  for (long long e = 0; e < d->c2csOffsets[N]; ++e)
-    if (d->c2csMembers[e] < 1 || d->c2csMembers[e] > N) return RFGPU_ERR_ARG;
+    if (d->c2csOffsets[c + 1] < d->c2csOffsets[c]) bad = 1;
+  if (bad) return RFGPU_ERR_ARG;
+  const long long nMem = d->c2csOffsets[N];
+#pragma omp parallel for schedule(static) reduction(| : bad)
+  for (long long e = 0; e < nMem; ++e)
+    if (d->c2csMembers[e] < 1 || d->c2csMembers[e] > N) bad = 1;
+  if (bad) return RFGPU_ERR_ARG;
   // stencils are at most 10x the minimum size (RFLU_ModStencilsCells.F90:2865-2873)
   // in the reference; the engine stages up to 400 members per cell on chip
+#pragma omp parallel for schedule(static) reduction(| : bad)
   for (long long c = 0; c < N; ++c)
-    if (d->c2csOffsets[c + 1] - d->c2csOffsets[c] > 400) return RFGPU_ERR_UNSUPPORTED;
+    if (d->c2csOffsets[c + 1] - d->c2csOffsets[c] > 400) bad = 1;
+  if (bad) return RFGPU_ERR_UNSUPPORTED;
   for (int ip = 0; ip < d->nPatches; ++ip)
     for (int b = 0; b < d->patches[ip].nBFaces; ++b)
       if (d->patches[ip].bf2c[b] < 1 || d->patches[ip].bf2c[b] > N) return RFGPU_ERR_ARG;
@@ -266,7 +276,11 @@ int check_desc(const rfgpu_region_desc_t *d) {
 
 template <typename R>
 std::vector<R> cast(const std::vector<double> &v) {
-  return std::vector<R>(v.begin(), v.end());
+  std::vector<R> out(v.size());
+  const long long n = (long long)v.size();
+#pragma omp parallel for schedule(static)
+  for (long long i = 0; i < n; ++i) out[i] = (R)v[i];
+  return out;
 }
 
 template <typename R>
@@ -372,6 +386,7 @@ Order locality_order(const rfgpu_region_desc_t *d) {
   const double scale = ext > 0.0 ? 2097151.0 / ext : 0.0;
   std::vector<unsigned long long> key(N), key2(N);
   std::vector<int> idx(N), idx2(N);
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < N; ++c) {
     unsigned long long m = 0;
     for (int k = 0; k < 3; ++k) {
@@ -452,6 +467,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.ph = ph;
   // ---- cells
   std::vector<double> cofg(3 * (size_t)N), vol(N), epsq(N), moms(6 * (size_t)N);
+#pragma omp parallel for schedule(static)
   for (int c = 0; c < N; ++c) {
     const size_t oc = (size_t)o.oc(c);
     for (int k = 0; k < 3; ++k) cofg[(size_t)k * N + c] = d->cofg[3 * oc + k];
@@ -464,6 +480,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.vol = M.upload(vol, s);
   {
     std::vector<float> iv(N);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; ++c) iv[c] = (float)(1.0 / vol[c]);
     g.ivolF = M.upload(iv, s);
   }
@@ -473,6 +490,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   // 1029-1042, 1064-1076 expanded): cwt = Axx, Axy, Axz, Ayy, Ayz, Azz
   if (sizeof(R) == 4) {
     std::vector<double> cw(6 * (size_t)N);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; ++c) {
       const double *mo = d->xyzMoms + 10 * (size_t)o.oc(c);
       double c11 = 1.0 / mo[0], c22 = 1.0 / mo[2], c33 = 1.0 / mo[5];
@@ -492,10 +510,12 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   // ---- stencil SELL
   {
     std::vector<int> cnt(N);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; ++c) cnt[c] = d->c2csOffsets[o.oc(c) + 1] - d->c2csOffsets[o.oc(c)];
     Sell sl;
     sl.build(cnt);
     std::vector<int> idx(sl.total, 0);
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; ++c) {
       const int *mem = d->c2csMembers + d->c2csOffsets[o.oc(c)];
       for (int k = 0; k < cnt[c]; ++k) idx[sl.at(c, k)] = o.nc(mem[k] - 1);  // stored order
@@ -520,6 +540,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   // ---- faces
   std::vector<int> f2c(2 * (size_t)F);
   std::vector<double> fnA(4 * (size_t)F), fdl(3 * (size_t)F), fdr(3 * (size_t)F);
+#pragma omp parallel for schedule(static)
   for (int f = 0; f < F; ++f) {
     const long long of = o.of(f);
     int c1 = o.nc(d->f2c[of * d->f2cLd] - 1), c2 = o.nc(d->f2c[of * d->f2cLd + 1] - 1);
@@ -636,6 +657,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   g.rhs = M.alloc<double>(5 * (size_t)N);
   {
     std::vector<double> recx(8 * (size_t)N, 0.0);  // centroid slots; state filled by k_prim
+#pragma omp parallel for schedule(static)
     for (int c = 0; c < N; ++c)
       for (int k = 0; k < 3; ++k) recx[8 * (size_t)c + 5 + k] = cofg[(size_t)k * N + c];
     g.rec = M.upload(cast<R>(recx), s);
