@@ -663,6 +663,42 @@ __device__ __forceinline__ void dt_block_min(unsigned long long bits, unsigned l
   __syncthreads();
 }
 
+// The per-face terms of cell_dt, shared with the gradient pass that folds the
+// time step into its limiter face loop.
+template <typename R>
+__device__ __forceinline__ R dt_sound(const RegionDev<R> &g, int c, const R r[8]) {
+  const R gg = PC<R>{g.ph}.gvG();
+  return sizeof(R) == 8 ? R(g.dv[2 * g.nCells + c]) : R(sqrtf(float(gg * r[4] / r[0])));
+}
+template <typename R>
+__device__ __forceinline__ void dt_interior_term(const RegionDev<R> &g, int code, const R r0[8],
+                                                 R a0, int nb, const R rn[8], R &acc) {
+  R nrm[4];
+  ld4(g.fnA + 4 * (size_t)(code >> 1), nrm);
+  const R an = dt_sound(g, nb, rn);
+  // the face's c1 values first, as in the reference
+  const bool first = (code & 1) == 0;
+  const R u1 = first ? r0[1] : rn[1], u2 = first ? rn[1] : r0[1];
+  const R v1 = first ? r0[2] : rn[2], v2 = first ? rn[2] : r0[2];
+  const R w1 = first ? r0[3] : rn[3], w2 = first ? rn[3] : r0[3];
+  const R a1 = first ? a0 : an, a2 = first ? an : a0;
+  R vc = R(0.5) * ((u1 + u2) * nrm[0] + (v1 + v2) * nrm[1] + (w1 + w2) * nrm[2]);
+  R as = R(0.5) * (a1 + a2);
+  acc = acc + (fabs(vc - R(0)) + as) * nrm[3];
+}
+template <typename R>
+__device__ __forceinline__ void dt_boundary_term(const RegionDev<R> &g, int code, const R r0[8],
+                                                 R a0, R &acc) {
+  R nrm[4];
+  ld4(g.bfnA + 4 * (size_t)(-code - 1), nrm);
+  R vc = r0[1] * nrm[0] + r0[2] * nrm[1] + r0[3] * nrm[2];
+  acc = acc + (fabs(vc - R(0)) + a0) * nrm[3];
+}
+template <typename R>
+__device__ __forceinline__ double dt_of(const RegionDev<R> &g, int c, R acc) {
+  return sizeof(R) == 8 ? double(R(g.vol[c]) / acc) : double(float(g.vol[c]) / float(acc));
+}
+
 // Local time-step sum of RFLU_TimeStepInviscid (rocflu/RFLU_TimeStepInviscid.F90:
 // 165-297) for one cell, as a gather over its faces in the reference order:
 // sum of (|v_n| + a) * area with face-averaged velocity and sound speed
@@ -671,38 +707,23 @@ __device__ __forceinline__ void dt_block_min(unsigned long long bits, unsigned l
 // FP32 on the mixed path.  Returns dt(c) = vol / sum.
 template <typename R>
 __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R r0[8]) {
-  const int N = g.nCells;
-  const R gg = PC<R>{g.ph}.gvG();
-  const R a0 = sizeof(R) == 8 ? R(g.dv[2 * N + c]) : R(sqrtf(float(gg * r0[4] / r0[0])));
+  const R a0 = dt_sound(g, c, r0);
   R acc = R(0);
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
   for (int k = 0; k < n; ++k) {
     const long long e = e0 + (long long)k * kSlice;
     const int code = g.cfCode[e];
-    R nrm[4];
     if (code >= 0) {
       const int nb = g.cfNb[e];
-      ld4(g.fnA + 4 * (size_t)(code >> 1), nrm);
       R rn[8];
       ld8(g.rec + 8 * (size_t)nb, rn);
-      const R an = sizeof(R) == 8 ? R(g.dv[2 * N + nb]) : R(sqrtf(float(gg * rn[4] / rn[0])));
-      // the face's c1 values first, as in the reference
-      const bool first = (code & 1) == 0;
-      const R u1 = first ? r0[1] : rn[1], u2 = first ? rn[1] : r0[1];
-      const R v1 = first ? r0[2] : rn[2], v2 = first ? rn[2] : r0[2];
-      const R w1 = first ? r0[3] : rn[3], w2 = first ? rn[3] : r0[3];
-      const R a1 = first ? a0 : an, a2 = first ? an : a0;
-      R vc = R(0.5) * ((u1 + u2) * nrm[0] + (v1 + v2) * nrm[1] + (w1 + w2) * nrm[2]);
-      R as = R(0.5) * (a1 + a2);
-      acc = acc + (fabs(vc - R(0)) + as) * nrm[3];
+      dt_interior_term(g, code, r0, a0, nb, rn, acc);
     } else {
-      ld4(g.bfnA + 4 * (size_t)(-code - 1), nrm);
-      R vc = r0[1] * nrm[0] + r0[2] * nrm[1] + r0[3] * nrm[2];
-      acc = acc + (fabs(vc - R(0)) + a0) * nrm[3];
+      dt_boundary_term(g, code, r0, a0, acc);
     }
   }
-  return sizeof(R) == 8 ? double(R(g.vol[c]) / acc) : double(float(g.vol[c]) / float(acc));
+  return dt_of(g, c, acc);
 }
 
 // WLSQ gradients of (rho,u,v,w,p) (RFLU_ComputeGradCellsFast_3D,
@@ -836,16 +857,30 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
         const long long T = g.cfTotal;
         const long long e0 = g.cfOff[c >> 5] + (c & 31);
         const int nf = g.cfCnt[c];
+        // stage 1: the time-step sum rides on this face loop (same faces, same
+        // order and arithmetic as cell_dt)
+        R dtacc = R(0), a0 = R(0);
+        if constexpr (fuseDt) a0 = dt_sound(g, c, r0);
         for (int k = 0; k < nf; ++k) {
           const long long ee = e0 + (long long)k * kSlice;
-          if (g.cfCode[ee] < 0) continue;
+          const int code = g.cfCode[ee];
+          if (code < 0) {
+            if constexpr (fuseDt) dt_boundary_term(g, code, r0, a0, dtacc);
+            continue;
+          }
+          const int nb = g.cfNb[ee];
           R rn[8];
-          ld8(rec + 8 * (size_t)g.cfNb[ee], rn);
+          ld8(rec + 8 * (size_t)nb, rn);
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             vmin[v] = rmin(vmin[v], rn[v]);
             vmax[v] = rmax(vmax[v], rn[v]);
           }
+          if constexpr (fuseDt) dt_interior_term(g, code, r0, a0, nb, rn, dtacc);
+        }
+        if constexpr (fuseDt) {
+          dtbits = (unsigned long long)__double_as_longlong(dt_of(g, c, dtacc));
+          if (c >= g.nAct) dtbits = 0x7FF0000000000000ull;  // actual cells only
         }
         const R epsq = g.epsq[c];
         const int guard = g.ph.venkatGuard;
@@ -870,8 +905,10 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
       out[15] = R(0);
       st16(g.grad + 16 * (size_t)c, out);
       if constexpr (fuseDt) {
-        dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
-        if (c >= regs[tl.region].nAct) dtbits = 0x7FF0000000000000ull;  // actual cells only
+        if (g.ph.reconst != 11) {  // no limiter face loop to ride on
+          dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
+          if (c >= regs[tl.region].nAct) dtbits = 0x7FF0000000000000ull;
+        }
       }
     }
     if constexpr (fuseDt) dt_block_min<R>(dtbits, smin, g.dtBits);
