@@ -280,6 +280,27 @@ def from_files(grid_path: str, flow_path: str, bcs: List[PatchBC],
                 meta={"time": fl.time, "grid": grid_path, "flow": flow_path})
 
 
+def from_case_files(grid_path: str, flow_path: str, inp_path: str, bc_path: str,
+                    binary: bool = False, endian: str = "<", threads: int = 0,
+                    stencils: str = "host", strict: bool = True):
+    """A case from a RocfluMP case's files: the grid and flow files, the `.inp`
+    numerics and the `.bc` boundary conditions (rocflupicl_gb300.rfluinput).
+    Returns (case, CaseInput, unsupported settings); strict raises ValueError
+    when the files ask for anything outside the engine's envelope."""
+    from . import rfluinput as RI
+    from . import rfluio as IO
+    ci = RI.read_inp(inp_path)
+    g = IO.read_grid_binary(grid_path, endian) if binary else IO.read_grid_ascii(grid_path)
+    bcs, bad_bc = RI.read_bc(bc_path, len(g.patches), ci.order_bfaces)
+    bad = ci.unsupported + bad_bc
+    if strict and bad:
+        raise ValueError("settings outside the engine's envelope: " + "; ".join(bad))
+    c = from_files(grid_path, flow_path, bcs, ci.numerics, binary, endian, threads, stencils)
+    c.meta["dt_imposed"], c.meta["max_time"] = ci.dt_imposed, ci.max_time
+    c.t_end = ci.max_time
+    return c, ci, bad
+
+
 def write_flow(path: str, cv: np.ndarray, time: float = 0.0, binary: bool = False,
                endian: str = "<") -> None:
     """Write a state (nCells, 5) as the reference's v2 flow file."""
