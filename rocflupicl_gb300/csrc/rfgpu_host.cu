@@ -126,6 +126,10 @@ struct rfgpu_region_s {
   std::vector<BorderH> borders;
   double *bbuf = nullptr;                   // border buffer, 5 x the largest border
   cudaEvent_t evA = nullptr, evB = nullptr; // ordering of border copies between streams
+  // mixed-path transfers: copies on xstream, conversions on stream, chunk by
+  // chunk, so a chunk's copy overlaps its neighbour's conversion
+  cudaStream_t xstream = nullptr;
+  cudaEvent_t xev[9] = {};
   int rkScheme = 2, nSteps = 3, spaceOrder = 2, reconst = 11;
   cudaStream_t stream = nullptr;
   DevAlloc mem;
@@ -705,17 +709,58 @@ const RegionDev<R> *regs_of(rfgpu_region_s *h) {
   return (const RegionDev<R> *)h->regsDev;
 }
 
+constexpr int kXChunks = 8;  // transfer chunks of the mixed path
+
+// The second stream and events of the chunked transfers, made on first use.
+int transfer_setup(rfgpu_region_s *h) {
+  if (h->xstream) return RFGPU_OK;
+  if (cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  for (cudaEvent_t &e : h->xev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return RFGPU_ERR_CUDA;
+  return RFGPU_OK;
+}
+
+// Tiles [t0, t1) of chunk k, and its host cells [c0, c1).
+void chunk_range(const rfgpu_region_s *h, int k, int nk, int &t0, int &t1, size_t &c0,
+                 size_t &c1) {
+  const int nT = h->work.nCellTiles;
+  t0 = (int)((long long)nT * k / nk);
+  t1 = (int)((long long)nT * (k + 1) / nk);
+  c0 = (size_t)t0 * h->work.block;
+  c1 = std::min((size_t)t1 * h->work.block, (size_t)h->nCells);
+}
+
 int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
   cudaStream_t s = h->stream;
   const int N = h->nCells;
-  if (h->prec) {  // mixed: DMA copies into the staging buffers, one fused conversion pass
-    if (cudaMemcpyAsync(h->stage, cv, 5 * (size_t)N * 8, cudaMemcpyHostToDevice, s) != cudaSuccess)
+  if (h->prec) {  // mixed: DMA copies into the staging buffers, fused conversion, chunk by chunk
+    int rc = transfer_setup(h);
+    if (rc != RFGPU_OK) return rc;
+    cudaStream_t x = h->xstream;
+    // the copies start after the work already queued on the region's stream
+    if (cudaEventRecord(h->xev[kXChunks], s) != cudaSuccess ||
+        cudaStreamWaitEvent(x, h->xev[kXChunks], 0) != cudaSuccess)
       return RFGPU_ERR_CUDA;
-    if (dv && cudaMemcpyAsync(h->stage2, dv, 3 * (size_t)N * 8, cudaMemcpyHostToDevice, s) !=
-                  cudaSuccess)
-      return RFGPU_ERR_CUDA;
-    launch_upload_direct<float>(regs_of<float>(h), h->work, h->stage, dv ? h->stage2 : nullptr, s);
-    h->launches++;
+    const int nk = std::min(kXChunks, std::max(1, h->work.nCellTiles));
+    for (int k = 0; k < nk; ++k) {
+      int t0, t1;
+      size_t c0, c1;
+      chunk_range(h, k, nk, t0, t1, c0, c1);
+      if (t1 <= t0) continue;
+      if (cudaMemcpyAsync(h->stage + 5 * c0, cv + 5 * c0, 5 * (c1 - c0) * 8,
+                          cudaMemcpyHostToDevice, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (dv && cudaMemcpyAsync(h->stage2 + 3 * c0, dv + 3 * c0, 3 * (c1 - c0) * 8,
+                                cudaMemcpyHostToDevice, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (cudaEventRecord(h->xev[k], x) != cudaSuccess ||
+          cudaStreamWaitEvent(s, h->xev[k], 0) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      launch_upload_direct<float>(regs_of<float>(h), h->work, t0, t1 - t0, h->stage,
+                                  dv ? h->stage2 : nullptr, s);
+      h->launches++;
+    }
     return cuda_rc(cudaGetLastError());
   }
   // FP64 path: staged copies into the SoA state, then records (and dv) from it
@@ -845,6 +890,13 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   rc = upload_state(h, d->cv, d->dv);
   if (rc == RFGPU_OK) rc = cuda_rc(cudaStreamSynchronize(h->stream));
   if (rc != RFGPU_OK) {
+    cudaStreamSynchronize(h->stream);
+    if (h->xstream) {
+      cudaStreamSynchronize(h->xstream);
+      for (cudaEvent_t e : h->xev)
+        if (e) cudaEventDestroy(e);
+      cudaStreamDestroy(h->xstream);
+    }
     h->mem.free_all();
     cudaStreamDestroy(h->stream);
     delete h;
@@ -860,6 +912,12 @@ int rfgpu_region_destroy(rfgpu_region_t h) {
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->evA) cudaEventDestroy(h->evA);
   if (h->evB) cudaEventDestroy(h->evB);
+  if (h->xstream) {
+    cudaStreamSynchronize(h->xstream);
+    for (cudaEvent_t e : h->xev)
+      if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(h->xstream);
+  }
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
   h->prof.destroy();
@@ -943,18 +1001,32 @@ int rfgpu_residual(rfgpu_region_t h, double *rhs) {
 int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
   if (!h) return RFGPU_ERR_ARG;
   const int N = h->nCells;
-  if (h->prec) {  // mixed: one fused pass into the staging buffers, then the DMA copies
+  if (h->prec) {  // mixed: fused conversion into the staging buffers and DMA copies, chunk by chunk
     if (!cv && !dv) return RFGPU_OK;
-    launch_download_direct<float>(regs_of<float>(h), h->work, cv ? h->stage : nullptr,
-                                  dv ? h->stage2 : nullptr, h->stream);
-    h->launches++;
-    if (cv && cudaMemcpyAsync(cv, h->stage, 5 * (size_t)N * 8, cudaMemcpyDeviceToHost,
-                              h->stream) != cudaSuccess)
-      return RFGPU_ERR_CUDA;
-    if (dv && cudaMemcpyAsync(dv, h->stage2, 3 * (size_t)N * 8, cudaMemcpyDeviceToHost,
-                              h->stream) != cudaSuccess)
-      return RFGPU_ERR_CUDA;
-    return cuda_rc(cudaStreamSynchronize(h->stream));
+    int rc = transfer_setup(h);
+    if (rc != RFGPU_OK) return rc;
+    cudaStream_t x = h->xstream;
+    const int nk = std::min(kXChunks, std::max(1, h->work.nCellTiles));
+    for (int k = 0; k < nk; ++k) {
+      int t0, t1;
+      size_t c0, c1;
+      chunk_range(h, k, nk, t0, t1, c0, c1);
+      if (t1 <= t0) continue;
+      launch_download_direct<float>(regs_of<float>(h), h->work, t0, t1 - t0,
+                                    cv ? h->stage : nullptr, dv ? h->stage2 : nullptr, h->stream);
+      h->launches++;
+      if (cudaEventRecord(h->xev[k], h->stream) != cudaSuccess ||
+          cudaStreamWaitEvent(x, h->xev[k], 0) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (cv && cudaMemcpyAsync(cv + 5 * c0, h->stage + 5 * c0, 5 * (c1 - c0) * 8,
+                                cudaMemcpyDeviceToHost, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (dv && cudaMemcpyAsync(dv + 3 * c0, h->stage2 + 3 * c0, 3 * (c1 - c0) * 8,
+                                cudaMemcpyDeviceToHost, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+    }
+    if (cudaGetLastError() != cudaSuccess) return RFGPU_ERR_CUDA;
+    return cuda_rc(cudaStreamSynchronize(x));
   }
   if (cv) {
     launch_soa_to_aos(h->rd64.cv, h->stage, N, 5, h->cellNew, h->stream);

@@ -180,14 +180,15 @@ struct Prof {
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
 // Mixed path: fused conversion between the Fortran images cv(5,N), dv(3,N)
-// (host numbering, in device staging buffers) and the device state; either
-// buffer may be null where the call allows it.
+// (host numbering, in device staging buffers) and the device state, for the
+// host cells of cell tiles [firstTile, firstTile + nTiles); either buffer may
+// be null where the call allows it.
 template <typename R>
-void launch_upload_direct(const RegionDev<R> *regs, const Work &w, const double *cvH,
-                          const double *dvH, cudaStream_t s);
+void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
+                          const double *cvH, const double *dvH, cudaStream_t s);
 template <typename R>
-void launch_download_direct(const RegionDev<R> *regs, const Work &w, double *cvH, double *dvH,
-                            cudaStream_t s);
+void launch_download_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
+                            double *cvH, double *dvH, cudaStream_t s);
 template <typename R>
 int configure_grad_smem(int maxW, int block);
 // Halo exchange: the links of a coupled batch (regs indexed by region), or

@@ -1923,17 +1923,18 @@ int configure_grad_smem(int maxW, int block) {
 }
 
 template <typename R>
-void launch_upload_direct(const RegionDev<R> *regs, const Work &w, const double *cvH,
-                          const double *dvH, cudaStream_t s) {
-  int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
-  if (grid > 0) k_upload_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, cvH, dvH);
+void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
+                          const double *cvH, const double *dvH, cudaStream_t s) {
+  int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
+  if (grid > 0)
+    k_upload_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles + firstTile, nTiles, cvH, dvH);
 }
 template <typename R>
-void launch_download_direct(const RegionDev<R> *regs, const Work &w, double *cvH, double *dvH,
-                            cudaStream_t s) {
-  int grid = w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles;
+void launch_download_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
+                            double *cvH, double *dvH, cudaStream_t s) {
+  int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
   if (grid > 0)
-    k_download_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, cvH, dvH);
+    k_download_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles + firstTile, nTiles, cvH, dvH);
 }
 
 // ---- residual without device allocation ---------------------------------------
@@ -2062,10 +2063,10 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
 
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
-  template void launch_upload_direct<R>(const RegionDev<R> *, const Work &, const double *,   \
-                                        const double *, cudaStream_t);                        \
-  template void launch_download_direct<R>(const RegionDev<R> *, const Work &, double *,       \
-                                          double *, cudaStream_t);                            \
+  template void launch_upload_direct<R>(const RegionDev<R> *, const Work &, int, int,         \
+                                        const double *, const double *, cudaStream_t);        \
+  template void launch_download_direct<R>(const RegionDev<R> *, const Work &, int, int,       \
+                                          double *, double *, cudaStream_t);                  \
   template int configure_grad_smem<R>(int, int);                                              \
   template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
                                            const Work &, int, R *, double *, cudaStream_t);    \
