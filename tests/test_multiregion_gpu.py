@@ -261,3 +261,13 @@ def test_partition_variants_bitwise_oracle(name):
     if name != "inflow":
         assert all(x == t for x in times)
     assert st == 0 and sts == [0] * len(parts)
+
+
+def test_residual_noalloc_with_virtual_cells():
+    p = P.partition_case(tube(n=12), 2)[1]
+    r = E.Region(p)
+    a = r.residual()
+    b = r.residual_noalloc()
+    r.close()
+    assert np.array_equal(a, b)
+    assert not np.any(b[p.mesh.nCells:])

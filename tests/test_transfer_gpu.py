@@ -44,3 +44,31 @@ def test_pinned_and_pageable_transfers_agree(order, with_dv):
         p.close()
     direct.close()
     staged.close()
+
+
+@pytest.mark.parametrize("dims", [(1, 1, 1), (5, 3, 7), (40, 7, 3), (50, 9, 11)])
+@pytest.mark.parametrize("order", [E.ORDER_HOST, E.ORDER_LOCALITY])
+def test_chunked_upload_download_round_trip(dims, order):
+    """Upload then download with no step between: the transfers run in up to 8
+    chunks of cell tiles (a region smaller than 8 tiles in fewer, the last tile
+    partial); cv comes back as the float-float split of the input joined again,
+    bit for bit, for every cell."""
+    nx, ny, nz = dims
+    c = K.tet_shock_box(nx, ny=ny, nz=nz, seed=5,
+                        numerics=K.Numerics(precision=K.PREC_MIXED, venkatGuard=1))
+    r = E.Region(c, cell_order=order)
+    q = np.ascontiguousarray(c.cv, np.float64)
+    hi = q.astype(np.float32)
+    lo = (q - hi.astype(np.float64)).astype(np.float32)
+    want = hi.astype(np.float64) + lo.astype(np.float64)
+    for pinned in (False, True):
+        if pinned:
+            src = E.PinnedArray(q.shape)
+            src.array[:] = q
+            r.upload(src.array)
+        else:
+            r.upload(q.copy())
+        cv, dv = r.download()
+        assert np.array_equal(cv, want)
+        assert np.allclose(dv, K.eos_dv(c.numerics, want), rtol=1e-13, atol=0)
+    r.close()
