@@ -147,7 +147,6 @@ struct rfgpu_region_s {
   long long perStep = 0;
   ProfState prof;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
-  int maxStW = 0;
   const int *cellNew = nullptr, *cellOld = nullptr;  // device numbering (null: host's)
 };
 
@@ -528,8 +527,6 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.stCnt = M.upload(sl.cnt, s);
     g.stIdx = M.upload(idx, s);
     g.stTotal = sl.total;
-    for (size_t q = 0; q + 1 < sl.off.size(); ++q)
-      h->maxStW = std::max(h->maxStW, (int)((sl.off[q + 1] - sl.off[q]) / kSlice));
     if (sizeof(R) == 8) {
       // weights on the device with the reference arithmetic (FP64 unit)
       double *dcofg = M.alloc<double>(cofg.size());
@@ -874,10 +871,7 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
     h->faceTiles = h->mem.upload(ft, h->stream);
     h->bfaceTiles = h->mem.upload(bt, h->stream);
     h->work = Work{h->cellTiles, h->faceTiles, h->bfaceTiles, (int)ct.size(), (int)ft.size(),
-                   (int)bt.size(), 0, block, 1, h->maxStW};
-    if ((h->prec ? configure_grad_smem<float>(h->maxStW, block)
-                 : configure_grad_smem<double>(h->maxStW, block)) != 0)
-      throw std::bad_alloc();
+                   (int)bt.size(), 0, block, 1};
     h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
     if (h->prec) h->stage2 = h->mem.alloc<double>(3 * (size_t)h->nCells);
     cudaStreamSynchronize(h->stream);
@@ -1262,10 +1256,7 @@ int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    int maxW = 0;
-    for (int i = 0; i < n; ++i) maxW = std::max(maxW, regions[i]->maxStW);
-    b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n,
-                   maxW};
+    b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n};
     if (coupled) {
       b->work.coupled = 1;
       b->work.halo = links.empty() ? nullptr : b->mem.upload(links, b->stream);

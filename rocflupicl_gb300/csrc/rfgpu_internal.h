@@ -135,7 +135,6 @@ struct Work {
   int grid;     // blocks per launch (persistent when smaller than the tile count)
   int block;    // items per tile == threads per block
   int nRegions;
-  int maxStW;   // widest stencil SELL slice over the regions (shared-memory staging)
   // coupled batches: one time step for all regions, and the halo exchange
   // after every stage's update
   int coupled;
@@ -189,8 +188,6 @@ void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile
 template <typename R>
 void launch_download_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
                             double *cvH, double *dvH, cudaStream_t s);
-template <typename R>
-int configure_grad_smem(int maxW, int block);
 // Halo exchange: the links of a coupled batch (regs indexed by region), or
 // one border between two handles (send cells of src -> receive cells of dst,
 // device numbering).  Copies the conserved state and rebuilds the received

@@ -1912,16 +1912,6 @@ void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int 
   }
 }
 
-// Shared-memory configuration of the gradient pass.  Staging the stencil
-// indices in shared memory was measured slower (the carve-out shrinks the L1
-// that serves the neighbour-record gathers), so none is requested.
-template <typename R>
-int configure_grad_smem(int maxW, int block) {
-  (void)maxW;
-  (void)block;
-  return 0;  // the gradient pass keeps L1 for record gathers: no dynamic smem
-}
-
 template <typename R>
 void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
                           const double *cvH, const double *dvH, cudaStream_t s) {
@@ -2067,7 +2057,6 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
                                         const double *, const double *, cudaStream_t);        \
   template void launch_download_direct<R>(const RegionDev<R> *, const Work &, int, int,       \
                                           double *, double *, cudaStream_t);                  \
-  template int configure_grad_smem<R>(int, int);                                              \
   template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
                                            const Work &, int, R *, double *, cudaStream_t);    \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
