@@ -272,6 +272,69 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 // sectors.  ld8/ld4 read through the non-coherent path and are for data no
 // thread writes during the kernel; ld8_rw is the coherent form for a thread's
 // own record that the same kernel rewrites.
+// Read-once streams (per-face and per-cell arrays a pass reads exactly once):
+// with H = 1 loaded L1::evict_first so L1 keeps the gathered records the pass
+// reuses; H = 0 plain loads.  lds_rw is the coherent form for data the same
+// kernel later overwrites (the thread's own state rows).
+#ifndef RF_HINT_G
+#define RF_HINT_G 0   // gradient pass: cell->face lists, WLSQ factor terms
+#endif
+#ifndef RF_HINT_F
+#define RF_HINT_F 0   // face pass: f2c, normals, reconstruction offsets
+#endif
+#ifndef RF_HINT_U
+#define RF_HINT_U 0   // update pass: face codes, state rows, increments, 1/vol
+#endif
+template <int H>
+__device__ __forceinline__ int lds(const int *__restrict__ p) {
+  if constexpr (H) {
+    int v;
+    asm("ld.global.nc.L1::evict_first.s32 %0, [%1];" : "=r"(v) : "l"(p));
+    return v;
+  } else {
+    return *p;
+  }
+}
+template <int H>
+__device__ __forceinline__ float lds(const float *__restrict__ p) {
+  if constexpr (H) {
+    float v;
+    asm("ld.global.nc.L1::evict_first.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+  } else {
+    return *p;
+  }
+}
+template <int H>
+__device__ __forceinline__ double lds(const double *__restrict__ p) {
+  if constexpr (H) {
+    double v;
+    asm("ld.global.nc.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+  } else {
+    return *p;
+  }
+}
+template <int H>
+__device__ __forceinline__ float lds_rw(const float *p) {
+  if constexpr (H) {
+    float v;
+    asm volatile("ld.global.L1::evict_first.f32 %0, [%1];" : "=f"(v) : "l"(p));
+    return v;
+  } else {
+    return *p;
+  }
+}
+
+// The stencil-index stream of the mixed gradient pass: each index is read
+// once, so it is loaded L1::evict_first and leaves L1 to the neighbour records
+// the member gathers reuse (measured 1.955 -> 1.924 ms per pass on the
+// 128^3 tet box; evict_last on the record gathers themselves changed nothing).
+__device__ __forceinline__ int ld_index(const int *__restrict__ p) {
+  int v;
+  asm("ld.global.nc.L1::evict_first.s32 %0, [%1];" : "=r"(v) : "l"(p));
+  return v;
+}
 __device__ __forceinline__ void ld8(const float *__restrict__ p, float v[8]) {
   asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
       : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]), "=f"(v[4]), "=f"(v[5]), "=f"(v[6]),
@@ -305,6 +368,22 @@ __device__ __forceinline__ void ld8_rw(const double *p, double v[8]) {
 __device__ __forceinline__ void ld4(const float *__restrict__ p, float v[4]) {
   float4 a = *reinterpret_cast<const float4 *>(p);
   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+}
+template <int H>
+__device__ __forceinline__ void ld4s(const float *__restrict__ p, float v[4]) {
+  if constexpr (H)
+    asm("ld.global.nc.L1::evict_first.v4.f32 {%0,%1,%2,%3}, [%4];"
+        : "=f"(v[0]), "=f"(v[1]), "=f"(v[2]), "=f"(v[3]) : "l"(p));
+  else
+    ld4(p, v);
+}
+template <int H>
+__device__ __forceinline__ void ld4s(const double *__restrict__ p, double v[4]) {
+  if constexpr (H)
+    asm("ld.global.nc.L1::evict_first.v4.f64 {%0,%1,%2,%3}, [%4];"
+        : "=d"(v[0]), "=d"(v[1]), "=d"(v[2]), "=d"(v[3]) : "l"(p));
+  else
+    ld4(p, v);
 }
 __device__ __forceinline__ void st8(float *p, const float v[8]) {
   asm volatile("st.global.v8.f32 [%0], {%1,%2,%3,%4,%5,%6,%7,%8};" ::"l"(p), "f"(v[0]), "f"(v[1]),
@@ -827,17 +906,20 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
         for (; k + RF_GRAD_UNROLL <= n; k += RF_GRAD_UNROLL) {
           R ra[RF_GRAD_UNROLL][8];
 #pragma unroll
-          for (int u = 0; u < RF_GRAD_UNROLL; ++u) ld8(rec + 8 * (size_t)sidx[(k + u) * kSlice], ra[u]);
+          for (int u = 0; u < RF_GRAD_UNROLL; ++u)
+            ld8(rec + 8 * (size_t)ld_index(sidx + (k + u) * kSlice), ra[u]);
 #pragma unroll
           for (int u = 0; u < RF_GRAD_UNROLL; ++u) member(ra[u]);
         }
         for (; k < n; ++k) {
           R ra[8];
-          ld8(rec + 8 * (size_t)sidx[k * kSlice], ra);
+          ld8(rec + 8 * (size_t)ld_index(sidx + k * kSlice), ra);
           member(ra);
         }
-        const R axx = g.cwt[c], axy = g.cwt[N + c], axz = g.cwt[2 * N + c];
-        const R ayy = g.cwt[3 * N + c], ayz = g.cwt[4 * N + c], azz = g.cwt[5 * N + c];
+        const R axx = lds<RF_HINT_G>(g.cwt + c), axy = lds<RF_HINT_G>(g.cwt + N + c),
+                axz = lds<RF_HINT_G>(g.cwt + 2 * N + c);
+        const R ayy = lds<RF_HINT_G>(g.cwt + 3 * N + c), ayz = lds<RF_HINT_G>(g.cwt + 4 * N + c),
+                azz = lds<RF_HINT_G>(g.cwt + 5 * N + c);
 #pragma unroll
         for (int v = 0; v < 5; ++v) {
           const R sx = acc[3 * v], sy = acc[3 * v + 1], sz = acc[3 * v + 2];
@@ -868,7 +950,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
             if constexpr (fuseDt) dt_boundary_term(g, code, r0, a0, dtacc);
             continue;
           }
-          const int nb = g.cfNb[ee];
+          const int nb = lds<RF_HINT_G>(g.cfNb + ee);
           R rn[8];
           ld8(rec + 8 * (size_t)nb, rn);
 #pragma unroll
@@ -882,12 +964,13 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
           dtbits = (unsigned long long)__double_as_longlong(dt_of(g, c, dtacc));
           if (c >= g.nAct) dtbits = 0x7FF0000000000000ull;  // actual cells only
         }
-        const R epsq = g.epsq[c];
+        const R epsq = lds<RF_HINT_G>(g.epsq + c);
         const int guard = g.ph.venkatGuard;
         for (int k = 0; k < nf; ++k) {
           const long long ee = e0 + (long long)k * kSlice;
-          if (g.cfCode[ee] < 0) continue;
-          const R dx = g.cfD[ee], dy = g.cfD[T + ee], dz = g.cfD[2 * T + ee];
+          if (lds<RF_HINT_G>(g.cfCode + ee) < 0) continue;  // its last read
+          const R dx = lds<RF_HINT_G>(g.cfD + ee), dy = lds<RF_HINT_G>(g.cfD + T + ee),
+                  dz = lds<RF_HINT_G>(g.cfD + 2 * T + ee);
 #pragma unroll
           for (int v = 0; v < 5; ++v) {
             R d2 = acc[3 * v] * dx + acc[3 * v + 1] * dy + acc[3 * v + 2] * dz;
@@ -979,9 +1062,9 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
     const int f = tl.first + threadIdx.x;
     const int F = g.nFaces;
     if (f >= F) continue;
-    const int c1 = g.f2c[f], c2 = g.f2c[F + f];
+    const int c1 = lds<RF_HINT_F>(g.f2c + f), c2 = lds<RF_HINT_F>(g.f2c + F + f);
     R nrm[4];
-    ld4(g.fnA + 4 * (size_t)f, nrm);
+    ld4s<RF_HINT_F>(g.fnA + 4 * (size_t)f, nrm);
     R r1[8], r2[8];
     ld8(g.rec + 8 * (size_t)c1, r1);
     ld8(g.rec + 8 * (size_t)c2, r2);
@@ -991,9 +1074,11 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
     if (g.ph.spaceOrder > 1) {
       R G[16];
       ld16(g.grad + 16 * (size_t)c1, G);
-      reconstruct(G, g.fdl[f], g.fdl[F + f], g.fdl[2 * F + f], L);
+      reconstruct(G, lds<RF_HINT_F>(g.fdl + f), lds<RF_HINT_F>(g.fdl + F + f),
+                  lds<RF_HINT_F>(g.fdl + 2 * F + f), L);
       ld16(g.grad + 16 * (size_t)c2, G);
-      reconstruct(G, g.fdr[f], g.fdr[F + f], g.fdr[2 * F + f], Rt);
+      reconstruct(G, lds<RF_HINT_F>(g.fdr + f), lds<RF_HINT_F>(g.fdr + F + f),
+                  lds<RF_HINT_F>(g.fdr + 2 * F + f), Rt);
     }
     R flx[8];
     face_riemann(g, c1, c2, L, Rt, irl, irr, nrm, flx);
@@ -1383,19 +1468,20 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   if (a.update) {
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-      qh[j] = cvF[(size_t)j * N + c];
-      ql[j] = cvF[(size_t)(5 + j) * N + c];
+      qh[j] = lds_rw<RF_HINT_U>(cvF + (size_t)j * N + c);
+      ql[j] = lds_rw<RF_HINT_U>(cvF + (size_t)(5 + j) * N + c);
     }
 #pragma unroll
-    for (int j = 0; j < 5; ++j) rsOld[j] = (is > 1) ? g.rhsSumF[j * N + c] : 0.f;
+    for (int j = 0; j < 5; ++j)
+      rsOld[j] = (is > 1) ? lds_rw<RF_HINT_U>(g.rhsSumF + j * N + c) : 0.f;
     ld8_rw(g.rec + 8 * (size_t)c, r);
-    ivol = g.ivolF[c];
+    ivol = lds<RF_HINT_U>(g.ivolF + c);
   }
   float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
   for (int k = 0; k < n; ++k) {
-    const int code = g.cfCode[e0 + (long long)k * kSlice];
+    const int code = lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice);
     float fl[8];
     if (code >= 0) {
       ld8(g.flux + 8 * (size_t)(code >> 1), fl);
