@@ -276,14 +276,17 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 // with H = 1 loaded L1::evict_first so L1 keeps the gathered records the pass
 // reuses; H = 0 plain loads.  lds_rw is the coherent form for data the same
 // kernel later overwrites (the thread's own state rows).
+// Measured on the 128^3 tet box (mixed): update pass 0.650 -> 0.636 ms with
+// its hint, gradient pass 1.928 -> 1.925 ms, face pass unchanged (0.636 ms),
+// so the face pass keeps plain loads.
 #ifndef RF_HINT_G
-#define RF_HINT_G 0   // gradient pass: cell->face lists, WLSQ factor terms
+#define RF_HINT_G 1   // gradient pass: cell->face lists, WLSQ factor terms
 #endif
 #ifndef RF_HINT_F
 #define RF_HINT_F 0   // face pass: f2c, normals, reconstruction offsets
 #endif
 #ifndef RF_HINT_U
-#define RF_HINT_U 0   // update pass: face codes, state rows, increments, 1/vol
+#define RF_HINT_U 1   // update pass: face codes, state rows, increments, 1/vol
 #endif
 template <int H>
 __device__ __forceinline__ int lds(const int *__restrict__ p) {
