@@ -197,6 +197,19 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv);
 /* Restart / host edits: cv(5,nCellsTot); dv NULL recomputes dv from cv. */
 int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv);
 
+/* One time step of a state the host keeps: the body of the time-step loop of
+ * rocflu/RFLU_TimeStepping.F90:458-520 (dt, the nrkSteps stages of
+ * libfloflu/RungeKuttaMP.F90, time += dtMin) for a caller whose cv lives in its
+ * own arrays.  cv(5,nCells) is read and overwritten with the new state; dv
+ * (3,nCells) is output only, or NULL.  Results equal rfgpu_upload(cv, NULL) +
+ * rfgpu_step + rfgpu_download(cv, dv) bit for bit; on the mixed path at second
+ * order the copies overlap the step (the first stage's gradient pass starts on
+ * the cells whose neighbourhoods have arrived, the last stage's update hands
+ * cells back as they finish).  Synchronous; pinned host memory lets the copies
+ * run at full rate.  Regions with borders: RFGPU_ERR_UNSUPPORTED. */
+int rfgpu_step_host(rfgpu_region_t h, double *cv, double *dv, double cfl, double dtImposed,
+                    double dtMinLimit, double endTime);
+
 /* Limited gradients of the last residual/stage: grad(3,5,nCellsTot). */
 int rfgpu_download_grad(rfgpu_region_t h, double *grad);
 

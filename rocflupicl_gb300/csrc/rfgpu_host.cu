@@ -130,6 +130,20 @@ struct rfgpu_region_s {
   // chunk, so a chunk's copy overlaps its neighbour's conversion
   cudaStream_t xstream = nullptr;
   cudaEvent_t xev[9] = {};
+  // rfgpu_step_host (mixed path): cell tiles grouped by transfer phase, made on
+  // first use; phOff[0] gradient phases over phGrad, phOff[1] update phases over phUpd
+  Tile *phGrad = nullptr, *phUpd = nullptr;
+  int phOff[2][9] = {};
+  int phN = 0;
+  // mixed-path transfers: the device cells of each chunk in ascending device
+  // order (xList[xOff[k] .. xOff[k+1])), so the conversions touch the device
+  // state coalesced
+  int *xList = nullptr;
+  int xOff[9] = {};
+  // rfgpu_step_host: the upload's conversions run on their own stream, beside
+  // the first stage's gradient phases on the region's stream
+  cudaStream_t cstream = nullptr;
+  cudaEvent_t cev[9] = {};
   int rkScheme = 2, nSteps = 3, spaceOrder = 2, reconst = 11;
   cudaStream_t stream = nullptr;
   DevAlloc mem;
@@ -708,16 +722,6 @@ const RegionDev<R> *regs_of(rfgpu_region_s *h) {
 
 constexpr int kXChunks = 8;  // transfer chunks of the mixed path
 
-// The second stream and events of the chunked transfers, made on first use.
-int transfer_setup(rfgpu_region_s *h) {
-  if (h->xstream) return RFGPU_OK;
-  if (cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking) != cudaSuccess)
-    return RFGPU_ERR_CUDA;
-  for (cudaEvent_t &e : h->xev)
-    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return RFGPU_ERR_CUDA;
-  return RFGPU_OK;
-}
-
 // Tiles [t0, t1) of chunk k, and its host cells [c0, c1).
 void chunk_range(const rfgpu_region_s *h, int k, int nk, int &t0, int &t1, size_t &c0,
                  size_t &c1) {
@@ -726,6 +730,63 @@ void chunk_range(const rfgpu_region_s *h, int k, int nk, int &t0, int &t1, size_
   t1 = (int)((long long)nT * (k + 1) / nk);
   c0 = (size_t)t0 * h->work.block;
   c1 = std::min((size_t)t1 * h->work.block, (size_t)h->nCells);
+}
+
+int n_chunks(const rfgpu_region_s *h) { return std::min(kXChunks, std::max(1, h->work.nCellTiles)); }
+
+// The second stream, the events and the per-chunk device cell lists of the
+// chunked transfers, made on first use.
+int transfer_setup(rfgpu_region_s *h) {
+  if (h->xstream) return RFGPU_OK;
+  const int N = h->nCells;
+  const int nk = n_chunks(h);
+  std::vector<int> old(N), chunk(N), list(N);
+  if (h->cellOld) {
+    if (cudaMemcpyAsync(old.data(), h->cellOld, (size_t)N * 4, cudaMemcpyDeviceToHost,
+                        h->stream) != cudaSuccess ||
+        cudaStreamSynchronize(h->stream) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+  } else {
+    for (int d = 0; d < N; ++d) old[d] = d;
+  }
+  std::vector<int> cnt(nk + 1, 0);
+  for (int k = 0; k < nk; ++k) {
+    int t0, t1;
+    size_t c0, c1;
+    chunk_range(h, k, nk, t0, t1, c0, c1);
+    for (size_t i = c0; i < c1; ++i) chunk[i] = k;
+  }
+  for (int d = 0; d < N; ++d) cnt[chunk[old[d]] + 1]++;
+  for (int k = 0; k < nk; ++k) cnt[k + 1] += cnt[k];
+  for (int k = 0; k <= nk; ++k) h->xOff[k] = cnt[k];
+  for (int d = 0; d < N; ++d) list[cnt[chunk[old[d]]]++] = d;
+  try {
+    h->xList = h->mem.upload(list, h->stream);
+  } catch (const std::bad_alloc &) {
+    return RFGPU_ERR_NOMEM;
+  }
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  for (cudaEvent_t &e : h->xev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return RFGPU_ERR_CUDA;
+  for (cudaEvent_t &e : h->cev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return RFGPU_ERR_CUDA;
+  return RFGPU_OK;
+}
+
+// Conversions of chunk k between the staged Fortran images and the device state.
+void upload_chunk(rfgpu_region_s *h, int k, const double *cvS, const double *dvS,
+                  cudaStream_t s) {
+  launch_upload_list<float>(regs_of<float>(h), h->xList + h->xOff[k], h->xOff[k + 1] - h->xOff[k],
+                            cvS, dvS, s);
+  h->launches++;
+}
+void download_chunk(rfgpu_region_s *h, int k, double *cvS, double *dvS) {
+  launch_download_list<float>(regs_of<float>(h), h->xList + h->xOff[k],
+                              h->xOff[k + 1] - h->xOff[k], cvS, dvS, h->stream);
+  h->launches++;
 }
 
 int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
@@ -739,7 +800,7 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
     if (cudaEventRecord(h->xev[kXChunks], s) != cudaSuccess ||
         cudaStreamWaitEvent(x, h->xev[kXChunks], 0) != cudaSuccess)
       return RFGPU_ERR_CUDA;
-    const int nk = std::min(kXChunks, std::max(1, h->work.nCellTiles));
+    const int nk = n_chunks(h);
     for (int k = 0; k < nk; ++k) {
       int t0, t1;
       size_t c0, c1;
@@ -754,9 +815,7 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
       if (cudaEventRecord(h->xev[k], x) != cudaSuccess ||
           cudaStreamWaitEvent(s, h->xev[k], 0) != cudaSuccess)
         return RFGPU_ERR_CUDA;
-      launch_upload_direct<float>(regs_of<float>(h), h->work, t0, t1 - t0, h->stage,
-                                  dv ? h->stage2 : nullptr, s);
-      h->launches++;
+      upload_chunk(h, k, h->stage, dv ? h->stage2 : nullptr, s);
     }
     return cuda_rc(cudaGetLastError());
   }
@@ -772,6 +831,140 @@ int upload_state(rfgpu_region_s *h, const double *cv, const double *dv) {
   launch_prim<double>(regs_of<double>(h), h->work, dv ? 0 : 1, s);
   h->launches += dv ? 3 : 2;
   return cuda_rc(cudaGetLastError());
+}
+
+// Groups the cell tiles by transfer phase for rfgpu_step_host, once per region.
+// Gradient phase j holds the tiles whose every gathered record (own, stencil
+// members, face neighbours) travels in chunks 0..j, so it runs as soon as chunk
+// j is converted; update phase k holds the tiles whose first own cell travels
+// in chunk k, so chunk k can go back to the host once update phases 0..k ran.
+int phase_setup(rfgpu_region_s *h) {
+  if (h->phN) return RFGPU_OK;
+  const Work &w = h->work;
+  const int nT = w.nCellTiles;
+  const int nk = n_chunks(h);
+  ChunkMap m{};
+  m.nk = nk;
+  m.block = w.block;
+  for (int k = 0; k < nk; ++k) {
+    int t0, t1;
+    size_t c0, c1;
+    chunk_range(h, k, nk, t0, t1, c0, c1);
+    m.tEnd[k] = t1;
+  }
+  cudaStream_t s = h->stream;
+  int *d = h->mem.alloc<int>(2 * (size_t)std::max(1, nT));
+  std::vector<int> last(nT), first(nT);
+  std::vector<Tile> tiles(nT);
+  if (nT > 0) {
+    if (cudaMemsetAsync(d, 0, (size_t)nT * 4, s) != cudaSuccess ||
+        cudaMemsetAsync(d + nT, 0x7f, (size_t)nT * 4, s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    launch_tile_phases<float>(regs_of<float>(h), w, m, d, d + nT, s);
+    h->launches++;
+    if (cudaMemcpyAsync(last.data(), d, (size_t)nT * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaMemcpyAsync(first.data(), d + nT, (size_t)nT * 4, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(tiles.data(), w.cellTiles, (size_t)nT * sizeof(Tile),
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+  }
+  std::vector<Tile> grad, upd;
+  grad.reserve(nT);
+  upd.reserve(nT);
+  auto clampk = [&](int v) { return std::min(nk - 1, std::max(0, v)); };
+  for (int j = 0; j < nk; ++j) {
+    h->phOff[0][j] = (int)grad.size();
+    h->phOff[1][j] = (int)upd.size();
+    for (int t = 0; t < nT; ++t) {
+      if (clampk(last[t]) == j) grad.push_back(tiles[t]);
+      if (clampk(first[t]) == j) upd.push_back(tiles[t]);
+    }
+  }
+  h->phOff[0][nk] = h->phOff[1][nk] = nT;
+  h->phGrad = h->mem.upload(grad, s);
+  h->phUpd = h->mem.upload(upd, s);
+  if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
+  h->phN = nk;
+  return RFGPU_OK;
+}
+
+// One time step of a host-resident state (mixed path), its transfers
+// overlapped with the step: chunk k of cv goes up on the copy stream while a
+// conversion stream converts chunk k-1 and the region's stream runs the
+// stage-1 gradient phases whose records have all arrived; the last stage's
+// update runs phase by phase, each followed by its chunk's conversion and copy
+// back.  The arithmetic per cell is that of rfgpu_upload + rfgpu_step +
+// rfgpu_download.  Second order only (the stage-1 gradient pass carries the
+// time step).
+int step_host_mixed(rfgpu_region_s *h, double *cv, double *dv, const DtArgs &da) {
+  int rc = transfer_setup(h);
+  if (rc != RFGPU_OK) return rc;
+  rc = phase_setup(h);
+  if (rc != RFGPU_OK) return rc;
+  cudaStream_t s = h->stream, x = h->xstream;
+  const RegionDev<float> *regs = regs_of<float>(h);
+  const Work &w = h->work;
+  const int nk = h->phN;
+  const int nS = h->nSteps;
+  const Prof *prof = h->prof.hookp();
+  cudaStream_t cs = h->cstream;
+  if (cudaEventRecord(h->xev[kXChunks], s) != cudaSuccess ||
+      cudaStreamWaitEvent(x, h->xev[kXChunks], 0) != cudaSuccess ||
+      cudaStreamWaitEvent(cs, h->xev[kXChunks], 0) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  // upload: copies on x, conversions on cs, the stage-1 gradient phases on s
+  // behind the conversions they need (cs runs in order, so the last wait
+  // covers every earlier chunk)
+  for (int k = 0; k < nk; ++k) {
+    int t0, t1;
+    size_t c0, c1;
+    chunk_range(h, k, nk, t0, t1, c0, c1);
+    if (cudaMemcpyAsync(h->stage + 5 * c0, cv + 5 * c0, 5 * (c1 - c0) * 8,
+                        cudaMemcpyHostToDevice, x) != cudaSuccess ||
+        cudaEventRecord(h->xev[k], x) != cudaSuccess ||
+        cudaStreamWaitEvent(cs, h->xev[k], 0) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    upload_chunk(h, k, h->stage, nullptr, cs);
+    if (cudaEventRecord(h->cev[k], cs) != cudaSuccess ||
+        cudaStreamWaitEvent(s, h->cev[k], 0) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    const int n = h->phOff[0][k + 1] - h->phOff[0][k];
+    if (n > 0) {
+      launch_grad_tiles<float>(regs, w, h->phGrad + h->phOff[0][k], n, 1, s);
+      h->launches++;
+    }
+  }
+  for (int is = 1; is <= nS; ++is) {
+    StepArgs sa{is, 1, 0.0, 0, 1, is == 1 ? 1 : 0, da};
+    const int parts = (is == 1 ? 0 : SP_GRADIENT) | SP_FLUX | (is == nS ? 0 : SP_UPDATE);
+    launch_stage<float>(regs, w, sa, s, &h->launches, h->spaceOrder, h->reconst, prof, parts);
+    if (is < nS) continue;
+    // last update phase by phase, each chunk converted and copied back behind it
+    for (int k = 0; k < nk; ++k) {
+      const int n = h->phOff[1][k + 1] - h->phOff[1][k];
+      if (n > 0) {
+        launch_update_tiles<float>(regs, w, h->phUpd + h->phOff[1][k], n, sa, s);
+        h->launches++;
+      }
+      int t0, t1;
+      size_t c0, c1;
+      chunk_range(h, k, nk, t0, t1, c0, c1);
+      download_chunk(h, k, h->stage, dv ? h->stage2 : nullptr);
+      if (cudaEventRecord(h->xev[k], s) != cudaSuccess ||
+          cudaStreamWaitEvent(x, h->xev[k], 0) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (cudaMemcpyAsync(cv + 5 * c0, h->stage + 5 * c0, 5 * (c1 - c0) * 8,
+                          cudaMemcpyDeviceToHost, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      if (dv && cudaMemcpyAsync(dv + 3 * c0, h->stage2 + 3 * c0, 3 * (c1 - c0) * 8,
+                                cudaMemcpyDeviceToHost, x) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+    }
+  }
+  if (cudaGetLastError() != cudaSuccess) return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaStreamSynchronize(x));
 }
 
 void stage_launch(rfgpu_region_s *h, const StepArgs &a) {
@@ -887,9 +1080,13 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
     cudaStreamSynchronize(h->stream);
     if (h->xstream) {
       cudaStreamSynchronize(h->xstream);
+      cudaStreamSynchronize(h->cstream);
       for (cudaEvent_t e : h->xev)
         if (e) cudaEventDestroy(e);
+      for (cudaEvent_t e : h->cev)
+        if (e) cudaEventDestroy(e);
       cudaStreamDestroy(h->xstream);
+      if (h->cstream) cudaStreamDestroy(h->cstream);
     }
     h->mem.free_all();
     cudaStreamDestroy(h->stream);
@@ -908,9 +1105,13 @@ int rfgpu_region_destroy(rfgpu_region_t h) {
   if (h->evB) cudaEventDestroy(h->evB);
   if (h->xstream) {
     cudaStreamSynchronize(h->xstream);
+    cudaStreamSynchronize(h->cstream);
     for (cudaEvent_t e : h->xev)
       if (e) cudaEventDestroy(e);
+    for (cudaEvent_t e : h->cev)
+      if (e) cudaEventDestroy(e);
     cudaStreamDestroy(h->xstream);
+    if (h->cstream) cudaStreamDestroy(h->cstream);
   }
   if (h->t0) cudaEventDestroy(h->t0);
   if (h->t1) cudaEventDestroy(h->t1);
@@ -1000,15 +1201,13 @@ int rfgpu_download(rfgpu_region_t h, double *cv, double *dv) {
     int rc = transfer_setup(h);
     if (rc != RFGPU_OK) return rc;
     cudaStream_t x = h->xstream;
-    const int nk = std::min(kXChunks, std::max(1, h->work.nCellTiles));
+    const int nk = n_chunks(h);
     for (int k = 0; k < nk; ++k) {
       int t0, t1;
       size_t c0, c1;
       chunk_range(h, k, nk, t0, t1, c0, c1);
       if (t1 <= t0) continue;
-      launch_download_direct<float>(regs_of<float>(h), h->work, t0, t1 - t0,
-                                    cv ? h->stage : nullptr, dv ? h->stage2 : nullptr, h->stream);
-      h->launches++;
+      download_chunk(h, k, cv ? h->stage : nullptr, dv ? h->stage2 : nullptr);
       if (cudaEventRecord(h->xev[k], h->stream) != cudaSuccess ||
           cudaStreamWaitEvent(x, h->xev[k], 0) != cudaSuccess)
         return RFGPU_ERR_CUDA;
@@ -1044,6 +1243,26 @@ int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv) {
   int rc = upload_state(h, cv, dv);
   if (rc != RFGPU_OK) return rc;
   return cuda_rc(cudaStreamSynchronize(h->stream));
+}
+
+int rfgpu_step_host(rfgpu_region_t h, double *cv, double *dv, double cfl, double dtImposed,
+                    double dtMinLimit, double endTime) {
+  if (!h || !cv) return RFGPU_ERR_ARG;
+  if (!h->borders.empty()) return RFGPU_ERR_UNSUPPORTED;  // needs its neighbours between stages
+  DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
+  if (h->prec && h->spaceOrder > 1 && h->work.nCellTiles > 0) {
+    try {
+      return step_host_mixed(h, cv, dv, da);
+    } catch (const std::bad_alloc &) {
+      return RFGPU_ERR_NOMEM;
+    }
+  }
+  // FP64 path and first order: the three calls in sequence
+  int rc = upload_state(h, cv, nullptr);
+  if (rc != RFGPU_OK) return rc;
+  step_launch(h, cfl, dtImposed, dtMinLimit, endTime);
+  if (cudaGetLastError() != cudaSuccess) return RFGPU_ERR_CUDA;
+  return rfgpu_download(h, cv, dv);
 }
 
 int rfgpu_download_grad(rfgpu_region_t h, double *grad) {

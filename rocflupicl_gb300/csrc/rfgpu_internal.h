@@ -159,6 +159,17 @@ struct StepArgs {
   DtArgs dt;         // time-step parameters when fuseDt
 };
 
+// Parts of a stage, for a caller that launches some passes itself over subsets
+// of the cell tiles: the gradient pass; the time-step finalisation (when the
+// gradient pass reduces it) and the face passes; the update (and halo).
+enum { SP_GRADIENT = 1, SP_FLUX = 2, SP_UPDATE = 4, SP_ALL = 7 };
+
+// Host-state step (rfgpu_step_host): the host images move in chunks of cell
+// tiles, chunk k covering host cells [tEnd[k-1], tEnd[k]) * block.
+struct ChunkMap {
+  int nk, block;
+  int tEnd[8];
+};
 
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
@@ -179,15 +190,15 @@ struct Prof {
 template <typename R>
 void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStream_t s);
 // Mixed path: fused conversion between the Fortran images cv(5,N), dv(3,N)
-// (host numbering, in device staging buffers) and the device state, for the
-// host cells of cell tiles [firstTile, firstTile + nTiles); either buffer may
-// be null where the call allows it.
+// (host numbering, in device staging buffers) and the device state of one
+// region (regs[0]), for the device cells list[0..n) (ascending); either image
+// may be null where the call allows it.
 template <typename R>
-void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
-                          const double *cvH, const double *dvH, cudaStream_t s);
+void launch_upload_list(const RegionDev<R> *regs, const int *list, int n, const double *cvH,
+                        const double *dvH, cudaStream_t s);
 template <typename R>
-void launch_download_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
-                            double *cvH, double *dvH, cudaStream_t s);
+void launch_download_list(const RegionDev<R> *regs, const int *list, int n, double *cvH,
+                          double *dvH, cudaStream_t s);
 // Halo exchange: the links of a coupled batch (regs indexed by region), or
 // one border between two handles (send cells of src -> receive cells of dst,
 // device numbering).  Copies the conserved state and rebuilds the received
@@ -212,7 +223,23 @@ void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, co
                              int spaceOrder, R *flux, double *rhs, cudaStream_t s);
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
-                  long long *launches, int spaceOrder, int reconst, const Prof *prof);
+                  long long *launches, int spaceOrder, int reconst, const Prof *prof,
+                  int parts = SP_ALL);
+// Phases of the host-state step, per cell tile (index into w.cellTiles): the
+// last transfer chunk its gradient pass reads from (own record, stencil
+// members, face neighbours) and the first chunk among its own cells.
+// tileLast must hold zeros and tileFirst values >= m.nk on entry.
+template <typename R>
+void launch_tile_phases(const RegionDev<R> *regs, const Work &w, const ChunkMap &m,
+                        int *tileLast, int *tileFirst, cudaStream_t s);
+// The gradient pass (with the stage-1 time-step reduction when fuseDt) and the
+// update of one stage over a list of cell tiles.
+template <typename R>
+void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                       int fuseDt, cudaStream_t s);
+template <typename R>
+void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                         const StepArgs &a, cudaStream_t s);
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
                long long *launches, const Prof *prof);

@@ -577,35 +577,41 @@ __device__ __forceinline__ void set_vars_cell(const RegionDev<R> &g, int c, int 
   st8(g.rec + 8 * (size_t)c, r);
 }
 
+// Mixed path: the record (rho, u, v, w, p) of a cell from its float-float
+// conserved state, in FP32 (the total energy keeps its low part, so p loses
+// only the kinetic term's rounding).  The one state-to-record map of the mixed
+// path: the update, the upload and the border receive all use it.
+__device__ __forceinline__ void record_from_pairs(const Phys &ph, const float qh[5],
+                                                  const float ql[5], float r[5]) {
+  const float rf = qh[0];
+  const float irf = 1.0f / rf;
+  r[0] = rf;
+  r[1] = qh[1] * irf;
+  r[2] = qh[2] * irf;
+  r[3] = qh[3] * irf;
+  const float kin = 0.5f * (qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]) * irf;
+  r[4] = (ph.gvGF - 1.0f) * ((qh[4] - kin) + ql[4]);
+}
+
 // Mixed path: a cell's state from an FP64 conserved vector (upload, border
-// receive): float-float split and the record, with p from dv when given, else
-// from the FP64 EOS.
+// receive): float-float split, then the record from the pairs, with p from dv
+// when given.  FP64 work is the split alone (GB300's FP64 rate bounds these
+// conversions).
 __device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c, const double q[5],
                                                 const double *pGiven) {
   const int N = g.nCells;
-  const double ir = 1.0 / q[0];
-  double p;
-  if (pGiven) {
-    p = *pGiven;
-  } else {
-    const double gg = g.ph.gvG;
-    const double Eo = ir * q[4];
-    const double Vm2 = ir * ir * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
-    p = (gg - 1.0) * q[0] * (Eo - 0.5 * Vm2 - 0.0);
-  }
+  float qh[5], ql[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) {
-    const float hi = (float)q[j];
-    g.cvF[(size_t)j * N + c] = hi;
-    g.cvF[(size_t)(5 + j) * N + c] = (float)(q[j] - (double)hi);
+    qh[j] = (float)q[j];
+    ql[j] = (float)(q[j] - (double)qh[j]);
+    g.cvF[(size_t)j * N + c] = qh[j];
+    g.cvF[(size_t)(5 + j) * N + c] = ql[j];
   }
   float r[8];
   ld8_rw(g.rec + 8 * (size_t)c, r);
-  r[0] = float(q[0]);
-  r[1] = float(ir * q[1]);
-  r[2] = float(ir * q[2]);
-  r[3] = float(ir * q[3]);
-  r[4] = float(p);
+  record_from_pairs(g.ph, qh, ql, r);
+  if (pGiven) r[4] = float(*pGiven);
   st8(g.rec + 8 * (size_t)c, r);
 }
 
@@ -1563,13 +1569,11 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
     ql[j] = ol[j];
     ff_sub(qh[j], ql[j], dU);
   }
-  // EOS of the new state in FP32 from the pairs (the total energy keeps its
-  // low part, so p loses only the kinetic term's rounding)
-  const float rf = qh[0];
-  const float irf = 1.0f / rf;
-  const float uf = qh[1] * irf, vf = qh[2] * irf, wf = qh[3] * irf;
-  const float kin = 0.5f * (qh[1] * qh[1] + qh[2] * qh[2] + qh[3] * qh[3]) * irf;
-  float pf = (ph.gvGF - 1.0f) * ((qh[4] - kin) + ql[4]);
+  // EOS of the new state in FP32 from the pairs
+  float rr[5];
+  record_from_pairs(ph, qh, ql, rr);
+  const float rf = rr[0], uf = rr[1], vf = rr[2], wf = rr[3];
+  float pf = rr[4];
   if (!(rf > 0.f) || !(pf > 1.0e-12f) || isnan(uf) || isnan(vf) || isnan(wf)) {
     // exact FP64 checks and bounds of AfterUpdateMP on the joined state
     const double gg = ph.gvG;
@@ -1742,58 +1746,55 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
 }
 
 // Mixed path transfers: the host's Fortran images cv(5,N) / dv(3,N), copied
-// by DMA into device staging buffers, are converted in one pass per
-// direction, one thread per host cell, fusing the numbering, layout and
-// precision conversions (upload: cons -> record with the EOS of k_prim,
-// float-float split; download: float-float join, FP64 dv).  Kernels reading
-// or writing page-locked host memory directly over the CPU-GPU link were
-// measured slower than the DMA copies (32 against 20 ms per end-to-end step).
+// by DMA into device staging buffers, are converted in one pass per direction
+// and chunk, fusing the numbering, layout and precision conversions (upload:
+// cons -> record with the EOS of k_prim, float-float split; download:
+// float-float join, FP64 dv).  One thread per device cell of the chunk's list
+// (its cells in ascending device order), so the device-side state is read and
+// written coalesced and the Fortran images are addressed by host cell; one
+// thread per host cell scattered the state's ten SoA rows instead.  Kernels
+// reading or writing page-locked host memory directly over the CPU-GPU link
+// were measured slower than the DMA copies (32 against 20 ms per end-to-end
+// step).
 template <typename R>
-__global__ void k_upload_direct(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
-                                int nTiles, const double *__restrict__ cvH,
-                                const double *__restrict__ dvH) {
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    const int i = tl.first + threadIdx.x;  // host cell
-    const int N = g.nCells;
-    if (i >= N) continue;
-    const int c = g.cellNew ? g.cellNew[i] : i;
-    double q[5];
+__global__ void k_upload_list(const RegionDev<R> *__restrict__ regs, const int *__restrict__ list,
+                              int n, const double *__restrict__ cvH, const double *__restrict__ dvH) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const RegionDev<R> &g = regs[0];
+  const int c = list[i];
+  const int h = g.cellOld ? g.cellOld[c] : c;
+  double q[5];
 #pragma unroll
-    for (int j = 0; j < 5; ++j) q[j] = cvH[5 * (size_t)i + j];
-    if constexpr (sizeof(R) == 4) state_from_fp64(g, c, q, dvH ? dvH + 3 * (size_t)i : nullptr);
-  }
+  for (int j = 0; j < 5; ++j) q[j] = cvH[5 * (size_t)h + j];
+  if constexpr (sizeof(R) == 4) state_from_fp64(g, c, q, dvH ? dvH + 3 * (size_t)h : nullptr);
 }
 
 template <typename R>
-__global__ void k_download_direct(const RegionDev<R> *__restrict__ regs,
-                                  const Tile *__restrict__ tiles, int nTiles, double *__restrict__ cvH,
-                                  double *__restrict__ dvH) {
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    const int i = tl.first + threadIdx.x;  // host cell
-    const int N = g.nCells;
-    if (i >= N) continue;
-    const int c = g.cellNew ? g.cellNew[i] : i;
-    double q[5];
+__global__ void k_download_list(const RegionDev<R> *__restrict__ regs, const int *__restrict__ list,
+                                int n, double *__restrict__ cvH, double *__restrict__ dvH) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const RegionDev<R> &g = regs[0];
+  const int c = list[i];
+  const int h = g.cellOld ? g.cellOld[c] : c;
+  const int N = g.nCells;
+  double q[5];
 #pragma unroll
-    for (int j = 0; j < 5; ++j)
-      q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
-    if (cvH) {
+  for (int j = 0; j < 5; ++j)
+    q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+  if (cvH) {
 #pragma unroll
-      for (int j = 0; j < 5; ++j) cvH[5 * (size_t)i + j] = q[j];
-    }
-    if (dvH) {
-      const double gc = g.ph.gvR, gg = g.ph.gvG;
-      const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
-      const double p = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
-      const double T = p / (q[0] * gc);
-      dvH[3 * (size_t)i] = p;
-      dvH[3 * (size_t)i + 1] = T;
-      dvH[3 * (size_t)i + 2] = sqrt(gg * gc * T);
-    }
+    for (int j = 0; j < 5; ++j) cvH[5 * (size_t)h + j] = q[j];
+  }
+  if (dvH) {
+    const double gc = g.ph.gvR, gg = g.ph.gvG;
+    const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
+    const double p = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
+    const double T = p / (q[0] * gc);
+    dvH[3 * (size_t)h] = p;
+    dvH[3 * (size_t)h + 1] = T;
+    dvH[3 * (size_t)h + 2] = sqrt(gg * gc * T);
   }
 }
 
@@ -1921,13 +1922,16 @@ int resident_blocks(K kernel) {
 
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
-                  long long *launches, int spaceOrder, int reconst, const Prof *prof) {
+                  long long *launches, int spaceOrder, int reconst, const Prof *prof,
+                  int parts) {
   static const int pfFace = resident_blocks(k_face_flux<R>);
   static const int pfUpd = resident_blocks(k_gather_update<R>);
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   (void)reconst;
   long long n = 0;
-  const bool grad = spaceOrder > 1 && w.nCellTiles > 0;
+  const bool hasGrad = spaceOrder > 1 && w.nCellTiles > 0;
+  const bool grad = hasGrad && (parts & SP_GRADIENT);
+  const bool flux = parts & SP_FLUX, upd = parts & SP_UPDATE;
   if (grad) {
     RF_MARK(KP_GRADIENT, 0);
     if (a.fuseDt)
@@ -1937,32 +1941,32 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
     RF_MARK(KP_GRADIENT, 1);
     ++n;
   }
-  if (a.fuseDt && grad) {
+  if (a.fuseDt && hasGrad && flux) {
     RF_MARK(KP_DT_FINAL, 0);
     launch_dt_finalize<R>(regs, w, a.dt, s);
     RF_MARK(KP_DT_FINAL, 1);
     ++n;
   }
-  if (w.nFaceTiles > 0) {
+  if (flux && w.nFaceTiles > 0) {
     RF_MARK(KP_FACE_FLUX, 0);
     k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles, pfFace);
     RF_MARK(KP_FACE_FLUX, 1);
     ++n;
   }
-  if (w.nBFaceTiles > 0) {
+  if (flux && w.nBFaceTiles > 0) {
     RF_MARK(KP_BFACE_FLUX, 0);
     k_bface_flux<R><<<gsz(w.nBFaceTiles), w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);
     RF_MARK(KP_BFACE_FLUX, 1);
     ++n;
   }
-  if (w.nCellTiles > 0) {
+  if (upd && w.nCellTiles > 0) {
     RF_MARK(KP_GATHER_UPDATE, 0);
     k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a,
                                                               pfUpd);
     RF_MARK(KP_GATHER_UPDATE, 1);
     ++n;
   }
-  if (w.nHalo > 0 && a.update) {  // coupled regions: virtual cells from their owners
+  if (upd && w.nHalo > 0 && a.update) {  // coupled regions: virtual cells from their owners
     RF_MARK(KP_HALO, 0);
     k_halo<R><<<(w.nHalo + 127) / 128, 128, 0, s>>>(regs, w.halo, w.nHalo);
     RF_MARK(KP_HALO, 1);
@@ -2002,18 +2006,80 @@ void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int 
 }
 
 template <typename R>
-void launch_upload_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
-                          const double *cvH, const double *dvH, cudaStream_t s) {
-  int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
-  if (grid > 0)
-    k_upload_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles + firstTile, nTiles, cvH, dvH);
+void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                       int fuseDt, cudaStream_t s) {
+  const int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
+  if (grid <= 0) return;
+  if (fuseDt)
+    k_grad_lim<R, 1><<<grid, w.block, 0, s>>>(regs, tiles, nTiles);
+  else
+    k_grad_lim<R, 0><<<grid, w.block, 0, s>>>(regs, tiles, nTiles);
+}
+
+template <typename R>
+void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                         const StepArgs &a, cudaStream_t s) {
+  static const int pfUpd = resident_blocks(k_gather_update<R>);
+  const int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
+  if (grid > 0) k_gather_update<R><<<grid, w.block, 0, s>>>(regs, tiles, nTiles, a, pfUpd);
+}
+
+// The transfer chunk a host cell travels in.
+__device__ __forceinline__ int host_chunk(const ChunkMap &m, int hostCell) {
+  const int t = hostCell / m.block;
+  int k = 0;
+  while (k < m.nk - 1 && t >= m.tEnd[k]) ++k;
+  return k;
+}
+
+// Per cell tile: the last chunk holding a record its gradient pass reads (the
+// cell's own, its stencil members', its face neighbours') and the first chunk
+// among its own cells.  Runs once per region.
+template <typename R>
+__global__ void k_tile_phases(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+                              int nTiles, ChunkMap m, int *__restrict__ tileLast,
+                              int *__restrict__ tileFirst) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    if (c >= g.nCells) continue;
+    auto chunk = [&](int d) { return host_chunk(m, g.cellOld ? g.cellOld[d] : d); };
+    const int own = chunk(c);
+    int last = own;
+    if (g.stOff) {
+      const long long b = g.stOff[c >> 5] + (c & 31);
+      const int n = g.stCnt[c];
+      for (int k = 0; k < n; ++k) last = max(last, chunk(g.stIdx[b + (long long)k * kSlice]));
+    }
+    const long long e0 = g.cfOff[c >> 5] + (c & 31);
+    const int nf = g.cfCnt[c];
+    for (int k = 0; k < nf; ++k) {
+      const long long e = e0 + (long long)k * kSlice;
+      if (g.cfCode[e] >= 0) last = max(last, chunk(g.cfNb[e]));
+    }
+    atomicMax(tileLast + t_, last);
+    atomicMin(tileFirst + t_, own);
+  }
+}
+
+template <typename R>
+void launch_tile_phases(const RegionDev<R> *regs, const Work &w, const ChunkMap &m,
+                        int *tileLast, int *tileFirst, cudaStream_t s) {
+  if (w.nCellTiles > 0)
+    k_tile_phases<R><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, m,
+                                                       tileLast, tileFirst);
+}
+
+template <typename R>
+void launch_upload_list(const RegionDev<R> *regs, const int *list, int n, const double *cvH,
+                        const double *dvH, cudaStream_t s) {
+  if (n > 0) k_upload_list<R><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
 }
 template <typename R>
-void launch_download_direct(const RegionDev<R> *regs, const Work &w, int firstTile, int nTiles,
-                            double *cvH, double *dvH, cudaStream_t s) {
-  int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
-  if (grid > 0)
-    k_download_direct<R><<<grid, w.block, 0, s>>>(regs, w.cellTiles + firstTile, nTiles, cvH, dvH);
+void launch_download_list(const RegionDev<R> *regs, const int *list, int n, double *cvH,
+                          double *dvH, cudaStream_t s) {
+  if (n > 0) k_download_list<R><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
 }
 
 // ---- residual without device allocation ---------------------------------------
@@ -2142,14 +2208,20 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
 
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
-  template void launch_upload_direct<R>(const RegionDev<R> *, const Work &, int, int,         \
-                                        const double *, const double *, cudaStream_t);        \
-  template void launch_download_direct<R>(const RegionDev<R> *, const Work &, int, int,       \
-                                          double *, double *, cudaStream_t);                  \
+  template void launch_upload_list<R>(const RegionDev<R> *, const int *, int, const double *,  \
+                                      const double *, cudaStream_t);                          \
+  template void launch_download_list<R>(const RegionDev<R> *, const int *, int, double *,     \
+                                        double *, cudaStream_t);                              \
   template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
                                            const Work &, int, R *, double *, cudaStream_t);    \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \
-                                cudaStream_t, long long *, int, int, const Prof *);           \
+                                cudaStream_t, long long *, int, int, const Prof *, int);      \
+  template void launch_tile_phases<R>(const RegionDev<R> *, const Work &, const ChunkMap &,   \
+                                      int *, int *, cudaStream_t);                            \
+  template void launch_grad_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int,   \
+                                     int, cudaStream_t);                                      \
+  template void launch_update_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int, \
+                                       const StepArgs &, cudaStream_t);                       \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
                              long long *, const Prof *);                                      \
   template void launch_step<R>(const RegionDev<R> *, const Work &, const DtArgs &, int,       \

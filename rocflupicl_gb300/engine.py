@@ -75,7 +75,8 @@ ORDER_LOCALITY, ORDER_HOST = 0, 1
 
 SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_dt",
            "rfgpu_step", "rfgpu_steps_graph", "rfgpu_residual", "rfgpu_download",
-           "rfgpu_upload", "rfgpu_download_grad", "rfgpu_time", "rfgpu_set_time",
+           "rfgpu_upload", "rfgpu_step_host", "rfgpu_download_grad", "rfgpu_time",
+           "rfgpu_set_time",
            "rfgpu_status", "rfgpu_sync", "rfgpu_stream", "rfgpu_device_bytes",
            "rfgpu_launch_count", "rfgpu_set_tuning", "rfgpu_batch_create",
            "rfgpu_batch_destroy", "rfgpu_batch_step", "rfgpu_batch_steps_graph",
@@ -115,6 +116,7 @@ def load(path: Optional[str] = None):
         "rfgpu_residual": ([vp, dp], C.c_int),
         "rfgpu_download": ([vp, dp, dp], C.c_int),
         "rfgpu_upload": ([vp, dp, dp], C.c_int),
+        "rfgpu_step_host": ([vp, dp, dp, d, d, d, d], C.c_int),
         "rfgpu_download_grad": ([vp, dp], C.c_int),
         "rfgpu_time": ([vp, dp, dp], C.c_int),
         "rfgpu_set_time": ([vp, d], C.c_int),
@@ -422,6 +424,18 @@ class Region:
             dv = np.ascontiguousarray(dv, np.float64)
             dvp = _dp(dv)
         _check(self.lib.rfgpu_upload(self.h, _dp(cv), dvp), "rfgpu_upload")
+
+    def step_host(self, cv: np.ndarray, dv: Optional[np.ndarray], cfl: float, dtImposed: float,
+                  dtMinLimit: float = 0.0, endTime: float = 0.0):
+        """rfgpu_step_host: one time step of the host state cv (nCells, 5), C-contiguous
+        float64, overwritten in place; dv (nCells, 3) receives the dependent variables
+        (or None).  Use pinned arrays (PinnedArray) for full copy rates."""
+        for a, k in ((cv, 5), (dv, 3)):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous
+                                  or a.shape != (self.nCells, k)):
+                raise ValueError(f"step_host needs a C-contiguous float64 ({self.nCells}, {k}) array")
+        _check(self.lib.rfgpu_step_host(self.h, _dp(cv), _dp(dv) if dv is not None else None,
+                                        cfl, dtImposed, dtMinLimit, endTime), "rfgpu_step_host")
 
     def gradients(self):
         g = np.empty((self.nCells, 5, 3))

@@ -98,6 +98,8 @@ def test_null_handles_are_errors():
     assert lib.rfgpu_sync(None) == E.ERR_ARG
     assert lib.rfgpu_region_destroy(None) == E.ERR_ARG
     assert lib.rfgpu_launch_count(None) == -1
+    cv = np.zeros(5)
+    assert lib.rfgpu_step_host(None, E._dp(cv), None, 0.5, 0.0, 0.0, 0.0) == E.ERR_ARG
 
 
 def test_perfmodel_matches_pass_totals():

@@ -72,3 +72,69 @@ def test_chunked_upload_download_round_trip(dims, order):
         assert np.array_equal(cv, want)
         assert np.allclose(dv, K.eos_dv(c.numerics, want), rtol=1e-13, atol=0)
     r.close()
+
+
+def _case(dims, prec, discr=K.DISCR_UPW_ROE, rk=K.RK_SCHEME_3_WRAY, order=2):
+    nx, ny, nz = dims
+    num = K.Numerics(precision=prec, venkatGuard=1, spaceDiscr=discr, rkScheme=rk,
+                     spaceOrder=order)
+    return K.tet_shock_box(nx, ny=ny, nz=nz, seed=7, numerics=num)
+
+
+@pytest.mark.parametrize("dims", [(3, 3, 3), (5, 3, 7), (24, 8, 8), (50, 9, 11)])
+@pytest.mark.parametrize("variant", ["roe-wray", "hllc-rk4", "ausm+-euler", "first-order", "fp64"])
+@pytest.mark.parametrize("order", [E.ORDER_HOST, E.ORDER_LOCALITY])
+def test_step_host_equals_three_calls(dims, variant, order):
+    """rfgpu_step_host against rfgpu_upload + rfgpu_step + rfgpu_download on the
+    same host state, three steps: cv, dv and the device time agree bit for bit.
+    On the mixed path at second order the copies and conversions run in up to
+    8 chunks with the first stage's gradient pass split into phases by the
+    chunks its records travel in and the last stage's update split by the
+    chunks it hands back (regions smaller than 8 tiles in fewer chunks); the
+    FP64 path and first order run the three calls in sequence."""
+    prec, discr, rk, sord = K.PREC_MIXED, K.DISCR_UPW_ROE, K.RK_SCHEME_3_WRAY, 2
+    if variant == "hllc-rk4":
+        discr, rk = K.DISCR_UPW_HLLC, K.RK_SCHEME_4_CLASSICAL
+    elif variant == "ausm+-euler":
+        discr, rk = K.DISCR_UPW_AUSMPLUS, K.RK_SCHEME_1_EULER
+    elif variant == "first-order":
+        sord = 1
+    elif variant == "fp64":
+        prec = K.PREC_FP64
+    c = _case(dims, prec, discr, rk, sord)
+    cfl = 0.5
+    a = E.Region(c, cell_order=order)
+    b = E.Region(c, cell_order=order)
+    cv_a, dv_a = E.PinnedArray(c.cv.shape), E.PinnedArray(c.dv.shape)
+    cv_a.array[:] = c.cv
+    cv_b = np.ascontiguousarray(c.cv, np.float64).copy()
+    for _ in range(3):
+        a.step_host(cv_a.array, dv_a.array, cfl, 0.0)
+        b.upload(cv_b)
+        b.step(cfl, 0.0)
+        cv_b, dv_b = b.download()
+    assert np.all(np.isfinite(cv_b)) and np.all(np.isfinite(dv_b))
+    assert np.array_equal(cv_a.array, cv_b)
+    assert np.array_equal(dv_a.array, dv_b)
+    assert a.time() == b.time()
+    assert a.status() == 0 and not np.array_equal(cv_b, c.cv)
+    # dv is optional; pageable host memory works too
+    cv_c = cv_b.copy()
+    a.step_host(cv_c, None, cfl, 0.0)
+    b.upload(cv_b)
+    b.step(cfl, 0.0)
+    assert np.array_equal(cv_c, b.download()[0])
+    for p in (cv_a, dv_a):
+        p.close()
+    a.close()
+    b.close()
+
+
+def test_step_host_refuses_bad_arrays():
+    c = _case((3, 3, 3), K.PREC_MIXED)
+    r = E.Region(c)
+    with pytest.raises(ValueError):
+        r.step_host(np.zeros((r.nCells, 4)), None, 0.5, 1e-4)
+    with pytest.raises(ValueError):
+        r.step_host(np.zeros((r.nCells, 5), np.float32), None, 0.5, 1e-4)
+    r.close()
