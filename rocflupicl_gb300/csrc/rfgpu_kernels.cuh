@@ -827,8 +827,12 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 // (bitwise the reference's); mixed path: weights rebuilt in FP32 from the
 // records' centroids and the cell's WLSQ factor terms.  With fuseDt the pass
 // also reduces the time step (stage 1 of a step).
+// Record gathers issued together in the mixed member loop (software-pipelined
+// with the next group's index loads).  Measured on the 128^3 tet box: 4 ->
+// 1.923 ms, 6 -> 1.893, 8 -> 1.880, 10 -> 2.033 (spills), 12 -> 2.052; without
+// the index pipeline 8 -> 1.904, 12 -> 1.929.
 #ifndef RF_GRAD_UNROLL
-#define RF_GRAD_UNROLL 4   // record gathers issued together (mixed path)
+#define RF_GRAD_UNROLL 8
 #endif
 #ifndef RF_GRAD_MINB
 #define RF_GRAD_MINB 8     // resident 128-thread blocks per SM (mixed path)
@@ -911,19 +915,30 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
             acc[3 * v + 2] = acc[3 * v + 2] + dz * dVar;
           }
         };
-        int k = 0;
-        for (; k + RF_GRAD_UNROLL <= n; k += RF_GRAD_UNROLL) {
-          R ra[RF_GRAD_UNROLL][8];
+        // software pipeline: the next group's stencil indices are loaded while
+        // this group's records are in flight (same members, same order)
+        constexpr int U = RF_GRAD_UNROLL;
+        const int nFull = n - n % U;
+        int nx[U];
 #pragma unroll
-          for (int u = 0; u < RF_GRAD_UNROLL; ++u)
-            ld8(rec + 8 * (size_t)ld_index(sidx + (k + u) * kSlice), ra[u]);
+        for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(sidx + u * kSlice) : 0;
+        for (int k = 0; k < nFull; k += U) {
+          R ra[U][8];
 #pragma unroll
-          for (int u = 0; u < RF_GRAD_UNROLL; ++u) member(ra[u]);
+          for (int u = 0; u < U; ++u) ld8(rec + 8 * (size_t)nx[u], ra[u]);
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+            nx[u] = k + U + u < n ? ld_index(sidx + (k + U + u) * kSlice) : 0;
+#pragma unroll
+          for (int u = 0; u < U; ++u) member(ra[u]);
         }
-        for (; k < n; ++k) {
-          R ra[8];
-          ld8(rec + 8 * (size_t)ld_index(sidx + k * kSlice), ra);
-          member(ra);
+#pragma unroll
+        for (int u = 0; u < U - 1; ++u) {
+          if (nFull + u < n) {
+            R ra[8];
+            ld8(rec + 8 * (size_t)nx[u], ra);
+            member(ra);
+          }
         }
         const R axx = lds<RF_HINT_G>(g.cwt + c), axy = lds<RF_HINT_G>(g.cwt + N + c),
                 axz = lds<RF_HINT_G>(g.cwt + 2 * N + c);
