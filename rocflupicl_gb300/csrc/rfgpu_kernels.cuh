@@ -831,6 +831,13 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 // with the next group's index loads).  Measured on the 128^3 tet box: 4 ->
 // 1.923 ms, 6 -> 1.893, 8 -> 1.880, 10 -> 2.033 (spills), 12 -> 2.052; without
 // the index pipeline 8 -> 1.904, 12 -> 1.929.
+// Limiter face loop: codes and neighbours of the first RF_LIM_PRE faces loaded
+// ahead of the records (measured: gradient pass 1.881 -> 1.835 ms with 4,
+// 1.830 ms with 6; keeping the six codes live for the second face loop instead
+// of reading them again: 1.981 ms).
+#ifndef RF_LIM_PRE
+#define RF_LIM_PRE 6
+#endif
 #ifndef RF_GRAD_UNROLL
 #define RF_GRAD_UNROLL 8
 #endif
@@ -967,14 +974,11 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
         // order and arithmetic as cell_dt)
         R dtacc = R(0), a0 = R(0);
         if constexpr (fuseDt) a0 = dt_sound(g, c, r0);
-        for (int k = 0; k < nf; ++k) {
-          const long long ee = e0 + (long long)k * kSlice;
-          const int code = g.cfCode[ee];
+        auto face_minmax = [&](int code, int nb) {
           if (code < 0) {
             if constexpr (fuseDt) dt_boundary_term(g, code, r0, a0, dtacc);
-            continue;
+            return;
           }
-          const int nb = lds<RF_HINT_G>(g.cfNb + ee);
           R rn[8];
           ld8(rec + 8 * (size_t)nb, rn);
 #pragma unroll
@@ -983,6 +987,24 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
             vmax[v] = rmax(vmax[v], rn[v]);
           }
           if constexpr (fuseDt) dt_interior_term(g, code, r0, a0, nb, rn, dtacc);
+        };
+        // the first faces' codes and neighbours are loaded together, ahead of
+        // their records (same faces, same order); six covers every cell type
+        constexpr int MF = RF_LIM_PRE;
+        int cc[MF], nn[MF];
+#pragma unroll
+        for (int k = 0; k < MF; ++k) {
+          const long long ee = e0 + (long long)k * kSlice;
+          cc[k] = k < nf ? g.cfCode[ee] : -1;
+          nn[k] = k < nf ? lds<RF_HINT_G>(g.cfNb + ee) : -1;
+        }
+#pragma unroll
+        for (int k = 0; k < MF; ++k)
+          if (k < nf) face_minmax(cc[k], nn[k]);
+        for (int k = MF; k < nf; ++k) {
+          const long long ee = e0 + (long long)k * kSlice;
+          const int code = g.cfCode[ee];
+          face_minmax(code, code < 0 ? -1 : lds<RF_HINT_G>(g.cfNb + ee));
         }
         if constexpr (fuseDt) {
           dtbits = (unsigned long long)__double_as_longlong(dt_of(g, c, dtacc));
@@ -990,9 +1012,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
         }
         const R epsq = lds<RF_HINT_G>(g.epsq + c);
         const int guard = g.ph.venkatGuard;
-        for (int k = 0; k < nf; ++k) {
-          const long long ee = e0 + (long long)k * kSlice;
-          if (lds<RF_HINT_G>(g.cfCode + ee) < 0) continue;  // its last read
+        auto face_lim = [&](long long ee) {
           const R dx = lds<RF_HINT_G>(g.cfD + ee), dy = lds<RF_HINT_G>(g.cfD + T + ee),
                   dz = lds<RF_HINT_G>(g.cfD + 2 * T + ee);
 #pragma unroll
@@ -1000,6 +1020,10 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
             R d2 = acc[3 * v] * dx + acc[3 * v + 1] * dy + acc[3 * v + 2] * dz;
             venkat_term(d2, vmax[v] - r0[v], vmin[v] - r0[v], epsq, lim[v], guard);
           }
+        };
+        for (int k = 0; k < nf; ++k) {
+          const long long ee = e0 + (long long)k * kSlice;
+          if (lds<RF_HINT_G>(g.cfCode + ee) >= 0) face_lim(ee);  // its last read
         }
 #pragma unroll
         for (int v = 0; v < 5; ++v)
