@@ -279,6 +279,12 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 // Measured on the 128^3 tet box (mixed): update pass 0.650 -> 0.636 ms with
 // its hint, gradient pass 1.928 -> 1.925 ms, face pass unchanged (0.636 ms),
 // so the face pass keeps plain loads.
+// Update face loop: the first RF_UPD_PRE face codes loaded together ahead of
+// the flux gathers (measured: update pass 0.636 -> 0.596 ms with 4, 0.598 ms
+// with 6).
+#ifndef RF_UPD_PRE
+#define RF_UPD_PRE 6
+#endif
 #ifndef RF_HINT_G
 #define RF_HINT_G 1   // gradient pass: cell->face lists, WLSQ factor terms
 #endif
@@ -1528,8 +1534,7 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const long long e0 = g.cfOff[c >> 5] + (c & 31);
   const int n = g.cfCnt[c];
-  for (int k = 0; k < n; ++k) {
-    const int code = lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice);
+  auto face = [&](int code) {
     float fl[8];
     if (code >= 0) {
       ld8(g.flux + 8 * (size_t)(code >> 1), fl);
@@ -1541,7 +1546,17 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
 #pragma unroll
       for (int j = 0; j < 5; ++j) two_sum_acc(hi[j], lo[j], fl[j]);
     }
-  }
+  };
+  // the first faces' codes loaded together, ahead of their flux gathers
+  constexpr int MF = RF_UPD_PRE;
+  int cc[MF];
+#pragma unroll
+  for (int k = 0; k < MF; ++k)
+    cc[k] = k < n ? lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice) : 0;
+#pragma unroll
+  for (int k = 0; k < MF; ++k)
+    if (k < n) face(cc[k]);
+  for (int k = MF; k < n; ++k) face(lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice));
   if (a.writeRhs) {
 #pragma unroll
     for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = double(hi[j]) + double(lo[j]);
