@@ -285,6 +285,9 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 #ifndef RF_UPD_PRE
 #define RF_UPD_PRE 6
 #endif
+#ifndef RF_FACE_PF
+#define RF_FACE_PF 0
+#endif
 #ifndef RF_HINT_G
 #define RF_HINT_G 1   // gradient pass: cell->face lists, WLSQ factor terms
 #endif
@@ -475,6 +478,9 @@ __device__ __forceinline__ void venkat_term(R d2, R dmax, R dmin, R epsq, R &lim
 
 // Bulk prefetch into L2 of the 16-byte-aligned part of [p, p + bytes): one
 // instruction per contiguous range, issued by one lane.
+__device__ __forceinline__ void prefetch_l1(const void *p) {
+  asm volatile("prefetch.global.L1 [%0];" ::"l"(p));
+}
 __device__ __forceinline__ void prefetch_l2(const void *p, size_t bytes) {
   if (p == nullptr) return;  // an array this region does not hold
   const size_t a = ((size_t)p + 15) & ~(size_t)15, e = ((size_t)p + bytes) & ~(size_t)15;
@@ -1117,6 +1123,12 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
     const int F = g.nFaces;
     if (f >= F) continue;
     const int c1 = lds<RF_HINT_F>(g.f2c + f), c2 = lds<RF_HINT_F>(g.f2c + F + f);
+#if RF_FACE_PF
+    if (g.ph.spaceOrder > 1) {  // both gradient rows on their way while the records arrive
+      prefetch_l1(g.grad + 16 * (size_t)c1);
+      prefetch_l1(g.grad + 16 * (size_t)c2);
+    }
+#endif
     R nrm[4];
     ld4s<RF_HINT_F>(g.fnA + 4 * (size_t)f, nrm);
     R r1[8], r2[8];
