@@ -285,8 +285,10 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 #ifndef RF_UPD_PRE
 #define RF_UPD_PRE 6
 #endif
+// Face pass: both cells' gradient rows prefetched into L1 as soon as the
+// face's cells are known (measured 0.640 -> 0.631 ms).
 #ifndef RF_FACE_PF
-#define RF_FACE_PF 0
+#define RF_FACE_PF 1
 #endif
 #ifndef RF_HINT_G
 #define RF_HINT_G 1   // gradient pass: cell->face lists, WLSQ factor terms
