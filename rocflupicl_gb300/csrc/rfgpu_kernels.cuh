@@ -843,8 +843,8 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 // also reduces the time step (stage 1 of a step).
 // Record gathers issued together in the mixed member loop (software-pipelined
 // with the next group's index loads).  Measured on the 128^3 tet box: 4 ->
-// 1.923 ms, 6 -> 1.893, 8 -> 1.880, 10 -> 2.033 (spills), 12 -> 2.052; without
-// the index pipeline 8 -> 1.904, 12 -> 1.929.
+// 1.923 ms, 6 -> 1.893, 7 -> 1.897, 8 -> 1.880, 10 -> 2.033 (spills), 12 ->
+// 2.052; without the index pipeline 8 -> 1.904, 12 -> 1.929.
 // Limiter face loop: codes and neighbours of the first RF_LIM_PRE faces loaded
 // ahead of the records (measured: gradient pass 1.881 -> 1.835 ms with 4,
 // 1.830 ms with 6; keeping the six codes live for the second face loop instead
@@ -855,8 +855,11 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #ifndef RF_GRAD_UNROLL
 #define RF_GRAD_UNROLL 8
 #endif
+// Resident 128-thread blocks per SM requested for the gradient pass (mixed
+// path).  Measured on the 128^3 tet box with the loop above: 7 -> 1.878 ms
+// (72 registers), 8 -> 1.830 ms (64), 9 -> 2.075 ms (56, spills).
 #ifndef RF_GRAD_MINB
-#define RF_GRAD_MINB 8     // resident 128-thread blocks per SM (mixed path)
+#define RF_GRAD_MINB 8
 #endif
 #ifndef RF_GRAD_MINB_DT
 #define RF_GRAD_MINB_DT 8  // the same for the stage-1 pass that also reduces the time step
