@@ -27,6 +27,7 @@ const int BCOPT_FIXED_NO = 0;
 const int BCOPT_SUPERSONIC = 0, BCOPT_SUBSONIC = 1, BCOPT_MIXED = 2;
 const int DISCR_UPW_ROE = 1, DISCR_UPW_HLLC = 3, DISCR_UPW_AUSMPLUS = 4, DISCR_UPW_AUSMPLUSUP = 5;
 const int RECONST_LIM_VENKAT = 11;
+const int RECONST_WENO_XYZ = 2;  // modfloflu/ModParameters.F90:680
 const int RK_SCHEME_4_CLASSICAL = 1, RK_SCHEME_3_WRAY = 2, RK_SCHEME_1_EULER = 3;
 const double KSG = 0.0;
 
@@ -773,12 +774,99 @@ void venkat(const orc_region_t *r, const double *var, double *grad) {
       for (int d = 0; d < 3; ++d) grad[15 * c + 3 * v + d] = lim[5 * c + v] * grad[15 * c + 3 * v + d];
 }
 
+// RFLU_WENOGradCellsXYZFast_3D (modflu/RFLU_ModWENO.F90:1402-1588), the 3-D
+// branch RFLU_WENOGradCellsXYZWrapper takes (:1615-1668), for cell c: every
+// gradient component becomes the average of the cell's and its stencil
+// members' components weighted by s = 1/(g^2 + 1e-15), the cell first, the
+// members in stored order, sum(s g) / sum(s).  g0 holds every cell's
+// unweighted gradients (the reference writes gradENO, then copies).
+void weno_cell(const orc_region_t *r, const double *g0, double *grad, long c) {
+  for (int k = 0; k < 15; ++k) {
+    const double t = g0[15 * c + k];
+    double ssum = 1.0 / (t * t + 1.0E-15);
+    double acc = ssum * t;
+    for (int s = r->csOff[c]; s < r->csOff[c + 1]; ++s) {
+      const double tm = g0[15 * (long)(r->csMem[s] - 1) + k];
+      const double sm = 1.0 / (tm * tm + 1.0E-15);
+      ssum = ssum + sm;
+      acc = acc + sm * tm;
+    }
+    grad[15 * c + k] = acc / ssum;
+  }
+}
+
+// Faces of every cell (interior, then boundary as (patch, face) pairs), for
+// RFLU_LimitGradCellsSimple, which walks a cell's faces through tet2f / hex2f /
+// pri2f / pyr2f; its result does not depend on the order.
+struct CellFaces {
+  std::vector<long> off, item;  // item >= 0: interior face; < 0: -(boundary slot + 1)
+  std::vector<const double *> bfc;
+};
+CellFaces cell_faces(const orc_region_t *r) {
+  const long nC = n_tot(r);
+  CellFaces cf;
+  cf.off.assign(nC + 1, 0);
+  for (long f = 0; f < r->nFaces; ++f) {
+    cf.off[r->f2c[2 * f]]++;
+    cf.off[r->f2c[2 * f + 1]]++;
+  }
+  for (int ip = 0; ip < r->nPatches; ++ip)
+    for (int i = 0; i < r->patches[ip].nBFaces; ++i) cf.off[r->patches[ip].bf2c[i]]++;
+  for (long c = 0; c < nC; ++c) cf.off[c + 1] += cf.off[c];
+  cf.item.resize(cf.off[nC]);
+  std::vector<long> fill(cf.off.begin(), cf.off.end() - 1);
+  for (long f = 0; f < r->nFaces; ++f) {
+    cf.item[fill[r->f2c[2 * f] - 1]++] = f;
+    cf.item[fill[r->f2c[2 * f + 1] - 1]++] = f;
+  }
+  for (int ip = 0; ip < r->nPatches; ++ip)
+    for (int i = 0; i < r->patches[ip].nBFaces; ++i) {
+      cf.item[fill[r->patches[ip].bf2c[i] - 1]++] = -(long)cf.bfc.size() - 1;
+      cf.bfc.push_back(r->patches[ip].fc + 3 * i);
+    }
+  return cf;
+}
+
+// RFLU_LimitGradCellsSimple (modflu/RFLU_ModLimiters.F90:793-921) for cell c:
+// the gradient of a positive variable (density and pressure,
+// libflu/RFLU_SetVarInfo.F90:140-144) is set to zero when its reconstruction
+// var + grad . (fc - xc) at one of the cell's faces is not positive.
+void limit_simple_cell(const orc_region_t *r, const CellFaces &cf, const double *var,
+                       double *grad, long c) {
+  const double xc = r->cofg[3 * c], yc = r->cofg[3 * c + 1], zc = r->cofg[3 * c + 2];
+  for (int v = 0; v < 5; v += 4) {
+    const double varc = var[5 * c + v];
+    double *g = grad + 15 * c + 3 * v;
+    for (long e = cf.off[c]; e < cf.off[c + 1]; ++e) {
+      const long it = cf.item[e];
+      const double *fcx = it >= 0 ? r->fc + 3 * it : cf.bfc[-it - 1];
+      const double dx = fcx[0] - xc, dy = fcx[1] - yc, dz = fcx[2] - zc;
+      const double varf = varc + g[0] * dx + g[1] * dy + g[2] * dz;
+      if (varf <= 0.0) {
+        g[0] = 0.0;
+        g[1] = 0.0;
+        g[2] = 0.0;
+        break;
+      }
+    }
+  }
+}
+
+void weno_simple(const orc_region_t *r, const double *var, double *grad) {
+  const long nC = n_tot(r);
+  std::vector<double> g0(grad, grad + 15 * nC);
+  for (long c = 0; c < nC; ++c) weno_cell(r, g0.data(), grad, c);
+  CellFaces cf = cell_faces(r);
+  for (long c = 0; c < nC; ++c) limit_simple_cell(r, cf, var, grad, c);
+}
+
 // CellGradientsMP (libfloflu/CellGradientsMP.F90:158-253), in place on cv
 void cell_gradients(const orc_region_t *r, double *cv, const double *dv, double *grad) {
   if (r->spaceOrder <= 1) return;
   cons2prim(r, cv, dv, 0, n_tot(r));
   gradients(r, cv, grad, 0, n_tot(r));
   if (r->reconst == RECONST_LIM_VENKAT) venkat(r, cv, grad);
+  if (r->reconst == RECONST_WENO_XYZ) weno_simple(r, cv, grad);
   prim2cons(r, cv, dv, 0, n_tot(r));
 }
 
@@ -1030,6 +1118,14 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
       for (long c = 0; c < nT; ++c)
         for (int v = 0; v < 5; ++v)
           for (int d = 0; d < 3; ++d) grad[15 * c + 3 * v + d] = lim[5 * c + v] * grad[15 * c + 3 * v + d];
+    }
+    if (r->reconst == RECONST_WENO_XYZ) {
+      std::vector<double> g0(grad, grad + 15 * nT);
+#pragma omp parallel for schedule(static, 256)
+      for (long c = 0; c < nT; ++c) weno_cell(r, g0.data(), grad, c);
+      CellFaces cf = cell_faces(r);
+#pragma omp parallel for schedule(static, 256)
+      for (long c = 0; c < nT; ++c) limit_simple_cell(r, cf, cv, grad, c);
     }
 #pragma omp parallel for schedule(static)
     for (long i = 0; i < nT; ++i) prim2cons(r, cv, dv, i, i + 1);

@@ -55,7 +55,7 @@ typedef struct {
   /* numerics (libflu/RFLU_InitInputValues.F90 keys) */
   int spaceDiscr;   /* DISCR_UPW_ROE=1, HLLC=3, AUSMPLUS=4, AUSMPLUSUP=5 */
   int spaceOrder;   /* 1 or 2 */
-  int reconst;      /* RECONST_NONE=0, RECONST_LIM_VENKAT=11 */
+  int reconst;      /* RECONST_NONE=0, RECONST_WENO_XYZ=2, RECONST_LIM_VENKAT=11 */
   int rkScheme;     /* RK_SCHEME_4_CLASSICAL=1, RK_SCHEME_3_WRAY=2, RK_SCHEME_1_EULER=3 */
   double refCp, refGamma;  /* global%refCp, refGamma: used by the flux kernels */
   double gvCp, gvMol;      /* gv(GV_MIXT_CP), gv(GV_MIXT_MOL): used by EOS/conversions */

@@ -17,7 +17,7 @@ from . import mesh as _mesh
 
 # modfloflu/ModParameters.F90
 DISCR_UPW_ROE, DISCR_UPW_HLLC, DISCR_UPW_AUSMPLUS, DISCR_UPW_AUSMPLUSUP = 1, 3, 4, 5
-RECONST_NONE, RECONST_LIM_VENKAT = 0, 11
+RECONST_NONE, RECONST_WENO_XYZ, RECONST_LIM_VENKAT = 0, 2, 11
 RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
 BC_OUTFLOW, BC_SLIPWALL, BC_FARFIELD, BC_INJECTION = 20, 60, 80, 90
 BC_INFLOW_TOTANG, BC_INFLOW_VELTEMP = 10, 11

@@ -118,9 +118,13 @@ def test_reference_limiter_guard_cancels():
     assert st == 0
 
 
-@pytest.mark.parametrize("scheme", [K.DISCR_UPW_AUSMPLUS, K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC])
-def test_openmp_gather_equals_serial_scatter(scheme):
-    c = K.tet_shock_box(4, seed=6, numerics=K.Numerics(spaceDiscr=scheme, venkatGuard=1))
+@pytest.mark.parametrize("scheme,reconst", [(K.DISCR_UPW_AUSMPLUS, K.RECONST_LIM_VENKAT),
+                                            (K.DISCR_UPW_ROE, K.RECONST_LIM_VENKAT),
+                                            (K.DISCR_UPW_HLLC, K.RECONST_LIM_VENKAT),
+                                            (K.DISCR_UPW_ROE, K.RECONST_WENO_XYZ)])
+def test_openmp_gather_equals_serial_scatter(scheme, reconst):
+    c = K.tet_shock_box(4, seed=6, numerics=K.Numerics(spaceDiscr=scheme, venkatGuard=1,
+                                                       reconst=reconst))
     a, b = Oracle(c), Oracle(c)
     cva, dva = c.cv.copy(), c.dv.copy()
     cvb, dvb = c.cv.copy(), c.dv.copy()
@@ -233,3 +237,88 @@ def test_inflow_veltemp_preserves_consistent_uniform_flow(opt):
     c, scale = _uniform_inflow_case(bc)
     rhs, _ = Oracle(c).residual(c.cv, c.dv)
     assert np.abs(rhs).max() < 1e-9 * scale
+
+
+@pytest.mark.parametrize("kind", ["tet", "mixed"])
+def test_weno_xyz_keeps_linear_gradients(kind):
+    """RECONST 2 (RFLU_WENOGradCellsXYZFast_3D + RFLU_LimitGradCellsSimple): on a
+    linear field every stencil gradient is the same vector, so the weighted
+    average returns it, and a positive linear density and pressure never
+    reconstruct to zero at a face."""
+    num = K.Numerics(reconst=K.RECONST_WENO_XYZ)
+    c = K.tet_shock_box(4, seed=3, numerics=num) if kind == "tet" else K.mixed_box(6, numerics=num)
+    x = c.mesh.cofg
+    a = np.array([[1.0, 0.3, -0.2, 0.5], [0.2, 1.0, 0.5, -0.7], [-0.1, 0.4, 0.2, 0.3],
+                  [0.05, -0.3, 0.8, 0.1], [2.0, 0.7, -0.6, 0.9]])
+    lin = a[:, 0] + x @ a[:, 1:].T
+    r, u, v, w, p = lin.T
+    cv = np.stack([r, r * u, r * v, r * w, r], axis=1)
+    dv = np.stack([p, p, p], axis=1)
+    _, grad = Oracle(c).residual(cv, dv)
+    for var in range(5):
+        assert np.allclose(grad[:, var, :], a[var, 1:], rtol=0, atol=1e-10), var
+
+
+def _weno_simple_restated(c, prim, g0):
+    """RECONST 2 restated element by element in Python floats (IEEE double,
+    the reference's operation order): WENO-XYZ weights over the cell and its
+    members in stored order, then the positivity check of density and
+    pressure at every face of the cell."""
+    m = c.mesh
+    n = m.nCells
+    out = g0.copy()
+    for ci in range(n):
+        mem = (m.c2cs_mem[m.c2cs_off[ci]:m.c2cs_off[ci + 1]] - 1).tolist()
+        for var in range(5):
+            for d in range(3):
+                t = float(g0[ci, var, d])
+                ssum = 1.0 / (t * t + 1.0e-15)
+                acc = ssum * t
+                for mm in mem:
+                    tm = float(g0[mm, var, d])
+                    sm = 1.0 / (tm * tm + 1.0e-15)
+                    ssum = ssum + sm
+                    acc = acc + sm * tm
+                out[ci, var, d] = acc / ssum
+    faces = [[] for _ in range(n)]
+    for f in range(m.nFaces):
+        for side in range(2):
+            faces[m.f2c[f, side] - 1].append(m.fc[f])
+    for pa in m.patches:
+        for i in range(pa.bf2c.shape[0]):
+            faces[pa.bf2c[i] - 1].append(pa.fc[i])
+    zeroed = 0
+    for ci in range(n):
+        xc, yc, zc = (float(q) for q in m.cofg[ci])
+        for var in (0, 4):
+            g = out[ci, var]
+            for fcx in faces[ci]:
+                dx, dy, dz = float(fcx[0]) - xc, float(fcx[1]) - yc, float(fcx[2]) - zc
+                varf = float(prim[ci, var]) + float(g[0]) * dx + float(g[1]) * dy + float(g[2]) * dz
+                if varf <= 0.0:
+                    out[ci, var] = 0.0
+                    zeroed += 1
+                    break
+    return out, zeroed
+
+
+def test_weno_xyz_and_simple_limiter_restated():
+    """The oracle's RECONST 2 gradients equal the element-by-element
+    restatement bit for bit, on a shock box whose density dips close to zero
+    so that the positivity check zeroes some gradients."""
+    base = K.Numerics(spaceDiscr=K.DISCR_UPW_ROE, reconst=K.RECONST_NONE)
+    c0 = K.tet_shock_box(4, seed=5, numerics=base)
+    x = c0.mesh.cofg
+    cv = c0.cv.copy()
+    scale = 0.02 + 4.0 * (x[:, 0] - 0.5) ** 2     # density from 0.02 to about 1.0
+    cv *= scale[:, None]
+    dv = Oracle(c0).set_dv(cv)
+    _, g0 = Oracle(c0).residual(cv, dv)           # unweighted, unlimited gradients
+    c2 = K.tet_shock_box(4, seed=5, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_ROE,
+                                                        reconst=K.RECONST_WENO_XYZ))
+    _, g2 = Oracle(c2).residual(cv, dv)
+    prim = np.stack([cv[:, 0], cv[:, 1] / cv[:, 0], cv[:, 2] / cv[:, 0], cv[:, 3] / cv[:, 0],
+                     dv[:, 0]], axis=1)
+    want, zeroed = _weno_simple_restated(c2, prim, g0)
+    assert zeroed > 0
+    assert np.array_equal(g2, want)
