@@ -52,7 +52,7 @@ enum {
 enum {
   RFGPU_DISCR_UPW_ROE = 1, RFGPU_DISCR_UPW_HLLC = 3, RFGPU_DISCR_UPW_AUSMPLUS = 4,
   RFGPU_DISCR_UPW_AUSMPLUSUP = 5,
-  RFGPU_RECONST_NONE = 0, RFGPU_RECONST_LIM_VENKAT = 11,
+  RFGPU_RECONST_NONE = 0, RFGPU_RECONST_WENO_XYZ = 2, RFGPU_RECONST_LIM_VENKAT = 11,
   RFGPU_RK_SCHEME_4_CLASSICAL = 1, RFGPU_RK_SCHEME_3_WRAY = 2, RFGPU_RK_SCHEME_1_EULER = 3,
   RFGPU_BC_INFLOW_TOTANG = 10, RFGPU_BC_INFLOW_VELTEMP = 11,
   RFGPU_BC_OUTFLOW = 20, RFGPU_BC_SLIPWALL = 60, RFGPU_BC_FARFIELD = 80,

@@ -217,7 +217,12 @@ int check_desc(const rfgpu_region_desc_t *d) {
       d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUS && d->spaceDiscr != RFGPU_DISCR_UPW_AUSMPLUSUP)
     return RFGPU_ERR_UNSUPPORTED;
   if (d->spaceOrder != 1 && d->spaceOrder != 2) return RFGPU_ERR_UNSUPPORTED;
-  if (d->reconst != RFGPU_RECONST_NONE && d->reconst != RFGPU_RECONST_LIM_VENKAT)
+  if (d->reconst != RFGPU_RECONST_NONE && d->reconst != RFGPU_RECONST_LIM_VENKAT &&
+      d->reconst != RFGPU_RECONST_WENO_XYZ)
+    return RFGPU_ERR_UNSUPPORTED;
+  // RFLU_LimitGradCellsSimple walks every face of a virtual cell, including
+  // faces between two virtual cells, which a partitioned region does not hold
+  if (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1 && d->nCellsTot > d->nCells)
     return RFGPU_ERR_UNSUPPORTED;
   if (d->rkScheme < 1 || d->rkScheme > 3) return RFGPU_ERR_UNSUPPORTED;
   if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED) return RFGPU_ERR_UNSUPPORTED;
@@ -678,6 +683,9 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.rec = M.upload(cast<R>(recx), s);
   }
   g.grad = M.alloc<R>(16 * (size_t)N);
+  g.gradRaw = (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1)
+                  ? M.alloc<R>(16 * (size_t)N)
+                  : nullptr;
   cudaMemsetAsync(g.grad, 0, 16 * (size_t)N * sizeof(R), s);
   g.dtBits = M.alloc<unsigned long long>(1);
   unsigned long long inf = 0x7FF0000000000000ull;
@@ -1472,7 +1480,9 @@ int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch
     ft.insert(ft.end(), f.begin(), f.end());
     bt.insert(bt.end(), c.begin(), c.end());
     b->spaceOrder = std::max(b->spaceOrder, h->spaceOrder);
-    b->reconst = std::max(b->reconst, h->reconst);
+    // launch the WENO-XYZ pass when any region needs it (it skips the others)
+    if (b->reconst != RFGPU_RECONST_WENO_XYZ)
+      b->reconst = h->reconst == RFGPU_RECONST_WENO_XYZ ? h->reconst : std::max(b->reconst, h->reconst);
     if (i == 0) b->nSteps = h->nSteps;
     if (h->nSteps != b->nSteps) {
       cudaStreamDestroy(b->stream);

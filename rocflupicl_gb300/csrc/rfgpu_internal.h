@@ -76,6 +76,8 @@ struct RegionDev {
   const float *ivolF;  // 1/vol in FP32 (mixed-path update)
   const R *epsq;
   const R *cwt;   // [6][N] Axx,Axy,Axz,Ayy,Ayz,Azz: weight = A d/|d|^2 (mixed path)
+  // RECONST 2: the unweighted gradients the WENO-XYZ pass reads ([N][16]); null otherwise
+  R *gradRaw;
   // stencil (SELL-32)
   const long long *stOff;
   const int *stCnt, *stIdx;
@@ -174,9 +176,10 @@ struct ChunkMap {
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
        KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_HALO, KP_COUNT };
-// KP_GRADIENT times the fused gradient + limiter kernel; KP_LIMITER, KP_DT_FACE
-// and KP_DT_BFACE are no longer launched separately (kept for the ABI's
-// class numbering).
+// KP_GRADIENT times the fused gradient + limiter kernel; KP_LIMITER the
+// WENO-XYZ weighting and positivity pass of RECONST 2; KP_DT_FACE and
+// KP_DT_BFACE are no longer launched separately (kept for the ABI's class
+// numbering).
 
 // Optional hook called around every kernel launch (phase 0 before, 1 after),
 // used to record CUDA events on the launching stream.

@@ -1051,7 +1051,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
 #pragma unroll
       for (int k = 0; k < 15; ++k) out[k] = acc[k];
       out[15] = R(0);
-      st16(g.grad + 16 * (size_t)c, out);
+      st16((g.gradRaw ? g.gradRaw : g.grad) + 16 * (size_t)c, out);  // RECONST 2: weighted next
       if constexpr (fuseDt) {
         if (g.ph.reconst != 11) {  // no limiter face loop to ride on
           dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
@@ -1992,13 +1992,15 @@ int resident_blocks(K kernel) {
 }
 
 template <typename R>
+void launch_weno_xyz(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
+
+template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof,
                   int parts) {
   static const int pfFace = resident_blocks(k_face_flux<R>);
   static const int pfUpd = resident_blocks(k_gather_update<R>);
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
-  (void)reconst;
   long long n = 0;
   const bool hasGrad = spaceOrder > 1 && w.nCellTiles > 0;
   const bool grad = hasGrad && (parts & SP_GRADIENT);
@@ -2010,6 +2012,12 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
     else
       k_grad_lim<R, 0><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
     RF_MARK(KP_GRADIENT, 1);
+    ++n;
+  }
+  if (hasGrad && flux && reconst == 2) {  // after every cell's gradient
+    RF_MARK(KP_LIMITER, 0);
+    launch_weno_xyz<R>(regs, w, s);
+    RF_MARK(KP_LIMITER, 1);
     ++n;
   }
   if (a.fuseDt && hasGrad && flux) {
@@ -2074,6 +2082,96 @@ void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int 
     StepArgs sa{is, 1, 0.0, 0, 1, (fuse && is == 1) ? 1 : 0, da};
     launch_stage<R>(regs, w, sa, s, launches, spaceOrder, reconst, prof);
   }
+}
+
+// RECONST 2 (CellGradientsMP.F90:217-222): RFLU_WENOGradCellsXYZFast_3D
+// (modflu/RFLU_ModWENO.F90:1402-1588, the 3-D branch of the wrapper at
+// :1615-1668) then RFLU_LimitGradCellsSimple (modflu/RFLU_ModLimiters.F90:
+// 793-921), one thread per cell.  Every gradient component becomes the
+// average of the cell's and its stencil members' unweighted components
+// (gradRaw) weighted by s = 1/(g^2 + 1e-15), the cell first and the members in
+// stored order, sum(s g) / sum(s); then the gradient of density and pressure
+// (the positive variables, libflu/RFLU_SetVarInfo.F90:140-144) is zeroed when
+// var + grad . (fc - xc) is not positive at one of the cell's faces, interior
+// or boundary (the result does not depend on the face order).  Regions that
+// do not use RECONST 2 skip their tiles.
+template <typename R>
+__global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    if (!g.gradRaw) continue;
+    const int c = tl.first + threadIdx.x;
+    if (c >= g.nCells) continue;
+    const R eps = R(1.0E-15);
+    R ss[15], acc[15];
+    {
+      R g0[16];
+      ld16(g.gradRaw + 16 * (size_t)c, g0);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        const R t = g0[k];
+        ss[k] = R(1) / (t * t + eps);
+        acc[k] = ss[k] * t;
+      }
+    }
+    const long long base = g.stOff[c >> 5] + (c & 31);
+    const int n = g.stCnt[c];
+    for (int m = 0; m < n; ++m) {
+      R gm[16];
+      ld16(g.gradRaw + 16 * (size_t)g.stIdx[base + (long long)m * kSlice], gm);
+#pragma unroll
+      for (int k = 0; k < 15; ++k) {
+        const R t = gm[k];
+        const R sm = R(1) / (t * t + eps);
+        ss[k] = ss[k] + sm;
+        acc[k] = acc[k] + sm * t;
+      }
+    }
+    R out[16];
+#pragma unroll
+    for (int k = 0; k < 15; ++k) out[k] = acc[k] / ss[k];
+    out[15] = R(0);
+    // positivity of the face reconstructions of density (0) and pressure (4)
+    R r0[8];
+    ld8(g.rec + 8 * (size_t)c, r0);
+    const long long T = g.cfTotal;
+    const long long e0 = g.cfOff[c >> 5] + (c & 31);
+    const int nf = g.cfCnt[c];
+    const int B = g.nBFaces;
+#pragma unroll
+    for (int v = 0; v < 5; v += 4) {
+      for (int k = 0; k < nf; ++k) {
+        const long long e = e0 + (long long)k * kSlice;
+        const int code = g.cfCode[e];
+        R dx, dy, dz;
+        if (code >= 0) {  // the stored offset is xc - fc
+          dx = -g.cfD[e];
+          dy = -g.cfD[T + e];
+          dz = -g.cfD[2 * T + e];
+        } else {          // boundary: fc - xc
+          const int b = -code - 1;
+          dx = g.bfd[b];
+          dy = g.bfd[B + b];
+          dz = g.bfd[2 * B + b];
+        }
+        const R varf = r0[v] + out[3 * v] * dx + out[3 * v + 1] * dy + out[3 * v + 2] * dz;
+        if (varf <= R(0)) {
+          out[3 * v] = out[3 * v + 1] = out[3 * v + 2] = R(0);
+          break;
+        }
+      }
+    }
+    st16(g.grad + 16 * (size_t)c, out);
+  }
+}
+
+template <typename R>
+void launch_weno_xyz(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+  if (w.nCellTiles > 0)
+    k_weno_xyz<R><<<w.grid > 0 && w.grid < w.nCellTiles ? w.grid : w.nCellTiles, w.block, 0, s>>>(
+        regs, w.cellTiles, w.nCellTiles);
 }
 
 template <typename R>
@@ -2249,8 +2347,10 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
 template <typename R>
 void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
                              int spaceOrder, R *flux, double *rhs, cudaStream_t s) {
-  if (spaceOrder > 1 && w.nCellTiles > 0)
+  if (spaceOrder > 1 && w.nCellTiles > 0) {
     k_grad_lim<R, 0><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    if (g.gradRaw) launch_weno_xyz<R>(regs, w, s);
+  }
   if (g.nFaces > 0) k_face_flux_scratch<R><<<(g.nFaces + 127) / 128, 128, 0, s>>>(g, flux);
   if (w.nBFaceTiles > 0)
     k_bface_flux<R><<<w.nBFaceTiles, w.block, 0, s>>>(regs, w.bfaceTiles, w.nBFaceTiles);

@@ -141,9 +141,10 @@ def read_inp(path: str) -> CaseInput:
         bad.append(f"DISCR {n.spaceDiscr}: not one of 1 (Roe), 3 (HLLC), 4 (AUSM+), 5 (AUSM+up)")
     if n.spaceOrder not in (1, 2):
         bad.append(f"ORDER {n.spaceOrder}")
-    if n.spaceOrder == 2 and n.reconst not in (K.RECONST_NONE, K.RECONST_LIM_VENKAT):
+    if n.spaceOrder == 2 and n.reconst not in (K.RECONST_NONE, K.RECONST_WENO_XYZ,
+                                               K.RECONST_LIM_VENKAT):
         bad.append(f"RECONST {n.reconst}: the engine reconstructs with WLSQ gradients, "
-                   "unlimited (0) or Venkatakrishnan-limited (11)")
+                   "unlimited (0), WENO-XYZ weighted (2) or Venkatakrishnan-limited (11)")
     for k in ("CRECONSTC", "CRECONSTF"):
         if int(round(num.get(k, 0))) != 0:
             bad.append(f"{k} {int(num[k])}: constrained reconstruction")

@@ -179,3 +179,14 @@ def test_partition_splits_per_face_patch_values():
         assert np.array_equal(p.bcs[2].vals[:, 0], pa.global_faces.astype(float))
         got.append(pa.global_faces)
     assert np.array_equal(np.sort(np.concatenate(got)), np.arange(n0))
+
+
+def test_weno_partitioned_region_refused():
+    """RECONST 2's positivity check walks every face of a virtual cell, including
+    faces between two virtual cells that a partitioned region does not hold:
+    such a region is refused before any CUDA call."""
+    p = P.partition_case(tube(order=2, n=12), 2)[0]
+    lib, d, keep = _desc_of(p, reconst=K.RECONST_WENO_XYZ)
+    h = C.c_void_p()
+    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_UNSUPPORTED
+    assert not h.value

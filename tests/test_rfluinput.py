@@ -109,10 +109,10 @@ def test_inp_keys_sections_and_defaults(files):
 
 def test_inp_envelope_reported(tmp_path):
     p = tmp_path / "bad.inp"
-    p.write_text(INP.replace("RECONST  11", "RECONST  2").replace("CRECONSTC  0", "CRECONSTC  1")
+    p.write_text(INP.replace("RECONST  11", "RECONST  1").replace("CRECONSTC  0", "CRECONSTC  1")
                  .replace("FLOWTYPE   1", "FLOWTYPE   0").replace("MODEL    0", "MODEL    1"))
     bad = RI.read_inp(str(p)).unsupported
-    assert any(b.startswith("RECONST 2") for b in bad)
+    assert any(b.startswith("RECONST 1") for b in bad)
     assert any(b.startswith("CRECONSTC 1") for b in bad)
     assert any(b.startswith("FLOWTYPE 0") for b in bad)
     assert any("Euler only" in b for b in bad)
@@ -147,15 +147,18 @@ REF_INP = "/root/reference/input_files/AirShock/rectshktb.inp"
 
 @pytest.mark.skipif(not os.path.exists(REF_INP), reason="reference tree not present")
 def test_reference_airshock_input_read():
-    """The reference's own AirShock deck: AUSM+up second order with RK3, and
-    WENO-XYZ reconstruction with constrained reconstruction and particle
-    coupling, which the engine reports as outside its envelope."""
+    """The reference's own AirShock deck: AUSM+up second order with RK3 and
+    WENO-XYZ reconstruction (all in the envelope), with constrained
+    reconstruction and particle coupling, which the engine reports as outside
+    it."""
     ci = RI.read_inp(REF_INP)
     n = ci.numerics
     assert (n.spaceDiscr, n.spaceOrder, n.rkScheme, n.cfl) == (5, 2, 2, 0.5)
     assert (n.ausmSigma, n.ausmKp, n.ausmKu, n.ausmMInf) == (1.0, 0.25, 0.75, 0.1)
     assert ci.dt_min_limit == 2.0e-10 and n.refCp == 1004.64
-    assert any(b.startswith("RECONST 2") for b in ci.unsupported)
+    assert ci.numerics.reconst == K.RECONST_WENO_XYZ
+    assert not any(b.startswith("RECONST") for b in ci.unsupported)
+    assert any(b.startswith("CRECONSTC 1") for b in ci.unsupported)
     assert any(b.startswith("PICL USED") for b in ci.unsupported)
 
 
@@ -191,9 +194,9 @@ def test_case_files_strict_refuses(tmp_path):
     c = K.tet_shock_box(3, seed=3)
     IO.write_grid_ascii(str(tmp_path / "c.grda"), IO.grid_of_mesh(c.mesh))
     K.write_flow(str(tmp_path / "c.flo"), c.cv)
-    (tmp_path / "c.inp").write_text("# NUMERICS\nDISCR 1\nORDER 2\nRECONST 2\n#\n"
+    (tmp_path / "c.inp").write_text("# NUMERICS\nDISCR 1\nORDER 2\nRECONST 1\n#\n"
                                     "# TIMESTEP\nFLOWTYPE 1\n#\n")
     (tmp_path / "c.bc").write_text("# BC_SLIPW\nPATCH 1 6\n#\n")
-    with pytest.raises(ValueError, match="RECONST 2"):
+    with pytest.raises(ValueError, match="RECONST 1"):
         K.from_case_files(str(tmp_path / "c.grda"), str(tmp_path / "c.flo"),
                           str(tmp_path / "c.inp"), str(tmp_path / "c.bc"))
