@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--n", "--hexes", dest="n", type=int, default=128,
                     help="base hexes per direction")
     ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
+    ap.add_argument("--reconst", default="venkat", choices=["venkat", "weno-xyz", "none"],
+                    help="RECONST 11 (the benchmark's), 2 (the reference's default) or 0")
     ap.add_argument("--cell-order", default="locality", choices=["locality", "host"],
                     help="device numbering of cells and faces (results are identical)")
     ap.add_argument("--no-fp64", action="store_true")
@@ -168,15 +170,21 @@ def ncu_traffic():
         return {}
 
 
+RECONST = {"venkat": K.RECONST_LIM_VENKAT, "weno-xyz": K.RECONST_WENO_XYZ, "none": K.RECONST_NONE}
+RECONST_NAME = {"venkat": "WLSQ+Venkatakrishnan", "weno-xyz": "WLSQ+WENO-XYZ+positivity",
+                "none": "WLSQ unlimited"}
+
+
 def build_case(a):
-    num = K.Numerics(spaceDiscr=SCHEME[a.scheme], venkatGuard=1, precision=K.PREC_MIXED)
+    num = K.Numerics(spaceDiscr=SCHEME[a.scheme], venkatGuard=1, precision=K.PREC_MIXED,
+                     reconst=RECONST[getattr(a, "reconst", "venkat")])
     return K.tet_shock_box(a.n, numerics=num)
 
 
 def workload_config(c, a):
     m = c.mesh
     return {"workload": f"tet_shock_box {a.n}^3x6 Kuhn tets, jitter 0.1h, Ms=2, lognormal rho sigma 0.1; "
-                        f"{a.scheme} flux, WLSQ+Venkatakrishnan, Wray RK3",
+                        f"{a.scheme} flux, {RECONST_NAME[getattr(a, 'reconst', 'venkat')]}, Wray RK3",
             "cells": m.nCells, "faces": m.nFaces, "bfaces": m.nBFaces, "stencil_members": m.nMembs,
             "precision": "mixed: FP32 gradient/limiter/reconstruction/flux/EOS, compensated FP32 residual sums, "
                          "float-float conserved state; FP64 geometry masters and FP64 cv/dv on download",

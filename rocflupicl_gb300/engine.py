@@ -92,7 +92,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
 
 BATCH_COUPLED = 1
 
-KERNELS = ["gradient", "limiter", "face_flux", "bface_flux", "gather_update", "dt_face",
+KERNELS = ["gradient", "weno_xyz", "face_flux", "bface_flux", "gather_update", "dt_face",
            "dt_bface", "dt_cell", "dt_finalize", "halo"]
 
 _lib = None
