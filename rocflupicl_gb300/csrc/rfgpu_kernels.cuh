@@ -285,6 +285,17 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 #ifndef RF_UPD_PRE
 #define RF_UPD_PRE 6
 #endif
+// RECONST 2 pass, mixed path: gradient rows gathered together per group and
+// the weights from the hardware reciprocal.  Measured on the 128^3 tet box:
+// exact division 4.95 ms (2 rows: 5.80, 4 rows: 6.62, the division code's
+// registers), reciprocal 4.08 ms, with 2 rows 3.61 ms, with 4 rows 3.48 ms.
+// The FP64 path keeps the IEEE division and one row at a time.
+#ifndef RF_WENO_U
+#define RF_WENO_U 4
+#endif
+#ifndef RF_WENO_FASTRCP
+#define RF_WENO_FASTRCP 1
+#endif
 // Face pass: both cells' gradient rows prefetched into L1 as soon as the
 // face's cells are known (measured 0.640 -> 0.631 ms).
 #ifndef RF_FACE_PF
@@ -2105,6 +2116,12 @@ __global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict
     const int c = tl.first + threadIdx.x;
     if (c >= g.nCells) continue;
     const R eps = R(1.0E-15);
+    // the weight 1/(g^2 + 1e-15): IEEE division on the FP64 path; on the
+    // mixed path optionally the hardware reciprocal (it only weights an average)
+    auto weight = [&](R t) -> R {
+      if constexpr (sizeof(R) == 4 && RF_WENO_FASTRCP) return __fdividef(1.0f, t * t + eps);
+      else return R(1) / (t * t + eps);
+    };
     R ss[15], acc[15];
     {
       R g0[16];
@@ -2112,21 +2129,46 @@ __global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict
 #pragma unroll
       for (int k = 0; k < 15; ++k) {
         const R t = g0[k];
-        ss[k] = R(1) / (t * t + eps);
+        ss[k] = weight(t);
         acc[k] = ss[k] * t;
       }
     }
-    const long long base = g.stOff[c >> 5] + (c & 31);
-    const int n = g.stCnt[c];
-    for (int m = 0; m < n; ++m) {
-      R gm[16];
-      ld16(g.gradRaw + 16 * (size_t)g.stIdx[base + (long long)m * kSlice], gm);
+    auto member = [&](const R gm[16]) {
 #pragma unroll
       for (int k = 0; k < 15; ++k) {
         const R t = gm[k];
-        const R sm = R(1) / (t * t + eps);
+        const R sm = weight(t);
         ss[k] = ss[k] + sm;
         acc[k] = acc[k] + sm * t;
+      }
+    };
+    const long long base = g.stOff[c >> 5] + (c & 31);
+    const int n = g.stCnt[c];
+    {
+      // members in stored order, RF_WENO_U gathers issued together with the
+      // next group's indices loaded while they are in flight
+      constexpr int U = sizeof(R) == 4 ? RF_WENO_U : 1;
+      const int nFull = n - n % U;
+      int nx[U];
+#pragma unroll
+      for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(g.stIdx + base + (long long)u * kSlice) : 0;
+      for (int m = 0; m < nFull; m += U) {
+        R gm[U][16];
+#pragma unroll
+        for (int u = 0; u < U; ++u) ld16(g.gradRaw + 16 * (size_t)nx[u], gm[u]);
+#pragma unroll
+        for (int u = 0; u < U; ++u)
+          nx[u] = m + U + u < n ? ld_index(g.stIdx + base + (long long)(m + U + u) * kSlice) : 0;
+#pragma unroll
+        for (int u = 0; u < U; ++u) member(gm[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < U - 1; ++u) {
+        if (nFull + u < n) {
+          R gm[16];
+          ld16(g.gradRaw + 16 * (size_t)nx[u], gm);
+          member(gm);
+        }
       }
     }
     R out[16];
