@@ -684,7 +684,7 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
   }
   g.grad = M.alloc<R>(16 * (size_t)N);
   g.gradRaw = (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1)
-                  ? M.alloc<R>(16 * (size_t)N)
+                  ? M.alloc<R>((sizeof(R) == 8 ? 32 : 16) * (size_t)N)
                   : nullptr;
   cudaMemsetAsync(g.grad, 0, 16 * (size_t)N * sizeof(R), s);
   g.dtBits = M.alloc<unsigned long long>(1);

@@ -76,7 +76,9 @@ struct RegionDev {
   const float *ivolF;  // 1/vol in FP32 (mixed-path update)
   const R *epsq;
   const R *cwt;   // [6][N] Axx,Axy,Axz,Ayy,Ayz,Azz: weight = A d/|d|^2 (mixed path)
-  // RECONST 2: the unweighted gradients the WENO-XYZ pass reads ([N][16]); null otherwise
+  // RECONST 2, what the WENO-XYZ pass reads (null otherwise): mixed path the
+  // unweighted gradients [N][16]; FP64 path each component's weight
+  // s = 1/(g^2 + 1e-15) and s*g, [N][32] (s in 0..14, s*g in 16..30)
   R *gradRaw;
   // stencil (SELL-32)
   const long long *stOff;

@@ -1062,7 +1062,23 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
 #pragma unroll
       for (int k = 0; k < 15; ++k) out[k] = acc[k];
       out[15] = R(0);
-      st16((g.gradRaw ? g.gradRaw : g.grad) + 16 * (size_t)c, out);  // RECONST 2: weighted next
+      if (!g.gradRaw) {
+        st16(g.grad + 16 * (size_t)c, out);
+      } else if constexpr (sizeof(R) == 8) {
+        // RECONST 2, FP64: the WENO weight of each component and its product,
+        // as RFLU_WENOGradCellsXYZFast_3D forms them (same operations), once
+        // per cell instead of once per stencil visit
+        R w[16];
+#pragma unroll
+        for (int k = 0; k < 15; ++k) w[k] = R(1) / (out[k] * out[k] + R(1.0E-15));
+        w[15] = R(0);
+        st16(g.gradRaw + 32 * (size_t)c, w);
+#pragma unroll
+        for (int k = 0; k < 15; ++k) w[k] = w[k] * out[k];
+        st16(g.gradRaw + 32 * (size_t)c + 16, w);
+      } else {
+        st16(g.gradRaw + 16 * (size_t)c, out);  // RECONST 2, mixed: weighted next
+      }
       if constexpr (fuseDt) {
         if (g.ph.reconst != 11) {  // no limiter face loop to ride on
           dtbits = (unsigned long long)__double_as_longlong(cell_dt(g, c, r0));
@@ -2123,51 +2139,71 @@ __global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict
       else return R(1) / (t * t + eps);
     };
     R ss[15], acc[15];
-    {
-      R g0[16];
-      ld16(g.gradRaw + 16 * (size_t)c, g0);
-#pragma unroll
-      for (int k = 0; k < 15; ++k) {
-        const R t = g0[k];
-        ss[k] = weight(t);
-        acc[k] = ss[k] * t;
-      }
-    }
-    auto member = [&](const R gm[16]) {
-#pragma unroll
-      for (int k = 0; k < 15; ++k) {
-        const R t = gm[k];
-        const R sm = weight(t);
-        ss[k] = ss[k] + sm;
-        acc[k] = acc[k] + sm * t;
-      }
-    };
     const long long base = g.stOff[c >> 5] + (c & 31);
     const int n = g.stCnt[c];
-    {
-      // members in stored order, RF_WENO_U gathers issued together with the
-      // next group's indices loaded while they are in flight
-      constexpr int U = sizeof(R) == 4 ? RF_WENO_U : 1;
-      const int nFull = n - n % U;
-      int nx[U];
+    if constexpr (sizeof(R) == 8) {
+      // weights and products precomputed by the gradient pass: sums only
+      R w[16];
+      ld16(g.gradRaw + 32 * (size_t)c, w);
 #pragma unroll
-      for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(g.stIdx + base + (long long)u * kSlice) : 0;
-      for (int m = 0; m < nFull; m += U) {
-        R gm[U][16];
+      for (int k = 0; k < 15; ++k) ss[k] = w[k];
+      ld16(g.gradRaw + 32 * (size_t)c + 16, w);
 #pragma unroll
-        for (int u = 0; u < U; ++u) ld16(g.gradRaw + 16 * (size_t)nx[u], gm[u]);
+      for (int k = 0; k < 15; ++k) acc[k] = w[k];
+      for (int m = 0; m < n; ++m) {
+        const R *row = g.gradRaw + 32 * (size_t)g.stIdx[base + (long long)m * kSlice];
+        ld16(row, w);
 #pragma unroll
-        for (int u = 0; u < U; ++u)
-          nx[u] = m + U + u < n ? ld_index(g.stIdx + base + (long long)(m + U + u) * kSlice) : 0;
+        for (int k = 0; k < 15; ++k) ss[k] = ss[k] + w[k];
+        ld16(row + 16, w);
 #pragma unroll
-        for (int u = 0; u < U; ++u) member(gm[u]);
+        for (int k = 0; k < 15; ++k) acc[k] = acc[k] + w[k];
       }
+    } else {
+      {
+        R g0[16];
+        ld16(g.gradRaw + 16 * (size_t)c, g0);
 #pragma unroll
-      for (int u = 0; u < U - 1; ++u) {
-        if (nFull + u < n) {
-          R gm[16];
-          ld16(g.gradRaw + 16 * (size_t)nx[u], gm);
-          member(gm);
+        for (int k = 0; k < 15; ++k) {
+          const R t = g0[k];
+          ss[k] = weight(t);
+          acc[k] = ss[k] * t;
+        }
+      }
+      auto member = [&](const R gm[16]) {
+#pragma unroll
+        for (int k = 0; k < 15; ++k) {
+          const R t = gm[k];
+          const R sm = weight(t);
+          ss[k] = ss[k] + sm;
+          acc[k] = acc[k] + sm * t;
+        }
+      };
+      {
+        // members in stored order, RF_WENO_U gathers issued together with the
+        // next group's indices loaded while they are in flight
+        constexpr int U = RF_WENO_U;
+        const int nFull = n - n % U;
+        int nx[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(g.stIdx + base + (long long)u * kSlice) : 0;
+        for (int m = 0; m < nFull; m += U) {
+          R gm[U][16];
+#pragma unroll
+          for (int u = 0; u < U; ++u) ld16(g.gradRaw + 16 * (size_t)nx[u], gm[u]);
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+            nx[u] = m + U + u < n ? ld_index(g.stIdx + base + (long long)(m + U + u) * kSlice) : 0;
+#pragma unroll
+          for (int u = 0; u < U; ++u) member(gm[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U - 1; ++u) {
+          if (nFull + u < n) {
+            R gm[16];
+            ld16(g.gradRaw + 16 * (size_t)nx[u], gm);
+            member(gm);
+          }
         }
       }
     }
