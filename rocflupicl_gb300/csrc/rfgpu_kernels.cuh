@@ -277,8 +277,9 @@ __device__ __forceinline__ void hllc_flux(const Phys &ph, const R L[5], const R 
 // reuses; H = 0 plain loads.  lds_rw is the coherent form for data the same
 // kernel later overwrites (the thread's own state rows).
 // Measured on the 128^3 tet box (mixed): update pass 0.650 -> 0.636 ms with
-// its hint, gradient pass 1.928 -> 1.925 ms, face pass unchanged (0.636 ms),
-// so the face pass keeps plain loads.
+// its hint, gradient pass 1.928 -> 1.925 ms, face pass unchanged (0.636 ms;
+// 0.631 ms with and without it once the gradient rows are prefetched), so the
+// face pass keeps plain loads.
 // Update face loop: the first RF_UPD_PRE face codes loaded together ahead of
 // the flux gathers (measured: update pass 0.636 -> 0.596 ms with 4, 0.598 ms
 // with 6).
@@ -1572,7 +1573,7 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
 #pragma unroll
     for (int j = 0; j < 5; ++j)
       rsOld[j] = (is > 1) ? lds_rw<RF_HINT_U>(g.rhsSumF + j * N + c) : 0.f;
-    ld8_rw(g.rec + 8 * (size_t)c, r);
+    ld8_rw(g.rec + 8 * (size_t)c, r);  // the non-coherent path measured the same (0.598 ms)
     ivol = lds<RF_HINT_U>(g.ivolF + c);
   }
   float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
