@@ -10,8 +10,9 @@ synthetic data of those shapes.
 
 One step = one RK3 time step (device time step + 3 stages) over the whole
 mesh; the metric counts face-flux evaluations (interior + boundary faces per
-stage).  `value` is the mixed-precision path (FP32 reconstruction/flux, FP64
-accumulation/update/EOS) with the state resident in HBM; the FP64 path, the
+stage).  `value` is the mixed-precision path (FP32 gradients, limiter,
+reconstruction and flux; compensated FP32 residual sums and a float-float
+conserved state updated in FP32) with the state resident in HBM; the FP64 path, the
 L1(rho)/L1(p) error of mixed against FP64 and the end-to-end figure through
 the C ABI with host buffers are reported beside it.
 

@@ -250,6 +250,9 @@ int rfgpu_timer_stop(rfgpu_region_t h, double *ms);
 int rfgpu_set_device(int device);
 /* Free and total device memory of the current GPU (admission control). */
 int rfgpu_mem_info(long long *freeBytes, long long *totalBytes);
+/* Streaming multiprocessors of the current GPU (cudaDevAttrMultiProcessorCount):
+ * the unit the autotuner sizes persistent grids in. */
+int rfgpu_sm_count(int *sms);
 void *rfgpu_host_alloc(long long bytes);
 int rfgpu_host_free(void *p);
 
@@ -321,9 +324,12 @@ int rfgpu_batch_timer_stop(rfgpu_batch_t b, double *ms);
  * that every GPU loading the library reserves until the process exits; a
  * region needs 8*sizeof(working precision) bytes per interior face (rounded
  * up to 256) plus 40 bytes per cell, and larger regions get
- * RFGPU_ERR_NOALLOC_LIMIT before anything runs.  The first call on a device
- * looks up the array's device address (cudaGetSymbolAddress) with that
- * device current; make that first call before any stream capture.  All calls
+ * RFGPU_ERR_NOALLOC_LIMIT before anything runs.  The call runs on the device
+ * the region was created on (made current for the call, the caller's current
+ * device restored after); the first call on a device looks up the array's
+ * device address there (cudaGetSymbolAddress); make that first call before
+ * any stream capture.  The mixed path's result equals rfgpu_residual's bit
+ * for bit, like the FP64 path's.  All calls
  * share the one array, which keeps the last call's contents: calls whose work
  * overlaps on the GPU (other threads, other handles' streams) race on it and
  * must be serialised by the caller.  Synchronous, like rfgpu_residual. */

@@ -16,15 +16,8 @@ from . import engine as E
 
 
 def sm_count() -> int:
-    try:
-        import subprocess
-        out = subprocess.run(["nvidia-smi", "--query-gpu=name", "--format=csv,noheader"],
-                             capture_output=True, text=True).stdout
-        if "GB300" in out or "B300" in out:
-            return 152
-    except Exception:
-        pass
-    return 148
+    """The current GPU's SM count (cudaDevAttrMultiProcessorCount)."""
+    return E.sm_count()
 
 
 def tune_batch(batch: "E.Batch", cfl: float, dt_imposed: float = 1.0, end_time: float = 0.0,

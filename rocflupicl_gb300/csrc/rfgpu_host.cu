@@ -119,6 +119,7 @@ struct BorderH {
 
 struct rfgpu_region_s {
   int prec = 0;
+  int device = 0;                           // the GPU the region was created on
   int nCells = 0, nFaces = 0, nBFaces = 0;  // nCells: actual + virtual (nCellsTot)
   int nAct = 0;                             // actual cells
   int iRegionGlobal = 0;
@@ -1025,6 +1026,10 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   rfgpu_region_s *h = new (std::nothrow) rfgpu_region_s();
   if (!h) return RFGPU_ERR_NOMEM;
   h->prec = d->precision;
+  if (cudaGetDevice(&h->device) != cudaSuccess) {
+    delete h;
+    return RFGPU_ERR_CUDA;
+  }
   h->nCells = d->nCellsTot > 0 ? d->nCellsTot : d->nCells;
   h->nAct = d->nCells;
   h->iRegionGlobal = d->iRegionGlobal;
@@ -1683,6 +1688,13 @@ int rfgpu_mem_info(long long *freeBytes, long long *totalBytes) {
   return RFGPU_OK;
 }
 
+int rfgpu_sm_count(int *sms) {
+  if (!sms) return RFGPU_ERR_ARG;
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return RFGPU_ERR_CUDA;
+  return cuda_rc(cudaDeviceGetAttribute(sms, cudaDevAttrMultiProcessorCount, dev));
+}
+
 void *rfgpu_host_alloc(long long bytes) {
   void *p = nullptr;
   if (bytes <= 0 || cudaHostAlloc(&p, (size_t)bytes, cudaHostAllocDefault) != cudaSuccess) return nullptr;
@@ -1706,6 +1718,19 @@ static __device__ __align__(256) unsigned char g_noallocScratch[RFGPU_NOALLOC_SC
 namespace {
 std::mutex g_noallocMutex;
 void *g_noallocPtr[256] = {nullptr};
+// Makes a device current for a scope and restores the caller's on exit.
+struct DeviceScope {
+  int prev = -1;
+  bool ok = false;
+  explicit DeviceScope(int dev) {
+    if (cudaGetDevice(&prev) != cudaSuccess) return;
+    ok = prev == dev || cudaSetDevice(dev) == cudaSuccess;
+    if (prev == dev) prev = -1;
+  }
+  ~DeviceScope() {
+    if (prev >= 0) cudaSetDevice(prev);
+  }
+};
 }  // namespace
 
 extern "C" {
@@ -1716,8 +1741,13 @@ int rfgpu_residual_noalloc(rfgpu_region_t h, double *rhs) {
   const long long fluxBytes = F * 8 * (h->prec ? 4 : 8);
   const long long fluxAligned = (fluxBytes + 255) / 256 * 256;
   if (fluxAligned + N * 5 * 8 > (long long)RFGPU_NOALLOC_SCRATCH_BYTES) return RFGPU_ERR_NOALLOC_LIMIT;
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 256) return RFGPU_ERR_CUDA;
+  // everything runs with the region's device current: the scratch address
+  // is that device's (looked up once per device) and the launches go to the
+  // region's stream; the caller's current device is restored on return
+  const int dev = h->device;
+  if (dev < 0 || dev >= 256) return RFGPU_ERR_CUDA;
+  DeviceScope scope(dev);
+  if (!scope.ok) return RFGPU_ERR_CUDA;
   void *base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_noallocMutex);

@@ -2,8 +2,10 @@
 // precision R of reconstruction, limiter and flux arithmetic.  Included by
 // rfgpu_fp64.cu (R = double, built with --fmad=false so every expression
 // rounds exactly like the unfused reference expression) and rfgpu_mixed.cu
-// (R = float).  Residual accumulation, RK update, EOS and time step are FP64
-// in both.
+// (R = float).  On the FP64 path residual accumulation, RK update, EOS and
+// time step are FP64 in the reference's operation order; on the mixed path
+// they are FP32 with compensation (TwoSum residual sums, a float-float
+// conserved state, gather_update_mixed below).
 //
 // Every kernel walks a tile list (region, first item); a tile is blockDim.x
 // consecutive cells / faces / boundary faces of one region, so one launch

@@ -84,7 +84,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_batch_profile", "rfgpu_batch_profile_read", "rfgpu_batch_launch_count",
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
-           "rfgpu_mem_info", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
+           "rfgpu_mem_info", "rfgpu_sm_count", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
            "rfgpu_mesh_stencils", "rfgpu_border_copy", "rfgpu_border_pack",
            "rfgpu_border_unpack", "rfgpu_batch_create_ex", "rfgpu_mesh_build",
            "rfgpu_mesh_sizes", "rfgpu_mesh_faces", "rfgpu_mesh_cells", "rfgpu_mesh_patch",
@@ -145,6 +145,7 @@ def load(path: Optional[str] = None):
         "rfgpu_host_alloc": ([C.c_longlong], vp),
         "rfgpu_host_free": ([vp], C.c_int),
         "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
+        "rfgpu_sm_count": ([ip], C.c_int),
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
         "rfgpu_batch_set_tuning": ([vp, C.c_int], C.c_int),
         "rfgpu_mesh_stencils": ([C.c_int, C.c_int, ip, ip, ip, ip, dp, ip, ip, dp], C.c_int),
@@ -199,6 +200,13 @@ def mem_info():
     f, t = C.c_longlong(), C.c_longlong()
     _check(load().rfgpu_mem_info(C.byref(f), C.byref(t)), "rfgpu_mem_info")
     return f.value, t.value
+
+
+def sm_count() -> int:
+    """Streaming multiprocessors of the current GPU, asked of the device."""
+    n = C.c_int()
+    _check(load().rfgpu_sm_count(C.byref(n)), "rfgpu_sm_count")
+    return n.value
 
 
 def mesh_stencils(n_cells: int, n_verts: int, cell_verts, cell_nverts, v2c_off, v2c, cofg):

@@ -142,10 +142,14 @@ def test_bc_unassigned_and_unsupported(tmp_path):
     assert bcs[1].bcType == K.BC_INJECTION
 
 
-REF_INP = "/root/reference/input_files/AirShock/rectshktb.inp"
+# The reference tree's root comes from RFLU_REFERENCE_ROOT; the test is skipped
+# where it is not set or the deck is not there.
+REF_INP = os.path.join(os.environ.get("RFLU_REFERENCE_ROOT", ""), "input_files", "AirShock",
+                       "rectshktb.inp")
 
 
-@pytest.mark.skipif(not os.path.exists(REF_INP), reason="reference tree not present")
+@pytest.mark.skipif(not os.environ.get("RFLU_REFERENCE_ROOT") or not os.path.exists(REF_INP),
+                    reason="reference tree not present (set RFLU_REFERENCE_ROOT)")
 def test_reference_airshock_input_read():
     """The reference's own AirShock deck: AUSM+up second order with RK3 and
     WENO-XYZ reconstruction (all in the envelope), with constrained
