@@ -54,15 +54,21 @@ def parse():
     ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
     ap.add_argument("--reconst", default="venkat", choices=["venkat", "weno-xyz", "none"],
                     help="RECONST 11 (the benchmark's), 2 (the reference's default) or 0")
-    ap.add_argument("--cell-order", default="locality", choices=["locality", "host"],
-                    help="device numbering of cells and faces (results are identical)")
+    ap.add_argument("--cell-order", default="auto", choices=["auto", "locality", "host"],
+                    help="device numbering of cells and faces (results are identical); auto: "
+                         "the faster one, timed")
+    ap.add_argument("--no-tune", dest="tune", action="store_false",
+                    help="keep the default launch shapes instead of autotuning them")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--l1-steps", type=int, default=10)
-    ap.add_argument("--serve-requests", type=int, default=16,
-                    help="requests of the serving measurement (0 disables it)")
-    ap.add_argument("--serve-rate", type=float, default=4.0, help="Poisson rate, requests/s")
+    ap.add_argument("--precision", default="auto", choices=["auto", "mixed", "split"],
+                    help="headline precision mode; auto measures both and reports the faster "
+                         "one within L1 <= 1e-5 of the FP64 path")
+    ap.add_argument("--l1-steps", type=int, default=100)
+    ap.add_argument("--serve-requests", type=int, default=100,
+                    help="requests per Poisson rate of the serving measurement (0 disables it)")
+    ap.add_argument("--serve-rates", default="1,4,16", help="Poisson rates swept, requests/s")
     ap.add_argument("--serve-tend", type=float, default=2.0e-4, help="end time of each solve")
     return ap.parse_args()
 
@@ -213,7 +219,10 @@ def cpu_sample(c, threads: int):
 
 def run_reference(a, dist):
     """--impl reference: the reference path's CPU restatement (the Fortran
-    reference cannot be built here), all host threads, rank 0 only."""
+    reference cannot be built here, nor on the GPU machine: no Fortran compiler or
+    MPI there), all host threads, rank 0 only.  One step of this arm is one
+    RK3 time step of the full mesh, as in the GPU arm: RFLU_TimeStepInviscid +
+    RFLU_MinimumTimeStep, then the three Wray stages."""
     if dist.rank != 0:
         return
     threads = os.cpu_count() or 1
@@ -223,26 +232,32 @@ def run_reference(a, dist):
     cv, dv = c.cv.copy(), c.dv.copy()
     num = c.numerics
     dti = o.dt(cv, dv, num.cfl, 1.0, 0.0, 1.0)
-    dtm = o.dt(cv, dv, num.cfl, dti, 0.0, 0.0)
-    st = 1
+    t = 0.0
+
+    def step():
+        nonlocal t
+        dtm = o.dt(cv, dv, num.cfl, dti, 0.0, t)
+        for s in (1, 2, 3):
+            o.stage(cv, dv, s, dtm, threads=threads)
+        t += dtm
+
     for _ in range(min(a.warmup, 1)):
-        o.stage(cv, dv, st, dtm, threads=threads)
-        st = st % 3 + 1
+        step()
     t0 = time.perf_counter()
-    for _ in range(a.steps):  # one step of this arm = one RK stage of the full mesh
-        o.stage(cv, dv, st, dtm, threads=threads)
-        st = st % 3 + 1
+    for _ in range(a.steps):
+        step()
     el = time.perf_counter() - t0
-    evals = (c.mesh.nFaces + c.mesh.nBFaces) * a.steps
+    evals = 3 * (c.mesh.nFaces + c.mesh.nBFaces) * a.steps
     v = evals / el
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": a.gpus,
             "steps": a.steps, "warmup": a.warmup, "ms_per_step": el / a.steps * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": workload_config(c, a),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": f"{a.steps} RK stages of the full mesh, OpenMP C++ FP64 "
-                                       f"restatement of the reference residual/RK path "
-                                       f"(reference Fortran+MPI not buildable here)"},
+                             "sample": f"{a.steps} RK3 steps (time step + 3 Wray stages) of the "
+                                       f"full mesh, OpenMP C++ FP64 restatement of the reference "
+                                       f"residual/RK path (reference Fortran+MPI not buildable: no "
+                                       f"Fortran compiler or MPI here or on the GPU box)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)
 
@@ -290,6 +305,102 @@ def run_secondary(a, dist):
         print(json.dumps({"impl": "ours", "secondary": a.workload, **out}), flush=True)
 
 
+PREC = {"mixed": K.PREC_MIXED, "split": K.PREC_SPLIT}
+PREC_NAME = {
+    "mixed": "mixed: FP32 gradient/limiter/reconstruction/flux, compensated FP32 residual sums, "
+             "float-float conserved state updated in FP32, FP32 EOS of the pairs; FP64 geometry "
+             "masters and FP64 cv/dv on download",
+    "split": "split: FP32 gradient/limiter/reconstruction/flux; FP64 residual accumulation, FP64 "
+             "conserved state and RK update, FP64 EOS (rounded to FP32 for the gathers)"}
+
+
+def measure_mode(c, mode, a, dist, order, peak, peak_kind, clocks_on=False):
+    """Resident steps of one precision mode: CUDA events on the engine's stream
+    around the timed steps, per-kernel event means inside the same region, the
+    dominant kernel's roofline; the launch shapes chosen by the autotuner
+    first (its steps are not timed).  Returns (result dict, region)."""
+    from rocflupicl_gb300 import autotune
+    from rocflupicl_gb300 import engine as E
+    m = c.mesh
+    cm = c.with_numerics(precision=PREC[mode])
+    evals_step = 3 * (m.nFaces + m.nBFaces)
+    cfl = cm.numerics.cfl
+    r = E.Region(cm, cell_order=order)
+    dti = r.time_step(cfl, 1.0, 0.0, 1.0)
+    r.set_time(0.0)
+    tune = autotune.tune_region(r, cfl, dti) if a.tune else None
+    clocks = Clocks(dist.local) if clocks_on else None
+    if clocks:
+        # the sampler runs from the warm-up through the timed region (its 50 ms
+        # period is longer than a few steps)
+        clocks.start()
+        time.sleep(0.3)
+    for _ in range(a.warmup):
+        r.step(cfl, dti)
+    r.sync()
+    dist.barrier()
+    ms, launches, pr = timed_steps(r, a.steps, cfl, dti)
+    clk = clocks.stop() if clocks else None
+    dist.barrier()
+    ms_max = dist.max(ms)
+    s = 4
+    kb = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
+    per = {}
+    for k, (t, n) in pr.items():
+        if n:
+            per[k] = {"ms_total": t, "launches": n, "ms_avg": t / n}
+            if k in kb:
+                per[k]["gbs"] = kb[k] / (t / n * 1e-3) / 1e9
+    dom = max((k for k in per if k in kb), key=lambda k: per[k]["ms_total"])
+    traffic = ncu_traffic().get(dom) if mode == "mixed" else None
+    achieved = per[dom]["gbs"]
+    stage_b = perfmodel.stage_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
+    step_gbs = 3 * stage_b / (ms / a.steps * 1e-3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic,
+            "algorithmic_bytes_per_launch": kb[dom],
+            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured"
+            else "fallback 6.8 TB/s",
+            "step_gbs": step_gbs, "step_frac": step_gbs / peak}
+    if dom == "gradient":
+        roof["note"] = ("the gradient pass gathers every stencil member's record (~40 per tet) through "
+                        "L1/L2; its limit is the L1TEX data pipe and gather latency (one wavefront per "
+                        "gathered record per lane), DRAM traffic is below the algorithmic bytes")
+    out = {"value": evals_step * a.steps * dist.world / (ms_max * 1e-3), "ms_per_step": ms_max / a.steps,
+           "ms_local": ms, "launches": launches, "kernels": per, "roofline": roof, "clocks": clk,
+           "status": r.status(), "device_bytes": r.device_bytes, "dti": dti,
+           "precision": PREC_NAME[mode], "tuning": tune}
+    return out, r
+
+
+def l1_against_fp64(c, modes, steps, order, cfl):
+    """L1(rho), L1(p) of each reduced-precision mode against the FP64 path
+    after `steps` RK3 steps driven with the FP64 path's time steps."""
+    from rocflupicl_gb300 import engine as E
+    c64 = c.with_numerics(precision=K.PREC_FP64)
+    f = E.Region(c64, cell_order=order)
+    regs = {md: E.Region(c.with_numerics(precision=PREC[md]), cell_order=order) for md in modes}
+    dti = f.time_step(cfl, 1.0, 0.0, 1.0)
+    t = 0.0
+    for _ in range(steps):
+        dt = f.time_step(cfl, dti, 0.0, t)
+        for st in (1, 2, 3):
+            f.rk_stage(st, dt)
+            for r in regs.values():
+                r.rk_stage(st, dt)
+        t += dt
+    cvf, dvf = f.download()
+    out = {}
+    for md, r in regs.items():
+        cvm, dvm = r.download()
+        out[md] = {"l1_rho": float(np.mean(np.abs(cvm[:, 0] / cvf[:, 0] - 1.0))),
+                   "l1_p": float(np.mean(np.abs(dvm[:, 0] / dvf[:, 0] - 1.0))),
+                   "l1_steps": steps, "status": r.status()}
+        r.close()
+    f.close()
+    return out
+
+
 def main():
     a = parse()
     dist = Dist()
@@ -308,54 +419,61 @@ def main():
     evals_step = 3 * (m.nFaces + m.nBFaces)
     cfl = c.numerics.cfl
     peak, peak_kind = peaks()
-    res = {}
+    modes = ["mixed", "split"] if a.precision == "auto" else [a.precision]
+    order_tune = None
+    if a.cell_order == "auto":
+        from rocflupicl_gb300 import autotune
+        order_tune = autotune.tune_order(c.with_numerics(precision=PREC[modes[0]]))
+        order = order_tune["order"]
+    else:
+        order = E.ORDER_LOCALITY if a.cell_order == "locality" else E.ORDER_HOST
 
-    # ---- mixed path, resident ------------------------------------------------
-    order = E.ORDER_LOCALITY if a.cell_order == "locality" else E.ORDER_HOST
-    r = E.Region(c, cell_order=order)
-    dti = r.time_step(cfl, 1.0, 0.0, 1.0)
-    r.set_time(0.0)
-    # the clock sampler runs from the warm-up through the timed region (its
-    # 50 ms period is longer than a few steps)
-    clocks = Clocks(dist.local)
-    clocks.start()
-    time.sleep(0.3)
-    for _ in range(a.warmup):
-        r.step(cfl, dti)
-    r.sync()
-    dist.barrier()
-    ms, launches, pr = timed_steps(r, a.steps, cfl, dti)
-    clk = clocks.stop()
-    dist.barrier()
-    ms_max = dist.max(ms)
-    status = r.status()
-    value = evals_step * a.steps * dist.world / (ms_max * 1e-3)
-    s = 4
-    kb = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
-    per = {}
-    for k, (t, n) in pr.items():
-        if n:
-            per[k] = {"ms_total": t, "launches": n, "ms_avg": t / n}
-            if k in kb:
-                per[k]["gbs"] = kb[k] / (t / n * 1e-3) / 1e9
-    dom = max((k for k in per if k in kb), key=lambda k: per[k]["ms_total"])
-    traffic = ncu_traffic().get(dom)
-    achieved = per[dom]["gbs"]
-    stage_b = perfmodel.stage_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, s)
-    step_gbs = 3 * stage_b / (ms / a.steps * 1e-3) / 1e9
-    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "traffic": traffic,
-            "algorithmic_bytes_per_launch": kb[dom],
-            "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else "fallback 6.8 TB/s",
-            "step_gbs": step_gbs, "step_frac": step_gbs / peak}
-    if dom == "gradient":
-        roof["note"] = ("the gradient pass gathers every stencil member's record (~40 per tet) through "
-                        "L1/L2; its limit is the L1TEX data pipe (one wavefront per gathered record per "
-                        "lane), DRAM traffic is below the algorithmic bytes")
+    # ---- resident steps of each precision mode ---------------------------------
+    res = {}
+    for i, md in enumerate(modes):
+        out, r = measure_mode(c, md, a, dist, order, peak, peak_kind, clocks_on=True)
+        r.close()
+        res[md] = out
+
+    # ---- accuracy against the FP64 path (same dt sequence), FP64 throughput -----
+    fp64 = None
+    if not a.no_fp64:
+        c64 = c.with_numerics(precision=K.PREC_FP64)
+        f = E.Region(c64, cell_order=order)
+        dti = res[modes[0]]["dti"]
+        for _ in range(min(a.warmup, 2)):
+            f.step(cfl, dti)
+        f.sync()
+        nst = max(2, min(a.steps, 5))
+        ms64, _, pr64 = timed_steps(f, nst, cfl, dti)
+        kb64 = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, 8)
+        dom64 = max((k for k in pr64 if k in kb64 and pr64[k][1]), key=lambda k: pr64[k][0])
+        t64 = pr64[dom64][0] / pr64[dom64][1]
+        fp64 = {"value": evals_step * nst / (ms64 * 1e-3), "ms_per_step": ms64 / nst,
+                "steps": nst, "dominant_kernel": dom64, "dominant_gbs": kb64[dom64] / (t64 * 1e-3) / 1e9,
+                "bound": "fp64 ALU (GB300 non-tensor FP64 rate), not HBM",
+                "kernel_ms": {k: v[0] / v[1] for k, v in pr64.items() if v[1]}}
+        f.close()
+        for md, acc in l1_against_fp64(c, modes, a.l1_steps, order, cfl).items():
+            res[md].update(acc)
+            res[md]["speedup_vs_fp64"] = res[md]["value"] / dist.world / fp64["value"]
+
+    # ---- the headline mode, chosen by the numbers: the fastest mode within the
+    # accuracy target (L1(rho), L1(p) <= 1e-5 against FP64 after l1_steps) --------
+    def within(md):
+        return "l1_rho" in res[md] and res[md]["l1_rho"] <= 1e-5 and res[md]["l1_p"] <= 1e-5
+    ok = [md for md in modes if within(md)] or modes
+    head = max(ok, key=lambda md: res[md]["value"])
+    H = res[head]
 
     # ---- e2e through the C ABI with host buffers --------------------------------
     e2e = None
     if not a.no_e2e:
+        r = E.Region(c.with_numerics(precision=PREC[head]), cell_order=order)
+        if H["tuning"]:
+            r.set_tuning(**H["tuning"]["shape"])
+        dti = H["dti"]
+        r.set_time(0.0)
         cvh = E.PinnedArray((m.nCells, 5))
         dvh = E.PinnedArray((m.nCells, 3))
         r.download_into(cvh.array, dvh.array)
@@ -388,62 +506,25 @@ def main():
                "three_calls_path": "rfgpu_upload(cv) + rfgpu_step + rfgpu_download(cv,dv)"}
         cvh.close()
         dvh.close()
-    dev_bytes = r.device_bytes
-    r.close()
+        r.close()
 
-    # ---- FP64 path and accuracy of mixed vs FP64 -------------------------------
-    fp64 = None
-    if not a.no_fp64:
-        c64 = c.with_numerics(precision=K.PREC_FP64)
-        f = E.Region(c64, cell_order=order)
-        for _ in range(min(a.warmup, 2)):
-            f.step(cfl, dti)
-        f.sync()
-        nst = max(2, min(a.steps, 5))
-        ms64, _, pr64 = timed_steps(f, nst, cfl, dti)
-        kb64 = perfmodel.engine_kernel_bytes(m.nCells, m.nFaces, m.nBFaces, m.nMembs, 8)
-        dom64 = max((k for k in pr64 if k in kb64 and pr64[k][1]), key=lambda k: pr64[k][0])
-        t64 = pr64[dom64][0] / pr64[dom64][1]
-        fp64 = {"value": evals_step * nst / (ms64 * 1e-3), "ms_per_step": ms64 / nst,
-                "steps": nst, "dominant_kernel": dom64, "dominant_gbs": kb64[dom64] / (t64 * 1e-3) / 1e9,
-                "bound": "fp64 ALU (GB300 non-tensor FP64 rate), not HBM",
-                "kernel_ms": {k: v[0] / v[1] for k, v in pr64.items() if v[1]}}
-        f.close()
-        # identical dt sequence (from the FP64 path) for both precisions
-        f = E.Region(c64, cell_order=order)
-        mm = E.Region(c, cell_order=order)
-        t = 0.0
-        for _ in range(a.l1_steps):
-            dt = f.time_step(cfl, dti, 0.0, t)
-            for st in (1, 2, 3):
-                f.rk_stage(st, dt)
-                mm.rk_stage(st, dt)
-            t += dt
-        cvf, dvf = f.download()
-        cvm, dvm = mm.download()
-        fp64["l1_rho"] = float(np.mean(np.abs(cvm[:, 0] / cvf[:, 0] - 1.0)))
-        fp64["l1_p"] = float(np.mean(np.abs(dvm[:, 0] / dvf[:, 0] - 1.0)))
-        fp64["l1_steps"] = a.l1_steps
-        fp64["speedup_mixed_vs_fp64"] = value / dist.world / fp64["value"]
-        f.close()
-        mm.close()
-
-    # ---- serving: continuous batching of a seeded Poisson stream ---------------
+    # ---- serving: continuous batching of seeded Poisson streams -----------------
     serving = None
     if a.serve_requests > 0:
         from rocflupicl_gb300 import serving as S
-        reqs = S.poisson_requests(a.serve_requests, a.serve_rate, seed=17 + dist.rank)
-        srv = S.Server(a.serve_tend, prepare_workers=4, mesh_threads=4)
-        t0 = time.perf_counter()
-        rs = srv.run(reqs)
-        wall = time.perf_counter() - t0
-        serving = S.summarize(rs, wall)
-        serving.update({"rate_per_s": a.serve_rate, "t_end": a.serve_tend,
-                        "max_active": srv.max_active, "batch_iterations": srv.iterations,
-                        "cells": "6k^3, log-uniform 10k-4M", "precision": "mixed",
-                        "latency": "arrival -> state read back, including mesh preparation "
-                                   "(vertices and cells on the host; face list, geometry and "
-                                   "stencils on the GPU), registration and queueing"})
+        serving = {"requests_per_rate": a.serve_requests, "t_end": a.serve_tend,
+                   "cells": "6k^3, log-uniform 10k-4M", "precision": "mixed",
+                   "latency": "arrival -> state read back, including mesh preparation "
+                              "(vertices and cells on the host; face list, geometry and "
+                              "stencils on the GPU), registration and queueing", "rates": {}}
+        for lam in [float(x) for x in a.serve_rates.split(",")]:
+            reqs = S.poisson_requests(a.serve_requests, lam, seed=17 + dist.rank)
+            srv = S.Server(a.serve_tend, prepare_workers=4, mesh_threads=4)
+            t0 = time.perf_counter()
+            rs = srv.run(reqs)
+            o = S.summarize(rs, time.perf_counter() - t0)
+            o.update({"max_active": srv.max_active, "batch_iterations": srv.iterations})
+            serving["rates"][str(lam)] = o
 
     # ---- CPU baseline (rank 0) --------------------------------------------------
     cpu = None
@@ -455,13 +536,21 @@ def main():
                          f"OpenMP C++ FP64 restatement of the reference path, {el:.1f} s"}
 
     if dist.rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": dist.world,
-                "steps": a.steps, "warmup": a.warmup, "ms_per_step": ms_max / a.steps,
+        cfg = workload_config(c, a)
+        cfg["precision"] = H["precision"]
+        cfg["cell_order"] = "locality" if order == E.ORDER_LOCALITY else "host"
+        cfg["autotune"] = {"order": order_tune, "launch": H["tuning"]}
+        line = {"metric": METRIC, "value": H["value"], "unit": UNIT, "n_gpus": dist.world,
+                "steps": a.steps, "warmup": a.warmup, "ms_per_step": H["ms_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-                "dtype": "f32 (float-float state)", "data": "synthetic (seeded)",
-                "config": workload_config(c, a), "roofline": roof, "cpu_baseline": cpu,
-                "e2e": e2e, "gpu_launches": launches, "clocks": clk, "status": status,
-                "kernels": per, "fp64": fp64, "device_bytes": dev_bytes, "serving": serving}
+                "dtype": "f32 flux (" + head + ")", "data": "synthetic (seeded)",
+                "config": cfg, "roofline": H["roofline"], "cpu_baseline": cpu,
+                "e2e": e2e, "gpu_launches": H["launches"], "clocks": H["clocks"],
+                "status": H["status"], "kernels": H["kernels"], "headline_mode": head,
+                "modes": {md: {k: v for k, v in res[md].items()
+                               if k not in ("ms_local", "dti", "kernels", "clocks")}
+                          for md in modes},
+                "fp64": fp64, "device_bytes": H["device_bytes"], "serving": serving}
         print(json.dumps(line), flush=True)
     dist.close()
 

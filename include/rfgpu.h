@@ -62,7 +62,13 @@ enum {
   RFGPU_PREC_FP64 = 0,   /* everything FP64; bit-identical to the reference order */
   RFGPU_PREC_MIXED = 1,  /* FP32 prim/gradients/limiter/flux with compensated
                             residual sums; float-float (~48-bit) conserved
-                            state and RK update; FP64 cv/dv on download */
+                            state and RK update; FP32 EOS for the next stage
+                            (the energy's low part kept); FP64 cv/dv on
+                            download */
+  RFGPU_PREC_SPLIT = 2,  /* FP32 prim/gradients/limiter/reconstruction/flux;
+                            FP64 residual accumulation, FP64 conserved state
+                            and RK update, FP64 EOS of the new state (rounded
+                            to FP32 for the next stage's gathers) */
   /* Device numbering.  LOCALITY: cells renumbered along a Morton curve of
    * their centroids and interior faces grouped by their lower-numbered cell,
    * so a block's stencil and face gathers stay within a compact patch of the
@@ -226,8 +232,25 @@ void *rfgpu_stream(rfgpu_region_t h);
 long long rfgpu_device_bytes(rfgpu_region_t h);
 /* Kernel launches issued by the handle since creation. */
 long long rfgpu_launch_count(rfgpu_region_t h);
-/* Launch configuration used by the kernels (block size); 0 = default. */
-int rfgpu_set_tuning(rfgpu_region_t h, int blockCells, int blockFaces);
+/* Launch shapes of the stage passes, chosen by the autotuner
+ * (rocflupicl_gb300/autotune.py) by timing real steps; results do not depend
+ * on them.  A zero field keeps the default.  No counterpart in the reference
+ * (its loops run serially on the host). */
+typedef struct {
+  int gridCap;         /* blocks per launch of every tiled pass; a grid smaller than
+                          the tile count walks the tiles persistently; 0 = one
+                          block per tile */
+  int gradBlock;       /* threads (= cells) per block of the gradient + limiter
+                          pass: 64, 128 (default) or 256 */
+  int faceBlock;       /* threads per block of the interior-face flux pass: 64,
+                          128 (default) or 256 */
+  int facesPerThread;  /* interior faces per thread of that pass: 1 (default) or 2 */
+  int cellBlock;       /* threads (= cells) per block of the residual gather and
+                          update pass: 64, 128 (default) or 256 */
+} rfgpu_tuning_t;
+/* RFGPU_ERR_ARG for a shape outside the values above.  Drops a captured
+ * graph (the next rfgpu_steps_graph captures again). */
+int rfgpu_set_tuning(rfgpu_region_t h, const rfgpu_tuning_t *t);
 
 /* Per-kernel profiler (the engine's counterpart of the reference's ROCPROF
  * FPROFILER_BEGINS/ENDS markers): while enabled, CUDA events are recorded on
@@ -302,9 +325,8 @@ int rfgpu_batch_step(rfgpu_batch_t b, double cfl, double dtImposed, double dtMin
 int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtImposed,
                             double dtMinLimit, double endTime);
 int rfgpu_batch_sync(rfgpu_batch_t b);
-/* Persistent grid size of the batch's launches (blocks; 0 = one block per
- * tile).  Chosen by the autotuner (rocflupicl_gb300/autotune.py). */
-int rfgpu_batch_set_tuning(rfgpu_batch_t b, int gridCap);
+/* Launch shapes of the batch's passes (rfgpu_tuning_t, as for a region). */
+int rfgpu_batch_set_tuning(rfgpu_batch_t b, const rfgpu_tuning_t *t);
 void *rfgpu_batch_stream(rfgpu_batch_t b);
 int rfgpu_batch_profile(rfgpu_batch_t b, int enable);
 int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int n);

@@ -22,7 +22,10 @@ RK_SCHEME_4_CLASSICAL, RK_SCHEME_3_WRAY, RK_SCHEME_1_EULER = 1, 2, 3
 BC_OUTFLOW, BC_SLIPWALL, BC_FARFIELD, BC_INJECTION = 20, 60, 80, 90
 BC_INFLOW_TOTANG, BC_INFLOW_VELTEMP = 10, 11
 BCOPT_SUPERSONIC, BCOPT_SUBSONIC, BCOPT_MIXED = 0, 1, 2
-PREC_FP64, PREC_MIXED = 0, 1
+# precision modes (rfgpu.h RFGPU_PREC_*): FP64; mixed = FP32 flux with a
+# float-float state updated in FP32; split = FP32 flux with FP64 residual sums,
+# RK update and EOS
+PREC_FP64, PREC_MIXED, PREC_SPLIT = 0, 1, 2
 
 SCHEME_NAMES = {DISCR_UPW_ROE: "roe", DISCR_UPW_HLLC: "hllc", DISCR_UPW_AUSMPLUS: "ausm+",
                 DISCR_UPW_AUSMPLUSUP: "ausm+up"}
@@ -199,6 +202,34 @@ def tet_shock_box(n: int = 128, seed: int = 2024, jitter: float = 0.1, Ms: float
     cv = prim_to_cv(num, r, u, z, z, p)
     return Case("tet_shock_box", m, num, tube_bcs(2), cv, eos_dv(num, cv), n_steps=n_steps,
                 meta={"n": n, "seed": seed, "Ms": Ms, "sigma": sigma})
+
+
+def cold_stream_box(n: int = 12, mach: float = 8.0, T: float = 100.0, seed: int = 5,
+                    jitter: float = 0.1, sigma: float = 0.1, dp: float = 0.05,
+                    numerics: Optional[Numerics] = None) -> Case:
+    """A cold supersonic stream along +x through the jittered Kuhn-tet box:
+    kinetic energy far above internal energy (1/2 |u|^2 / e = g (g-1) M^2 / 2,
+    18 at Mach 8), where recovering p from E - |m|^2/(2 rho) cancels.  rho =
+    p/(R T) times a lognormal factor exp(sigma Z) per cell (contacts carried by
+    the stream), p times 1 + dp sin(2 pi x) sin(2 pi y) (acoustic waves), u =
+    M a of the base state.  Slip walls on y/z, extrapolation on the x ends."""
+    num = numerics or Numerics(spaceDiscr=DISCR_UPW_ROE)
+    m = _mesh.box(_mesh.TET, n, n, n, jitter=jitter, seed=seed)
+    rng = np.random.default_rng(seed)
+    g = num.gamma_gv
+    R = 8314.3 / num.gv[1]
+    p0 = 1.0e5
+    rho0 = p0 / (R * T)
+    u0 = mach * np.sqrt(g * R * T)
+    x, y = m.cofg[:, 0], m.cofg[:, 1]
+    p = p0 * (1.0 + dp * np.sin(2.0 * np.pi * x) * np.sin(2.0 * np.pi * y))
+    r = rho0 * np.exp(sigma * rng.standard_normal(m.nCells))
+    u = np.full(m.nCells, u0)
+    z = np.zeros_like(r)
+    cv = prim_to_cv(num, r, u, z, z, p)
+    return Case("cold_stream_box", m, num, tube_bcs(2), cv, eos_dv(num, cv),
+                meta={"n": n, "seed": seed, "mach": mach, "T": T,
+                      "kinetic_over_internal": 0.5 * g * (g - 1.0) * mach * mach})
 
 
 def fourier_state(xyz: np.ndarray, seed: int, n_modes: int = 8):

@@ -8,6 +8,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <mutex>
 #include <new>
 #include <vector>
@@ -106,6 +107,12 @@ struct ProfState {
   }
 };
 
+// Tile lists of the tuned launch shapes, made once per item stride and kept
+// for the handle's lifetime (a few bytes per 64 items).
+struct TileCache {
+  std::map<int, std::pair<Tile *, int>> cells, faces;
+};
+
 }  // namespace
 
 // One border of a partitioned region: its send and receive cells in the
@@ -163,6 +170,7 @@ struct rfgpu_region_s {
   ProfState prof;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
   const int *cellNew = nullptr, *cellOld = nullptr;  // device numbering (null: host's)
+  TileCache tiles;
 };
 
 struct rfgpu_batch_s {
@@ -179,6 +187,8 @@ struct rfgpu_batch_s {
   long long perStep = 0;
   ProfState prof;
   cudaEvent_t t0 = nullptr, t1 = nullptr;
+  TileCache tiles;
+  std::vector<int> nCells, nFaces;  // per member region, for its tile lists
 };
 
 namespace {
@@ -226,7 +236,9 @@ int check_desc(const rfgpu_region_desc_t *d) {
   if (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1 && d->nCellsTot > d->nCells)
     return RFGPU_ERR_UNSUPPORTED;
   if (d->rkScheme < 1 || d->rkScheme > 3) return RFGPU_ERR_UNSUPPORTED;
-  if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED) return RFGPU_ERR_UNSUPPORTED;
+  if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED &&
+      d->precision != RFGPU_PREC_SPLIT)
+    return RFGPU_ERR_UNSUPPORTED;
   if (d->cellOrder != RFGPU_ORDER_LOCALITY && d->cellOrder != RFGPU_ORDER_HOST)
     return RFGPU_ERR_UNSUPPORTED;
   for (int ip = 0; ip < d->nPatches; ++ip) {
@@ -669,6 +681,16 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
     g.rhsSum = M.alloc<double>(5 * (size_t)N);
     cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
+  } else if (h->prec == RFGPU_PREC_SPLIT) {
+    // FP64 state, history and 1/V; dv only as the download's image
+    g.cv = M.alloc<double>(5 * (size_t)N);
+    g.cvOld = ph.rkScheme == RFGPU_RK_SCHEME_4_CLASSICAL ? M.alloc<double>(5 * (size_t)N) : nullptr;
+    g.rhsSum = M.alloc<double>(5 * (size_t)N);
+    cudaMemsetAsync(g.rhsSum, 0, 5 * (size_t)N * sizeof(double), s);
+    std::vector<double> iv(N);
+#pragma omp parallel for schedule(static)
+    for (int c = 0; c < N; ++c) iv[c] = 1.0 / vol[c];
+    g.ivol = M.upload(iv, s);
   } else {
     g.rhsSumF = M.alloc<float>(5 * (size_t)N);
     cudaMemsetAsync(g.rhsSumF, 0, 5 * (size_t)N * sizeof(float), s);
@@ -800,12 +822,13 @@ int transfer_setup(rfgpu_region_s *h) {
 void upload_chunk(rfgpu_region_s *h, int k, const double *cvS, const double *dvS,
                   cudaStream_t s) {
   launch_upload_list<float>(regs_of<float>(h), h->xList + h->xOff[k], h->xOff[k + 1] - h->xOff[k],
-                            cvS, dvS, s);
+                            cvS, dvS, h->prec == RFGPU_PREC_SPLIT, s);
   h->launches++;
 }
 void download_chunk(rfgpu_region_s *h, int k, double *cvS, double *dvS) {
   launch_download_list<float>(regs_of<float>(h), h->xList + h->xOff[k],
-                              h->xOff[k + 1] - h->xOff[k], cvS, dvS, h->stream);
+                              h->xOff[k + 1] - h->xOff[k], cvS, dvS,
+                              h->prec == RFGPU_PREC_SPLIT, h->stream);
   h->launches++;
 }
 
@@ -1003,6 +1026,61 @@ void dt_launch(rfgpu_region_s *h, const DtArgs &a) {
     launch_dt<double>(regs_of<double>(h), h->work, a, h->stream, &h->launches, h->prof.hookp());
 }
 
+// The launch shapes of rfgpu_tuning_t applied to a Work: tile lists of the
+// requested strides over the regions whose cell / face counts are given (in
+// batch order), made on first use.
+int apply_tuning(Work &w, TileCache &tc, DevAlloc &M, cudaStream_t s, const rfgpu_tuning_t &t,
+                 const std::vector<int> &nCells, const std::vector<int> &nFaces) {
+  auto okBlock = [](int b) { return b == 0 || b == 64 || b == 128 || b == 256; };
+  if (t.gridCap < 0 || !okBlock(t.gradBlock) || !okBlock(t.faceBlock) || !okBlock(t.cellBlock) ||
+      t.facesPerThread < 0 || t.facesPerThread > 2)
+    return RFGPU_ERR_ARG;
+  auto list = [&](std::map<int, std::pair<Tile *, int>> &cache, const std::vector<int> &counts,
+                  int stride) -> std::pair<Tile *, int> {
+    auto it = cache.find(stride);
+    if (it != cache.end()) return it->second;
+    std::vector<Tile> v;
+    for (size_t r = 0; r < counts.size(); ++r) {
+      auto a = make_tiles((int)r, counts[r], stride);
+      v.insert(v.end(), a.begin(), a.end());
+    }
+    Tile *d = M.upload(v, s);
+    if (cudaStreamSynchronize(s) != cudaSuccess) throw std::bad_alloc();
+    return cache[stride] = {d, (int)v.size()};
+  };
+  try {
+    const int gb = t.gradBlock ? t.gradBlock : 128, cb = t.cellBlock ? t.cellBlock : 128;
+    const int fb = t.faceBlock ? t.faceBlock : 128, fpt = t.facesPerThread ? t.facesPerThread : 1;
+    w.grid = t.gridCap;
+    if (gb == 128) {
+      w.gradTiles = nullptr;
+      w.nGradTiles = 0;
+    } else {
+      auto p = list(tc.cells, nCells, gb);
+      w.gradTiles = p.first;
+      w.nGradTiles = p.second;
+    }
+    w.gradBlock = gb;
+    if (cb == 128) {
+      w.updTiles = nullptr;
+      w.nUpdTiles = 0;
+    } else {
+      auto p = list(tc.cells, nCells, cb);
+      w.updTiles = p.first;
+      w.nUpdTiles = p.second;
+    }
+    w.cellBlock = cb;
+    auto p = list(tc.faces, nFaces, fb * fpt);
+    w.faceTiles = p.first;
+    w.nFaceTiles = p.second;
+    w.faceBlock = fb;
+    w.facesPerThread = fpt;
+  } catch (const std::bad_alloc &) {
+    return RFGPU_ERR_NOMEM;
+  }
+  return RFGPU_OK;
+}
+
 void step_launch(rfgpu_region_s *h, double cfl, double dtImposed, double dtMinLimit,
                  double endTime) {
   DtArgs da{cfl, dtImposed, dtMinLimit, endTime, 1, 0.0};
@@ -1089,6 +1167,8 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
     h->bfaceTiles = h->mem.upload(bt, h->stream);
     h->work = Work{h->cellTiles, h->faceTiles, h->bfaceTiles, (int)ct.size(), (int)ft.size(),
                    (int)bt.size(), 0, block, 1};
+    h->tiles.faces[block] = {h->faceTiles, (int)ft.size()};
+    h->work.split = h->prec == RFGPU_PREC_SPLIT;
     h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
     if (h->prec) h->stage2 = h->mem.alloc<double>(3 * (size_t)h->nCells);
     cudaStreamSynchronize(h->stream);
@@ -1345,10 +1425,11 @@ void *rfgpu_stream(rfgpu_region_t h) { return h ? (void *)h->stream : nullptr; }
 long long rfgpu_device_bytes(rfgpu_region_t h) { return h ? h->mem.bytes : -1; }
 long long rfgpu_launch_count(rfgpu_region_t h) { return h ? h->launches : -1; }
 
-int rfgpu_set_tuning(rfgpu_region_t h, int gridCap, int unused) {
-  (void)unused;
-  if (!h || gridCap < 0) return RFGPU_ERR_ARG;
-  h->work.grid = gridCap;
+int rfgpu_set_tuning(rfgpu_region_t h, const rfgpu_tuning_t *t) {
+  if (!h || !t) return RFGPU_ERR_ARG;
+  if (cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  const int rc = apply_tuning(h->work, h->tiles, h->mem, h->stream, *t, {h->nCells}, {h->nFaces});
+  if (rc != RFGPU_OK) return rc;
   if (h->graph) {
     cudaGraphExecDestroy(h->graph);
     h->graph = nullptr;
@@ -1484,6 +1565,8 @@ int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch
     ct.insert(ct.end(), a.begin(), a.end());
     ft.insert(ft.end(), f.begin(), f.end());
     bt.insert(bt.end(), c.begin(), c.end());
+    b->nCells.push_back(h->nCells);
+    b->nFaces.push_back(h->nFaces);
     b->spaceOrder = std::max(b->spaceOrder, h->spaceOrder);
     // launch the WENO-XYZ pass when any region needs it (it skips the others)
     if (b->reconst != RFGPU_RECONST_WENO_XYZ)
@@ -1502,6 +1585,8 @@ int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n};
+    b->tiles.faces[block] = {dft, (int)ft.size()};
+    b->work.split = prec == RFGPU_PREC_SPLIT;
     if (coupled) {
       b->work.coupled = 1;
       b->work.halo = links.empty() ? nullptr : b->mem.upload(links, b->stream);
@@ -1589,9 +1674,11 @@ int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtIm
   return RFGPU_OK;
 }
 
-int rfgpu_batch_set_tuning(rfgpu_batch_t b, int gridCap) {
-  if (!b || gridCap < 0) return RFGPU_ERR_ARG;
-  b->work.grid = gridCap;
+int rfgpu_batch_set_tuning(rfgpu_batch_t b, const rfgpu_tuning_t *t) {
+  if (!b || !t) return RFGPU_ERR_ARG;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  const int rc = apply_tuning(b->work, b->tiles, b->mem, b->stream, *t, b->nCells, b->nFaces);
+  if (rc != RFGPU_OK) return rc;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;

@@ -64,7 +64,8 @@ struct RegionDev {
   // as float-float pairs, cvF[2][5][N] (hi rows, then lo rows; the pair's sum
   // carries about 48 significand bits) with the RK increment history in FP32
   // (rhsSumF); its cv and dv exist only as host images, converted in one pass
-  // on upload / download.
+  // on upload / download.  The split path (R = float, cvF null) keeps cv,
+  // cvOld and rhsSum in FP64 SoA like the FP64 path, and no dv on the device.
   double *cv, *cvOld, *rhsSum, *dv, *rhs;
   float *rhsSumF;
   float *cvF, *cvOldF;
@@ -74,6 +75,7 @@ struct RegionDev {
   // geometry
   const double *vol;
   const float *ivolF;  // 1/vol in FP32 (mixed-path update)
+  const double *ivol;  // 1/vol in FP64 (split-path update)
   const R *epsq;
   const R *cwt;   // [6][N] Axx,Axy,Axz,Ayy,Ayz,Azz: weight = A d/|d|^2 (mixed path)
   // RECONST 2, what the WENO-XYZ pass reads (null otherwise): mixed path the
@@ -144,6 +146,16 @@ struct Work {
   int coupled;
   const HaloLink *halo;
   int nHalo;
+  // tuned launch shapes (zero: 128 threads, one item per thread, the cell
+  // tiles above): the gradient pass over gradTiles of gradBlock cells, the
+  // interior-face pass over faceTiles of faceBlock * facesPerThread faces
+  // (faceBlock threads, facesPerThread faces each), the gather/update pass
+  // over updTiles of cellBlock cells
+  const Tile *gradTiles, *updTiles;
+  int nGradTiles, nUpdTiles;
+  int gradBlock, faceBlock, facesPerThread, cellBlock;
+  // 1: the regions run the split precision mode (R = float, FP64 state)
+  int split;
 };
 
 struct DtArgs {
@@ -200,10 +212,10 @@ void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStr
 // may be null where the call allows it.
 template <typename R>
 void launch_upload_list(const RegionDev<R> *regs, const int *list, int n, const double *cvH,
-                        const double *dvH, cudaStream_t s);
+                        const double *dvH, int split, cudaStream_t s);
 template <typename R>
 void launch_download_list(const RegionDev<R> *regs, const int *list, int n, double *cvH,
-                          double *dvH, cudaStream_t s);
+                          double *dvH, int split, cudaStream_t s);
 // Halo exchange: the links of a coupled batch (regs indexed by region), or
 // one border between two handles (send cells of src -> receive cells of dst,
 // device numbering).  Copies the conserved state and rebuilds the received

@@ -353,6 +353,16 @@ __device__ __forceinline__ float lds_rw(const float *p) {
     return *p;
   }
 }
+template <int H>
+__device__ __forceinline__ double lds_rw(const double *p) {
+  if constexpr (H) {
+    double v;
+    asm volatile("ld.global.L1::evict_first.f64 %0, [%1];" : "=d"(v) : "l"(p));
+    return v;
+  } else {
+    return *p;
+  }
+}
 
 // The stencil-index stream of the mixed gradient pass: each index is read
 // once, so it is loaded L1::evict_first and leaves L1 to the neighbour records
@@ -436,6 +446,39 @@ __device__ __forceinline__ void st16(R *p, const R v[16]) {
   st8(p + 8, v + 8);
 }
 
+// ---- packed FP32 pairs (f32x2, sm_100 and later): two FP32 lanes per
+// instruction, a pair held in one 64-bit register (low half first) --------
+typedef unsigned long long f2x;
+__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
+  f2x r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ void f2_unpack(f2x a, float &lo, float &hi) {
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
+}
+__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
+  f2x r;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
+  f2x r;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
+  return r;
+}
+__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
+  f2x r;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
+  return r;
+}
+// a 32-byte record as four pairs, one 256-bit load
+__device__ __forceinline__ void ld4p(const float *__restrict__ p, f2x v[4]) {
+  asm("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];"
+      : "=l"(v[0]), "=l"(v[1]), "=l"(v[2]), "=l"(v[3])
+      : "l"(p));
+}
+
 // Cell-centre values the *_ComputeFlux2_TCP loops start from: rho, u = rhou *
 // (1/rho) with rhou the conserved momentum as CellGradientsMP's Prim2Cons
 // left it (rho * u_prim), p from dv.  On the mixed path the FP32 primitive
@@ -474,18 +517,29 @@ __device__ __forceinline__ void reconstruct(const R G[16], R dx, R dy, R dz, R S
 // One face term of RFLU_ComputeLimiterVenkat (modflu/RFLU_ModLimiters.F90:482-504).
 // guard = 0 keeps the reference's denom + TINY; guard = 1 adds TINY with the
 // sign of denom (for d2 < 0 the reference sum can cancel).
+// Mixed path: with RF_LIM_FASTDIV the quotient is the hardware approximate
+// division (__fdividef, within 2 ulp for denominators below 2^126; the terms
+// here stay far below), the FP64 path keeps IEEE division.
+#ifndef RF_LIM_FASTDIV
+#define RF_LIM_FASTDIV 0
+#endif
+template <typename R>
+__device__ __forceinline__ R venkat_div(R a, R b) {
+  if constexpr (sizeof(R) == 4 && RF_LIM_FASTDIV) return __fdividef(a, b);
+  else return a / b;
+}
 template <typename R>
 __device__ __forceinline__ void venkat_term(R d2, R dmax, R dmin, R epsq, R &lim, int guard) {
   const R TINY = R(1.0e-12);
   if (d2 > R(0)) {
     R numer = (dmax * dmax + epsq) * d2 + R(2) * d2 * d2 * dmax;
     R denom = d2 * (dmax * dmax + R(2) * d2 * d2 + dmax * d2 + epsq);
-    R term = numer / (denom + TINY);
+    R term = venkat_div(numer, denom + TINY);
     lim = rmin(term, lim);
   } else if (d2 < R(0)) {
     R numer = (dmin * dmin + epsq) * d2 + R(2) * d2 * d2 * dmin;
     R denom = d2 * (dmin * dmin + R(2) * d2 * d2 + dmin * d2 + epsq);
-    R term = numer / (denom + (guard ? -TINY : TINY));
+    R term = venkat_div(numer, denom + (guard ? -TINY : TINY));
     lim = rmin(term, lim);
   }
 }
@@ -532,11 +586,11 @@ __device__ __forceinline__ void prefetch_grad_tile(const RegionDev<R> &g, int fi
 }
 
 template <typename R>
-__device__ __forceinline__ void prefetch_face_tile(const RegionDev<R> &g, int first) {
+__device__ __forceinline__ void prefetch_face_tile(const RegionDev<R> &g, int first, int count) {
   if (threadIdx.x != 0) return;
   const int F = g.nFaces;
   if (first >= F) return;
-  const size_t n = (size_t)(F - first < (int)blockDim.x ? F - first : (int)blockDim.x);
+  const size_t n = (size_t)(F - first < count ? F - first : count);
   prefetch_l2(g.f2c + first, n * sizeof(int));
   prefetch_l2(g.f2c + F + first, n * sizeof(int));
   prefetch_l2(g.fnA + 4 * (size_t)first, n * 4 * sizeof(R));
@@ -555,10 +609,14 @@ __device__ __forceinline__ void prefetch_update_tile(const RegionDev<R> &g, int 
   const long long f0 = g.cfOff[sl], f1 = g.cfOff[sl + 1];
   prefetch_l2(g.cfCode + f0, (size_t)(f1 - f0) * sizeof(int));
   const int c0 = sl * kSlice, nc = N - c0 < kSlice ? N - c0 : kSlice;
-  if (sizeof(R) == 4) {  // float-float state rows, increment history, 1/vol
+  if (sizeof(R) == 4 && g.cvF) {  // float-float state rows, increment history, 1/vol
     for (int j = 0; j < 10; ++j) prefetch_l2(g.cvF + (size_t)j * N + c0, (size_t)nc * sizeof(float));
     for (int j = 0; j < 5; ++j) prefetch_l2(g.rhsSumF + (size_t)j * N + c0, (size_t)nc * sizeof(float));
     prefetch_l2(g.ivolF + c0, (size_t)nc * sizeof(float));
+  } else if (sizeof(R) == 4) {    // split path: FP64 state rows, increment history, 1/vol
+    for (int j = 0; j < 5; ++j) prefetch_l2(g.cv + (size_t)j * N + c0, (size_t)nc * sizeof(double));
+    for (int j = 0; j < 5; ++j) prefetch_l2(g.rhsSum + (size_t)j * N + c0, (size_t)nc * sizeof(double));
+    prefetch_l2(g.ivol + c0, (size_t)nc * sizeof(double));
   } else {
     for (int j = 0; j < 5; ++j) prefetch_l2(g.cv + (size_t)j * N + c0, (size_t)nc * sizeof(double));
   }
@@ -621,12 +679,47 @@ __device__ __forceinline__ void record_from_pairs(const Phys &ph, const float qh
   r[4] = (ph.gvGF - 1.0f) * ((qh[4] - kin) + ql[4]);
 }
 
+// Pressure of RFLU_SetDependentVars (libflu/RFLU_SetDependentVars.F90:256-287,
+// libfloflu/MixtPerf_P.F90:78) from an FP64 conserved vector, in the
+// reference's operation order; ir = 1/rho is returned for the velocities.
+__device__ __forceinline__ double eos_p(const Phys &ph, const double q[5], double &ir) {
+  const double rr = q[0];
+  ir = 1.0 / rr;
+  const double Eo = ir * q[4];
+  const double Vm2 = ir * ir * (q[1] * q[1] + q[2] * q[2] + q[3] * q[3]);
+  return (ph.gvG - 1.0) * rr * (Eo - 0.5 * Vm2 - 0.0);
+}
+
+// Split path: the FP32 record of a cell from its FP64 conserved state and
+// FP64 pressure (velocities u = (1/rho) rhou as Cons2Prim forms them).
+__device__ __forceinline__ void record_from_fp64(const double q[5], double ir, double p,
+                                                 float r[8]) {
+  r[0] = float(q[0]);
+  r[1] = float(ir * q[1]);
+  r[2] = float(ir * q[2]);
+  r[3] = float(ir * q[3]);
+  r[4] = float(p);
+}
+
 // Mixed path: a cell's state from an FP64 conserved vector (upload, border
 // receive): float-float split, then the record from the pairs, with p from dv
 // when given.  FP64 work is the split alone (GB300's FP64 rate bounds these
-// conversions).
-__device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c, const double q[5],
-                                                const double *pGiven) {
+// conversions).  Split path (no pairs): the FP64 rows, and the record from
+// the FP64 EOS (p from dv when given).
+__device__ __forceinline__ void state_from_fp64_split(const RegionDev<float> &g, int c,
+                                                      const double q[5], const double *pGiven) {
+  const int N = g.nCells;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) g.cv[(size_t)j * N + c] = q[j];
+  double ir;
+  const double p = eos_p(g.ph, q, ir);
+  float r[8];
+  ld8_rw(g.rec + 8 * (size_t)c, r);
+  record_from_fp64(q, ir, pGiven ? *pGiven : p, r);
+  st8(g.rec + 8 * (size_t)c, r);
+}
+__device__ __forceinline__ void state_from_fp64_ff(const RegionDev<float> &g, int c,
+                                                   const double q[5], const double *pGiven) {
   const int N = g.nCells;
   float qh[5], ql[5];
 #pragma unroll
@@ -642,13 +735,20 @@ __device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c
   if (pGiven) r[4] = float(*pGiven);
   st8(g.rec + 8 * (size_t)c, r);
 }
+__device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c, const double q[5],
+                                                const double *pGiven) {
+  if (g.cvF)
+    state_from_fp64_ff(g, c, q, pGiven);
+  else
+    state_from_fp64_split(g, c, q, pGiven);
+}
 
 // Conserved state of a cell as FP64 (the float-float pair joined on the
 // mixed path).
 template <typename R>
 __device__ __forceinline__ void cons_fp64(const RegionDev<R> &g, int c, double q[5]) {
   const int N = g.nCells;
-  if constexpr (sizeof(R) == 4) {
+  if (sizeof(R) == 4 && g.cvF) {
 #pragma unroll
     for (int j = 0; j < 5; ++j)
       q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
@@ -687,8 +787,13 @@ __device__ __forceinline__ void halo_cell(const RegionDev<R> &gs, int cs, const 
     for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = gs.cv[(size_t)j * Ns + cs];
     set_vars_cell(gd, cd, 1);
   } else {
+    if (gd.cvF) {
 #pragma unroll
-    for (int j = 0; j < 10; ++j) gd.cvF[(size_t)j * Nd + cd] = gs.cvF[(size_t)j * Ns + cs];
+      for (int j = 0; j < 10; ++j) gd.cvF[(size_t)j * Nd + cd] = gs.cvF[(size_t)j * Ns + cs];
+    } else {  // split path: the FP64 rows
+#pragma unroll
+      for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = gs.cv[(size_t)j * Ns + cs];
+    }
     R a[8], b[8];
     ld8_rw(gs.rec + 8 * (size_t)cs, a);
     ld8_rw(gd.rec + 8 * (size_t)cd, b);
@@ -866,6 +971,9 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #ifndef RF_LIM_PRE
 #define RF_LIM_PRE 6
 #endif
+#ifndef RF_GRAD_PACKED
+#define RF_GRAD_PACKED 0
+#endif
 #ifndef RF_GRAD_UNROLL
 #define RF_GRAD_UNROLL 8
 #endif
@@ -878,8 +986,11 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #ifndef RF_GRAD_MINB_DT
 #define RF_GRAD_MINB_DT 8  // the same for the stage-1 pass that also reduces the time step
 #endif
-template <typename R, int FUSE_DT>
-__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MINB_DT : RF_GRAD_MINB) : 4)
+// BS threads per block (one cell each, a tile of BS cells); the requested
+// residency keeps the same number of resident threads per SM for every BS.
+template <typename R, int FUSE_DT, int BS>
+__global__ void __launch_bounds__(BS, ((sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MINB_DT : RF_GRAD_MINB)
+                                                        : 4) * 128 / BS)
     k_grad_lim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles, int nTiles) {
   constexpr bool fuseDt = FUSE_DT != 0;
   __shared__ unsigned long long smin[32];
@@ -960,6 +1071,60 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
         int nx[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(sidx + u * kSlice) : 0;
+#if RF_GRAD_PACKED
+        // The same sums on packed FP32 pairs: a record is four pairs (rho,u)
+        // (v,w) (p,x) (y,z), so four pair subtractions give the five variable
+        // differences and the three offsets, and each direction's five sums
+        // take two pair FMAs and one FMA (9 instead of 15 per member).
+        (void)member;
+        f2x q0[4];
+        ld4p(rec + 8 * (size_t)c, q0);
+        f2x A01[3] = {0ull, 0ull, 0ull}, A23[3] = {0ull, 0ull, 0ull};
+        float a4[3] = {0.f, 0.f, 0.f};
+        auto pmember = [&](const f2x p[4]) {
+          const f2x D0 = f2_sub(p[0], q0[0]), D1 = f2_sub(p[1], q0[1]);
+          const f2x D2 = f2_sub(p[2], q0[2]), D3 = f2_sub(p[3], q0[3]);
+          float dp, dx, sy, sz;
+          f2_unpack(D2, dp, dx);
+          f2_unpack(f2_mul(D3, D3), sy, sz);
+          float t = rsqrtf(dx * dx + sy + sz);
+          t = t * t;
+          float wy, wz;
+          f2_unpack(f2_mul(D3, f2_pack(t, t)), wy, wz);
+          const float w[3] = {t * dx, wy, wz};
+#pragma unroll
+          for (int d = 0; d < 3; ++d) {
+            const f2x W = f2_pack(w[d], w[d]);
+            A01[d] = f2_fma(W, D0, A01[d]);
+            A23[d] = f2_fma(W, D1, A23[d]);
+            a4[d] = fmaf(w[d], dp, a4[d]);
+          }
+        };
+        for (int k = 0; k < nFull; k += U) {
+          f2x ra[U][4];
+#pragma unroll
+          for (int u = 0; u < U; ++u) ld4p(rec + 8 * (size_t)nx[u], ra[u]);
+#pragma unroll
+          for (int u = 0; u < U; ++u)
+            nx[u] = k + U + u < n ? ld_index(sidx + (k + U + u) * kSlice) : 0;
+#pragma unroll
+          for (int u = 0; u < U; ++u) pmember(ra[u]);
+        }
+#pragma unroll
+        for (int u = 0; u < U - 1; ++u) {
+          if (nFull + u < n) {
+            f2x ra[4];
+            ld4p(rec + 8 * (size_t)nx[u], ra);
+            pmember(ra);
+          }
+        }
+#pragma unroll
+        for (int d = 0; d < 3; ++d) {
+          f2_unpack(A01[d], acc[d], acc[3 + d]);
+          f2_unpack(A23[d], acc[6 + d], acc[9 + d]);
+          acc[12 + d] = a4[d];
+        }
+#else
         for (int k = 0; k < nFull; k += U) {
           R ra[U][8];
 #pragma unroll
@@ -978,6 +1143,7 @@ __global__ void __launch_bounds__(128, (sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
             member(ra);
           }
         }
+#endif
         const R axx = lds<RF_HINT_G>(g.cwt + c), axy = lds<RF_HINT_G>(g.cwt + N + c),
                 axz = lds<RF_HINT_G>(g.cwt + 2 * N + c);
         const R ayy = lds<RF_HINT_G>(g.cwt + 3 * N + c), ayz = lds<RF_HINT_G>(g.cwt + 4 * N + c),
@@ -1141,22 +1307,13 @@ __device__ __forceinline__ void face_riemann(const RegionDev<R> &g, int c1, int 
 }
 
 // Interior face fluxes, *_ComputeFlux2_TCP face loops (AUSM+ :2726-2846,
-// Roe :2646-2855, HLLC :2239-2409), written to the face flux buffer.
+// Roe :2646-2855, HLLC :2239-2409), written to the face flux buffer.  A tile
+// is BS * FPT consecutive faces; thread i of the block takes faces i, i + BS,
+// ... of it (FPT faces per thread).
 template <typename R>
-__global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restrict__ regs,
-                                                   const Tile *__restrict__ tiles, int nTiles,
-                                                   int pfDist) {
-  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    prefetch_ahead(t_, nTiles, dist, [&](int t) {
-      const Tile tp = tiles[t];
-      prefetch_face_tile(regs[tp.region], tp.first);
-    });
-    const int f = tl.first + threadIdx.x;
-    const int F = g.nFaces;
-    if (f >= F) continue;
+__device__ __forceinline__ void face_flux_one(const RegionDev<R> &g, int f) {
+  const int F = g.nFaces;
+  {
     const int c1 = lds<RF_HINT_F>(g.f2c + f), c2 = lds<RF_HINT_F>(g.f2c + F + f);
 #if RF_FACE_PF
     if (g.ph.spaceOrder > 1) {  // both gradient rows on their way while the records arrive
@@ -1185,6 +1342,26 @@ __global__ void __launch_bounds__(128) k_face_flux(const RegionDev<R> *__restric
     face_riemann(g, c1, c2, L, Rt, irl, irr, nrm, flx);
     flx[5] = flx[6] = flx[7] = R(0);
     st8(g.flux + 8 * (size_t)f, flx);
+  }
+}
+
+template <typename R, int BS, int FPT>
+__global__ void __launch_bounds__(BS) k_face_flux(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles,
+                                                  int pfDist) {
+  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    prefetch_ahead(t_, nTiles, dist, [&](int t) {
+      const Tile tp = tiles[t];
+      prefetch_face_tile(regs[tp.region], tp.first, BS * FPT);
+    });
+#pragma unroll
+    for (int k = 0; k < FPT; ++k) {
+      const int f = tl.first + threadIdx.x + k * BS;
+      if (f < g.nFaces) face_flux_one(g, f);
+    }
   }
 }
 
@@ -1709,15 +1886,153 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   st8(g.rec + 8 * (size_t)c, r);
 }
 
+// FP64 sum of a cell's face fluxes in the reference accumulation order
+// (ConvectiveFluxes' scatter restated as a gather: +flux where the cell is the
+// face's first cell, -flux where it is the second, boundary faces added),
+// starting from -0.0 as the FP64 path does.  The first RF_UPD_PRE face codes
+// are loaded together ahead of the flux gathers.
+template <typename R>
+__device__ __forceinline__ void face_sum64(const RegionDev<R> &g, const R *__restrict__ flux,
+                                           int c, double acc[5]) {
+  const long long e0 = g.cfOff[c >> 5] + (c & 31);
+  const int n = g.cfCnt[c];
+#pragma unroll
+  for (int j = 0; j < 5; ++j) acc[j] = -0.0;
+  auto face = [&](int code) {
+    R fl[8];
+    if (code >= 0) {
+      ld8(flux + 8 * (size_t)(code >> 1), fl);
+      if (code & 1) {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(fl[j]);
+      } else {
+#pragma unroll
+        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
+      }
+    } else {
+      ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
+#pragma unroll
+      for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
+    }
+  };
+  constexpr int MF = RF_UPD_PRE;
+  int cc[MF];
+#pragma unroll
+  for (int k = 0; k < MF; ++k)
+    cc[k] = k < n ? lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice) : 0;
+#pragma unroll
+  for (int k = 0; k < MF; ++k)
+    if (k < n) face(cc[k]);
+  for (int k = MF; k < n; ++k) face(lds<RF_HINT_U>(g.cfCode + e0 + (long long)k * kSlice));
+}
+
+// Split-path gather + update: the FP32 face fluxes summed in FP64, the RK
+// update of the FP64 conserved state (libfloflu/RkUpdateGeneric.F90:229-314)
+// and the EOS (libflu/RFLU_SetDependentVars.F90:256-287) in FP64, with the
+// reference's operation order except that a*dt/V is a*dt times the stored
+// 1/V.  The FP32 record (rho, u, v, w, p) for the next stage's gathers is
+// rounded from the FP64 values.  AfterUpdateMP's checks
+// (libfloflu/AfterUpdateMP.F90:134-136) change nothing and set no bit when
+// rho > 0, p > 0 and the velocities are not NaN, so only other cells run them.
+__device__ __forceinline__ void gather_update_split(const RegionDev<float> &g, int c,
+                                                    const StepArgs &a) {
+  const int N = g.nCells;
+  const Phys &ph = g.ph;
+  const int is = a.istage;
+  double q[5], rsOld[5];
+  float r[8];
+  double ivol = 0.0;
+  if (a.update) {  // own-cell loads first: independent of the flux gathers
+#pragma unroll
+    for (int j = 0; j < 5; ++j) q[j] = lds_rw<RF_HINT_U>(g.cv + (size_t)j * N + c);
+    const bool hist = is > 1 && ph.rkScheme != 3;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) rsOld[j] = hist ? lds_rw<RF_HINT_U>(g.rhsSum + (size_t)j * N + c) : 0.0;
+    ld8_rw(g.rec + 8 * (size_t)c, r);
+    ivol = lds<RF_HINT_U>(g.ivol + c);
+  }
+  double acc[5];
+  face_sum64(g, g.flux, c, acc);
+  if (a.writeRhs) {
+#pragma unroll
+    for (int j = 0; j < 5; ++j) g.rhs[(size_t)j * N + c] = acc[j];
+  }
+  if (!a.update) return;
+  const double fac = a.useDeviceDt ? g.scal[3 + is - 1] : ph.ark[is - 1] * a.dtHost;
+  const double adtv = fac * ivol;
+  const double grk = ph.grk[is - 1];
+  double old[5];
+  if (ph.rkScheme == 1) {  // RK4: cvOld saved at stage 1 only
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+      if (is == 1) {
+        old[j] = q[j];
+        g.cvOld[(size_t)j * N + c] = q[j];
+      } else {
+        old[j] = g.cvOld[(size_t)j * N + c];
+      }
+    }
+  } else {  // Wray / Euler: cvOld = cv at every stage start
+#pragma unroll
+    for (int j = 0; j < 5; ++j) old[j] = q[j];
+  }
+  double *rs = g.rhsSum;
+#pragma unroll
+  for (int j = 0; j < 5; ++j) {
+    const double rhs = acc[j];
+    if (ph.rkScheme == 2) {
+      if (is == 1) {
+        q[j] = old[j] - adtv * rhs;
+        rs[(size_t)j * N + c] = rhs;
+      } else if (is == 2) {
+        q[j] = old[j] - adtv * (rhs - grk * rsOld[j]);
+        rs[(size_t)j * N + c] = rhs;
+      } else {
+        q[j] = old[j] - adtv * (rhs - grk * rsOld[j]);
+      }
+    } else if (ph.rkScheme == 1) {
+      if (is == 1) {
+        q[j] = old[j] - adtv * rhs;
+        rs[(size_t)j * N + c] = rhs;
+      } else if (is == ph.nSteps) {
+        q[j] = old[j] - adtv * (rhs + rsOld[j]);
+      } else {
+        q[j] = old[j] - adtv * rhs;
+        rs[(size_t)j * N + c] = rsOld[j] + grk * rhs;
+      }
+    } else {
+      q[j] = old[j] - adtv * rhs;
+    }
+  }
+  double ir;
+  double p = eos_p(ph, q, ir);
+  if (!(q[0] > 0.0 && p > 0.0) || isnan(ir * q[1]) || isnan(ir * q[2]) || isnan(ir * q[3])) {
+    double d[3];
+    d[0] = p;
+    d[1] = p / (q[0] * ph.gvR);
+    d[2] = 0.0;
+    const unsigned st = after_update(ph.gvR, ph.gvG, q, d);
+    if (st) atomicOr(g.status, st);
+    p = d[0];
+    ir = 1.0 / q[0];
+  }
+#pragma unroll
+  for (int j = 0; j < 5; ++j) g.cv[(size_t)j * N + c] = q[j];
+  record_from_fp64(q, ir, p, r);
+  st8(g.rec + 8 * (size_t)c, r);
+}
+
 // Face->cell residual gather in the reference accumulation order, then the
 // RK update (libfloflu/RkUpdateGeneric.F90:229-314), EOS
 // (libflu/RFLU_SetDependentVars.F90:256-287), AfterUpdate checks and
 // Cons2Prim of the new state for the next stage.  With update = 0 only the
 // residual is written (rfgpu_residual).
-template <typename R>
-__global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__restrict__ regs,
-                                                       const Tile *__restrict__ tiles,
-                                                       int nTiles, StepArgs a, int pfDist) {
+// SPLIT selects the split path's update at compile time (a run-time branch
+// between the two FP32-flux updates costs the mixed path registers).
+template <typename R, int BS, int SPLIT>
+__global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__restrict__ regs,
+                                                      const Tile *__restrict__ tiles,
+                                                      int nTiles, StepArgs a, int pfDist) {
   const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
   RF_TILE_LOOP(tiles, nTiles) {
     const Tile tl = tiles[t_];
@@ -1737,7 +2052,10 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
       continue;
     }
     if constexpr (sizeof(R) == 4) {
-      gather_update_mixed(g, c, a);
+      if constexpr (SPLIT)
+        gather_update_split(g, c, a);
+      else
+        gather_update_mixed(g, c, a);
       continue;
     }
     double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
@@ -1857,7 +2175,7 @@ __global__ void __launch_bounds__(128) k_gather_update(const RegionDev<R> *__res
 // reading or writing page-locked host memory directly over the CPU-GPU link
 // were measured slower than the DMA copies (32 against 20 ms per end-to-end
 // step).
-template <typename R>
+template <typename R, int SPLIT>
 __global__ void k_upload_list(const RegionDev<R> *__restrict__ regs, const int *__restrict__ list,
                               int n, const double *__restrict__ cvH, const double *__restrict__ dvH) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1868,10 +2186,15 @@ __global__ void k_upload_list(const RegionDev<R> *__restrict__ regs, const int *
   double q[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) q[j] = cvH[5 * (size_t)h + j];
-  if constexpr (sizeof(R) == 4) state_from_fp64(g, c, q, dvH ? dvH + 3 * (size_t)h : nullptr);
+  if constexpr (sizeof(R) == 4) {
+    if constexpr (SPLIT)
+      state_from_fp64_split(g, c, q, dvH ? dvH + 3 * (size_t)h : nullptr);
+    else
+      state_from_fp64_ff(g, c, q, dvH ? dvH + 3 * (size_t)h : nullptr);
+  }
 }
 
-template <typename R>
+template <typename R, int SPLIT>
 __global__ void k_download_list(const RegionDev<R> *__restrict__ regs, const int *__restrict__ list,
                                 int n, double *__restrict__ cvH, double *__restrict__ dvH) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1881,14 +2204,27 @@ __global__ void k_download_list(const RegionDev<R> *__restrict__ regs, const int
   const int h = g.cellOld ? g.cellOld[c] : c;
   const int N = g.nCells;
   double q[5];
+  if constexpr (SPLIT) {
 #pragma unroll
-  for (int j = 0; j < 5; ++j)
-    q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+    for (int j = 0; j < 5; ++j) q[j] = g.cv[(size_t)j * N + c];
+  } else {
+#pragma unroll
+    for (int j = 0; j < 5; ++j)
+      q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+  }
   if (cvH) {
 #pragma unroll
     for (int j = 0; j < 5; ++j) cvH[5 * (size_t)h + j] = q[j];
   }
-  if (dvH) {
+  if (dvH && SPLIT) {  // split path: the EOS of its update
+    const double gc = g.ph.gvR, gg = g.ph.gvG;
+    double ir;
+    const double p = eos_p(g.ph, q, ir);
+    const double T = p / (q[0] * gc);
+    dvH[3 * (size_t)h] = p;
+    dvH[3 * (size_t)h + 1] = T;
+    dvH[3 * (size_t)h + 2] = sqrt(gg * gc * T);
+  } else if (dvH) {
     const double gc = g.ph.gvR, gg = g.ph.gvG;
     const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
     const double p = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
@@ -2010,26 +2346,102 @@ void launch_prim(const RegionDev<R> *regs, const Work &w, int computeDv, cudaStr
 #define RF_MARK(kind, phase) \
   if (prof) prof->mark(prof->ctx, (kind), (phase), s)
 
-// Blocks of `kernel` (128 threads) resident on the whole device at once: the
-// prefetch distance in tiles.
+// Blocks of `kernel` (`threads` per block) resident on the whole device at
+// once: the prefetch distance in tiles.
 template <typename K>
-int resident_blocks(K kernel) {
+int resident_blocks(K kernel, int threads = 128) {
   int dev = 0, nsm = 0, per = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, threads, 0);
   return per > 0 && nsm > 0 ? per * nsm : 1;
 }
 
 template <typename R>
 void launch_weno_xyz(const RegionDev<R> *regs, const Work &w, cudaStream_t s);
 
+// ---- tuned launches: block size (and faces per thread) picked at run time
+// from the Work's launch shapes, one template instance per shape -------------
+inline int grid_for(int cap, int nTiles) { return cap > 0 && cap < nTiles ? cap : nTiles; }
+
+template <typename R, int F, int BS>
+void grad_launch(const RegionDev<R> *regs, const Tile *tiles, int nTiles, int cap, cudaStream_t s) {
+  const int grid = grid_for(cap, nTiles);
+  if (grid > 0) k_grad_lim<R, F, BS><<<grid, BS, 0, s>>>(regs, tiles, nTiles);
+}
+
+template <typename R>
+void launch_grad_tuned(const RegionDev<R> *regs, const Work &w, int fuseDt, cudaStream_t s) {
+  const bool tuned = w.gradTiles != nullptr;
+  const Tile *t = tuned ? w.gradTiles : w.cellTiles;
+  const int n = tuned ? w.nGradTiles : w.nCellTiles;
+  const int bs = tuned ? w.gradBlock : 128;
+  if (bs == 64) {
+    if (fuseDt) grad_launch<R, 1, 64>(regs, t, n, w.grid, s);
+    else grad_launch<R, 0, 64>(regs, t, n, w.grid, s);
+  } else if (bs == 256) {
+    if (fuseDt) grad_launch<R, 1, 256>(regs, t, n, w.grid, s);
+    else grad_launch<R, 0, 256>(regs, t, n, w.grid, s);
+  } else {
+    if (fuseDt) grad_launch<R, 1, 128>(regs, t, n, w.grid, s);
+    else grad_launch<R, 0, 128>(regs, t, n, w.grid, s);
+  }
+}
+
+template <typename R, int BS, int FPT>
+void face_launch(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+  static const int pf = resident_blocks(k_face_flux<R, BS, FPT>, BS);
+  const int grid = grid_for(w.grid, w.nFaceTiles);
+  if (grid > 0) k_face_flux<R, BS, FPT><<<grid, BS, 0, s>>>(regs, w.faceTiles, w.nFaceTiles, pf);
+}
+
+template <typename R>
+void launch_faces_tuned(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
+  const int bs = w.faceBlock ? w.faceBlock : 128, fpt = w.facesPerThread ? w.facesPerThread : 1;
+  if (bs == 64) {
+    if (fpt == 2) face_launch<R, 64, 2>(regs, w, s);
+    else face_launch<R, 64, 1>(regs, w, s);
+  } else if (bs == 256) {
+    if (fpt == 2) face_launch<R, 256, 2>(regs, w, s);
+    else face_launch<R, 256, 1>(regs, w, s);
+  } else {
+    if (fpt == 2) face_launch<R, 128, 2>(regs, w, s);
+    else face_launch<R, 128, 1>(regs, w, s);
+  }
+}
+
+template <typename R, int BS, int SPLIT>
+void update_launch_k(const RegionDev<R> *regs, const Tile *tiles, int nTiles, int cap,
+                     const StepArgs &a, cudaStream_t s) {
+  static const int pf = resident_blocks(k_gather_update<R, BS, SPLIT>, BS);
+  const int grid = grid_for(cap, nTiles);
+  if (grid > 0) k_gather_update<R, BS, SPLIT><<<grid, BS, 0, s>>>(regs, tiles, nTiles, a, pf);
+}
+template <typename R, int BS>
+void update_launch(const RegionDev<R> *regs, const Tile *tiles, int nTiles, int cap,
+                   const StepArgs &a, int split, cudaStream_t s) {
+  if (sizeof(R) == 4 && split)
+    update_launch_k<R, BS, 1>(regs, tiles, nTiles, cap, a, s);
+  else
+    update_launch_k<R, BS, 0>(regs, tiles, nTiles, cap, a, s);
+}
+
+template <typename R>
+void launch_update_tuned(const RegionDev<R> *regs, const Work &w, const StepArgs &a,
+                         cudaStream_t s) {
+  const bool tuned = w.updTiles != nullptr;
+  const Tile *t = tuned ? w.updTiles : w.cellTiles;
+  const int n = tuned ? w.nUpdTiles : w.nCellTiles;
+  const int bs = tuned ? w.cellBlock : 128;
+  if (bs == 64) update_launch<R, 64>(regs, t, n, w.grid, a, w.split, s);
+  else if (bs == 256) update_launch<R, 256>(regs, t, n, w.grid, a, w.split, s);
+  else update_launch<R, 128>(regs, t, n, w.grid, a, w.split, s);
+}
+
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof,
                   int parts) {
-  static const int pfFace = resident_blocks(k_face_flux<R>);
-  static const int pfUpd = resident_blocks(k_gather_update<R>);
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   long long n = 0;
   const bool hasGrad = spaceOrder > 1 && w.nCellTiles > 0;
@@ -2037,10 +2449,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   const bool flux = parts & SP_FLUX, upd = parts & SP_UPDATE;
   if (grad) {
     RF_MARK(KP_GRADIENT, 0);
-    if (a.fuseDt)
-      k_grad_lim<R, 1><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
-    else
-      k_grad_lim<R, 0><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    launch_grad_tuned<R>(regs, w, a.fuseDt, s);
     RF_MARK(KP_GRADIENT, 1);
     ++n;
   }
@@ -2058,7 +2467,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   }
   if (flux && w.nFaceTiles > 0) {
     RF_MARK(KP_FACE_FLUX, 0);
-    k_face_flux<R><<<gsz(w.nFaceTiles), w.block, 0, s>>>(regs, w.faceTiles, w.nFaceTiles, pfFace);
+    launch_faces_tuned<R>(regs, w, s);
     RF_MARK(KP_FACE_FLUX, 1);
     ++n;
   }
@@ -2070,8 +2479,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
   }
   if (upd && w.nCellTiles > 0) {
     RF_MARK(KP_GATHER_UPDATE, 0);
-    k_gather_update<R><<<gsz(w.nCellTiles), w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, a,
-                                                              pfUpd);
+    launch_update_tuned<R>(regs, w, a, s);
     RF_MARK(KP_GATHER_UPDATE, 1);
     ++n;
   }
@@ -2258,20 +2666,17 @@ void launch_weno_xyz(const RegionDev<R> *regs, const Work &w, cudaStream_t s) {
 template <typename R>
 void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                        int fuseDt, cudaStream_t s) {
-  const int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
-  if (grid <= 0) return;
+  // the phase tile lists hold 128-cell tiles
   if (fuseDt)
-    k_grad_lim<R, 1><<<grid, w.block, 0, s>>>(regs, tiles, nTiles);
+    grad_launch<R, 1, 128>(regs, tiles, nTiles, w.grid, s);
   else
-    k_grad_lim<R, 0><<<grid, w.block, 0, s>>>(regs, tiles, nTiles);
+    grad_launch<R, 0, 128>(regs, tiles, nTiles, w.grid, s);
 }
 
 template <typename R>
 void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                          const StepArgs &a, cudaStream_t s) {
-  static const int pfUpd = resident_blocks(k_gather_update<R>);
-  const int grid = w.grid > 0 && w.grid < nTiles ? w.grid : nTiles;
-  if (grid > 0) k_gather_update<R><<<grid, w.block, 0, s>>>(regs, tiles, nTiles, a, pfUpd);
+  update_launch<R, 128>(regs, tiles, nTiles, w.grid, a, w.split, s);  // 128-cell phase tiles
 }
 
 // The transfer chunk a host cell travels in.
@@ -2323,13 +2728,21 @@ void launch_tile_phases(const RegionDev<R> *regs, const Work &w, const ChunkMap 
 
 template <typename R>
 void launch_upload_list(const RegionDev<R> *regs, const int *list, int n, const double *cvH,
-                        const double *dvH, cudaStream_t s) {
-  if (n > 0) k_upload_list<R><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
+                        const double *dvH, int split, cudaStream_t s) {
+  if (n <= 0) return;
+  if (split)
+    k_upload_list<R, 1><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
+  else
+    k_upload_list<R, 0><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
 }
 template <typename R>
 void launch_download_list(const RegionDev<R> *regs, const int *list, int n, double *cvH,
-                          double *dvH, cudaStream_t s) {
-  if (n > 0) k_download_list<R><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
+                          double *dvH, int split, cudaStream_t s) {
+  if (n <= 0) return;
+  if (split)
+    k_download_list<R, 1><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
+  else
+    k_download_list<R, 0><<<(n + 255) / 256, 256, 0, s>>>(regs, list, n, cvH, dvH);
 }
 
 // ---- residual without device allocation ---------------------------------------
@@ -2380,29 +2793,16 @@ __global__ void __launch_bounds__(128) k_gather_rhs_scratch(const RegionDev<R> g
     for (int j = 0; j < 5; ++j) rhs[5 * hc + j] = 0.0;
     return;
   }
-  if constexpr (sizeof(R) == 8) {
-    double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
-    for (int k = 0; k < n; ++k) {
-      const int code = g.cfCode[e0 + (long long)k * kSlice];
-      R fl[8];
-      if (code >= 0) {
-        ld8(flux + 8 * (size_t)(code >> 1), fl);
-        if (code & 1) {
-#pragma unroll
-          for (int j = 0; j < 5; ++j) acc[j] = acc[j] - double(fl[j]);
-        } else {
-#pragma unroll
-          for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
-        }
-      } else {
-        ld8(g.bflux + 8 * (size_t)(-code - 1), fl);
-#pragma unroll
-        for (int j = 0; j < 5; ++j) acc[j] = acc[j] + double(fl[j]);
-      }
-    }
+  bool sum64 = true;  // FP64 and split paths: FP64 sums
+  if constexpr (sizeof(R) == 4) sum64 = !g.cvF;
+  if (sum64) {
+    double acc[5];
+    face_sum64(g, flux, c, acc);
 #pragma unroll
     for (int j = 0; j < 5; ++j) rhs[5 * hc + j] = acc[j];
-  } else {
+    return;
+  }
+  if constexpr (sizeof(R) == 4) {
     float hi[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, lo[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int k = 0; k < n; ++k) {
       const int code = g.cfCode[e0 + (long long)k * kSlice];
@@ -2429,7 +2829,7 @@ template <typename R>
 void launch_residual_scratch(const RegionDev<R> *regs, const RegionDev<R> &g, const Work &w,
                              int spaceOrder, R *flux, double *rhs, cudaStream_t s) {
   if (spaceOrder > 1 && w.nCellTiles > 0) {
-    k_grad_lim<R, 0><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles);
+    grad_launch<R, 0, 128>(regs, w.cellTiles, w.nCellTiles, 0, s);
     if (g.gradRaw) launch_weno_xyz<R>(regs, w, s);
   }
   if (g.nFaces > 0) k_face_flux_scratch<R><<<(g.nFaces + 127) / 128, 128, 0, s>>>(g, flux);
@@ -2461,9 +2861,9 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
 #define RFGPU_INSTANTIATE(R)                                                                  \
   template void launch_prim<R>(const RegionDev<R> *, const Work &, int, cudaStream_t);        \
   template void launch_upload_list<R>(const RegionDev<R> *, const int *, int, const double *,  \
-                                      const double *, cudaStream_t);                          \
+                                      const double *, int, cudaStream_t);                     \
   template void launch_download_list<R>(const RegionDev<R> *, const int *, int, double *,     \
-                                        double *, cudaStream_t);                              \
+                                        double *, int, cudaStream_t);                         \
   template void launch_residual_scratch<R>(const RegionDev<R> *, const RegionDev<R> &,         \
                                            const Work &, int, R *, double *, cudaStream_t);    \
   template void launch_stage<R>(const RegionDev<R> *, const Work &, const StepArgs &,         \

@@ -20,7 +20,7 @@ from typing import List, Optional, Sequence
 import numpy as np
 
 from . import _build
-from .case import Case, PREC_FP64, PREC_MIXED  # noqa: F401
+from .case import Case, PREC_FP64, PREC_MIXED, PREC_SPLIT  # noqa: F401
 
 OK, ERR_ARG, ERR_UNSUPPORTED, ERR_CUDA, ERR_NOMEM, ERR_STATE, ERR_TIMEOUT, ERR_NOALLOC_LIMIT = range(8)
 NOALLOC_SCRATCH_BYTES = 32 << 20
@@ -67,6 +67,24 @@ class RegionDescT(C.Structure):
                 ("ausmKu", C.c_double), ("ausmMInf", C.c_double), ("nCellsTot", C.c_int),
                 ("iRegionGlobal", C.c_int), ("nBorders", C.c_int),
                 ("borders", C.POINTER(BorderT))]
+
+
+class TuningT(C.Structure):
+    """rfgpu_tuning_t: launch shapes of the stage passes (0 = default)."""
+    _fields_ = [("gridCap", C.c_int), ("gradBlock", C.c_int), ("faceBlock", C.c_int),
+                ("facesPerThread", C.c_int), ("cellBlock", C.c_int)]
+
+
+TUNING_KEYS = [f for f, _ in TuningT._fields_]
+
+
+def _tuning(**kw) -> TuningT:
+    t = TuningT()
+    for k, v in kw.items():
+        if k not in TUNING_KEYS:
+            raise KeyError(k)
+        setattr(t, k, int(v))
+    return t
 
 
 # device numbering of cells and faces (rfgpu.h RFGPU_ORDER_*)
@@ -125,7 +143,7 @@ def load(path: Optional[str] = None):
         "rfgpu_stream": ([vp], vp),
         "rfgpu_device_bytes": ([vp], C.c_longlong),
         "rfgpu_launch_count": ([vp], C.c_longlong),
-        "rfgpu_set_tuning": ([vp, C.c_int, C.c_int], C.c_int),
+        "rfgpu_set_tuning": ([vp, C.POINTER(TuningT)], C.c_int),
         "rfgpu_batch_create": ([C.POINTER(vp), C.c_int, C.POINTER(vp)], C.c_int),
         "rfgpu_batch_destroy": ([vp], C.c_int),
         "rfgpu_batch_step": ([vp, d, d, d, d], C.c_int),
@@ -147,7 +165,7 @@ def load(path: Optional[str] = None):
         "rfgpu_mem_info": ([C.POINTER(C.c_longlong), C.POINTER(C.c_longlong)], C.c_int),
         "rfgpu_sm_count": ([ip], C.c_int),
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
-        "rfgpu_batch_set_tuning": ([vp, C.c_int], C.c_int),
+        "rfgpu_batch_set_tuning": ([vp, C.POINTER(TuningT)], C.c_int),
         "rfgpu_mesh_stencils": ([C.c_int, C.c_int, ip, ip, ip, ip, dp, ip, ip, dp], C.c_int),
         "rfgpu_border_copy": ([vp, C.c_int, vp], C.c_int),
         "rfgpu_border_pack": ([vp, C.c_int, dp], C.c_int),
@@ -512,8 +530,14 @@ class Region:
         """{kernel: (total ms, launches)} since profiling was enabled/read."""
         return _prof_read(self.lib.rfgpu_profile_read, self.h)
 
+    def set_tuning(self, **kw):
+        """rfgpu_set_tuning: gridCap, gradBlock, faceBlock, facesPerThread,
+        cellBlock (omitted keys: the default)."""
+        t = _tuning(**kw)
+        _check(self.lib.rfgpu_set_tuning(self.h, C.byref(t)), "rfgpu_set_tuning")
+
     def set_grid_cap(self, blocks: int):
-        _check(self.lib.rfgpu_set_tuning(self.h, blocks, 0), "rfgpu_set_tuning")
+        self.set_tuning(gridCap=blocks)
 
     def solve(self, t_end: Optional[float] = None, n_steps: Optional[int] = None,
               dt_imposed: Optional[float] = None, graph: bool = False):
@@ -585,8 +609,12 @@ class Batch:
         _check(self.lib.rfgpu_batch_timer_stop(self.h, C.byref(ms)), "rfgpu_batch_timer_stop")
         return ms.value
 
+    def set_tuning(self, **kw):
+        t = _tuning(**kw)
+        _check(self.lib.rfgpu_batch_set_tuning(self.h, C.byref(t)), "rfgpu_batch_set_tuning")
+
     def set_grid_cap(self, blocks: int):
-        _check(self.lib.rfgpu_batch_set_tuning(self.h, blocks), "rfgpu_batch_set_tuning")
+        self.set_tuning(gridCap=blocks)
 
     def profile(self, enable: bool = True):
         _check(self.lib.rfgpu_batch_profile(self.h, int(enable)), "rfgpu_batch_profile")

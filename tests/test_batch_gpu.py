@@ -16,7 +16,7 @@ def tubes(prec, count=5):
                            numerics=K.Numerics(precision=prec, venkatGuard=1))
 
 
-@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED])
+@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED, K.PREC_SPLIT])
 def test_batch_equals_individual_runs(prec):
     cases = tubes(prec)
     cfl = cases[0].numerics.cfl

@@ -153,9 +153,10 @@ def test_option_envelope_bitwise(variant):
     r.close()
 
 
+@pytest.mark.parametrize("prec", [K.PREC_MIXED, K.PREC_SPLIT], ids=["mixed", "split"])
 @pytest.mark.parametrize("scheme", SCHEMES)
-def test_mixed_precision_l1(scheme):
-    c = make("tet", scheme, precision=K.PREC_MIXED)
+def test_mixed_precision_l1(scheme, prec):
+    c = make("tet", scheme, precision=prec)
     o = _oracle(c)
     cv, dv = c.cv.copy(), c.dv.copy()
     # impose the same dt sequence on both: the FP64 oracle's first dt
@@ -209,7 +210,7 @@ def test_unsupported_option_refused():
     assert ei.value.code == E.ERR_UNSUPPORTED
 
 
-@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED])
+@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED, K.PREC_SPLIT])
 @pytest.mark.parametrize("kind", ["tube", "tet", "mixed"])
 def test_locality_order_equals_host_order(prec, kind):
     """The engine's locality numbering changes where cells and faces live in

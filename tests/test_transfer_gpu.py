@@ -46,21 +46,26 @@ def test_pinned_and_pageable_transfers_agree(order, with_dv):
     staged.close()
 
 
+@pytest.mark.parametrize("prec", [K.PREC_MIXED, K.PREC_SPLIT], ids=["mixed", "split"])
 @pytest.mark.parametrize("dims", [(1, 1, 1), (5, 3, 7), (40, 7, 3), (50, 9, 11)])
 @pytest.mark.parametrize("order", [E.ORDER_HOST, E.ORDER_LOCALITY])
-def test_chunked_upload_download_round_trip(dims, order):
+def test_chunked_upload_download_round_trip(dims, order, prec):
     """Upload then download with no step between: the transfers run in up to 8
     chunks of cell tiles (a region smaller than 8 tiles in fewer, the last tile
-    partial); cv comes back as the float-float split of the input joined again,
-    bit for bit, for every cell."""
+    partial); cv comes back, bit for bit for every cell, as the float-float
+    split of the input joined again (mixed path) or as the input itself (split
+    path, FP64 state)."""
     nx, ny, nz = dims
     c = K.tet_shock_box(nx, ny=ny, nz=nz, seed=5,
-                        numerics=K.Numerics(precision=K.PREC_MIXED, venkatGuard=1))
+                        numerics=K.Numerics(precision=prec, venkatGuard=1))
     r = E.Region(c, cell_order=order)
     q = np.ascontiguousarray(c.cv, np.float64)
-    hi = q.astype(np.float32)
-    lo = (q - hi.astype(np.float64)).astype(np.float32)
-    want = hi.astype(np.float64) + lo.astype(np.float64)
+    if prec == K.PREC_MIXED:
+        hi = q.astype(np.float32)
+        lo = (q - hi.astype(np.float64)).astype(np.float32)
+        want = hi.astype(np.float64) + lo.astype(np.float64)
+    else:
+        want = q
     for pinned in (False, True):
         if pinned:
             src = E.PinnedArray(q.shape)
@@ -82,7 +87,8 @@ def _case(dims, prec, discr=K.DISCR_UPW_ROE, rk=K.RK_SCHEME_3_WRAY, order=2):
 
 
 @pytest.mark.parametrize("dims", [(3, 3, 3), (5, 3, 7), (24, 8, 8), (50, 9, 11)])
-@pytest.mark.parametrize("variant", ["roe-wray", "hllc-rk4", "ausm+-euler", "first-order", "fp64"])
+@pytest.mark.parametrize("variant", ["roe-wray", "hllc-rk4", "ausm+-euler", "first-order", "fp64",
+                                     "split", "split-rk4"])
 @pytest.mark.parametrize("order", [E.ORDER_HOST, E.ORDER_LOCALITY])
 def test_step_host_equals_three_calls(dims, variant, order):
     """rfgpu_step_host against rfgpu_upload + rfgpu_step + rfgpu_download on the
@@ -101,6 +107,10 @@ def test_step_host_equals_three_calls(dims, variant, order):
         sord = 1
     elif variant == "fp64":
         prec = K.PREC_FP64
+    elif variant == "split":
+        prec = K.PREC_SPLIT
+    elif variant == "split-rk4":
+        prec, discr, rk = K.PREC_SPLIT, K.DISCR_UPW_HLLC, K.RK_SCHEME_4_CLASSICAL
     c = _case(dims, prec, discr, rk, sord)
     cfl = 0.5
     a = E.Region(c, cell_order=order)

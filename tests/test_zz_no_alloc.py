@@ -22,7 +22,7 @@ def _cases():
     yield K.mixed_box(6, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_HLLC, venkatGuard=1))
 
 
-@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED])
+@pytest.mark.parametrize("prec", [K.PREC_FP64, K.PREC_MIXED, K.PREC_SPLIT])
 def test_noalloc_residual_matches_residual_twice(prec):
     for c in _cases():
         r = E.Region(c, precision=prec)
