@@ -97,6 +97,11 @@ typedef struct {
   int distrib;
   int nData;             /* leading dimension of vals; 0 is read as 1 */
   int bcOptFixed;        /* inflow TOTANG FIXED switch (BCOPT_FIXED_NO 0 / YES 1) */
+  int nBFacesTot;        /* pPatch%nBFacesTot: in a partitioned region the patch's
+                            faces on actual cells (1..nBFaces) are followed in bf2c,
+                            fn and fc by its faces on virtual cells (FACE_KIND_VB);
+                            only RECONST 2's positivity check of the virtual cells
+                            reads those.  0 is read as nBFaces */
 } rfgpu_patch_t;
 
 /* One border of a partitioned region: the cells it sends to one neighbour
@@ -159,6 +164,14 @@ typedef struct {
   int iRegionGlobal;       /* pRegion%iRegionGlobal: matches borders between regions */
   int nBorders;            /* grid%nBorders */
   const rfgpu_border_t *borders;
+  /* Interior faces of every kind in f2c, fn and fc (0 is read as nFaces):
+   * the flux faces 1..nFaces (FACE_KIND_AA and AV), then the faces between
+   * two virtual cells (FACE_KIND_VV) and between a virtual cell and a cell
+   * outside the region (FACE_KIND_VX, modflu/RFLU_ModFaceList.F90:1317-1360),
+   * an f2c entry outside 1..nCellsTot marking the outside side.  Only
+   * RECONST 2's positivity check of the virtual cells reads faces past nFaces
+   * (RFLU_LimitGradCellsSimple walks every face of every cell). */
+  int nFacesAll;
 } rfgpu_region_desc_t;
 
 /* Register a region: copies and reorders the arrays to device-resident SoA.

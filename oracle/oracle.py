@@ -40,7 +40,7 @@ class OrcPatch(C.Structure):
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
                 ("distrib", C.c_int), ("nData", C.c_int),
-                ("bcOptFixed", C.c_int)]
+                ("bcOptFixed", C.c_int), ("nBFacesTot", C.c_int)]
 
 
 class OrcRegion(C.Structure):
@@ -55,7 +55,7 @@ class OrcRegion(C.Structure):
                 ("gvCp", C.c_double), ("gvMol", C.c_double), ("epsentr", C.c_double),
                 ("dissFact", C.c_double), ("venkatGuard", C.c_int),
                 ("ausmSigma", C.c_double), ("ausmKp", C.c_double), ("ausmKu", C.c_double),
-                ("ausmMInf", C.c_double), ("nCellsTot", C.c_int)]
+                ("ausmMInf", C.c_double), ("nCellsTot", C.c_int), ("nFacesAll", C.c_int)]
 
 
 def _load():
@@ -102,9 +102,11 @@ class Oracle:
         reg = OrcRegion()
         reg.nCells, reg.nFaces = m.nCells, m.nFaces
         reg.nCellsTot = m.nTot
-        reg.f2c = _ip(keep(m.f2c, np.int32))
-        reg.fn = _dp(keep(m.fn, np.float64))
-        reg.fc = _dp(keep(m.fc, np.float64))
+        f2c, fn, fc = m.all_faces()   # flux faces, then a region's VV / VX faces
+        reg.nFacesAll = m.nFacesAll
+        reg.f2c = _ip(keep(f2c, np.int32))
+        reg.fn = _dp(keep(fn, np.float64))
+        reg.fc = _dp(keep(fc, np.float64))
         reg.cofg = _dp(keep(m.cofg, np.float64))
         reg.vol = _dp(keep(m.vol, np.float64))
         reg.csOff = _ip(keep(m.c2cs_off, np.int32))
@@ -112,13 +114,15 @@ class Oracle:
         reg.xyzMoms = _dp(keep(m.xyzmoms, np.float64))
         np_ = 0
         for p, bc in zip(m.patches, case.bcs):
-            if p.n == 0:
+            if p.n == 0 and p.n_vb == 0:
                 continue
             P = reg.patches[np_]
             P.bcType, P.spaceOrder, P.bcOptType, P.nBFaces = bc.bcType, bc.spaceOrder, bc.bcOptType, p.n
-            P.bf2c = _ip(keep(p.bf2c, np.int32))
-            P.fn = _dp(keep(p.fn, np.float64))
-            P.fc = _dp(keep(p.fc, np.float64))
+            bf2c, bfn, bfc = p.all_faces()   # a region's VB faces after the actual ones
+            P.nBFacesTot = p.n + p.n_vb
+            P.bf2c = _ip(keep(bf2c, np.int32))
+            P.fn = _dp(keep(bfn, np.float64))
+            P.fc = _dp(keep(bfc, np.float64))
             vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(keep(vals, np.float64))
             P.distrib, P.nData = dist, nd

@@ -802,25 +802,30 @@ struct CellFaces {
   std::vector<long> off, item;  // item >= 0: interior face; < 0: -(boundary slot + 1)
   std::vector<const double *> bfc;
 };
+// In a partitioned region the virtual cells' lists also hold the faces
+// between two virtual cells and to cells outside the region (nFaces ..
+// nFacesAll, outside side 0) and the patches' faces on virtual cells
+// (nBFaces .. nBFacesTot).
 CellFaces cell_faces(const orc_region_t *r) {
   const long nC = n_tot(r);
+  const long nFA = r->nFacesAll > 0 ? r->nFacesAll : r->nFaces;
+  auto nbt = [](const orc_patch_t &p) { return p.nBFacesTot > 0 ? p.nBFacesTot : p.nBFaces; };
+  auto in = [&](int c) { return c >= 1 && c <= nC; };
   CellFaces cf;
   cf.off.assign(nC + 1, 0);
-  for (long f = 0; f < r->nFaces; ++f) {
-    cf.off[r->f2c[2 * f]]++;
-    cf.off[r->f2c[2 * f + 1]]++;
-  }
+  for (long f = 0; f < nFA; ++f)
+    for (int k = 0; k < 2; ++k)
+      if (in(r->f2c[2 * f + k])) cf.off[r->f2c[2 * f + k]]++;
   for (int ip = 0; ip < r->nPatches; ++ip)
-    for (int i = 0; i < r->patches[ip].nBFaces; ++i) cf.off[r->patches[ip].bf2c[i]]++;
+    for (int i = 0; i < nbt(r->patches[ip]); ++i) cf.off[r->patches[ip].bf2c[i]]++;
   for (long c = 0; c < nC; ++c) cf.off[c + 1] += cf.off[c];
   cf.item.resize(cf.off[nC]);
   std::vector<long> fill(cf.off.begin(), cf.off.end() - 1);
-  for (long f = 0; f < r->nFaces; ++f) {
-    cf.item[fill[r->f2c[2 * f] - 1]++] = f;
-    cf.item[fill[r->f2c[2 * f + 1] - 1]++] = f;
-  }
+  for (long f = 0; f < nFA; ++f)
+    for (int k = 0; k < 2; ++k)
+      if (in(r->f2c[2 * f + k])) cf.item[fill[r->f2c[2 * f + k] - 1]++] = f;
   for (int ip = 0; ip < r->nPatches; ++ip)
-    for (int i = 0; i < r->patches[ip].nBFaces; ++i) {
+    for (int i = 0; i < nbt(r->patches[ip]); ++i) {
       cf.item[fill[r->patches[ip].bf2c[i] - 1]++] = -(long)cf.bfc.size() - 1;
       cf.bfc.push_back(r->patches[ip].fc + 3 * i);
     }

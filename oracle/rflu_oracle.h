@@ -39,6 +39,10 @@ typedef struct {
   int distrib;
   int nData;            /* leading dimension of vals (0 read as 1) */
   int bcOptFixed;       /* inflow TOTANG FIXED switch */
+  /* pPatch%nBFacesTot: the patch's faces on actual cells (1..nBFaces), then
+   * on virtual cells (FACE_KIND_VB); bf2c/fn/fc hold nBFacesTot rows.  0 is
+   * read as nBFaces.  Only RFLU_LimitGradCellsSimple walks the VB faces. */
+  int nBFacesTot;
 } orc_patch_t;
 
 typedef struct {
@@ -74,6 +78,12 @@ typedef struct {
    * checks and time step cover 1..nCells; every per-cell array is sized
    * nCellsTot. */
   int nCellsTot;
+  /* Interior faces of every kind (0: nFaces): the flux faces 1..nFaces
+   * (FACE_KIND_AA, AV), then FACE_KIND_VV and FACE_KIND_VX faces, which only
+   * the virtual cells' face lists hold (tet2f / hex2f / ... of
+   * RFLU_LimitGradCellsSimple); f2c/fn/fc hold nFacesAll rows, a VX face's
+   * outside side is 0. */
+  int nFacesAll;
 } orc_region_t;
 
 /* status bits, shared with the engine */

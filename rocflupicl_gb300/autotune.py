@@ -56,17 +56,19 @@ def _measure(h, shape: Dict[str, int], step, steps: int, kernel) -> float:
 def _descend(h, step, steps: int, knobs: Dict[str, Sequence[int]]) -> Dict[str, object]:
     shape = {k: 0 for k in E.TUNING_KEYS}
     timings: Dict[str, Dict[int, float]] = {}
+    taken = 0
     for knob, cands in knobs.items():
         kernel = KNOB_KERNEL[knob]
         res = {}
         for v in cands:
             trial = dict(shape, **{knob: v})
             res[v] = _measure(h, trial, step, steps, kernel)
+            taken += steps + 1
         best = min(res, key=res.get)
         shape[knob] = best
         timings[knob] = res
     h.set_tuning(**shape)
-    return {"shape": shape, "ms": timings}
+    return {"shape": shape, "ms": timings, "steps_taken": taken}
 
 
 def tune_region(region: "E.Region", cfl: float, dt_imposed: float, end_time: float = 0.0,

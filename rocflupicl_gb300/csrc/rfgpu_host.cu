@@ -231,10 +231,6 @@ int check_desc(const rfgpu_region_desc_t *d) {
   if (d->reconst != RFGPU_RECONST_NONE && d->reconst != RFGPU_RECONST_LIM_VENKAT &&
       d->reconst != RFGPU_RECONST_WENO_XYZ)
     return RFGPU_ERR_UNSUPPORTED;
-  // RFLU_LimitGradCellsSimple walks every face of a virtual cell, including
-  // faces between two virtual cells, which a partitioned region does not hold
-  if (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1 && d->nCellsTot > d->nCells)
-    return RFGPU_ERR_UNSUPPORTED;
   if (d->rkScheme < 1 || d->rkScheme > 3) return RFGPU_ERR_UNSUPPORTED;
   if (d->precision != RFGPU_PREC_FP64 && d->precision != RFGPU_PREC_MIXED &&
       d->precision != RFGPU_PREC_SPLIT)
@@ -244,6 +240,7 @@ int check_desc(const rfgpu_region_desc_t *d) {
   for (int ip = 0; ip < d->nPatches; ++ip) {
     const rfgpu_patch_t &p = d->patches[ip];
     if (p.nBFaces < 0 || (p.nBFaces > 0 && (!p.bf2c || !p.fn || !p.fc))) return RFGPU_ERR_ARG;
+    if (p.nBFacesTot != 0 && (p.nBFacesTot < p.nBFaces || !p.bf2c || !p.fc)) return RFGPU_ERR_ARG;
     if (p.bcType != RFGPU_BC_SLIPWALL && p.bcType != RFGPU_BC_OUTFLOW &&
         p.bcType != RFGPU_BC_FARFIELD && p.bcType != RFGPU_BC_INJECTION &&
         p.bcType != RFGPU_BC_INFLOW_TOTANG && p.bcType != RFGPU_BC_INFLOW_VELTEMP)
@@ -287,6 +284,15 @@ int check_desc(const rfgpu_region_desc_t *d) {
       if (c < 1 || c > N) bad = 1;
     }
   if (bad) return RFGPU_ERR_ARG;
+  // faces past the flux faces (VV, VX): at least one side a virtual cell; the
+  // other a cell of the region or outside it (any value outside 1..N)
+  if (d->nFacesAll != 0 && d->nFacesAll < d->nFaces) return RFGPU_ERR_ARG;
+  for (int f = d->nFaces; f < d->nFacesAll; ++f) {
+    const int a = d->f2c[(long long)f * d->f2cLd], b = d->f2c[(long long)f * d->f2cLd + 1];
+    const bool va = a > d->nCells && a <= N, vb = b > d->nCells && b <= N;
+    const bool ina = a >= 1 && a <= N, inb = b >= 1 && b <= N;
+    if (!(va || vb) || (ina && !va && !vb) || (inb && !va && !vb)) return RFGPU_ERR_ARG;
+  }
   if (d->c2csOffsets[0] != 0) return RFGPU_ERR_ARG;
 #pragma omp parallel for schedule(static) reduction(| : bad)
   for (long long c = 0; c < N; ++c)
@@ -303,9 +309,13 @@ int check_desc(const rfgpu_region_desc_t *d) {
   for (long long c = 0; c < N; ++c)
     if (d->c2csOffsets[c + 1] - d->c2csOffsets[c] > 400) bad = 1;
   if (bad) return RFGPU_ERR_UNSUPPORTED;
-  for (int ip = 0; ip < d->nPatches; ++ip)
-    for (int b = 0; b < d->patches[ip].nBFaces; ++b)
-      if (d->patches[ip].bf2c[b] < 1 || d->patches[ip].bf2c[b] > N) return RFGPU_ERR_ARG;
+  for (int ip = 0; ip < d->nPatches; ++ip) {
+    const rfgpu_patch_t &p = d->patches[ip];
+    for (int b = 0; b < p.nBFaces; ++b)
+      if (p.bf2c[b] < 1 || p.bf2c[b] > N) return RFGPU_ERR_ARG;
+    for (int b = p.nBFaces; b < p.nBFacesTot; ++b)  // faces on virtual cells
+      if (p.bf2c[b] <= d->nCells || p.bf2c[b] > N) return RFGPU_ERR_ARG;
+  }
   return RFGPU_OK;
 }
 
@@ -673,6 +683,44 @@ void build_region(rfgpu_region_s *h, const rfgpu_region_desc_t *d, const Phys &p
     g.cfNb = M.upload(nb, s);
     g.cfD = M.upload(cast<R>(cd), s);
     g.cfTotal = sl.total;
+  }
+  // ---- RECONST 2 in a partitioned region: each virtual cell's offsets fc - xc
+  // to all of its faces (flux faces, VV and VX faces, the patches' faces on
+  // virtual cells) for RFLU_LimitGradCellsSimple, which walks every face of
+  // every cell; CSR over the virtual cells, SoA offsets
+  if (d->reconst == RFGPU_RECONST_WENO_XYZ && d->spaceOrder > 1 && N > d->nCells) {
+    const int nA = d->nCells, nV = N - nA;
+    const int nFA = d->nFacesAll > d->nFaces ? d->nFacesAll : d->nFaces;
+    std::vector<long long> off(nV + 1, 0);
+    auto dev = [&](int oneBased) { return oneBased >= 1 && oneBased <= N ? o.nc(oneBased - 1) : -1; };
+    auto each = [&](auto fn) {
+      for (int f = 0; f < nFA; ++f)
+        for (int k = 0; k < 2; ++k) {
+          const int c = dev(d->f2c[(long long)f * d->f2cLd + k]);
+          if (c >= nA) fn(c - nA, d->fc + 3 * (size_t)f);
+        }
+      for (int ip = 0; ip < d->nPatches; ++ip) {
+        const rfgpu_patch_t &p = d->patches[ip];
+        const int nb = p.nBFacesTot > p.nBFaces ? p.nBFacesTot : p.nBFaces;
+        for (int b = 0; b < nb; ++b) {
+          const int c = dev(p.bf2c[b]);
+          if (c >= nA) fn(c - nA, p.fc + 3 * (size_t)b);
+        }
+      }
+    };
+    each([&](int v, const double *) { off[v + 1]++; });
+    for (int v = 0; v < nV; ++v) off[v + 1] += off[v];
+    const long long P = off[nV];
+    std::vector<double> pd(3 * (size_t)P);
+    std::vector<long long> fill(off.begin(), off.end() - 1);
+    each([&](int v, const double *fcx) {
+      const long long e = fill[v]++;
+      const int c = nA + v;
+      for (int k = 0; k < 3; ++k) pd[(size_t)k * P + e] = fcx[k] - cofg[(size_t)k * N + c];
+    });
+    g.vposOff = M.upload(off, s);
+    g.vposD = M.upload(cast<R>(pd), s);
+    g.vposTotal = P;
   }
   // ---- state (FP64 SoA on the FP64 path; float-float pairs on the mixed path)
   if (sizeof(R) == 8) {

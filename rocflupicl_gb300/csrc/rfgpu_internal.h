@@ -92,6 +92,12 @@ struct RegionDev {
   const int *cfCnt, *cfCode, *cfNb;
   const R *cfD;
   long long cfTotal;
+  // RECONST 2 in a partitioned region: per virtual cell (index c - nAct) the
+  // offsets fc - xc to all its faces, CSR vposOff[nCells - nAct + 1],
+  // vposD[3][vposTotal]; null otherwise
+  const long long *vposOff;
+  const R *vposD;
+  long long vposTotal;
   // faces
   const int *f2c;      // [2][F]
   const R *fnA;        // [F][4] nx,ny,nz,area

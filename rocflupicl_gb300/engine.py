@@ -41,7 +41,7 @@ class PatchT(C.Structure):
                 ("nBFaces", C.c_int), ("bf2c", C.POINTER(C.c_int)), ("fn", C.POINTER(C.c_double)),
                 ("fc", C.POINTER(C.c_double)), ("vals", C.POINTER(C.c_double)),
                 ("distrib", C.c_int), ("nData", C.c_int),
-                ("bcOptFixed", C.c_int)]
+                ("bcOptFixed", C.c_int), ("nBFacesTot", C.c_int)]
 
 
 class BorderT(C.Structure):
@@ -66,7 +66,7 @@ class RegionDescT(C.Structure):
                 ("cellOrder", C.c_int), ("ausmSigma", C.c_double), ("ausmKp", C.c_double),
                 ("ausmKu", C.c_double), ("ausmMInf", C.c_double), ("nCellsTot", C.c_int),
                 ("iRegionGlobal", C.c_int), ("nBorders", C.c_int),
-                ("borders", C.POINTER(BorderT))]
+                ("borders", C.POINTER(BorderT)), ("nFacesAll", C.c_int)]
 
 
 class TuningT(C.Structure):
@@ -333,23 +333,27 @@ class Region:
             keep.append(a)
             return a
 
-        patches = [(p, bc) for p, bc in zip(m.patches, case.bcs) if p.n > 0]
+        patches = [(p, bc) for p, bc in zip(m.patches, case.bcs) if p.n + p.n_vb > 0]
         parr = (PatchT * max(1, len(patches)))()
         for i, (p, bc) in enumerate(patches):
             P = parr[i]
             P.bcType, P.spaceOrder, P.bcOptType, P.nBFaces = bc.bcType, bc.spaceOrder, bc.bcOptType, p.n
-            P.bf2c = _ip(k(p.bf2c, np.int32))
-            P.fn = _dp(k(p.fn, np.float64))
-            P.fc = _dp(k(p.fc, np.float64))
+            bf2c, bfn, bfc = p.all_faces()   # a region's VB faces after the actual ones
+            P.nBFacesTot = p.n + p.n_vb
+            P.bf2c = _ip(k(bf2c, np.int32))
+            P.fn = _dp(k(bfn, np.float64))
+            P.fc = _dp(k(bfc, np.float64))
             vals, nd, dist = bc.vals_array(p.n)
             P.vals = _dp(k(vals, np.float64))
             P.distrib, P.nData = dist, nd
             P.bcOptFixed = bc.bcOptFixed
         d = RegionDescT()
         d.nCells, d.nFaces, d.f2cLd = m.nCells, m.nFaces, 2
-        d.f2c = _ip(k(m.f2c, np.int32))
-        d.fn = _dp(k(m.fn, np.float64))
-        d.fc = _dp(k(m.fc, np.float64))
+        f2c, fn, fc = m.all_faces()   # flux faces, then a region's VV / VX faces
+        d.nFacesAll = m.nFacesAll
+        d.f2c = _ip(k(f2c, np.int32))
+        d.fn = _dp(k(fn, np.float64))
+        d.fc = _dp(k(fc, np.float64))
         d.cofg = _dp(k(m.cofg, np.float64))
         d.vol = _dp(k(m.vol, np.float64))
         d.c2csOffsets = _ip(k(m.c2cs_off, np.int32))

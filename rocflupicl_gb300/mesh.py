@@ -94,10 +94,27 @@ class Patch:
     bf2v: Optional[np.ndarray] = None
     # partitioned regions: positions of these faces in the whole mesh's patch
     global_faces: Optional[np.ndarray] = None
+    # partitioned regions: the patch's faces on virtual cells (the reference's
+    # FACE_KIND_VB faces, pPatch%nBFaces+1..nBFacesTot), bf2c (1-based local),
+    # fn, fc; only the positivity check of RECONST 2 reads them
+    vb_bf2c: Optional[np.ndarray] = None
+    vb_fn: Optional[np.ndarray] = None
+    vb_fc: Optional[np.ndarray] = None
 
     @property
     def n(self) -> int:
         return int(self.bf2c.shape[0])
+
+    @property
+    def n_vb(self) -> int:
+        return 0 if self.vb_bf2c is None else int(self.vb_bf2c.shape[0])
+
+    def all_faces(self):
+        """(bf2c, fn, fc) of the actual faces followed by the virtual ones."""
+        if not self.n_vb:
+            return self.bf2c, self.fn, self.fc
+        return (np.concatenate([self.bf2c, self.vb_bf2c]), np.concatenate([self.fn, self.vb_fn]),
+                np.concatenate([self.fc, self.vb_fc]))
 
 
 @dataclass
@@ -141,6 +158,13 @@ class BoxMesh:
     borders: List[Border] = field(default_factory=list)
     # whole-mesh (0-based) ids of a partitioned region's cells, actual then virtual
     global_cells: Optional[np.ndarray] = None
+    # partitioned regions: the interior faces beyond the flux faces, between
+    # two virtual cells (FACE_KIND_VV) and between a virtual cell and a cell
+    # outside the region (FACE_KIND_VX, outside side 0), f2c (n,2) 1-based
+    # local, fn, fc; only the positivity check of RECONST 2 reads them
+    vf2c: Optional[np.ndarray] = None
+    vfn: Optional[np.ndarray] = None
+    vfc: Optional[np.ndarray] = None
 
     @property
     def nTot(self) -> int:
@@ -153,6 +177,18 @@ class BoxMesh:
     @property
     def nMembs(self) -> int:
         return int(self.c2cs_mem.shape[0])
+
+    @property
+    def nFacesAll(self) -> int:
+        """Interior faces of every kind: the flux faces, then VV and VX faces."""
+        return self.nFaces + (0 if self.vf2c is None else int(self.vf2c.shape[0]))
+
+    def all_faces(self):
+        """(f2c, fn, fc) of all interior faces, flux faces first."""
+        if self.nFacesAll == self.nFaces:
+            return self.f2c, self.fn, self.fc
+        return (np.concatenate([self.f2c, self.vf2c]), np.concatenate([self.fn, self.vfn]),
+                np.concatenate([self.fc, self.vfc]))
 
 
 RFMESH_DEFER_STENCILS = 1

@@ -18,8 +18,14 @@ checked here:
     the stencil members of the virtual cells added last, each layer in
     ascending global id after the actual cells (the reference's ``vc`` list
     is kept sorted the same way);
-  * faces: every interior face with an actual cell, in the whole mesh's face
-    order; boundary faces of the actual cells, patch by patch;
+  * faces: every interior face with an actual cell (the flux faces, AA and
+    AV), in the whole mesh's face order; then, for the virtual cells' own
+    face lists, the faces between two virtual cells (VV) and between a
+    virtual cell and a cell outside the region (VX, the outside side 0),
+    each in the whole mesh's order, as the reference's face list orders
+    face kinds (modflu/RFLU_ModFaceList.F90:1317-1360); boundary faces of
+    the actual cells patch by patch, and after them each patch's faces on
+    virtual cells (VB);
   * stencils and WLSQ moments rebuilt over the region's own cells, as the
     reference's solver builds them for nCellsTot cells;
   * borders: one per neighbour region in ascending region id; send cell k of
@@ -106,13 +112,22 @@ def partition(m: M.BoxMesh, n_regions: int, axis: int = 0, layers: int = 2,
         fsel = np.flatnonzero(inA[a] | inA[b])
         if np.any(g2l[f2c0[fsel]] < 0):
             raise RuntimeError("a face of an actual cell leads outside the region")
+        inV = np.zeros(nC, bool)
+        inV[virt] = True
+        vv = np.flatnonzero(inV[a] & inV[b])
+        vx = np.flatnonzero((inV[a] & (g2l[b] < 0)) | (inV[b] & (g2l[a] < 0)))
+        vsel = np.concatenate([vv, vx])
+        vf2c = np.where(g2l[f2c0[vsel]] >= 0, g2l[f2c0[vsel]] + 1, 0).astype(np.int32)
         patches = []
         for p in m.patches:
             sel = np.flatnonzero(inA[p.bf2c - 1])
+            vbs = np.flatnonzero(inV[p.bf2c - 1])
             patches.append(M.Patch(bf2c=(g2l[p.bf2c[sel] - 1] + 1).astype(np.int32),
                                    fn=p.fn[sel].copy(), fc=p.fc[sel].copy(),
                                    bf2v=None if p.bf2v is None else p.bf2v[sel].copy(),
-                                   global_faces=sel))
+                                   global_faces=sel,
+                                   vb_bf2c=(g2l[p.bf2c[vbs] - 1] + 1).astype(np.int32),
+                                   vb_fn=p.fn[vbs].copy(), vb_fc=p.fc[vbs].copy()))
         # stencils over the region's own cells: vertex-to-cell lists of the
         # region's cells in ascending local id
         lcv = cv8[loc]
@@ -135,7 +150,8 @@ def partition(m: M.BoxMesh, n_regions: int, axis: int = 0, layers: int = 2,
             f2c=(g2l[f2c0[fsel]] + 1).astype(np.int32), fn=m.fn[fsel].copy(),
             fc=m.fc[fsel].copy(), c2cs_off=soff, c2cs_mem=smem, xyzmoms=moms,
             cell_type=m.cell_type[loc].copy(), patches=patches, n_of_type=m.n_of_type, conn=[],
-            nCellsTot=int(nT), iRegionGlobal=r + 1, borders=[], global_cells=loc))
+            nCellsTot=int(nT), iRegionGlobal=r + 1, borders=[], global_cells=loc,
+            vf2c=vf2c, vfn=m.fn[vsel].copy(), vfc=m.fc[vsel].copy()))
 
     # borders
     recv = {}

@@ -109,6 +109,7 @@ int main(int argc, char **argv) {
     p.distrib = 0;
     p.nData = 0;
     p.bcOptFixed = 0;
+    p.nBFacesTot = 0;   // one region: no faces on virtual cells
   }
   rfgpu_region_desc_t d{};
   d.nCells = nCells;

@@ -69,7 +69,7 @@ def layout_header(path):
 
 def test_bindc_types_cover_the_header_structs():
     t = bindc_types()
-    assert set(t) == {"rfgpu_patch_t", "rfgpu_border_t", "rfgpu_region_desc_t"}
+    assert set(t) == {"rfgpu_patch_t", "rfgpu_border_t", "rfgpu_region_desc_t", "rfgpu_tuning_t"}
     hdr = open(os.path.join(ROOT, "include", "rfgpu.h")).read()
     for name, fields in t.items():
         body = re.search(r"typedef struct \{([^{}]*)\} " + name + ";", hdr).group(1)
@@ -89,7 +89,7 @@ def test_header_layout_at_compile_time(tmp_path):
 
 def test_ctypes_mirrors_match_the_bindc_layout():
     mirrors = {"rfgpu_patch_t": E.PatchT, "rfgpu_border_t": E.BorderT,
-               "rfgpu_region_desc_t": E.RegionDescT}
+               "rfgpu_region_desc_t": E.RegionDescT, "rfgpu_tuning_t": E.TuningT}
     for name, fields in bindc_types().items():
         off, size = layout(fields)
         S = mirrors[name]

@@ -88,6 +88,34 @@ def stage_run(parts, n_steps=N_STEPS, mode="copy", prec=None, dts=None):
     return out, t, used
 
 
+@pytest.mark.parametrize("discr", [K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC])
+@pytest.mark.parametrize("kind", ["tets", "mixed_dip"])
+def test_weno_xyz_partitioned_fp64_bitwise_oracle(discr, kind):
+    """RECONST 2 (the reference's default reconstruction) on partitioned
+    regions: the virtual cells' positivity check walks all their faces (AV,
+    VV, VX and the patches' faces on virtual cells), as
+    RFLU_LimitGradCellsSimple does; the coupled batch and the stage API with
+    border copies equal the oracle's multi-region loop bit for bit."""
+    from test_partition import weno_dip_case
+    num = K.Numerics(spaceDiscr=discr, reconst=K.RECONST_WENO_XYZ, venkatGuard=1)
+    if kind == "tets":
+        c = K.tet_shock_box(18, ny=4, nz=4, length=(4.5, 1.0, 1.0), x_shock=1.5, numerics=num)
+    else:
+        c = weno_dip_case(num)  # the virtual faces decide some virtual cells' gradients
+    parts = P.partition_case(c, 3)
+    assert all(p.mesh.nFacesAll > p.mesh.nFaces for p in parts)
+    t, cvs, dvs, st = oracle_run(parts)
+    assert st == 0
+    out, times, sts = batch_run(parts)
+    for (cv, dv), ocv, odv in zip(out, cvs, dvs):
+        assert np.array_equal(cv, ocv) and np.array_equal(dv, odv)
+    assert all(x == t for x in times) and sts == [0, 0, 0]
+    out2, t2, _ = stage_run(parts, mode="copy")
+    assert t2 == t
+    for (cv, dv), ocv, odv in zip(out2, cvs, dvs):
+        assert np.array_equal(cv, ocv) and np.array_equal(dv, odv)
+
+
 @pytest.mark.parametrize("discr", [K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC, K.DISCR_UPW_AUSMPLUS])
 def test_coupled_batch_fp64_bitwise_oracle(discr):
     parts = P.partition_case(tube(discr=discr), 3)

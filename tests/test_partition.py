@@ -181,12 +181,91 @@ def test_partition_splits_per_face_patch_values():
     assert np.array_equal(np.sort(np.concatenate(got)), np.arange(n0))
 
 
-def test_weno_partitioned_region_refused():
-    """RECONST 2's positivity check walks every face of a virtual cell, including
-    faces between two virtual cells that a partitioned region does not hold:
-    such a region is refused before any CUDA call."""
-    p = P.partition_case(tube(order=2, n=12), 2)[0]
-    lib, d, keep = _desc_of(p, reconst=K.RECONST_WENO_XYZ)
+def test_region_face_lists_cover_every_face_of_every_cell():
+    """The flux faces (AA, AV), the virtual cells' VV and VX faces and the
+    patches' faces on actual and virtual cells give every cell of a region,
+    actual or virtual, exactly the faces of its type: RFLU_LimitGradCellsSimple
+    (RECONST 2) walks all of them."""
+    c = K.mixed_box(6, numerics=K.Numerics(reconst=K.RECONST_WENO_XYZ, venkatGuard=1))
+    per_type = {0: 4, 1: 6, 2: 5, 3: 5}   # tet, hex, prism, pyramid
+    for p in P.partition_case(c, 3):
+        m = p.mesh
+        f2c, fn, fc = m.all_faces()
+        assert f2c.shape[0] == fn.shape[0] == fc.shape[0] == m.nFacesAll > m.nFaces
+        extra = f2c[m.nFaces:]
+        virt = (extra > m.nCells) & (extra <= m.nTot)
+        assert np.all(virt.any(axis=1))                      # VV / VX: a virtual side
+        assert np.all(virt | (extra == 0))                   # the other virtual or outside
+        cnt = np.zeros(m.nTot + 1, int)
+        for k in (0, 1):
+            np.add.at(cnt, f2c[:, k], 1)
+        for pa in m.patches:
+            assert np.all(pa.bf2c <= m.nCells)
+            if pa.n_vb:
+                assert np.all(pa.vb_bf2c > m.nCells)
+            np.add.at(cnt, pa.all_faces()[0], 1)
+        assert np.array_equal(cnt[1:], [per_type[t] for t in m.cell_type])
+
+
+@pytest.mark.parametrize("bad", ["vv_actual", "vb_actual", "all_small"])
+def test_virtual_faces_refused_before_any_cuda_call(bad):
+    """Faces past the flux faces must have a virtual side, a patch's faces past
+    nBFaces must sit on virtual cells, nFacesAll may not undercut nFaces."""
+    p = P.partition_case(tube(order=2, n=12), 2)[0].with_numerics(reconst=K.RECONST_WENO_XYZ)
+    lib, d, keep = _desc_of(p)
+    m = p.mesh
+    f2c, fn, fc = (np.ascontiguousarray(a) for a in m.all_faces())
+    f2c = f2c.astype(np.int32)
+    keep += [f2c, fn, fc]
+    d.f2c, d.fn, d.fc, d.nFacesAll = E._ip(f2c), E._dp(fn), E._dp(fc), m.nFacesAll
+    if bad == "vv_actual":
+        f2c[m.nFaces] = (1, 2)
+    elif bad == "all_small":
+        d.nFacesAll = m.nFaces - 1
+    else:
+        pa = next(x for x in m.patches if x.n > 0)
+        bf = np.concatenate([pa.bf2c, [1]]).astype(np.int32)
+        bfn = np.concatenate([pa.fn, pa.fn[:1]])
+        bfc = np.concatenate([pa.fc, pa.fc[:1]])
+        keep += [bf, bfn, bfc]
+        parr = (E.PatchT * 1)()
+        parr[0].bcType, parr[0].spaceOrder, parr[0].nBFaces = K.BC_SLIPWALL, 2, pa.n
+        parr[0].nBFacesTot = pa.n + 1
+        parr[0].bf2c, parr[0].fn, parr[0].fc = E._ip(bf), E._dp(bfn), E._dp(bfc)
+        keep.append(parr)
+        d.nPatches, d.patches = 1, parr
     h = C.c_void_p()
-    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_UNSUPPORTED
+    assert lib.rfgpu_region_create(C.byref(d), C.byref(h)) == E.ERR_ARG
     assert not h.value
+
+
+def weno_dip_case(num):
+    """Mixed 8^3 box whose density dips to 0.02 at x = 0.65, inside the second
+    slab of a 3-region partition: RECONST 2's positivity check fires there,
+    and on some virtual cells only through a face between two virtual cells,
+    to a cell outside the region or on a patch."""
+    c = K.mixed_box(8, numerics=num)
+    x = c.mesh.cofg[:, 0]
+    c.cv *= (0.02 + 4.0 * (x - 0.65) ** 2)[:, None]
+    c.dv = K.eos_dv(c.numerics, c.cv)
+    return c
+
+
+def test_virtual_faces_decide_some_virtual_gradients():
+    """In the dip case the oracle's limited gradients of some virtual cells
+    change when their VV / VX / VB faces are left out (and of no actual cell):
+    those faces are on the tested path."""
+    import dataclasses
+    from oracle.oracle import Oracle
+    num = K.Numerics(spaceDiscr=K.DISCR_UPW_ROE, reconst=K.RECONST_WENO_XYZ, venkatGuard=1)
+    changed = 0
+    for p in P.partition_case(weno_dip_case(num), 3):
+        m = p.mesh
+        bare = dataclasses.replace(m, vf2c=None, vfn=None, vfc=None, patches=[
+            dataclasses.replace(pa, vb_bf2c=None, vb_fn=None, vb_fc=None) for pa in m.patches])
+        _, g1 = Oracle(p).residual(p.cv, p.dv)
+        _, g2 = Oracle(dataclasses.replace(p, mesh=bare)).residual(p.cv, p.dv)
+        diff = np.flatnonzero(np.any(g1 != g2, axis=(1, 2)))
+        assert np.all(diff >= m.nCells)
+        changed += diff.size
+    assert changed > 0
