@@ -246,9 +246,13 @@ long long rfgpu_device_bytes(rfgpu_region_t h);
 /* Kernel launches issued by the handle since creation. */
 long long rfgpu_launch_count(rfgpu_region_t h);
 /* Launch shapes of the stage passes, chosen by the autotuner
- * (rocflupicl_gb300/autotune.py) by timing real steps; results do not depend
- * on them.  A zero field keeps the default.  No counterpart in the reference
- * (its loops run serially on the host). */
+ * (rocflupicl_gb300/autotune.py) by timing real steps.  Block sizes, faces per
+ * thread and the grid leave every result bit for bit unchanged; the persistent
+ * stage does on the FP64 path, and on the reduced-precision paths changes
+ * results by FP32 rounding at most (the compiler may contract a product into
+ * an FMA differently inside the one large kernel).  A zero field keeps the
+ * default.  No counterpart in the reference (its loops run serially on the
+ * host). */
 typedef struct {
   int gridCap;         /* blocks per launch of every tiled pass; a grid smaller than
                           the tile count walks the tiles persistently; 0 = one
@@ -260,6 +264,13 @@ typedef struct {
   int facesPerThread;  /* interior faces per thread of that pass: 1 (default) or 2 */
   int cellBlock;       /* threads (= cells) per block of the residual gather and
                           update pass: 64, 128 (default) or 256 */
+  int persistentStage; /* 1: each RK stage is one cooperative launch that runs all
+                          its passes over every tile, separated by grid-wide
+                          barriers (the block sizes above must then be the
+                          defaults); 0: one launch per pass.  A barrier wait is
+                          bounded (about a second); one that runs out ends the
+                          launch and the next rfgpu_sync / rfgpu_batch_sync /
+                          rfgpu_status returns RFGPU_ERR_TIMEOUT */
 } rfgpu_tuning_t;
 /* RFGPU_ERR_ARG for a shape outside the values above.  Drops a captured
  * graph (the next rfgpu_steps_graph captures again). */
@@ -271,8 +282,9 @@ int rfgpu_set_tuning(rfgpu_region_t h, const rfgpu_tuning_t *t);
  * returns, per kernel class, the summed milliseconds and launch counts, then
  * resets.  Classes: 0 gradient, 1 limiter, 2 face flux, 3 boundary-face flux,
  * 4 gather+update, 5 dt faces, 6 dt boundary faces, 7 dt cells, 8 dt finalize,
- * 9 halo exchange.  Graph replays are not profiled. */
-#define RFGPU_NPROF 10
+ * 9 halo exchange, 10 a whole stage run as one persistent launch.  Graph
+ * replays are not profiled. */
+#define RFGPU_NPROF 11
 int rfgpu_profile(rfgpu_region_t h, int enable);
 int rfgpu_profile_read(rfgpu_region_t h, double *ms, long long *count, int n);
 
@@ -340,6 +352,13 @@ int rfgpu_batch_steps_graph(rfgpu_batch_t b, int nSteps, double cfl, double dtIm
 int rfgpu_batch_sync(rfgpu_batch_t b);
 /* Launch shapes of the batch's passes (rfgpu_tuning_t, as for a region). */
 int rfgpu_batch_set_tuning(rfgpu_batch_t b, const rfgpu_tuning_t *t);
+/* Failure-detection hook for tests (no counterpart in the reference): with
+ * extra > 0 the batch's persistent stage launches wait at their grid-wide
+ * barriers for `extra` blocks that never arrive, with a wait limit of
+ * spinCycles SM clock cycles (0 keeps the default), so the bounded wait runs
+ * out and rfgpu_batch_sync returns RFGPU_ERR_TIMEOUT; extra = 0 restores
+ * normal operation.  The state of a stage that timed out is not valid. */
+int rfgpu_batch_test_barrier(rfgpu_batch_t b, int extra, long long spinCycles);
 void *rfgpu_batch_stream(rfgpu_batch_t b);
 int rfgpu_batch_profile(rfgpu_batch_t b, int enable);
 int rfgpu_batch_profile_read(rfgpu_batch_t b, double *ms, long long *count, int n);

@@ -11,7 +11,9 @@ by timing real steps on the device:
   thread) and the residual gather + update pass (`cellBlock`), 64 / 128 / 256;
 * the persistent grid (`gridCap`): one block per tile, or a grid of a few
   blocks per SM walking the tiles (multiples of the SM count the device
-  reports).
+  reports);
+* one cooperative launch per RK stage (`persistentStage`) against one launch
+  per pass, on whole steps.
 
 The search is coordinate descent from the default shape: each knob in turn
 takes its candidates with the others fixed, judged by the CUDA-event time of
@@ -53,7 +55,8 @@ def _measure(h, shape: Dict[str, int], step, steps: int, kernel) -> float:
     return t / max(n, 1) if n else ms / steps
 
 
-def _descend(h, step, steps: int, knobs: Dict[str, Sequence[int]]) -> Dict[str, object]:
+def _descend(h, step, steps: int, knobs: Dict[str, Sequence[int]],
+             persistent: bool = False) -> Dict[str, object]:
     shape = {k: 0 for k in E.TUNING_KEYS}
     timings: Dict[str, Dict[int, float]] = {}
     taken = 0
@@ -67,6 +70,17 @@ def _descend(h, step, steps: int, knobs: Dict[str, Sequence[int]]) -> Dict[str, 
         best = min(res, key=res.get)
         shape[knob] = best
         timings[knob] = res
+    if persistent:
+        # one cooperative launch per stage (default block shapes, the chosen
+        # grid cap) against the best per-pass shape, whole steps
+        res = {0: _measure(h, shape, step, steps, None)}
+        coop = {k: 0 for k in E.TUNING_KEYS}
+        coop.update(gridCap=shape["gridCap"], persistentStage=1)
+        res[1] = _measure(h, coop, step, steps, None)
+        taken += 2 * (steps + 1)
+        timings["persistentStage"] = res
+        if res[1] < res[0]:
+            shape = coop
     h.set_tuning(**shape)
     return {"shape": shape, "ms": timings, "steps_taken": taken}
 
@@ -81,7 +95,8 @@ def tune_region(region: "E.Region", cfl: float, dt_imposed: float, end_time: flo
         grid_caps = [0] + [sms * k for k in (4, 8, 16)]
     knobs = {"gradBlock": BLOCKS, "faceBlock": BLOCKS, "facesPerThread": (1, 2),
              "cellBlock": BLOCKS, "gridCap": grid_caps}
-    out = _descend(region, lambda: region.step(cfl, dt_imposed, 0.0, end_time), steps, knobs)
+    out = _descend(region, lambda: region.step(cfl, dt_imposed, 0.0, end_time), steps, knobs,
+                   persistent=True)
     out["sms"] = sms
     return out
 
@@ -98,7 +113,8 @@ def tune_batch(batch: "E.Batch", cfl: float, dt_imposed: float = 1.0, end_time: 
     if blocks:
         knobs.update({"gradBlock": BLOCKS, "faceBlock": BLOCKS, "facesPerThread": (1, 2),
                       "cellBlock": BLOCKS})
-    out = _descend(batch, lambda: batch.step(cfl, dt_imposed, 0.0, end_time), steps, knobs)
+    out = _descend(batch, lambda: batch.step(cfl, dt_imposed, 0.0, end_time), steps, knobs,
+                   persistent=True)
     out["sms"] = sms
     out["grid_cap"] = out["shape"]["gridCap"]
     out["ms_per_step"] = out["ms"]["gridCap"]

@@ -195,6 +195,26 @@ namespace {
 
 int cuda_rc(cudaError_t e) { return e == cudaSuccess ? RFGPU_OK : RFGPU_ERR_CUDA; }
 
+// Limit of a persistent stage launch's grid-barrier wait, in SM clock cycles
+// (about a second at GB300's clocks).
+constexpr long long kBarrierSpin = 2000000000ll;
+
+// Synchronise a stream and report a persistent stage launch whose bounded
+// barrier wait ran out (the error word is read and cleared).
+int sync_and_check(cudaStream_t s, GridBar *bar) {
+  if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
+  if (!bar) return RFGPU_OK;
+  unsigned err = 0;
+  if (cudaMemcpyAsync(&err, &bar->err, sizeof(unsigned), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  if (!err) return RFGPU_OK;
+  if (cudaMemsetAsync(&bar->err, 0, sizeof(unsigned), s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  return RFGPU_ERR_TIMEOUT;
+}
+
 void rk_coeffs(int scheme, Phys &ph) {
   for (int i = 0; i < 5; ++i) ph.ark[i] = ph.grk[i] = 0.0;
   if (scheme == RFGPU_RK_SCHEME_4_CLASSICAL) {
@@ -1081,8 +1101,14 @@ int apply_tuning(Work &w, TileCache &tc, DevAlloc &M, cudaStream_t s, const rfgp
                  const std::vector<int> &nCells, const std::vector<int> &nFaces) {
   auto okBlock = [](int b) { return b == 0 || b == 64 || b == 128 || b == 256; };
   if (t.gridCap < 0 || !okBlock(t.gradBlock) || !okBlock(t.faceBlock) || !okBlock(t.cellBlock) ||
-      t.facesPerThread < 0 || t.facesPerThread > 2)
+      t.facesPerThread < 0 || t.facesPerThread > 2 || t.persistentStage < 0 ||
+      t.persistentStage > 1)
     return RFGPU_ERR_ARG;
+  auto dflt = [](int b) { return b == 0 || b == 128; };
+  if (t.persistentStage && !(dflt(t.gradBlock) && dflt(t.faceBlock) && dflt(t.cellBlock) &&
+                             t.facesPerThread <= 1))
+    return RFGPU_ERR_ARG;  // the persistent kernel walks the default 128-item tiles
+  if (t.persistentStage && !w.bar) return RFGPU_ERR_ARG;
   auto list = [&](std::map<int, std::pair<Tile *, int>> &cache, const std::vector<int> &counts,
                   int stride) -> std::pair<Tile *, int> {
     auto it = cache.find(stride);
@@ -1123,6 +1149,7 @@ int apply_tuning(Work &w, TileCache &tc, DevAlloc &M, cudaStream_t s, const rfgp
     w.nFaceTiles = p.second;
     w.faceBlock = fb;
     w.facesPerThread = fpt;
+    w.coop = t.persistentStage;
   } catch (const std::bad_alloc &) {
     return RFGPU_ERR_NOMEM;
   }
@@ -1217,6 +1244,9 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
                    (int)bt.size(), 0, block, 1};
     h->tiles.faces[block] = {h->faceTiles, (int)ft.size()};
     h->work.split = h->prec == RFGPU_PREC_SPLIT;
+    h->work.bar = h->mem.alloc<GridBar>(1);
+    h->work.barSpin = kBarrierSpin;
+    cudaMemsetAsync(h->work.bar, 0, sizeof(GridBar), h->stream);
     h->stage = h->mem.alloc<double>(5 * (size_t)h->nCells);
     if (h->prec) h->stage2 = h->mem.alloc<double>(3 * (size_t)h->nCells);
     cudaStreamSynchronize(h->stream);
@@ -1455,6 +1485,8 @@ int rfgpu_set_time(rfgpu_region_t h, double currentTime) {
 
 int rfgpu_status(rfgpu_region_t h, int *flags) {
   if (!h || !flags) return RFGPU_ERR_ARG;
+  const int brc = sync_and_check(h->stream, h->work.bar);
+  if (brc != RFGPU_OK) return brc;
   unsigned *st = h->prec ? h->rd32.status : h->rd64.status;
   unsigned v = 0;
   if (cudaMemcpyAsync(&v, st, 4, cudaMemcpyDeviceToHost, h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
@@ -1466,7 +1498,7 @@ int rfgpu_status(rfgpu_region_t h, int *flags) {
 
 int rfgpu_sync(rfgpu_region_t h) {
   if (!h) return RFGPU_ERR_ARG;
-  return cuda_rc(cudaStreamSynchronize(h->stream));
+  return sync_and_check(h->stream, h->work.bar);
 }
 
 void *rfgpu_stream(rfgpu_region_t h) { return h ? (void *)h->stream : nullptr; }
@@ -1635,6 +1667,9 @@ int rfgpu_batch_create_ex(rfgpu_region_t *regions, int n, int flags, rfgpu_batch
     b->work = Work{dct, dft, dbt, (int)ct.size(), (int)ft.size(), (int)bt.size(), sms * 8, block, n};
     b->tiles.faces[block] = {dft, (int)ft.size()};
     b->work.split = prec == RFGPU_PREC_SPLIT;
+    b->work.bar = b->mem.alloc<GridBar>(1);
+    b->work.barSpin = kBarrierSpin;
+    cudaMemsetAsync(b->work.bar, 0, sizeof(GridBar), b->stream);
     if (coupled) {
       b->work.coupled = 1;
       b->work.halo = links.empty() ? nullptr : b->mem.upload(links, b->stream);
@@ -1736,7 +1771,19 @@ int rfgpu_batch_set_tuning(rfgpu_batch_t b, const rfgpu_tuning_t *t) {
 
 int rfgpu_batch_sync(rfgpu_batch_t b) {
   if (!b) return RFGPU_ERR_ARG;
-  return cuda_rc(cudaStreamSynchronize(b->stream));
+  return sync_and_check(b->stream, b->work.bar);
+}
+
+int rfgpu_batch_test_barrier(rfgpu_batch_t b, int extra, long long spinCycles) {
+  if (!b || extra < 0 || spinCycles < 0) return RFGPU_ERR_ARG;
+  if (cudaStreamSynchronize(b->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  b->work.barExtra = extra;
+  b->work.barSpin = spinCycles > 0 ? spinCycles : kBarrierSpin;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  return RFGPU_OK;
 }
 
 void *rfgpu_batch_stream(rfgpu_batch_t b) { return b ? (void *)b->stream : nullptr; }

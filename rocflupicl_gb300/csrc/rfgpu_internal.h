@@ -141,6 +141,13 @@ struct HaloLink {
   int srcRegion, srcCell, dstRegion, dstCell;
 };
 
+// Grid-wide barrier of the persistent stage launch: arrivals and generation
+// (cleared before every launch) and a sticky error word (bit 0: a bounded
+// wait ran out), read and cleared by the host's sync calls.
+struct GridBar {
+  unsigned count, gen, err, pad;
+};
+
 struct Work {
   const Tile *cellTiles, *faceTiles, *bfaceTiles;
   int nCellTiles, nFaceTiles, nBFaceTiles;
@@ -162,6 +169,14 @@ struct Work {
   int gradBlock, faceBlock, facesPerThread, cellBlock;
   // 1: the regions run the split precision mode (R = float, FP64 state)
   int split;
+  // 1: a full stage is one cooperative launch (every pass, separated by
+  // grid-wide barriers) instead of one launch per pass
+  int coop;
+  GridBar *bar;
+  // barrier arrivals expected beyond the grid (0; a test sets it so the wait
+  // runs out) and the wait's limit in SM clock cycles
+  int barExtra;
+  long long barSpin;
 };
 
 struct DtArgs {
@@ -195,11 +210,11 @@ struct ChunkMap {
 
 // Kernel classes for the per-kernel event profiler.
 enum { KP_GRADIENT = 0, KP_LIMITER, KP_FACE_FLUX, KP_BFACE_FLUX, KP_GATHER_UPDATE, KP_DT_FACE,
-       KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_HALO, KP_COUNT };
+       KP_DT_BFACE, KP_DT_CELL, KP_DT_FINAL, KP_HALO, KP_STAGE, KP_COUNT };
 // KP_GRADIENT times the fused gradient + limiter kernel; KP_LIMITER the
 // WENO-XYZ weighting and positivity pass of RECONST 2; KP_DT_FACE and
 // KP_DT_BFACE are no longer launched separately (kept for the ABI's class
-// numbering).
+// numbering); KP_STAGE times a whole stage run as one persistent launch.
 
 // Optional hook called around every kernel launch (phase 0 before, 1 after),
 // used to record CUDA events on the launching stream.

@@ -779,24 +779,27 @@ __global__ void k_prim(const RegionDev<R> *__restrict__ regs, const Tile *__rest
 // from the copied cv with the EOS every cell uses; mixed path, the
 // float-float pair and the sender's record slots copied (the record is a
 // function of the pair and of the gas constants, which coupled regions share).
+// The source cell's state is read through L2 (__ldcg): in a persistent stage
+// launch other blocks updated it earlier in the same kernel.
 template <typename R>
 __device__ __forceinline__ void halo_cell(const RegionDev<R> &gs, int cs, const RegionDev<R> &gd,
                                           int cd) {
   const int Ns = gs.nCells, Nd = gd.nCells;
   if constexpr (sizeof(R) == 8) {
 #pragma unroll
-    for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = gs.cv[(size_t)j * Ns + cs];
+    for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = __ldcg(gs.cv + (size_t)j * Ns + cs);
     set_vars_cell(gd, cd, 1);
   } else {
     if (gd.cvF) {
 #pragma unroll
-      for (int j = 0; j < 10; ++j) gd.cvF[(size_t)j * Nd + cd] = gs.cvF[(size_t)j * Ns + cs];
+      for (int j = 0; j < 10; ++j) gd.cvF[(size_t)j * Nd + cd] = __ldcg(gs.cvF + (size_t)j * Ns + cs);
     } else {  // split path: the FP64 rows
 #pragma unroll
-      for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = gs.cv[(size_t)j * Ns + cs];
+      for (int j = 0; j < 5; ++j) gd.cv[(size_t)j * Nd + cd] = __ldcg(gs.cv + (size_t)j * Ns + cs);
     }
     R a[8], b[8];
-    ld8_rw(gs.rec + 8 * (size_t)cs, a);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) a[k] = __ldcg(gs.rec + 8 * (size_t)cs + k);
     ld8_rw(gd.rec + 8 * (size_t)cd, b);
 #pragma unroll
     for (int k = 0; k < 5; ++k) b[k] = a[k];
@@ -989,13 +992,13 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #endif
 // BS threads per block (one cell each, a tile of BS cells); the requested
 // residency keeps the same number of resident threads per SM for every BS.
-template <typename R, int FUSE_DT, int BS>
-__global__ void __launch_bounds__(BS, ((sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MINB_DT : RF_GRAD_MINB)
-                                                        : 4) * 128 / BS)
-    k_grad_lim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles, int nTiles) {
+// One tile of the gradient pass (every thread of the block, one cell each).
+template <typename R, int FUSE_DT>
+__device__ __forceinline__ void grad_tile(const RegionDev<R> *__restrict__ regs,
+                                          const Tile *__restrict__ tiles, int t_,
+                                          unsigned long long *smin) {
   constexpr bool fuseDt = FUSE_DT != 0;
-  __shared__ unsigned long long smin[32];
-  RF_TILE_LOOP(tiles, nTiles) {
+  {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int c = tl.first + threadIdx.x;
@@ -1262,6 +1265,14 @@ __global__ void __launch_bounds__(BS, ((sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MIN
   }
 }
 
+template <typename R, int FUSE_DT, int BS>
+__global__ void __launch_bounds__(BS, ((sizeof(R) == 4) ? (FUSE_DT ? RF_GRAD_MINB_DT : RF_GRAD_MINB)
+                                                        : 4) * 128 / BS)
+    k_grad_lim(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles, int nTiles) {
+  __shared__ unsigned long long smin[32];
+  RF_TILE_LOOP(tiles, nTiles) grad_tile<R, FUSE_DT>(regs, tiles, t_, smin);
+}
+
 // Riemann flux of one interior face on its (reconstructed) states, by DISCR.
 // AUSM+up sets up H and a as its face loops do: at second order from the
 // reconstructed state with refCp/refGamma (T = p/(rho R), a = sqrt(g R T),
@@ -1349,23 +1360,28 @@ __device__ __forceinline__ void face_flux_one(const RegionDev<R> &g, int f) {
 }
 
 template <typename R, int BS, int FPT>
+__device__ __forceinline__ void face_tile(const RegionDev<R> *__restrict__ regs,
+                                          const Tile *__restrict__ tiles, int nTiles, int t_,
+                                          int dist) {
+  const Tile tl = tiles[t_];
+  const RegionDev<R> &g = regs[tl.region];
+  prefetch_ahead(t_, nTiles, dist, [&](int t) {
+    const Tile tp = tiles[t];
+    prefetch_face_tile(regs[tp.region], tp.first, BS * FPT);
+  });
+#pragma unroll
+  for (int k = 0; k < FPT; ++k) {
+    const int f = tl.first + threadIdx.x + k * BS;
+    if (f < g.nFaces) face_flux_one(g, f);
+  }
+}
+
+template <typename R, int BS, int FPT>
 __global__ void __launch_bounds__(BS) k_face_flux(const RegionDev<R> *__restrict__ regs,
                                                   const Tile *__restrict__ tiles, int nTiles,
                                                   int pfDist) {
   const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
-  RF_TILE_LOOP(tiles, nTiles) {
-    const Tile tl = tiles[t_];
-    const RegionDev<R> &g = regs[tl.region];
-    prefetch_ahead(t_, nTiles, dist, [&](int t) {
-      const Tile tp = tiles[t];
-      prefetch_face_tile(regs[tp.region], tp.first, BS * FPT);
-    });
-#pragma unroll
-    for (int k = 0; k < FPT; ++k) {
-      const int f = tl.first + threadIdx.x + k * BS;
-      if (f < g.nFaces) face_flux_one(g, f);
-    }
-  }
+  RF_TILE_LOOP(tiles, nTiles) face_tile<R, BS, FPT>(regs, tiles, nTiles, t_, dist);
 }
 
 // Farfield rind state, RFLU_SetRindStateFarfieldPerf
@@ -1526,14 +1542,14 @@ __device__ __forceinline__ void bcond_outflow(int bcOpt, R pout, R sxn, R syn, R
 // as mass flux, the exact additive identity, since the reference leaves the
 // mass residual untouched there.
 template <typename R>
-__global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restrict__ regs,
-                                                    const Tile *__restrict__ tiles, int nTiles) {
-  RF_TILE_LOOP(tiles, nTiles) {
+__device__ __forceinline__ void bface_tile(const RegionDev<R> *__restrict__ regs,
+                                           const Tile *__restrict__ tiles, int t_) {
+  {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     const int b = tl.first + threadIdx.x;
     const int B = g.nBFaces;
-    if (b >= B) continue;
+    if (b >= B) return;
     const int N = g.nCells;
     const int c = g.bf2c[b];
     const int kind = g.bkind[b];
@@ -1658,6 +1674,12 @@ __global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restri
     flx[5] = flx[6] = flx[7] = R(0);
     st8(g.bflux + 8 * (size_t)b, flx);
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_bface_flux(const RegionDev<R> *__restrict__ regs,
+                                                    const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) bface_tile<R>(regs, tiles, t_);
 }
 
 // AfterUpdateMP checks for one cell (libfloflu/AfterUpdateMP.F90:134-136):
@@ -1792,7 +1814,9 @@ __device__ __forceinline__ void gather_update_mixed(const RegionDev<float> &g, i
   float rhs[5];
 #pragma unroll
   for (int j = 0; j < 5; ++j) rhs[j] = hi[j] + lo[j];
-  const float fac = a.useDeviceDt ? float(g.scal[3 + is - 1]) : float(ph.ark[is - 1] * a.dtHost);
+  // the device time step is read through L2 (__ldcg): in a persistent stage
+  // launch another block wrote it earlier in the same kernel
+  const float fac = a.useDeviceDt ? float(__ldcg(g.scal + 3 + is - 1)) : float(ph.ark[is - 1] * a.dtHost);
   const float adtv = fac * ivol;
   const float grk = ph.grkF[is - 1];
   float oh[5], ol[5];
@@ -1961,7 +1985,7 @@ __device__ __forceinline__ void gather_update_split(const RegionDev<float> &g, i
     for (int j = 0; j < 5; ++j) g.rhs[(size_t)j * N + c] = acc[j];
   }
   if (!a.update) return;
-  const double fac = a.useDeviceDt ? g.scal[3 + is - 1] : ph.ark[is - 1] * a.dtHost;
+  const double fac = a.useDeviceDt ? __ldcg(g.scal + 3 + is - 1) : ph.ark[is - 1] * a.dtHost;
   const double adtv = fac * ivol;
   const double grk = ph.grk[is - 1];
   double old[5];
@@ -2032,12 +2056,11 @@ __device__ __forceinline__ void gather_update_split(const RegionDev<float> &g, i
 // residual is written (rfgpu_residual).
 // SPLIT selects the split path's update at compile time (a run-time branch
 // between the two FP32-flux updates costs the mixed path registers).
-template <typename R, int BS, int SPLIT>
-__global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__restrict__ regs,
-                                                      const Tile *__restrict__ tiles,
-                                                      int nTiles, StepArgs a, int pfDist) {
-  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
-  RF_TILE_LOOP(tiles, nTiles) {
+template <typename R, int SPLIT>
+__device__ __forceinline__ void update_tile(const RegionDev<R> *__restrict__ regs,
+                                            const Tile *__restrict__ tiles, int nTiles, int t_,
+                                            const StepArgs &a, int dist) {
+  {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
     prefetch_ahead(t_, nTiles, dist, [&](int t) {
@@ -2046,20 +2069,20 @@ __global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__rest
     });
     const int c = tl.first + threadIdx.x;
     const int N = g.nCells;
-    if (c >= N) continue;
+    if (c >= N) return;
     if (c >= g.nAct) {  // virtual cell: ZeroDummyCellsMP, no update
       if (a.writeRhs) {
 #pragma unroll
         for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = 0.0;
       }
-      continue;
+      return;
     }
     if constexpr (sizeof(R) == 4) {
       if constexpr (SPLIT)
         gather_update_split(g, c, a);
       else
         gather_update_mixed(g, c, a);
-      continue;
+      return;
     }
     double acc[5] = {-0.0, -0.0, -0.0, -0.0, -0.0};
     const long long e0 = g.cfOff[c >> 5] + (c & 31);
@@ -2086,10 +2109,10 @@ __global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__rest
 #pragma unroll
       for (int j = 0; j < 5; ++j) g.rhs[j * N + c] = acc[j];
     }
-    if (!a.update) continue;
+    if (!a.update) return;
     const Phys &ph = g.ph;
     const int is = a.istage;
-    const double fac = a.useDeviceDt ? g.scal[3 + is - 1] : ph.ark[is - 1] * a.dtHost;
+    const double fac = a.useDeviceDt ? __ldcg(g.scal + 3 + is - 1) : ph.ark[is - 1] * a.dtHost;
     const double adtv = fac / g.vol[c];
     double q[5], old[5];
 #pragma unroll
@@ -2165,6 +2188,14 @@ __global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__rest
     r[4] = R(d[0]);
     st8(g.rec + 8 * (size_t)c, r);
   }
+}
+
+template <typename R, int BS, int SPLIT>
+__global__ void __launch_bounds__(BS) k_gather_update(const RegionDev<R> *__restrict__ regs,
+                                                      const Tile *__restrict__ tiles,
+                                                      int nTiles, StepArgs a, int pfDist) {
+  const int dist = (int)gridDim.x < nTiles ? (int)gridDim.x : pfDist;
+  RF_TILE_LOOP(tiles, nTiles) update_tile<R, SPLIT>(regs, tiles, nTiles, t_, a, dist);
 }
 
 // Mixed path transfers: the host's Fortran images cv(5,N) / dv(3,N), copied
@@ -2266,7 +2297,7 @@ template <typename R>
 __device__ __forceinline__ void dt_finalize_region(const RegionDev<R> &g, unsigned long long raw,
                                                    const DtArgs &a) {
   double dtMin = __longlong_as_double((long long)raw);
-  const double t = a.useDeviceTime ? g.scal[1] : a.timeHost;
+  const double t = a.useDeviceTime ? __ldcg(g.scal + 1) : a.timeHost;
   dtMin = a.cfl * dtMin;
   double wI = 0.0, wC = 0.0;
   if (t <= 1.0e-08) wI = 1.0; else wC = 1.0;
@@ -2324,6 +2355,43 @@ __global__ void k_dt_finalize_coupled(const RegionDev<R> *__restrict__ regs, int
   unsigned long long raw = smin[0];
   for (int w = 1; w < (int)(blockDim.x >> 5); ++w) raw = smin[w] < raw ? smin[w] : raw;
   for (int r = threadIdx.x; r < nRegions; r += blockDim.x) {
+    *regs[r].dtBits = 0x7FF0000000000000ull;
+    dt_finalize_region(regs[r], raw, a);
+  }
+}
+
+// The time-step finalisation of a whole Work by one block (the persistent
+// stage launch): per region, or the coupled minimum over all regions first,
+// as k_dt_finalize / k_dt_finalize_coupled do; the raw minima are read
+// through L2, other blocks reduced them earlier in the same kernel.
+template <typename R>
+__device__ __forceinline__ void dt_finalize_block(const RegionDev<R> *__restrict__ regs,
+                                                  const Work &w, const DtArgs &a,
+                                                  unsigned long long *smin) {
+  if (!w.coupled) {
+    for (int r = threadIdx.x; r < w.nRegions; r += blockDim.x) {
+      const RegionDev<R> &g = regs[r];
+      const unsigned long long raw = __ldcg(g.dtBits);
+      *g.dtBits = 0x7FF0000000000000ull;
+      dt_finalize_region(g, raw, a);
+    }
+    return;
+  }
+  unsigned long long v = 0x7FF0000000000000ull;
+  for (int r = threadIdx.x; r < w.nRegions; r += blockDim.x) {
+    const unsigned long long x = __ldcg(regs[r].dtBits);
+    v = x < v ? x : v;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    const unsigned long long x = __shfl_down_sync(0xffffffffu, v, o);
+    v = x < v ? x : v;
+  }
+  if ((threadIdx.x & 31) == 0) smin[threadIdx.x >> 5] = v;
+  __syncthreads();
+  unsigned long long raw = smin[0];
+  for (int k = 1; k < (int)(blockDim.x >> 5); ++k) raw = smin[k] < raw ? smin[k] : raw;
+  __syncthreads();
+  for (int r = threadIdx.x; r < w.nRegions; r += blockDim.x) {
     *regs[r].dtBits = 0x7FF0000000000000ull;
     dt_finalize_region(regs[r], raw, a);
   }
@@ -2441,10 +2509,127 @@ void launch_update_tuned(const RegionDev<R> *regs, const Work &w, const StepArgs
   else update_launch<R, 128>(regs, t, n, w.grid, a, w.split, s);
 }
 
+// ---- one launch per RK stage ---------------------------------------------------
+template <typename R>
+__device__ __forceinline__ void weno_tile(const RegionDev<R> *__restrict__ regs,
+                                          const Tile *__restrict__ tiles, int t_);
+
+// Grid-wide barrier of the persistent stage kernel, a cooperative launch (so
+// every block is resident).  Thread 0 of each block arrives; the last arrival
+// clears the count and releases the others by advancing the generation.  Every
+// wait is bounded by `spin` SM clock cycles: one that runs out sets bit 0 of
+// err, and every block returns as soon as it sees err set after a barrier, so
+// the kernel ends and the host reads RFGPU_ERR_TIMEOUT.
+__device__ __forceinline__ bool grid_sync(GridBar *b, unsigned expect, long long spin) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    volatile unsigned *vgen = &b->gen;
+    const unsigned g0 = *vgen;
+    __threadfence();
+    if (atomicAdd(&b->count, 1u) + 1u == expect) {
+      atomicExch(&b->count, 0u);
+      __threadfence();
+      atomicAdd(&b->gen, 1u);
+    } else {
+      const long long t0 = clock64();
+      while (*vgen == g0) {
+        if (clock64() - t0 > spin) {
+          atomicOr(&b->err, 1u);
+          break;
+        }
+        __nanosleep(32);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return *(volatile unsigned *)&b->err == 0;
+}
+
+// A whole RK stage of a Work (one region or a batch) in one launch: the
+// gradient pass over every cell tile, the WENO-XYZ pass (RECONST 2), the
+// time-step finalisation (stage 1 of a step), the interior and boundary face
+// passes, the gather + update, and for a coupled batch the halo exchange,
+// separated by grid-wide barriers.  The per-tile work is the device code the
+// one-pass-per-launch kernels run.  Arrays one phase writes and a later one
+// gathers through the read-only path (gradients, face fluxes) are first read
+// after the barrier that follows their writes, so no stale copy can be cached;
+// scalars and halo sources are read through L2.
+#ifndef RF_COOP_MINB
+#define RF_COOP_MINB 6  // resident blocks per SM requested for the persistent stage kernel
+#endif
+template <typename R, int SPLIT>
+__global__ void __launch_bounds__(128, (sizeof(R) == 4) ? RF_COOP_MINB : 4)
+    k_stage_coop(const RegionDev<R> *__restrict__ regs, Work w, StepArgs a, int grad, int weno) {
+  __shared__ unsigned long long smin[32];
+  const unsigned expect = gridDim.x + (unsigned)w.barExtra;
+  GridBar *bar = w.bar;
+  const long long spin = w.barSpin;
+  if (grad) {
+    for (int t = blockIdx.x; t < w.nCellTiles; t += gridDim.x) {
+      if (a.fuseDt)
+        grad_tile<R, 1>(regs, w.cellTiles, t, smin);
+      else
+        grad_tile<R, 0>(regs, w.cellTiles, t, smin);
+    }
+    if (!grid_sync(bar, expect, spin)) return;
+    if (weno) {
+      for (int t = blockIdx.x; t < w.nCellTiles; t += gridDim.x) weno_tile<R>(regs, w.cellTiles, t);
+      if (!grid_sync(bar, expect, spin)) return;
+    }
+    if (a.fuseDt) {
+      if (blockIdx.x == 0) dt_finalize_block<R>(regs, w, a.dt, smin);
+      if (!grid_sync(bar, expect, spin)) return;
+    }
+  }
+  for (int t = blockIdx.x; t < w.nFaceTiles; t += gridDim.x)
+    face_tile<R, 128, 1>(regs, w.faceTiles, w.nFaceTiles, t, gridDim.x);
+  for (int t = blockIdx.x; t < w.nBFaceTiles; t += gridDim.x) bface_tile<R>(regs, w.bfaceTiles, t);
+  if (!grid_sync(bar, expect, spin)) return;
+  for (int t = blockIdx.x; t < w.nCellTiles; t += gridDim.x)
+    update_tile<R, SPLIT>(regs, w.cellTiles, w.nCellTiles, t, a, gridDim.x);
+  if (w.nHalo > 0 && a.update) {
+    if (!grid_sync(bar, expect, spin)) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.nHalo; i += gridDim.x * blockDim.x) {
+      const HaloLink l = w.halo[i];
+      halo_cell(regs[l.srcRegion], l.srcCell, regs[l.dstRegion], l.dstCell);
+    }
+  }
+}
+
+template <typename R, int SPLIT>
+void coop_launch(const RegionDev<R> *regs, const Work &w, const StepArgs &a, int grad, int weno,
+                 cudaStream_t s) {
+  static const int resident = resident_blocks(k_stage_coop<R, SPLIT>, 128);
+  int grid = w.nCellTiles > w.nFaceTiles ? w.nCellTiles : w.nFaceTiles;
+  if (w.nBFaceTiles > grid) grid = w.nBFaceTiles;
+  if (w.grid > 0 && w.grid < grid) grid = w.grid;
+  if (grid > resident) grid = resident;
+  if (grid < 1) grid = 1;
+  cudaMemsetAsync(w.bar, 0, 2 * sizeof(unsigned), s);  // count and generation; err stays
+  Work wc = w;
+  StepArgs ac = a;
+  void *args[] = {(void *)&regs, (void *)&wc, (void *)&ac, (void *)&grad, (void *)&weno};
+  cudaLaunchCooperativeKernel((const void *)k_stage_coop<R, SPLIT>, dim3(grid), dim3(128), args, 0,
+                              s);
+}
+
 template <typename R>
 void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cudaStream_t s,
                   long long *launches, int spaceOrder, int reconst, const Prof *prof,
                   int parts) {
+  if (w.coop && parts == SP_ALL && w.bar) {
+    const int grad = spaceOrder > 1 && w.nCellTiles > 0;
+    const int weno = grad && reconst == 2;
+    RF_MARK(KP_STAGE, 0);
+    if (sizeof(R) == 4 && w.split)
+      coop_launch<R, 1>(regs, w, a, grad, weno, s);
+    else
+      coop_launch<R, 0>(regs, w, a, grad, weno, s);
+    RF_MARK(KP_STAGE, 1);
+    if (launches) *launches += 1;
+    return;
+  }
   auto gsz = [&](int nt) { return w.grid > 0 && w.grid < nt ? w.grid : nt; };
   long long n = 0;
   const bool hasGrad = spaceOrder > 1 && w.nCellTiles > 0;
@@ -2537,14 +2722,14 @@ void launch_step(const RegionDev<R> *regs, const Work &w, const DtArgs &da, int 
 // or boundary (the result does not depend on the face order).  Regions that
 // do not use RECONST 2 skip their tiles.
 template <typename R>
-__global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict__ regs,
-                                                  const Tile *__restrict__ tiles, int nTiles) {
-  RF_TILE_LOOP(tiles, nTiles) {
+__device__ __forceinline__ void weno_tile(const RegionDev<R> *__restrict__ regs,
+                                          const Tile *__restrict__ tiles, int t_) {
+  {
     const Tile tl = tiles[t_];
     const RegionDev<R> &g = regs[tl.region];
-    if (!g.gradRaw) continue;
+    if (!g.gradRaw) return;
     const int c = tl.first + threadIdx.x;
-    if (c >= g.nCells) continue;
+    if (c >= g.nCells) return;
     const R eps = R(1.0E-15);
     // the weight 1/(g^2 + 1e-15): IEEE division on the FP64 path; on the
     // mixed path optionally the hardware reciprocal (it only weights an average)
@@ -2643,7 +2828,7 @@ __global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict
         }
       }
       st16(g.grad + 16 * (size_t)c, out);
-      continue;
+      return;
     }
     const long long T = g.cfTotal;
     const long long e0 = g.cfOff[c >> 5] + (c & 31);
@@ -2674,6 +2859,12 @@ __global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict
     }
     st16(g.grad + 16 * (size_t)c, out);
   }
+}
+
+template <typename R>
+__global__ void __launch_bounds__(128) k_weno_xyz(const RegionDev<R> *__restrict__ regs,
+                                                  const Tile *__restrict__ tiles, int nTiles) {
+  RF_TILE_LOOP(tiles, nTiles) weno_tile<R>(regs, tiles, t_);
 }
 
 template <typename R>

@@ -72,7 +72,8 @@ class RegionDescT(C.Structure):
 class TuningT(C.Structure):
     """rfgpu_tuning_t: launch shapes of the stage passes (0 = default)."""
     _fields_ = [("gridCap", C.c_int), ("gradBlock", C.c_int), ("faceBlock", C.c_int),
-                ("facesPerThread", C.c_int), ("cellBlock", C.c_int)]
+                ("facesPerThread", C.c_int), ("cellBlock", C.c_int),
+                ("persistentStage", C.c_int)]
 
 
 TUNING_KEYS = [f for f, _ in TuningT._fields_]
@@ -103,6 +104,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
            "rfgpu_timer_start", "rfgpu_timer_stop", "rfgpu_batch_timer_start",
            "rfgpu_batch_timer_stop", "rfgpu_set_device", "rfgpu_host_alloc", "rfgpu_host_free",
            "rfgpu_mem_info", "rfgpu_sm_count", "rfgpu_residual_noalloc", "rfgpu_batch_set_tuning",
+           "rfgpu_batch_test_barrier",
            "rfgpu_mesh_stencils", "rfgpu_border_copy", "rfgpu_border_pack",
            "rfgpu_border_unpack", "rfgpu_batch_create_ex", "rfgpu_mesh_build",
            "rfgpu_mesh_sizes", "rfgpu_mesh_faces", "rfgpu_mesh_cells", "rfgpu_mesh_patch",
@@ -111,7 +113,7 @@ SYMBOLS = ["rfgpu_region_create", "rfgpu_region_destroy", "rfgpu_stage", "rfgpu_
 BATCH_COUPLED = 1
 
 KERNELS = ["gradient", "weno_xyz", "face_flux", "bface_flux", "gather_update", "dt_face",
-           "dt_bface", "dt_cell", "dt_finalize", "halo"]
+           "dt_bface", "dt_cell", "dt_finalize", "halo", "stage_persistent"]
 
 _lib = None
 
@@ -166,6 +168,7 @@ def load(path: Optional[str] = None):
         "rfgpu_sm_count": ([ip], C.c_int),
         "rfgpu_residual_noalloc": ([vp, dp], C.c_int),
         "rfgpu_batch_set_tuning": ([vp, C.POINTER(TuningT)], C.c_int),
+        "rfgpu_batch_test_barrier": ([vp, C.c_int, C.c_longlong], C.c_int),
         "rfgpu_mesh_stencils": ([C.c_int, C.c_int, ip, ip, ip, ip, dp, ip, ip, dp], C.c_int),
         "rfgpu_border_copy": ([vp, C.c_int, vp], C.c_int),
         "rfgpu_border_pack": ([vp, C.c_int, dp], C.c_int),
@@ -616,6 +619,12 @@ class Batch:
     def set_tuning(self, **kw):
         t = _tuning(**kw)
         _check(self.lib.rfgpu_batch_set_tuning(self.h, C.byref(t)), "rfgpu_batch_set_tuning")
+
+    def test_barrier(self, extra: int, spin_cycles: int = 0):
+        """rfgpu_batch_test_barrier: make the persistent stage's grid-wide
+        barrier wait for `extra` blocks that never arrive (0 restores)."""
+        _check(self.lib.rfgpu_batch_test_barrier(self.h, extra, spin_cycles),
+               "rfgpu_batch_test_barrier")
 
     def set_grid_cap(self, blocks: int):
         self.set_tuning(gridCap=blocks)
