@@ -92,7 +92,7 @@ def test_region_autotuner_keeps_a_valid_shape():
     r.set_time(0.0)
     t = autotune.tune_region(r, cfl, dti, steps=1, grid_caps=[0, 2 * autotune.sm_count()])
     assert t["shape"]["gradBlock"] in (0, 64, 128, 256)   # 0: the persistent stage won
-    assert t["shape"]["facesPerThread"] in (1, 2)
+    assert t["shape"]["facesPerThread"] in (0, 1, 2)
     assert t["sms"] == E.sm_count() > 0
     r.step(cfl, dti)
     assert r.status() == 0
