@@ -71,6 +71,14 @@ def _load():
         lib.orc_residual.argtypes = [R, dp, dp, dp, dp]
         lib.orc_dt.argtypes = [R, dp, dp, C.c_double, C.c_double, C.c_double, C.c_double]
         lib.orc_dt.restype = C.c_double
+        lib.orc_omp_plan_create.argtypes = [R]
+        lib.orc_omp_plan_create.restype = C.c_void_p
+        lib.orc_omp_plan_destroy.argtypes = [C.c_void_p]
+        lib.orc_rk_stage_omp_plan.argtypes = [R, C.c_void_p, C.c_int, C.c_double] + [dp] * 6 + [C.c_int]
+        lib.orc_rk_stage_omp_plan.restype = C.c_int
+        lib.orc_dt_omp.argtypes = [R, C.c_void_p, dp, dp, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_int]
+        lib.orc_dt_omp.restype = C.c_double
         lib.orc_set_dv.argtypes = [R, dp, dp]
         lib.orc_set_dv_range.argtypes = [R, dp, dp, C.c_long, C.c_long]
         lib.orc_face_flux.argtypes = [R, dp, dp, dp, dp]
@@ -147,13 +155,27 @@ class Oracle:
         self.rhsSum = np.zeros((n, 5))
         self.grad = np.zeros((n, 5, 3))
 
+    def _omp_plan(self):
+        """The OpenMP path's cell -> face lists, built on first use."""
+        if getattr(self, "_plan", None) is None:
+            self._plan = self.lib.orc_omp_plan_create(C.byref(self.reg))
+        return self._plan
+
+    def __del__(self):
+        plan = getattr(self, "_plan", None)
+        if plan is not None:
+            self.lib.orc_omp_plan_destroy(plan)
+            self._plan = None
+
     def stage(self, cv, dv, istage, dtMin, threads: int = 0) -> int:
-        """One RK stage in place on cv, dv (C-contiguous float64)."""
-        args = (C.byref(self.reg), istage, dtMin, _dp(cv), _dp(dv), _dp(self.cvOld),
-                _dp(self.rhs), _dp(self.rhsSum), _dp(self.grad))
+        """One RK stage in place on cv, dv (C-contiguous float64); threads > 0
+        runs the OpenMP form (bit-identical)."""
+        bufs = (_dp(cv), _dp(dv), _dp(self.cvOld), _dp(self.rhs), _dp(self.rhsSum),
+                _dp(self.grad))
         if threads:
-            return self.lib.orc_rk_stage_omp(*args, threads)
-        return self.lib.orc_rk_stage(*args)
+            return self.lib.orc_rk_stage_omp_plan(C.byref(self.reg), self._omp_plan(), istage,
+                                                  dtMin, *bufs, threads)
+        return self.lib.orc_rk_stage(C.byref(self.reg), istage, dtMin, *bufs)
 
     def residual(self, cv, dv):
         rhs = np.zeros((self.nCells, 5))
@@ -162,7 +184,10 @@ class Oracle:
                               _dp(np.ascontiguousarray(dv)), _dp(rhs), _dp(grad))
         return rhs, grad
 
-    def dt(self, cv, dv, cfl, dtImposed, dtMinLimit=0.0, currentTime=1.0):
+    def dt(self, cv, dv, cfl, dtImposed, dtMinLimit=0.0, currentTime=1.0, threads: int = 0):
+        if threads:
+            return self.lib.orc_dt_omp(C.byref(self.reg), self._omp_plan(), _dp(cv), _dp(dv),
+                                       cfl, dtImposed, dtMinLimit, currentTime, threads)
         return self.lib.orc_dt(C.byref(self.reg), _dp(cv), _dp(dv), cfl, dtImposed, dtMinLimit,
                                currentTime)
 
@@ -195,7 +220,7 @@ class Oracle:
                 break
             if t_end is not None and t >= t_end:
                 break
-            dtm = self.dt(cv, dv, self.num.cfl, dt_imposed, 0.0, t)
+            dtm = self.dt(cv, dv, self.num.cfl, dt_imposed, 0.0, t, threads)
             finished = False
             if t_end is not None and t + dtm > t_end:  # RFLU_TimeStepping.F90:490-493
                 dtm = t_end - t

@@ -1055,14 +1055,76 @@ void orc_residual(const orc_region_t *r, const double *cv, const double *dv, dou
   convective_fluxes(r, q.data(), dv, grad, rhs);
 }
 
-int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv, double *dv,
-                     double *cvOld, double *rhs, double *rhsSum, double *grad, int nThreads) {
+// Cell -> face lists of the OpenMP stage and time step, built once per
+// region: for every cell its signed interior faces ascending (+(f+1) where the
+// cell is f2c(1,f), -(f+1) where it is f2c(2,f)), then its boundary faces
+// patch by patch (nF + 1 + the face's index over all patches).  That is the
+// order in which the serial face loops add into the cell.
+// The plan also holds the stage's scratch (face fluxes, limiter values), so
+// that repeated stages neither allocate nor first-touch them again.
+struct orc_omp_plan_s {
+  long nF = 0, nT = 0;
+  std::vector<long> off, lst, poff;
+  std::vector<double> ff, bf, lim;
+  std::vector<char> bm;
+};
+
+orc_omp_plan_t orc_omp_plan_create(const orc_region_t *r) {
+  auto *pl = new orc_omp_plan_s;
+  const long nF = r->nFaces, nT = n_tot(r);
+  pl->nF = nF;
+  pl->nT = nT;
+  pl->poff.assign(r->nPatches + 1, 0);
+  for (int ip = 0; ip < r->nPatches; ++ip) pl->poff[ip + 1] = pl->poff[ip] + r->patches[ip].nBFaces;
+  std::vector<long> &off = pl->off;
+  off.assign(nT + 1, 0);
+  for (long f = 0; f < nF; ++f) {
+    off[r->f2c[2 * f]]++;
+    off[r->f2c[2 * f + 1]]++;
+  }
+  for (int ip = 0; ip < r->nPatches; ++ip)
+    for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl) off[r->patches[ip].bf2c[ifl]]++;
+  for (long i = 0; i < nT; ++i) off[i + 1] += off[i];
+  pl->lst.resize(off[nT]);
+  std::vector<long> fill(off.begin(), off.end() - 1);
+  for (long f = 0; f < nF; ++f) {
+    pl->lst[fill[r->f2c[2 * f] - 1]++] = f + 1;
+    pl->lst[fill[r->f2c[2 * f + 1] - 1]++] = -(f + 1);
+  }
+  for (int ip = 0; ip < r->nPatches; ++ip)
+    for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl)
+      pl->lst[fill[r->patches[ip].bf2c[ifl] - 1]++] = nF + 1 + pl->poff[ip] + ifl;
+  pl->ff.resize(5 * nF);
+  pl->bf.resize(5 * pl->poff[r->nPatches]);
+  pl->bm.resize(pl->poff[r->nPatches]);
+  pl->lim.resize(5 * nT);
+  return pl;
+}
+
+void orc_omp_plan_destroy(orc_omp_plan_t pl) { delete pl; }
+
+static void set_threads(int nThreads) {
 #ifdef _OPENMP
   if (nThreads > 0) omp_set_num_threads(nThreads);
 #else
   (void)nThreads;
 #endif
+}
+
+int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv, double *dv,
+                     double *cvOld, double *rhs, double *rhsSum, double *grad, int nThreads) {
+  orc_omp_plan_t pl = orc_omp_plan_create(r);
+  const int st = orc_rk_stage_omp_plan(r, pl, istage, dtMin, cv, dv, cvOld, rhs, rhsSum, grad, nThreads);
+  orc_omp_plan_destroy(pl);
+  return st;
+}
+
+int orc_rk_stage_omp_plan(const orc_region_t *r, orc_omp_plan_t pl, int istage, double dtMin,
+                          double *cv, double *dv, double *cvOld, double *rhs, double *rhsSum,
+                          double *grad, int nThreads) {
+  set_threads(nThreads);
   const long nC = r->nCells, nF = r->nFaces, nT = n_tot(r);
+  const std::vector<long> &off = pl->off, &lst = pl->lst, &poff = pl->poff;
   double ark[5], grk[5];
   int nSteps;
   rk_coeffs(r->rkScheme, ark, grk, &nSteps);
@@ -1078,25 +1140,15 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
     if (r->reconst == RECONST_LIM_VENKAT) {
       // per-cell gather form of the limiter: min/max and min over the cell's
       // interior faces are order independent, so this equals the face loop
-      std::vector<long> off(nT + 1, 0), lst(2 * nF);
-      for (long f = 0; f < nF; ++f) {
-        off[r->f2c[2 * f]]++;
-        off[r->f2c[2 * f + 1]]++;
-      }
-      for (long i = 0; i < nT; ++i) off[i + 1] += off[i];
-      std::vector<long> fill(off.begin(), off.end() - 1);
-      for (long f = 0; f < nF; ++f) {
-        lst[fill[r->f2c[2 * f] - 1]++] = f;
-        lst[fill[r->f2c[2 * f + 1] - 1]++] = f;
-      }
       const double THRD = 1.0 / 3.0;
-      std::vector<double> lim(5 * nT);
+      std::vector<double> &lim = pl->lim;
 #pragma omp parallel for schedule(static, 256)
       for (long c = 0; c < nT; ++c) {
         double vmin[5], vmax[5];
         for (int v = 0; v < 5; ++v) vmin[v] = vmax[v] = cv[5 * c + v];
         for (long e = off[c]; e < off[c + 1]; ++e) {
-          long f = lst[e];
+          if (lst[e] > nF) continue;  // boundary faces come last
+          long f = (lst[e] > 0 ? lst[e] : -lst[e]) - 1;
           long o = (r->f2c[2 * f] - 1 == c) ? r->f2c[2 * f + 1] - 1 : r->f2c[2 * f] - 1;
           for (int v = 0; v < 5; ++v) {
             vmin[v] = fmin_f(vmin[v], cv[5 * o + v]);
@@ -1107,7 +1159,8 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
         double epsq = ds * ds * ds;
         double l[5] = {1.0, 1.0, 1.0, 1.0, 1.0};
         for (long e = off[c]; e < off[c + 1]; ++e) {
-          long f = lst[e];
+          if (lst[e] > nF) continue;
+          long f = (lst[e] > 0 ? lst[e] : -lst[e]) - 1;
           const double *fcx = r->fc + 3 * f;
           double dx = r->cofg[3 * c] - fcx[0], dy = r->cofg[3 * c + 1] - fcx[1],
                  dz = r->cofg[3 * c + 2] - fcx[2];
@@ -1136,14 +1189,12 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
     for (long i = 0; i < nT; ++i) prim2cons(r, cv, dv, i, i + 1);
   }
   // face fluxes, then per-cell gather in reference order
-  std::vector<double> ff(5 * nF);
+  std::vector<double> &ff = pl->ff;
   Ctx ctx{r, cv, dv, grad};
 #pragma omp parallel for schedule(static, 1024)
   for (long f = 0; f < nF; ++f) interior_flux(ctx, (int)f, &ff[5 * f]);
-  std::vector<long> poff(r->nPatches + 1, 0);
-  for (int ip = 0; ip < r->nPatches; ++ip) poff[ip + 1] = poff[ip] + r->patches[ip].nBFaces;
-  std::vector<double> bf(5 * poff[r->nPatches]);
-  std::vector<char> bm(poff[r->nPatches]);
+  std::vector<double> &bf = pl->bf;
+  std::vector<char> &bm = pl->bm;
   for (int ip = 0; ip < r->nPatches; ++ip) {
 #pragma omp parallel for schedule(static, 1024)
     for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl) {
@@ -1152,27 +1203,7 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
       bm[poff[ip] + ifl] = hm;
     }
   }
-  // c2f in reference accumulation order: signed interior faces ascending,
-  // then boundary faces by patch
-  std::vector<long> off(nT + 1, 0);
-  for (long f = 0; f < nF; ++f) {
-    off[r->f2c[2 * f]]++;
-    off[r->f2c[2 * f + 1]]++;
-  }
-  for (int ip = 0; ip < r->nPatches; ++ip)
-    for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl) off[r->patches[ip].bf2c[ifl]]++;
-  for (long i = 0; i < nT; ++i) off[i + 1] += off[i];
-  std::vector<long> lst(off[nT]);
-  {
-    std::vector<long> fill(off.begin(), off.end() - 1);
-    for (long f = 0; f < nF; ++f) {
-      lst[fill[r->f2c[2 * f] - 1]++] = f + 1;
-      lst[fill[r->f2c[2 * f + 1] - 1]++] = -(f + 1);
-    }
-    for (int ip = 0; ip < r->nPatches; ++ip)
-      for (int ifl = 0; ifl < r->patches[ip].nBFaces; ++ifl)
-        lst[fill[r->patches[ip].bf2c[ifl] - 1]++] = nF + 1 + poff[ip] + ifl;
-  }
+  // per-cell gather over the plan's lists: the reference's accumulation order
   double fac = ark[istage - 1] * dtMin;
   double gc = R_M(r->gvMol), g = G_CpR(r->gvCp, gc);
   int st = 0;
@@ -1206,6 +1237,9 @@ int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv
   }
   return st;
 }
+
+static double minimum_time_step(double dtMin, double cfl, double dtImposed, double dtMinLimit,
+                                double currentTime);
 
 double orc_dt(const orc_region_t *r, const double *cv, const double *dv, double cfl,
               double dtImposed, double dtMinLimit, double currentTime) {
@@ -1243,6 +1277,81 @@ double orc_dt(const orc_region_t *r, const double *cv, const double *dv, double 
     dt[c] = r->vol[c] / dt[c];
     if (c == 0 || dt[c] < dtMin) dtMin = dt[c];
   }
+  return minimum_time_step(dtMin, cfl, dtImposed, dtMinLimit, currentTime);
+}
+
+// rocflu/RFLU_TimeStepInviscid.F90 over the OpenMP plan: the spectral radius
+// of every face in parallel, then each cell's sum in the serial loops' order
+// (interior faces ascending, then patches), so dt equals orc_dt bit for bit.
+double orc_dt_omp(const orc_region_t *r, orc_omp_plan_t pl, const double *cv, const double *dv,
+                  double cfl, double dtImposed, double dtMinLimit, double currentTime,
+                  int nThreads) {
+  set_threads(nThreads);
+  const long nC = r->nCells, nF = r->nFaces;
+  const std::vector<long> &off = pl->off, &lst = pl->lst, &poff = pl->poff;
+  const double fsu = 0.0;
+  std::vector<double> sr(nF + poff[r->nPatches]);
+#pragma omp parallel for schedule(static, 1024)
+  for (long f = 0; f < nF; ++f) {
+    long c1 = r->f2c[2 * f] - 1, c2 = r->f2c[2 * f + 1] - 1;
+    const double *n = r->fn + 4 * f;
+    double ir1 = 1.0 / cv[5 * c1], ir2 = 1.0 / cv[5 * c2];
+    double u1 = cv[5 * c1 + 1] * ir1, v1 = cv[5 * c1 + 2] * ir1, w1 = cv[5 * c1 + 3] * ir1;
+    double a1 = dv[3 * c1 + 2];
+    double u2 = cv[5 * c2 + 1] * ir2, v2 = cv[5 * c2 + 2] * ir2, w2 = cv[5 * c2 + 3] * ir2;
+    double a2 = dv[3 * c2 + 2];
+    double vc = 0.5 * ((u1 + u2) * n[0] + (v1 + v2) * n[1] + (w1 + w2) * n[2]);
+    double as = 0.5 * (a1 + a2);
+    sr[f] = (std::fabs(vc - fsu) + as) * n[3];
+  }
+  for (int ip = 0; ip < r->nPatches; ++ip) {
+    const orc_patch_t &p = r->patches[ip];
+#pragma omp parallel for schedule(static, 1024)
+    for (int ifl = 0; ifl < p.nBFaces; ++ifl) {
+      long c1 = p.bf2c[ifl] - 1;
+      const double *n = p.fn + 4 * (size_t)ifl;
+      double ir1 = 1.0 / cv[5 * c1];
+      double u1 = cv[5 * c1 + 1] * ir1, v1 = cv[5 * c1 + 2] * ir1, w1 = cv[5 * c1 + 3] * ir1;
+      double a1 = dv[3 * c1 + 2];
+      double vc = u1 * n[0] + v1 * n[1] + w1 * n[2];
+      sr[nF + poff[ip] + ifl] = (std::fabs(vc - fsu) + a1) * n[3];
+    }
+  }
+  // the serial minimum starts from cell 1 and skips NaN after it
+  double first = 0.0, dtMin = 0.0;
+  bool any = false;
+#pragma omp parallel
+  {
+    double m = 0.0;
+    bool have = false;
+#pragma omp for schedule(static, 1024)
+    for (long c = 0; c < nC; ++c) {
+      double acc = 0.0;
+      for (long e = off[c]; e < off[c + 1]; ++e) {
+        const long t = lst[e];
+        acc = acc + sr[t > nF ? t - 1 : (t > 0 ? t : -t) - 1];
+      }
+      const double d = r->vol[c] / acc;
+      if (c == 0) first = d;
+      if (!have || d < m) {
+        if (!std::isnan(d)) {
+          m = d;
+          have = true;
+        }
+      }
+    }
+#pragma omp critical
+    if (have && (!any || m < dtMin)) {
+      dtMin = m;
+      any = true;
+    }
+  }
+  if (nC > 0 && (std::isnan(first) || !any)) dtMin = first;
+  return minimum_time_step(dtMin, cfl, dtImposed, dtMinLimit, currentTime);
+}
+
+static double minimum_time_step(double dtMin, double cfl, double dtImposed, double dtMinLimit,
+                                double currentTime) {
   // rocflu/RFLU_MinimumTimeStep.F90:131-146,235-241
   dtMin = cfl * dtMin;
   double wtdtImposed = 0.0, wtdtComputed = 0.0;

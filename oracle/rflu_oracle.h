@@ -112,6 +112,19 @@ void orc_residual(const orc_region_t *r, const double *cv, const double *dv, dou
 int orc_rk_stage_omp(const orc_region_t *r, int istage, double dtMin, double *cv, double *dv,
                      double *cvOld, double *rhs, double *rhsSum, double *grad, int nThreads);
 
+/* The OpenMP stage's and time step's cell -> face lists, built once per
+ * region (orc_rk_stage_omp builds and frees them on every call). */
+typedef struct orc_omp_plan_s *orc_omp_plan_t;
+orc_omp_plan_t orc_omp_plan_create(const orc_region_t *r);
+void orc_omp_plan_destroy(orc_omp_plan_t plan);
+int orc_rk_stage_omp_plan(const orc_region_t *r, orc_omp_plan_t plan, int istage, double dtMin,
+                          double *cv, double *dv, double *cvOld, double *rhs, double *rhsSum,
+                          double *grad, int nThreads);
+/* orc_dt with OpenMP over faces and cells; bit-identical to orc_dt. */
+double orc_dt_omp(const orc_region_t *r, orc_omp_plan_t plan, const double *cv, const double *dv,
+                  double cfl, double dtImposed, double dtMinLimit, double currentTime,
+                  int nThreads);
+
 /* RFLU_TimeStepInviscid + RFLU_MinimumTimeStep for one region. */
 double orc_dt(const orc_region_t *r, const double *cv, const double *dv, double cfl,
               double dtImposed, double dtMinLimit, double currentTime);

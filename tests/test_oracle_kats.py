@@ -133,6 +133,24 @@ def test_openmp_gather_equals_serial_scatter(scheme, reconst):
     assert np.array_equal(cva, cvb) and np.array_equal(dva, dvb)
 
 
+def test_openmp_time_step_equals_serial():
+    """orc_dt_omp (faces in parallel, then each cell's sum in the serial loops'
+    order) equals orc_dt bit for bit, on the imposed and computed branches,
+    on a mixed mesh with every patch, and where cell 1's time step is NaN (the
+    serial minimum keeps it) or a later cell's is (the minimum skips it)."""
+    for c in (K.tet_shock_box(5, seed=3, numerics=K.Numerics(venkatGuard=1)), K.mixed_box(5)):
+        o = Oracle(c)
+        cv, dv = c.cv.copy(), c.dv.copy()
+        for args in ((c.numerics.cfl, 1.0, 0.0, 1.0), (c.numerics.cfl, 1e-3, 0.0, 0.0),
+                     (0.3, 2e-6, 1e-9, 0.5)):
+            assert o.dt(cv, dv, *args) == o.dt(cv, dv, *args, threads=3)
+        for bad in (0, c.mesh.nCells // 2):
+            cvn, dvn = cv.copy(), dv.copy()
+            dvn[bad, 2] = np.nan
+            a, b = o.dt(cvn, dvn, 0.5, 1.0, 0.0, 1.0), o.dt(cvn, dvn, 0.5, 1.0, 0.0, 1.0, threads=4)
+            assert (np.isnan(a) and np.isnan(b)) or a == b, (bad, a, b)
+
+
 def test_eos_numpy_matches_oracle():
     c = K.tet_shock_box(3, seed=2)
     assert np.array_equal(K.eos_dv(c.numerics, c.cv), Oracle(c).set_dv(c.cv))
