@@ -155,3 +155,51 @@ def test_cpp_caller_runs_the_time_step_loop(tmp_path, scheme):
     assert int(flags) == st_o == 0
     assert float(t) == t_o
     assert np.array_equal(cvg, cv) and np.array_equal(dvg, dv)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [K.PREC_MIXED, K.PREC_SPLIT], ids=["mixed", "split"])
+def test_cpp_caller_reduced_precision(tmp_path, prec):
+    """The compiled caller on the reduced-precision paths: the same calls
+    (rfgpu_dt, rfgpu_stage per stage, rfgpu_download) made through the Python
+    front end give the same state bit for bit, and it stays within 1e-5 of the
+    FP64 oracle in the reference's L1 sense."""
+    from oracle.oracle import Oracle
+    lib = _build.build_gpu()
+    hdr = tmp_path / "layout_expect.h"
+    layout_header(hdr)
+    exe = tmp_path / "rfgpu_abi_smoke"
+    r = subprocess.run(["g++", "-std=c++17", "-O2", f"-I{ROOT}/include", f'-DRFGPU_LAYOUT_H="{hdr}"',
+                        SRC, "-o", str(exe), f"-L{lib.parent}", "-lrfgpu",
+                        f"-Wl,-rpath,{lib.parent}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    c = K.tet_shock_box(6, seed=9, numerics=K.Numerics(spaceDiscr=K.DISCR_UPW_HLLC, venkatGuard=1,
+                                                       precision=prec))
+    n_steps = 3
+    _write_case(c, tmp_path, n_steps)
+    r = subprocess.run([str(exe), str(tmp_path)], capture_output=True, text=True, timeout=300)
+    assert r.returncode == 0, r.stderr
+    flags, t = (tmp_path / "out.txt").read_text().split()
+    cvg = np.fromfile(tmp_path / "out_cv.f64").reshape(-1, 5)
+    dvg = np.fromfile(tmp_path / "out_dv.f64").reshape(-1, 3)
+    # the caller registers in the locality order; so does this region
+    reg = E.Region(c, cell_order=E.ORDER_LOCALITY)
+    cfl = c.numerics.cfl
+    dti = reg.time_step(cfl, 1.0, 0.0, 1.0)
+    tp = 0.0
+    for _ in range(n_steps):
+        dtm = reg.time_step(cfl, dti, 0.0, tp)
+        for s in (1, 2, 3):
+            reg.rk_stage(s, dtm)
+        tp += dtm
+    cvp, dvp = reg.download()
+    assert int(flags) == reg.status() == 0
+    assert float(t) == tp
+    reg.close()
+    assert np.array_equal(cvg, cvp) and np.array_equal(dvg, dvp)
+    o = Oracle(c.with_numerics(precision=K.PREC_FP64))
+    cv, dv = c.cv.copy(), c.dv.copy()
+    dto = o.dt(cv, dv, cfl, 1.0, 0.0, 1.0)
+    o.run(cv, dv, n_steps=n_steps, dt_imposed=dto)
+    assert np.mean(np.abs(cvg[:, 0] / cv[:, 0] - 1.0)) <= 1e-5
+    assert np.mean(np.abs(dvg[:, 0] / dv[:, 0] - 1.0)) <= 1e-5
