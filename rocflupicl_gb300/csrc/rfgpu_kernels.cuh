@@ -446,39 +446,6 @@ __device__ __forceinline__ void st16(R *p, const R v[16]) {
   st8(p + 8, v + 8);
 }
 
-// ---- packed FP32 pairs (f32x2, sm_100 and later): two FP32 lanes per
-// instruction, a pair held in one 64-bit register (low half first) --------
-typedef unsigned long long f2x;
-__device__ __forceinline__ f2x f2_pack(float lo, float hi) {
-  f2x r;
-  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
-  return r;
-}
-__device__ __forceinline__ void f2_unpack(f2x a, float &lo, float &hi) {
-  asm("mov.b64 {%0, %1}, %2;" : "=f"(lo), "=f"(hi) : "l"(a));
-}
-__device__ __forceinline__ f2x f2_sub(f2x a, f2x b) {
-  f2x r;
-  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x f2_mul(f2x a, f2x b) {
-  f2x r;
-  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r) : "l"(a), "l"(b));
-  return r;
-}
-__device__ __forceinline__ f2x f2_fma(f2x a, f2x b, f2x c) {
-  f2x r;
-  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r) : "l"(a), "l"(b), "l"(c));
-  return r;
-}
-// a 32-byte record as four pairs, one 256-bit load
-__device__ __forceinline__ void ld4p(const float *__restrict__ p, f2x v[4]) {
-  asm("ld.global.nc.v4.b64 {%0,%1,%2,%3}, [%4];"
-      : "=l"(v[0]), "=l"(v[1]), "=l"(v[2]), "=l"(v[3])
-      : "l"(p));
-}
-
 // Cell-centre values the *_ComputeFlux2_TCP loops start from: rho, u = rhou *
 // (1/rho) with rhou the conserved momentum as CellGradientsMP's Prim2Cons
 // left it (rho * u_prim), p from dv.  On the mixed path the FP32 primitive
@@ -975,9 +942,6 @@ __device__ __forceinline__ double cell_dt(const RegionDev<R> &g, int c, const R 
 #ifndef RF_LIM_PRE
 #define RF_LIM_PRE 6
 #endif
-#ifndef RF_GRAD_PACKED
-#define RF_GRAD_PACKED 0
-#endif
 #ifndef RF_GRAD_UNROLL
 #define RF_GRAD_UNROLL 8
 #endif
@@ -1075,62 +1039,6 @@ __device__ __forceinline__ void grad_tile(const RegionDev<R> *__restrict__ regs,
         int nx[U];
 #pragma unroll
         for (int u = 0; u < U; ++u) nx[u] = u < n ? ld_index(sidx + u * kSlice) : 0;
-#if RF_GRAD_PACKED
-        // (measured on the 128^3 tet box and not kept: 1.948 against 1.831 ms,
-        // the pair packing costs more than the arithmetic it saves)
-        // The same sums on packed FP32 pairs: a record is four pairs (rho,u)
-        // (v,w) (p,x) (y,z), so four pair subtractions give the five variable
-        // differences and the three offsets, and each direction's five sums
-        // take two pair FMAs and one FMA (9 instead of 15 per member).
-        (void)member;
-        f2x q0[4];
-        ld4p(rec + 8 * (size_t)c, q0);
-        f2x A01[3] = {0ull, 0ull, 0ull}, A23[3] = {0ull, 0ull, 0ull};
-        float a4[3] = {0.f, 0.f, 0.f};
-        auto pmember = [&](const f2x p[4]) {
-          const f2x D0 = f2_sub(p[0], q0[0]), D1 = f2_sub(p[1], q0[1]);
-          const f2x D2 = f2_sub(p[2], q0[2]), D3 = f2_sub(p[3], q0[3]);
-          float dp, dx, sy, sz;
-          f2_unpack(D2, dp, dx);
-          f2_unpack(f2_mul(D3, D3), sy, sz);
-          float t = rsqrtf(dx * dx + sy + sz);
-          t = t * t;
-          float wy, wz;
-          f2_unpack(f2_mul(D3, f2_pack(t, t)), wy, wz);
-          const float w[3] = {t * dx, wy, wz};
-#pragma unroll
-          for (int d = 0; d < 3; ++d) {
-            const f2x W = f2_pack(w[d], w[d]);
-            A01[d] = f2_fma(W, D0, A01[d]);
-            A23[d] = f2_fma(W, D1, A23[d]);
-            a4[d] = fmaf(w[d], dp, a4[d]);
-          }
-        };
-        for (int k = 0; k < nFull; k += U) {
-          f2x ra[U][4];
-#pragma unroll
-          for (int u = 0; u < U; ++u) ld4p(rec + 8 * (size_t)nx[u], ra[u]);
-#pragma unroll
-          for (int u = 0; u < U; ++u)
-            nx[u] = k + U + u < n ? ld_index(sidx + (k + U + u) * kSlice) : 0;
-#pragma unroll
-          for (int u = 0; u < U; ++u) pmember(ra[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U - 1; ++u) {
-          if (nFull + u < n) {
-            f2x ra[4];
-            ld4p(rec + 8 * (size_t)nx[u], ra);
-            pmember(ra);
-          }
-        }
-#pragma unroll
-        for (int d = 0; d < 3; ++d) {
-          f2_unpack(A01[d], acc[d], acc[3 + d]);
-          f2_unpack(A23[d], acc[6 + d], acc[9 + d]);
-          acc[12 + d] = a4[d];
-        }
-#else
         for (int k = 0; k < nFull; k += U) {
           R ra[U][8];
 #pragma unroll
@@ -1149,7 +1057,6 @@ __device__ __forceinline__ void grad_tile(const RegionDev<R> *__restrict__ regs,
             member(ra);
           }
         }
-#endif
         const R axx = lds<RF_HINT_G>(g.cwt + c), axy = lds<RF_HINT_G>(g.cwt + N + c),
                 axz = lds<RF_HINT_G>(g.cwt + 2 * N + c);
         const R ayy = lds<RF_HINT_G>(g.cwt + 3 * N + c), ayz = lds<RF_HINT_G>(g.cwt + 4 * N + c),
