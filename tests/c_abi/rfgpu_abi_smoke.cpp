@@ -2,7 +2,7 @@
 // linked against librfgpu.so, standing in for the Fortran host of the
 // reference: it registers one region from arrays in the Fortran memory image
 // and drives the time-step loop the way rocflu/RFLU_TimeStepping.F90 and
-// libfloflu/RungeKuttaMP.F90 would after the edits of INTEGRATION.md
+// libfloflu/RungeKuttaMP.F90 would once their stage loop calls the C ABI
 // (rfgpu_dt, then rfgpu_stage for every RK stage, rfgpu_status, rfgpu_download,
 // rfgpu_region_destroy).
 //

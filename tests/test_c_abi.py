@@ -1,10 +1,10 @@
 """The C ABI seen from a compiled caller.
 
-The Fortran binding module of INTEGRATION.md declares BIND(C) derived types
-for the three structs of include/rfgpu.h; a BIND(C) type is laid out like the
+The Fortran binding module written out in the repository's integration notes
+declares BIND(C) derived types for the structs of include/rfgpu.h; a BIND(C) type is laid out like the
 C struct with the same fields in the same order.  The layout those Fortran
 types imply (C_INT 4 bytes, C_DOUBLE and C_PTR 8, each field at its natural
-alignment) is computed here from the text of INTEGRATION.md and checked three
+alignment) is computed here from the text of those notes and checked three
 ways: at compile time against the header (offsetof / sizeof static_asserts in
 a C++ translation unit that includes include/rfgpu.h, built with g++), and at
 run time against the Python front end's ctypes mirrors.  On a GPU the same
@@ -31,7 +31,7 @@ KINDS = {"INTEGER(C_INT)": 4, "REAL(C_DOUBLE)": 8, "TYPE(C_PTR)": 8}
 
 
 def bindc_types():
-    """{type name: [(field, size)]} from the BIND(C) types of INTEGRATION.md."""
+    """{type name: [(field, size)]} from the BIND(C) types of the integration notes."""
     txt = open(os.path.join(ROOT, "INTEGRATION.md")).read()
     out = {}
     for name, body in re.findall(r"TYPE, BIND\(C\) :: (\w+)\n(.*?)\n\s*END TYPE \1", txt, re.S):
