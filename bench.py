@@ -70,6 +70,9 @@ def parse():
                     help="requests per Poisson rate of the serving measurement (0 disables it)")
     ap.add_argument("--serve-rates", default="1,4,16", help="Poisson rates swept, requests/s")
     ap.add_argument("--serve-tend", type=float, default=2.0e-4, help="end time of each solve")
+    ap.add_argument("--configs", default="1,3,4",
+                    help="other workloads measured after the headline and reported in its line "
+                         "(1: Sod tube, 3: mixed-element residual, 4: 256 tubes; '' for none)")
     return ap.parse_args()
 
 
@@ -540,6 +543,21 @@ def main():
                "sample": f"1 RK3 step (dt + 3 stages, after 1 untimed step) of the same {m.nCells}-cell mesh, "
                          f"OpenMP C++ FP64 restatement of the reference path, {el:.1f} s"}
 
+    # ---- the other single-GPU workloads, reported in the same line (N = 1) ---
+    others = None
+    if a.configs and dist.world == 1:
+        from rocflupicl_gb300 import workloads as W
+        others = {}
+        for key in [k.strip() for k in a.configs.split(",") if k.strip()]:
+            if key == "1":
+                others["1"] = W.run_sod()
+            elif key == "3":
+                others["3"] = W.run_mixed_residual(repeats=1000)
+            elif key == "4":
+                o = W.run_tubes(steps=300)
+                o["autotune"] = {"shape": o.get("autotune", {}).get("shape")}
+                others["4"] = o
+
     if dist.rank == 0:
         cfg = workload_config(c, a)
         cfg["precision"] = H["precision"]
@@ -555,7 +573,8 @@ def main():
                 "modes": {md: {k: v for k, v in res[md].items()
                                if k not in ("ms_local", "dti", "kernels", "clocks")}
                           for md in modes},
-                "fp64": fp64, "device_bytes": H["device_bytes"], "serving": serving}
+                "fp64": fp64, "device_bytes": H["device_bytes"], "serving": serving,
+                "other_configs": others}
         print(json.dumps(line), flush=True)
     dist.close()
 
