@@ -51,7 +51,7 @@ def parse():
                     help="tet: the headline line; the others print their own measurement")
     ap.add_argument("--n", "--hexes", dest="n", type=int, default=128,
                     help="base hexes per direction")
-    ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+"])
+    ap.add_argument("--scheme", default="roe", choices=["roe", "hllc", "ausm+", "ausm+up"])
     ap.add_argument("--reconst", default="venkat", choices=["venkat", "weno-xyz", "none"],
                     help="RECONST 11 (the benchmark's), 2 (the reference's default) or 0")
     ap.add_argument("--cell-order", default="auto", choices=["auto", "locality", "host"],
@@ -76,7 +76,8 @@ def parse():
     return ap.parse_args()
 
 
-SCHEME = {"roe": K.DISCR_UPW_ROE, "hllc": K.DISCR_UPW_HLLC, "ausm+": K.DISCR_UPW_AUSMPLUS}
+SCHEME = {"roe": K.DISCR_UPW_ROE, "hllc": K.DISCR_UPW_HLLC, "ausm+": K.DISCR_UPW_AUSMPLUS,
+          "ausm+up": K.DISCR_UPW_AUSMPLUSUP}
 
 
 class Dist:
