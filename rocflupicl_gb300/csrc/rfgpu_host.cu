@@ -139,9 +139,10 @@ struct rfgpu_region_s {
   cudaStream_t xstream = nullptr;
   cudaEvent_t xev[9] = {};
   // rfgpu_step_host (mixed path): cell tiles grouped by transfer phase, made on
-  // first use; phOff[0] gradient phases over phGrad, phOff[1] update phases over phUpd
-  Tile *phGrad = nullptr, *phUpd = nullptr;
-  int phOff[2][9] = {};
+  // first use; phOff[0] gradient phases over phGrad, phOff[1] update phases over phUpd,
+  // phOff[2] the last stage's interior-face phases over phFace
+  Tile *phGrad = nullptr, *phUpd = nullptr, *phFace = nullptr;
+  int phOff[3][9] = {};
   int phN = 0;
   // mixed-path transfers: the device cells of each chunk in ascending device
   // order (xList[xOff[k] .. xOff[k+1])), so the conversions touch the device
@@ -996,6 +997,39 @@ int phase_setup(rfgpu_region_s *h) {
   h->phOff[0][nk] = h->phOff[1][nk] = nT;
   h->phGrad = h->mem.upload(grad, s);
   h->phUpd = h->mem.upload(upd, s);
+  // interior faces of the last stage by phase: a 128-face tile runs in the
+  // phase of the earliest update tile any of its faces feeds, so update phase
+  // k finds every face of its cells done (face phases 0..k run before it)
+  // (the region's own 128-face tiles, whatever face shape a tuning chose)
+  const int F = h->nFaces, nFT = (F + w.block - 1) / w.block;
+  std::vector<Tile> face;
+  if (nFT > 0) {
+    std::vector<int> f2c(2 * (size_t)F);
+    std::vector<Tile> ftiles(nFT);
+    if (cudaMemcpyAsync(f2c.data(), h->rd32.f2c, 2 * (size_t)F * 4, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(ftiles.data(), h->faceTiles, (size_t)nFT * sizeof(Tile),
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    std::vector<int> phase(nFT, nk - 1);
+    for (int t = 0; t < nFT; ++t) {
+      const int f0 = ftiles[t].first, f1 = std::min(F, f0 + w.block);
+      for (int f = f0; f < f1; ++f)
+        for (int j = 0; j < 2; ++j) {
+          const int c = f2c[(size_t)j * F + f];
+          phase[t] = std::min(phase[t], clampk(first[c / w.block]));
+        }
+    }
+    face.reserve(nFT);
+    for (int j = 0; j < nk; ++j) {
+      h->phOff[2][j] = (int)face.size();
+      for (int t = 0; t < nFT; ++t)
+        if (phase[t] == j) face.push_back(ftiles[t]);
+    }
+    h->phFace = h->mem.upload(face, s);
+  }
+  h->phOff[2][nk] = (int)face.size();
   if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
   h->phN = nk;
   return RFGPU_OK;
@@ -1049,11 +1083,19 @@ int step_host_mixed(rfgpu_region_s *h, double *cv, double *dv, const DtArgs &da)
   }
   for (int is = 1; is <= nS; ++is) {
     StepArgs sa{is, 1, 0.0, 0, 1, is == 1 ? 1 : 0, da};
-    const int parts = (is == 1 ? 0 : SP_GRADIENT) | SP_FLUX | (is == nS ? 0 : SP_UPDATE);
+    // the last stage runs its interior faces and its update phase by phase
+    const int parts = (is == 1 ? 0 : SP_GRADIENT) | SP_FLUX |
+                      (is == nS ? (h->phFace ? SP_NOFACE : 0) : SP_UPDATE);
     launch_stage<float>(regs, w, sa, s, &h->launches, h->spaceOrder, h->reconst, prof, parts);
     if (is < nS) continue;
-    // last update phase by phase, each chunk converted and copied back behind it
+    // last stage phase by phase: the faces the phase's update tiles need, the
+    // update, then each chunk converted and copied back behind it
     for (int k = 0; k < nk; ++k) {
+      const int nf = h->phFace ? h->phOff[2][k + 1] - h->phOff[2][k] : 0;
+      if (nf > 0) {
+        launch_face_tiles<float>(regs, w, h->phFace + h->phOff[2][k], nf, s);
+        h->launches++;
+      }
       const int n = h->phOff[1][k + 1] - h->phOff[1][k];
       if (n > 0) {
         launch_update_tiles<float>(regs, w, h->phUpd + h->phOff[1][k], n, sa, s);

@@ -199,7 +199,7 @@ struct StepArgs {
 // Parts of a stage, for a caller that launches some passes itself over subsets
 // of the cell tiles: the gradient pass; the time-step finalisation (when the
 // gradient pass reduces it) and the face passes; the update (and halo).
-enum { SP_GRADIENT = 1, SP_FLUX = 2, SP_UPDATE = 4, SP_ALL = 7 };
+enum { SP_GRADIENT = 1, SP_FLUX = 2, SP_UPDATE = 4, SP_ALL = 7, SP_NOFACE = 8 };
 
 // Host-state step (rfgpu_step_host): the host images move in chunks of cell
 // tiles, chunk k covering host cells [tEnd[k-1], tEnd[k]) * block.
@@ -278,6 +278,10 @@ void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tile
 template <typename R>
 void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                          const StepArgs &a, cudaStream_t s);
+// The interior-face pass over a list of 128-face tiles.
+template <typename R>
+void launch_face_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                       cudaStream_t s);
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
                long long *launches, const Prof *prof);

@@ -2577,7 +2577,7 @@ void launch_stage(const RegionDev<R> *regs, const Work &w, const StepArgs &a, cu
     RF_MARK(KP_DT_FINAL, 1);
     ++n;
   }
-  if (flux && w.nFaceTiles > 0) {
+  if (flux && !(parts & SP_NOFACE) && w.nFaceTiles > 0) {
     RF_MARK(KP_FACE_FLUX, 0);
     launch_faces_tuned<R>(regs, w, s);
     RF_MARK(KP_FACE_FLUX, 1);
@@ -2825,6 +2825,15 @@ void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tile
 }
 
 template <typename R>
+void launch_face_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                       cudaStream_t s) {
+  // the phase lists hold 128-face tiles, one face per thread
+  static const int pf = resident_blocks(k_face_flux<R, 128, 1>, 128);
+  const int grid = grid_for(w.grid, nTiles);
+  if (grid > 0) k_face_flux<R, 128, 1><<<grid, 128, 0, s>>>(regs, tiles, nTiles, pf);
+}
+
+template <typename R>
 void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                          const StepArgs &a, cudaStream_t s) {
   update_launch<R, 128>(regs, tiles, nTiles, w.grid, a, w.split, s);  // 128-cell phase tiles
@@ -3025,6 +3034,8 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
                                      int, cudaStream_t);                                      \
   template void launch_update_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int, \
                                        const StepArgs &, cudaStream_t);                       \
+  template void launch_face_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int,   \
+                                     cudaStream_t);                                           \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
                              long long *, const Prof *);                                      \
   template void launch_step<R>(const RegionDev<R> *, const Work &, const DtArgs &, int,       \
