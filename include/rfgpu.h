@@ -223,8 +223,8 @@ int rfgpu_upload(rfgpu_region_t h, const double *cv, const double *dv);
  * (3,nCells) is output only, or NULL.  Results equal rfgpu_upload(cv, NULL) +
  * rfgpu_step + rfgpu_download(cv, dv) bit for bit; on the mixed path at second
  * order the copies overlap the step (the first stage's gradient pass starts on
- * the cells whose neighbourhoods have arrived, the last stage's update hands
- * cells back as they finish).  Synchronous; pinned host memory lets the copies
+ * the cells whose neighbourhoods have arrived, the last stage runs in phases
+ * and hands cells back as they finish).  Synchronous; pinned host memory lets the copies
  * run at full rate.  Regions with borders: RFGPU_ERR_UNSUPPORTED. */
 int rfgpu_step_host(rfgpu_region_t h, double *cv, double *dv, double cfl, double dtImposed,
                     double dtMinLimit, double endTime);

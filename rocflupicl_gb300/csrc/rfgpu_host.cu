@@ -140,9 +140,11 @@ struct rfgpu_region_s {
   cudaEvent_t xev[9] = {};
   // rfgpu_step_host (mixed path): cell tiles grouped by transfer phase, made on
   // first use; phOff[0] gradient phases over phGrad, phOff[1] update phases over phUpd,
-  // phOff[2] the last stage's interior-face phases over phFace
-  Tile *phGrad = nullptr, *phUpd = nullptr, *phFace = nullptr;
-  int phOff[3][9] = {};
+  // phOff[2] the last stage's interior-face phases over phFace, phOff[3] its
+  // gradient phases over phGradL, phOff[4] its boundary-face phases over phBface
+  Tile *phGrad = nullptr, *phUpd = nullptr, *phFace = nullptr, *phGradL = nullptr,
+       *phBface = nullptr;
+  int phOff[5][9] = {};
   int phN = 0;
   // mixed-path transfers: the device cells of each chunk in ascending device
   // order (xList[xOff[k] .. xOff[k+1])), so the conversions touch the device
@@ -1030,6 +1032,76 @@ int phase_setup(rfgpu_region_s *h) {
     h->phFace = h->mem.upload(face, s);
   }
   h->phOff[2][nk] = (int)face.size();
+  // the last stage's gradient and boundary faces by phase too (stages after
+  // the first, without the WENO pass that needs every gradient): a boundary
+  // tile runs in the earliest update phase of its cells; a gradient tile no
+  // later than every face and boundary tile that reads its cells' gradients
+  // and than every update that rewrites a record it reads
+  if (nFT > 0 && nT > 0 && h->nSteps >= 2 && h->reconst != RFGPU_RECONST_WENO_XYZ) {
+    std::vector<int> u(nT), gam(nT, nk - 1);
+    for (int t = 0; t < nT; ++t) u[t] = clampk(first[t]);
+    int *du = h->mem.upload(u, s);
+    int *dg = h->mem.upload(gam, s);
+    launch_member_phase<float>(regs_of<float>(h), w, du, dg, s);
+    h->launches++;
+    if (cudaMemcpyAsync(gam.data(), dg, (size_t)nT * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    std::vector<int> f2c(2 * (size_t)F);
+    std::vector<Tile> ftiles(nFT);
+    if (cudaMemcpyAsync(f2c.data(), h->rd32.f2c, 2 * (size_t)F * 4, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(ftiles.data(), h->faceTiles, (size_t)nFT * sizeof(Tile),
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess)
+      return RFGPU_ERR_CUDA;
+    for (int j = 0; j < nk; ++j)
+      for (int i = h->phOff[2][j]; i < h->phOff[2][j + 1]; ++i) {
+        const int f0 = face[i].first, f1 = std::min(F, f0 + w.block);
+        for (int f = f0; f < f1; ++f)
+          for (int q = 0; q < 2; ++q) {
+            const int tc = f2c[(size_t)q * F + f] / w.block;
+            gam[tc] = std::min(gam[tc], j);
+          }
+      }
+    const int B = h->nBFaces, nBT = (B + w.block - 1) / w.block;
+    std::vector<Tile> bface;
+    if (nBT > 0) {
+      std::vector<int> bf2c(B);
+      std::vector<Tile> btiles(nBT);
+      if (cudaMemcpyAsync(bf2c.data(), h->rd32.bf2c, (size_t)B * 4, cudaMemcpyDeviceToHost, s) !=
+              cudaSuccess ||
+          cudaMemcpyAsync(btiles.data(), h->bfaceTiles, (size_t)nBT * sizeof(Tile),
+                          cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+          cudaStreamSynchronize(s) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      std::vector<int> beta(nBT, nk - 1);
+      for (int t = 0; t < nBT; ++t) {
+        const int b0 = btiles[t].first, b1 = std::min(B, b0 + w.block);
+        for (int b = b0; b < b1; ++b) beta[t] = std::min(beta[t], u[bf2c[b] / w.block]);
+        for (int b = b0; b < b1; ++b) {
+          const int tc = bf2c[b] / w.block;
+          gam[tc] = std::min(gam[tc], beta[t]);
+        }
+      }
+      for (int j = 0; j < nk; ++j) {
+        h->phOff[4][j] = (int)bface.size();
+        for (int t = 0; t < nBT; ++t)
+          if (beta[t] == j) bface.push_back(btiles[t]);
+      }
+    }
+    h->phOff[4][nk] = (int)bface.size();
+    std::vector<Tile> gradL;
+    gradL.reserve(nT);
+    for (int j = 0; j < nk; ++j) {
+      h->phOff[3][j] = (int)gradL.size();
+      for (int t = 0; t < nT; ++t)
+        if (gam[t] == j) gradL.push_back(tiles[t]);
+    }
+    h->phOff[3][nk] = (int)gradL.size();
+    h->phGradL = h->mem.upload(gradL, s);
+    if (!bface.empty()) h->phBface = h->mem.upload(bface, s);
+  }
   if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
   h->phN = nk;
   return RFGPU_OK;
@@ -1083,17 +1155,33 @@ int step_host_mixed(rfgpu_region_s *h, double *cv, double *dv, const DtArgs &da)
   }
   for (int is = 1; is <= nS; ++is) {
     StepArgs sa{is, 1, 0.0, 0, 1, is == 1 ? 1 : 0, da};
-    // the last stage runs its interior faces and its update phase by phase
+    // the last stage runs its interior faces and its update phase by phase,
+    // and with phGradL its gradient and boundary faces as well
+    const bool allPhased = is == nS && h->phGradL;
     const int parts = (is == 1 ? 0 : SP_GRADIENT) | SP_FLUX |
                       (is == nS ? (h->phFace ? SP_NOFACE : 0) : SP_UPDATE);
-    launch_stage<float>(regs, w, sa, s, &h->launches, h->spaceOrder, h->reconst, prof, parts);
+    if (!allPhased)
+      launch_stage<float>(regs, w, sa, s, &h->launches, h->spaceOrder, h->reconst, prof, parts);
     if (is < nS) continue;
-    // last stage phase by phase: the faces the phase's update tiles need, the
-    // update, then each chunk converted and copied back behind it
+    // last stage phase by phase: the gradients, faces and boundary faces the
+    // phase's update tiles need, the update, then each chunk converted and
+    // copied back behind it
     for (int k = 0; k < nk; ++k) {
+      if (allPhased) {
+        const int ng = h->phOff[3][k + 1] - h->phOff[3][k];
+        if (ng > 0) {
+          launch_grad_tiles<float>(regs, w, h->phGradL + h->phOff[3][k], ng, 0, s);
+          h->launches++;
+        }
+      }
       const int nf = h->phFace ? h->phOff[2][k + 1] - h->phOff[2][k] : 0;
       if (nf > 0) {
         launch_face_tiles<float>(regs, w, h->phFace + h->phOff[2][k], nf, s);
+        h->launches++;
+      }
+      const int nb = h->phBface && allPhased ? h->phOff[4][k + 1] - h->phOff[4][k] : 0;
+      if (nb > 0) {
+        launch_bface_tiles<float>(regs, w, h->phBface + h->phOff[4][k], nb, s);
         h->launches++;
       }
       const int n = h->phOff[1][k + 1] - h->phOff[1][k];

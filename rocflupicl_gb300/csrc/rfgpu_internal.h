@@ -278,10 +278,19 @@ void launch_grad_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tile
 template <typename R>
 void launch_update_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                          const StepArgs &a, cudaStream_t s);
-// The interior-face pass over a list of 128-face tiles.
+// The interior-face pass over a list of 128-face tiles; the boundary-face
+// pass over a list of boundary-face tiles.
 template <typename R>
 void launch_face_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
                        cudaStream_t s);
+template <typename R>
+void launch_bface_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                        cudaStream_t s);
+// Per cell tile, the minimum of tilePhase over the tiles of its cells, their
+// stencil members and face neighbours (atomicMin into out).
+template <typename R>
+void launch_member_phase(const RegionDev<R> *regs, const Work &w, const int *tilePhase, int *out,
+                         cudaStream_t s);
 template <typename R>
 void launch_dt(const RegionDev<R> *regs, const Work &w, const DtArgs &a, cudaStream_t s,
                long long *launches, const Prof *prof);

@@ -2878,6 +2878,50 @@ __global__ void k_tile_phases(const RegionDev<R> *__restrict__ regs, const Tile 
   }
 }
 
+// The earliest phase any cell of a tile reads a record from: the minimum
+// over its cells, their stencil members and face neighbours of the phase of
+// the update tile (tilePhase, per 128-cell tile) that rewrites that record.
+// A gradient tile of the last stage must run no later than that phase.
+template <typename R>
+__global__ void k_member_phase(const RegionDev<R> *__restrict__ regs, const Tile *__restrict__ tiles,
+                               int nTiles, const int *__restrict__ tilePhase, int block,
+                               int *__restrict__ out) {
+  RF_TILE_LOOP(tiles, nTiles) {
+    const Tile tl = tiles[t_];
+    const RegionDev<R> &g = regs[tl.region];
+    const int c = tl.first + threadIdx.x;
+    if (c >= g.nCells) continue;
+    int v = tilePhase[c / block];
+    if (g.stOff) {
+      const long long b = g.stOff[c >> 5] + (c & 31);
+      const int n = g.stCnt[c];
+      for (int k = 0; k < n; ++k) v = min(v, tilePhase[g.stIdx[b + (long long)k * kSlice] / block]);
+    }
+    const long long e0 = g.cfOff[c >> 5] + (c & 31);
+    const int nf = g.cfCnt[c];
+    for (int k = 0; k < nf; ++k) {
+      const long long e = e0 + (long long)k * kSlice;
+      if (g.cfCode[e] >= 0) v = min(v, tilePhase[g.cfNb[e] / block]);
+    }
+    atomicMin(out + t_, v);
+  }
+}
+
+template <typename R>
+void launch_member_phase(const RegionDev<R> *regs, const Work &w, const int *tilePhase, int *out,
+                         cudaStream_t s) {
+  if (w.nCellTiles > 0)
+    k_member_phase<R><<<w.nCellTiles, w.block, 0, s>>>(regs, w.cellTiles, w.nCellTiles, tilePhase,
+                                                       w.block, out);
+}
+
+template <typename R>
+void launch_bface_tiles(const RegionDev<R> *regs, const Work &w, const Tile *tiles, int nTiles,
+                        cudaStream_t s) {
+  const int grid = grid_for(w.grid, nTiles);
+  if (grid > 0) k_bface_flux<R><<<grid, w.block, 0, s>>>(regs, tiles, nTiles);
+}
+
 template <typename R>
 void launch_tile_phases(const RegionDev<R> *regs, const Work &w, const ChunkMap &m,
                         int *tileLast, int *tileFirst, cudaStream_t s) {
@@ -3036,6 +3080,10 @@ void launch_border_unpack(const RegionDev<R> *g, const int *cells, int n, const 
                                        const StepArgs &, cudaStream_t);                       \
   template void launch_face_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int,   \
                                      cudaStream_t);                                           \
+  template void launch_bface_tiles<R>(const RegionDev<R> *, const Work &, const Tile *, int,  \
+                                      cudaStream_t);                                          \
+  template void launch_member_phase<R>(const RegionDev<R> *, const Work &, const int *, int *, \
+                                       cudaStream_t);                                         \
   template void launch_dt<R>(const RegionDev<R> *, const Work &, const DtArgs &, cudaStream_t, \
                              long long *, const Prof *);                                      \
   template void launch_step<R>(const RegionDev<R> *, const Work &, const DtArgs &, int,       \
