@@ -999,47 +999,55 @@ int phase_setup(rfgpu_region_s *h) {
   h->phOff[0][nk] = h->phOff[1][nk] = nT;
   h->phGrad = h->mem.upload(grad, s);
   h->phUpd = h->mem.upload(upd, s);
-  // interior faces of the last stage by phase: a 128-face tile runs in the
-  // phase of the earliest update tile any of its faces feeds, so update phase
-  // k finds every face of its cells done (face phases 0..k run before it)
-  // (the region's own 128-face tiles, whatever face shape a tuning chose)
+  // The face tables on the host once (the region's own 128-face and
+  // 128-boundary-face tiles, whatever face shape a tuning chose).
   const int F = h->nFaces, nFT = (F + w.block - 1) / w.block;
-  std::vector<Tile> face;
-  if (nFT > 0) {
-    std::vector<int> f2c(2 * (size_t)F);
-    std::vector<Tile> ftiles(nFT);
-    if (cudaMemcpyAsync(f2c.data(), h->rd32.f2c, 2 * (size_t)F * 4, cudaMemcpyDeviceToHost, s) !=
+  const int B = h->nBFaces, nBT = (B + w.block - 1) / w.block;
+  std::vector<int> f2c(2 * (size_t)F), bf2c(B);
+  std::vector<Tile> ftiles(nFT), btiles(nBT);
+  if ((nFT > 0 &&
+       (cudaMemcpyAsync(f2c.data(), h->rd32.f2c, 2 * (size_t)F * 4, cudaMemcpyDeviceToHost, s) !=
             cudaSuccess ||
         cudaMemcpyAsync(ftiles.data(), h->faceTiles, (size_t)nFT * sizeof(Tile),
-                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return RFGPU_ERR_CUDA;
-    std::vector<int> phase(nFT, nk - 1);
-    for (int t = 0; t < nFT; ++t) {
-      const int f0 = ftiles[t].first, f1 = std::min(F, f0 + w.block);
-      for (int f = f0; f < f1; ++f)
-        for (int j = 0; j < 2; ++j) {
-          const int c = f2c[(size_t)j * F + f];
-          phase[t] = std::min(phase[t], clampk(first[c / w.block]));
-        }
-    }
-    face.reserve(nFT);
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess)) ||
+      (nBT > 0 &&
+       (cudaMemcpyAsync(bf2c.data(), h->rd32.bf2c, (size_t)B * 4, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(btiles.data(), h->bfaceTiles, (size_t)nBT * sizeof(Tile),
+                        cudaMemcpyDeviceToHost, s) != cudaSuccess)) ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return RFGPU_ERR_CUDA;
+  // tile lists by phase: list[j] holds the tiles whose phase is j
+  auto by_phase = [&](const std::vector<Tile> &all, const std::vector<int> &ph, int slot,
+                      Tile *&dev) {
+    std::vector<Tile> out;
+    out.reserve(all.size());
     for (int j = 0; j < nk; ++j) {
-      h->phOff[2][j] = (int)face.size();
-      for (int t = 0; t < nFT; ++t)
-        if (phase[t] == j) face.push_back(ftiles[t]);
+      h->phOff[slot][j] = (int)out.size();
+      for (size_t t = 0; t < all.size(); ++t)
+        if (ph[t] == j) out.push_back(all[t]);
     }
-    h->phFace = h->mem.upload(face, s);
-  }
-  h->phOff[2][nk] = (int)face.size();
-  // the last stage's gradient and boundary faces by phase too (stages after
-  // the first, without the WENO pass that needs every gradient): a boundary
-  // tile runs in the earliest update phase of its cells; a gradient tile no
-  // later than every face and boundary tile that reads its cells' gradients
-  // and than every update that rewrites a record it reads
-  if (nFT > 0 && nT > 0 && h->nSteps >= 2 && h->reconst != RFGPU_RECONST_WENO_XYZ) {
-    std::vector<int> u(nT), gam(nT, nk - 1);
-    for (int t = 0; t < nT; ++t) u[t] = clampk(first[t]);
+    h->phOff[slot][nk] = (int)out.size();
+    dev = out.empty() ? nullptr : h->mem.upload(out, s);
+  };
+  const int bs = w.block;
+  std::vector<int> u(nT);  // update phase of each cell tile
+  for (int t = 0; t < nT; ++t) u[t] = clampk(first[t]);
+  // interior faces of the last stage: a 128-face tile runs in the phase of
+  // the earliest update tile any of its faces feeds, so update phase k finds
+  // every face of its cells done (face phases 0..k run before it)
+  std::vector<int> phi(nFT, nk - 1);
+  for (int t = 0; t < nFT; ++t)
+    for (int f = ftiles[t].first; f < std::min(F, ftiles[t].first + bs); ++f)
+      for (int q = 0; q < 2; ++q) phi[t] = std::min(phi[t], u[f2c[(size_t)q * F + f] / bs]);
+  by_phase(ftiles, phi, 2, h->phFace);
+  if (nT > 0 && h->nSteps >= 2 && h->reconst != RFGPU_RECONST_WENO_XYZ) {
+    // the last stage's gradient and boundary faces by phase too (stages after
+    // the first, without the WENO pass that needs every gradient): a boundary
+    // tile runs in the earliest update phase of its cells; a gradient tile no
+    // later than every face and boundary tile that reads its cells'
+    // gradients and than every update that rewrites a record it reads
+    std::vector<int> gam(nT, nk - 1), beta(nBT, nk - 1);
     int *du = h->mem.upload(u, s);
     int *dg = h->mem.upload(gam, s);
     launch_member_phase<float>(regs_of<float>(h), w, du, dg, s);
@@ -1047,60 +1055,19 @@ int phase_setup(rfgpu_region_s *h) {
     if (cudaMemcpyAsync(gam.data(), dg, (size_t)nT * 4, cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
       return RFGPU_ERR_CUDA;
-    std::vector<int> f2c(2 * (size_t)F);
-    std::vector<Tile> ftiles(nFT);
-    if (cudaMemcpyAsync(f2c.data(), h->rd32.f2c, 2 * (size_t)F * 4, cudaMemcpyDeviceToHost, s) !=
-            cudaSuccess ||
-        cudaMemcpyAsync(ftiles.data(), h->faceTiles, (size_t)nFT * sizeof(Tile),
-                        cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-        cudaStreamSynchronize(s) != cudaSuccess)
-      return RFGPU_ERR_CUDA;
-    for (int j = 0; j < nk; ++j)
-      for (int i = h->phOff[2][j]; i < h->phOff[2][j + 1]; ++i) {
-        const int f0 = face[i].first, f1 = std::min(F, f0 + w.block);
-        for (int f = f0; f < f1; ++f)
-          for (int q = 0; q < 2; ++q) {
-            const int tc = f2c[(size_t)q * F + f] / w.block;
-            gam[tc] = std::min(gam[tc], j);
-          }
-      }
-    const int B = h->nBFaces, nBT = (B + w.block - 1) / w.block;
-    std::vector<Tile> bface;
-    if (nBT > 0) {
-      std::vector<int> bf2c(B);
-      std::vector<Tile> btiles(nBT);
-      if (cudaMemcpyAsync(bf2c.data(), h->rd32.bf2c, (size_t)B * 4, cudaMemcpyDeviceToHost, s) !=
-              cudaSuccess ||
-          cudaMemcpyAsync(btiles.data(), h->bfaceTiles, (size_t)nBT * sizeof(Tile),
-                          cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-          cudaStreamSynchronize(s) != cudaSuccess)
-        return RFGPU_ERR_CUDA;
-      std::vector<int> beta(nBT, nk - 1);
-      for (int t = 0; t < nBT; ++t) {
-        const int b0 = btiles[t].first, b1 = std::min(B, b0 + w.block);
-        for (int b = b0; b < b1; ++b) beta[t] = std::min(beta[t], u[bf2c[b] / w.block]);
-        for (int b = b0; b < b1; ++b) {
-          const int tc = bf2c[b] / w.block;
-          gam[tc] = std::min(gam[tc], beta[t]);
+    for (int t = 0; t < nFT; ++t)
+      for (int f = ftiles[t].first; f < std::min(F, ftiles[t].first + bs); ++f)
+        for (int q = 0; q < 2; ++q) {
+          int &g = gam[f2c[(size_t)q * F + f] / bs];
+          g = std::min(g, phi[t]);
         }
-      }
-      for (int j = 0; j < nk; ++j) {
-        h->phOff[4][j] = (int)bface.size();
-        for (int t = 0; t < nBT; ++t)
-          if (beta[t] == j) bface.push_back(btiles[t]);
-      }
+    for (int t = 0; t < nBT; ++t) {
+      const int b0 = btiles[t].first, b1 = std::min(B, b0 + bs);
+      for (int b = b0; b < b1; ++b) beta[t] = std::min(beta[t], u[bf2c[b] / bs]);
+      for (int b = b0; b < b1; ++b) gam[bf2c[b] / bs] = std::min(gam[bf2c[b] / bs], beta[t]);
     }
-    h->phOff[4][nk] = (int)bface.size();
-    std::vector<Tile> gradL;
-    gradL.reserve(nT);
-    for (int j = 0; j < nk; ++j) {
-      h->phOff[3][j] = (int)gradL.size();
-      for (int t = 0; t < nT; ++t)
-        if (gam[t] == j) gradL.push_back(tiles[t]);
-    }
-    h->phOff[3][nk] = (int)gradL.size();
-    h->phGradL = h->mem.upload(gradL, s);
-    if (!bface.empty()) h->phBface = h->mem.upload(bface, s);
+    by_phase(tiles, gam, 3, h->phGradL);
+    by_phase(btiles, beta, 4, h->phBface);
   }
   if (cudaStreamSynchronize(s) != cudaSuccess) return RFGPU_ERR_CUDA;
   h->phN = nk;
