@@ -879,8 +879,12 @@ int transfer_setup(rfgpu_region_s *h) {
     return RFGPU_ERR_NOMEM;
   }
   if (cudaStreamSynchronize(h->stream) != cudaSuccess) return RFGPU_ERR_CUDA;
+  // conversions run on a stream of the highest priority, so their blocks go
+  // before the stage kernels they run beside
+  int loPrio = 0, hiPrio = 0;
+  cudaDeviceGetStreamPriorityRange(&loPrio, &hiPrio);
   if (cudaStreamCreateWithFlags(&h->xstream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&h->cstream, cudaStreamNonBlocking) != cudaSuccess)
+      cudaStreamCreateWithPriority(&h->cstream, cudaStreamNonBlocking, hiPrio) != cudaSuccess)
     return RFGPU_ERR_CUDA;
   for (cudaEvent_t &e : h->xev)
     if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) return RFGPU_ERR_CUDA;
@@ -896,10 +900,11 @@ void upload_chunk(rfgpu_region_s *h, int k, const double *cvS, const double *dvS
                             cvS, dvS, h->prec == RFGPU_PREC_SPLIT, s);
   h->launches++;
 }
-void download_chunk(rfgpu_region_s *h, int k, double *cvS, double *dvS) {
+void download_chunk(rfgpu_region_s *h, int k, double *cvS, double *dvS,
+                    cudaStream_t st = nullptr) {
   launch_download_list<float>(regs_of<float>(h), h->xList + h->xOff[k],
                               h->xOff[k + 1] - h->xOff[k], cvS, dvS,
-                              h->prec == RFGPU_PREC_SPLIT, h->stream);
+                              h->prec == RFGPU_PREC_SPLIT, st ? st : h->stream);
   h->launches++;
 }
 
@@ -1159,8 +1164,14 @@ int step_host_mixed(rfgpu_region_s *h, double *cv, double *dv, const DtArgs &da)
       int t0, t1;
       size_t c0, c1;
       chunk_range(h, k, nk, t0, t1, c0, c1);
-      download_chunk(h, k, h->stage, dv ? h->stage2 : nullptr);
-      if (cudaEventRecord(h->xev[k], s) != cudaSuccess ||
+      // the chunk's conversion (FP64 state and EOS, FP64-pipe bound) on the
+      // high-priority conversion stream beside the next phase's FP32 kernels;
+      // its copy back behind it
+      if (cudaEventRecord(h->cev[k], s) != cudaSuccess ||
+          cudaStreamWaitEvent(cs, h->cev[k], 0) != cudaSuccess)
+        return RFGPU_ERR_CUDA;
+      download_chunk(h, k, h->stage, dv ? h->stage2 : nullptr, cs);
+      if (cudaEventRecord(h->xev[k], cs) != cudaSuccess ||
           cudaStreamWaitEvent(x, h->xev[k], 0) != cudaSuccess)
         return RFGPU_ERR_CUDA;
       if (cudaMemcpyAsync(cv + 5 * c0, h->stage + 5 * c0, 5 * (c1 - c0) * 8,
@@ -1301,6 +1312,7 @@ int rfgpu_region_create(const rfgpu_region_desc_t *d, rfgpu_region_t *out) {
   ph.gvMol = d->gvMol;
   ph.gvR = 8314.3 / d->gvMol;                     // MixtPerf_R_M
   ph.gvG = d->gvCp / (d->gvCp - ph.gvR);          // MixtPerf_G_CpR
+  ph.gvRinv = 1.0 / ph.gvR;
   ph.epsentr = d->epsentr;
   ph.dissFact = d->dissFact;
   rk_coeffs(d->rkScheme, ph);

@@ -52,6 +52,7 @@ struct Phys {
   // flux function 2 overwrites the factor that uses it)
   double ausmSigma, ausmKp, ausmKu, ausmMInf;
   float ausmSigmaF, ausmKpF, ausmKuF;
+  double gvRinv;  // 1 / gvR (mixed-path download EOS)
 };
 
 template <typename R>

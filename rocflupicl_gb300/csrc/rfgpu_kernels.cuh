@@ -2183,10 +2183,13 @@ __global__ void k_download_list(const RegionDev<R> *__restrict__ regs, const int
     dvH[3 * (size_t)h + 1] = T;
     dvH[3 * (size_t)h + 2] = sqrt(gg * gc * T);
   } else if (dvH) {
+    // FP64 EOS of the joined pairs with one division (by rho) instead of two:
+    // the conversion is FP64-pipe bound
     const double gc = g.ph.gvR, gg = g.ph.gvG;
     const double m2 = fma(q[3], q[3], fma(q[2], q[2], q[1] * q[1]));
-    const double p = (gg - 1.0) * (q[4] - 0.5 * m2 / q[0]);
-    const double T = p / (q[0] * gc);
+    const double ir = 1.0 / q[0];
+    const double p = (gg - 1.0) * (q[4] - 0.5 * m2 * ir);
+    const double T = p * ir * g.ph.gvRinv;
     dvH[3 * (size_t)h] = p;
     dvH[3 * (size_t)h + 1] = T;
     dvH[3 * (size_t)h + 2] = sqrt(gg * gc * T);
