@@ -79,16 +79,17 @@ def test_chunked_upload_download_round_trip(dims, order, prec):
     r.close()
 
 
-def _case(dims, prec, discr=K.DISCR_UPW_ROE, rk=K.RK_SCHEME_3_WRAY, order=2):
+def _case(dims, prec, discr=K.DISCR_UPW_ROE, rk=K.RK_SCHEME_3_WRAY, order=2,
+          reconst=K.RECONST_LIM_VENKAT):
     nx, ny, nz = dims
     num = K.Numerics(precision=prec, venkatGuard=1, spaceDiscr=discr, rkScheme=rk,
-                     spaceOrder=order)
+                     spaceOrder=order, reconst=reconst)
     return K.tet_shock_box(nx, ny=ny, nz=nz, seed=7, numerics=num)
 
 
 @pytest.mark.parametrize("dims", [(3, 3, 3), (5, 3, 7), (24, 8, 8), (50, 9, 11)])
 @pytest.mark.parametrize("variant", ["roe-wray", "hllc-rk4", "ausm+-euler", "first-order", "fp64",
-                                     "split", "split-rk4"])
+                                     "split", "split-rk4", "ausm+up-unlimited"])
 @pytest.mark.parametrize("order", [E.ORDER_HOST, E.ORDER_LOCALITY])
 def test_step_host_equals_three_calls(dims, variant, order):
     """rfgpu_step_host against rfgpu_upload + rfgpu_step + rfgpu_download on the
@@ -97,8 +98,11 @@ def test_step_host_equals_three_calls(dims, variant, order):
     8 chunks with the first stage's gradient pass split into phases by the
     chunks its records travel in and the last stage's update split by the
     chunks it hands back (regions smaller than 8 tiles in fewer chunks); the
-    FP64 path and first order run the three calls in sequence."""
+    FP64 path and first order run the three calls in sequence.  With more than
+    one stage and no WENO pass the whole last stage (gradient, faces, boundary
+    faces, update) runs in the download's phases."""
     prec, discr, rk, sord = K.PREC_MIXED, K.DISCR_UPW_ROE, K.RK_SCHEME_3_WRAY, 2
+    reconst = K.RECONST_LIM_VENKAT
     if variant == "hllc-rk4":
         discr, rk = K.DISCR_UPW_HLLC, K.RK_SCHEME_4_CLASSICAL
     elif variant == "ausm+-euler":
@@ -111,7 +115,9 @@ def test_step_host_equals_three_calls(dims, variant, order):
         prec = K.PREC_SPLIT
     elif variant == "split-rk4":
         prec, discr, rk = K.PREC_SPLIT, K.DISCR_UPW_HLLC, K.RK_SCHEME_4_CLASSICAL
-    c = _case(dims, prec, discr, rk, sord)
+    elif variant == "ausm+up-unlimited":
+        discr, reconst = K.DISCR_UPW_AUSMPLUSUP, K.RECONST_NONE
+    c = _case(dims, prec, discr, rk, sord, reconst)
     cfl = 0.5
     a = E.Region(c, cell_order=order)
     b = E.Region(c, cell_order=order)
