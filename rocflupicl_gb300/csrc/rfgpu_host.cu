@@ -1082,8 +1082,10 @@ int phase_setup(rfgpu_region_s *h) {
 // One time step of a host-resident state (mixed path), its transfers
 // overlapped with the step: chunk k of cv goes up on the copy stream while a
 // conversion stream converts chunk k-1 and the region's stream runs the
-// stage-1 gradient phases whose records have all arrived; the last stage's
-// update runs phase by phase, each followed by its chunk's conversion and copy
+// stage-1 gradient phases whose records have all arrived; the last stage runs
+// phase by phase (its faces and update always, its gradient and boundary
+// faces too when it is not the first stage and has no WENO pass), each phase
+// followed by its chunk's conversion on the conversion stream and the copy
 // back.  The arithmetic per cell is that of rfgpu_upload + rfgpu_step +
 // rfgpu_download.  Second order only (the stage-1 gradient pass carries the
 // time step).
