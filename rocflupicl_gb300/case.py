@@ -311,13 +311,18 @@ def from_files(grid_path: str, flow_path: str, bcs: List[PatchBC],
                 meta={"time": fl.time, "grid": grid_path, "flow": flow_path})
 
 
-def from_case_files(grid_path: str, flow_path: str, inp_path: str, bc_path: str,
+def from_case_files(grid_path: str, flow_path: Optional[str], inp_path: str, bc_path: str,
                     binary: bool = False, endian: str = "<", threads: int = 0,
-                    stencils: str = "host", strict: bool = True):
+                    stencils: str = "host", strict: bool = True,
+                    casename: Optional[str] = None):
     """A case from a RocfluMP case's files: the grid and flow files, the `.inp`
     numerics and the `.bc` boundary conditions (rocflupicl_gb300.rfluinput).
+    Without a flow file the initial state is the one rfluinit makes from the
+    `.inp` INITFLOW section (initial_cv; the case name defaults to the `.inp`
+    file's name, as RocfluMP names a case's files after it).
     Returns (case, CaseInput, unsupported settings); strict raises ValueError
     when the files ask for anything outside the engine's envelope."""
+    import os
     from . import rfluinput as RI
     from . import rfluio as IO
     ci = RI.read_inp(inp_path)
@@ -326,10 +331,102 @@ def from_case_files(grid_path: str, flow_path: str, inp_path: str, bc_path: str,
     bad = ci.unsupported + bad_bc
     if strict and bad:
         raise ValueError("settings outside the engine's envelope: " + "; ".join(bad))
-    c = from_files(grid_path, flow_path, bcs, ci.numerics, binary, endian, threads, stencils)
+    if flow_path is None:
+        name = casename or os.path.splitext(os.path.basename(inp_path))[0]
+        num = ci.numerics
+        m = IO.mesh_of_grid(g, threads=threads, stencils=stencils)
+        if len(bcs) != len(m.patches):
+            raise ValueError(f"{len(bcs)} boundary conditions for {len(m.patches)} patches")
+        cv = initial_cv(name, m.cofg[:m.nCells], num, ci.raw.get("INITFLOW", {}))
+        c = Case(f"files:{grid_path}", m, num, list(bcs), cv, eos_dv(num, cv),
+                 meta={"time": 0.0, "grid": grid_path, "casename": name})
+    else:
+        c = from_files(grid_path, flow_path, bcs, ci.numerics, binary, endian, threads,
+                       stencils)
     c.meta["dt_imposed"], c.meta["max_time"] = ci.dt_imposed, ci.max_time
     c.t_end = ci.max_time
     return c, ci, bad
+
+
+# INITFLOW FLAG values (modfloflu/ModParameters.F90:911-916)
+INITFLOW_FROMSCRATCH, INITFLOW_FROMFILE, INITFLOW_FROMHARDCODE = 1, 2, 3
+# the hard-coded initial states restated below (perfect gas only)
+HARDCODED_CASES = ("rectshktb", "cylds", "st_sod1", "st_sod1_mp2", "st_sod2", "st_sod2_mp2",
+                   "stg1d", "stg2d", "gtlin", "gttri")
+
+
+def hardcoded_prims(casename: str, xyz: np.ndarray, vals: dict):
+    """(rho, u, v, w, p) per cell of RFLU_InitFlowHardCode (utilities/init/
+    RFLU_InitFlowHardCode.F90) for the perfect-gas branch of the named cases,
+    from the cell centroids and the INITFLOW values (RVALn = prepRealValn)."""
+    x, y, z = xyz[:, 0], xyz[:, 1], xyz[:, 2]
+    zero = np.zeros_like(x)
+
+    def rv(i):
+        k = f"RVAL{i}"
+        if k not in vals:
+            raise ValueError(f"INITFLOW {k} is not defined, case {casename!r} needs it")
+        return float(vals[k])
+
+    def split(inner, a, b):
+        return tuple(np.where(inner, ai, bi) for ai, bi in zip(a, b))
+
+    if casename in ("rectshktb", "cylds"):  # :760-813
+        if casename == "cylds":
+            radius, theta = np.sqrt(x ** 2 + y ** 2), np.arctan2(y, x)
+            ur, ut = rv(3) * np.cos(theta), rv(3) * np.sin(theta)
+        else:
+            radius, ur, ut = x, np.full_like(x, rv(3)), zero
+        return split(radius < rv(1), (rv(2), ur, ut, zero, rv(4)), (rv(5), zero, zero, zero, rv(6)))
+    if casename in ("st_sod1", "st_sod1_mp2"):  # :4274-4300
+        return split(x < 0.5, (1.0, zero, zero, zero, 1.0e5), (0.125, zero, zero, zero, 1.0e4))
+    if casename in ("st_sod2", "st_sod2_mp2"):  # :4309-4340
+        return split(x < 0.0, (1.0, zero, zero, zero, 1.0e5), (0.01, zero, zero, zero, 1.0e3))
+    if casename in ("stg1d", "stg2d"):  # :4232-4270
+        a = (rv(2), rv(3), zero, zero, rv(4))
+        b = (rv(5), rv(6), zero, zero, rv(7))
+        c = (rv(12), rv(13), zero, zero, rv(14))
+        return split(x < rv(1), a, split(x < rv(11), b, c))
+    if casename == "gtlin":  # :2700-2750 with RFLU_SetExactFlowLinear (RFLU_ModExactFlow.F90:1451-1491)
+        def lin(iv, X, Y, Z):
+            a = 1.0 + (iv - 1) * 2.0       # 1 + (iVar-1)*(ZCOORD-XCOORD)
+            return a * X + (a + 1.0) * Y + (a + 2.0) * Z
+        dmin, pmin = lin(1, x.min(), y.min(), z.min()), lin(5, x.min(), y.min(), z.min())
+        doffs = -2.0 * dmin if dmin < 0.0 else 0.0
+        poffs = -2.0 * pmin if pmin < 0.0 else 0.0
+        return (lin(1, x, y, z) + doffs, lin(2, x, y, z), lin(3, x, y, z), lin(4, x, y, z),
+                lin(5, x, y, z) + poffs)
+    if casename == "gttri":  # :2757-2790 with RFLU_SetExactFlowTrig (RFLU_ModExactFlow.F90:1527-1568)
+        pi = 4.0 * np.arctan(1.0)
+        a, b, c = rv(1) * pi, rv(2) * pi, rv(3) * pi
+        var = np.cos(a * x) * np.sin(b * y) * np.cos(c * z)
+        return var + 2.0, var, var, var, var + 2.0
+    raise ValueError(f"hard-coded initial state {casename!r} is not restated "
+                     f"(restated: {', '.join(HARDCODED_CASES)})")
+
+
+def initial_cv(casename: str, xyz: np.ndarray, num: Numerics, initflow: dict) -> np.ndarray:
+    """The initial conserved state of rfluinit for an INITFLOW section: FLAG 1
+    a uniform state (RFLU_InitFlowScratch: DENS, VELX/Y/Z, PRESS), FLAG 3 the
+    hard-coded state of the case name (hardcoded_prims); E = rho Eo as
+    MixtPerf_Eo_DGPUVW forms it."""
+    if "FLAG" not in initflow:
+        raise ValueError("INITFLOW FLAG is not defined")
+    flag = int(round(initflow["FLAG"]))
+    n = xyz.shape[0]
+    if flag == INITFLOW_FROMSCRATCH:
+        need = ["VELX", "VELY", "VELZ", "PRESS", "DENS"]
+        missing = [k for k in need if k not in initflow]
+        if missing:
+            raise ValueError("INITFLOW FLAG 1 without " + ", ".join(missing))
+        r, u, v, w, p = (np.full(n, float(initflow[k]))
+                         for k in ("DENS", "VELX", "VELY", "VELZ", "PRESS"))
+    elif flag == INITFLOW_FROMHARDCODE:
+        r, u, v, w, p = (np.broadcast_to(np.asarray(a, np.float64), (n,)).copy()
+                         for a in hardcoded_prims(casename, xyz, initflow))
+    else:
+        raise ValueError(f"INITFLOW FLAG {flag}: the state comes from a flow file")
+    return prim_to_cv(num, r, u, v, w, p)
 
 
 def write_flow(path: str, cv: np.ndarray, time: float = 0.0, binary: bool = False,

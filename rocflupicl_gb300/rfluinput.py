@@ -1,16 +1,20 @@
-"""RocfluMP case input files: the numerics, time-stepping, reference and
-mixture sections of the `.inp` file and the boundary-condition sections of the
-`.bc` file, read the way the reference reads them, mapped onto the engine's
-options, with every setting outside the engine's envelope reported.
+"""RocfluMP case input files: the numerics, time-stepping, reference, mixture
+and initial-flow sections of the `.inp` file and the boundary-condition
+sections of the `.bc` file, read the way the reference reads them, mapped onto
+the engine's options, with every setting outside the engine's envelope
+reported.
 
 Reading rules (libfloflu/ReadInputUtil.F90, ReadSection / ReadPatchSection):
 a section starts at a line whose trimmed text is its header (`# NUMERICS`) and
 ends at the next line starting with `#`; a key matches a line that starts with
 the key's text, in key-list order, and each key takes the first value after it
 (a list-directed read) and is then defined (a later line does not redefine
-it).  Section and key lists: ReadNumericsSection.F90:110-130,
+it); a line defines at most one key, the first undefined one that matches.
+Section and key lists: ReadNumericsSection.F90:110-130,
 ReadTimestepSection.F90:108-136, ReadReferenceSection.F90:103-112,
 ReadMixtureSection.F90:123-124, ReadFlowSection.F90:105-107,
+ReadInitFlowSection.F90:46-102 (its numeric keys; case.initial_cv makes the
+state),
 modflu/RFLU_ModReadBcInputFile.F90 (BC sections, keys and the degree to
 radian conversion of angles).  Defaults where a key is absent:
 libflu/RFLU_InitInputValues.F90:181-200, libflu/RFLU_InitGlobal.F90:232-354.
@@ -36,6 +40,11 @@ TIMESTEP_KEYS = ["FLOWTYPE", "TIMESTEP", "MAXTIME", "WRITIME", "PRNTIME", "MAXIT
 REFERENCE_KEYS = ["ABSVEL", "PRESS", "DENS", "CP", "GAMMA", "LENGTH", "RENUM", "PRLAM",
                   "PRTURB", "SCNLAM"]
 MIXTURE_KEYS = ["FROZENFLAG", "GASMODEL"]
+# libfloflu/ReadInitFlowSection.F90:46-102 (numeric keys, in the reference's order)
+INITFLOW_KEYS = (["FLAG", "VELX", "VELY", "VELZ", "PRESS", "DENS", "TEMP"]
+                 + [f"IVAL{i}" for i in range(1, 17)] + [f"RVAL{i}" for i in range(1, 21)]
+                 + ["DX", "DY", "DZ", "RVAL24", "IVAL17", "IVAL18", "IVAL19", "RVAL25",
+                    "RBFLAG"])
 FLOWMODEL_KEYS = ["MODEL", "MOVEGRID", "PBAFLAG"]
 USED_KEYS = ["USED"]
 
@@ -69,12 +78,15 @@ def _value(text: str) -> float:
 
 
 def _read_keys(lines: List[str], keys: List[str]) -> Dict[str, float]:
-    """ReadSection: every line against the keys not yet defined, in key order."""
+    """ReadSection (libfloflu/ReadInputUtil.F90): every line against the keys
+    not yet defined, in key order; a line defines at most the first key whose
+    text begins it (so `RVAL10 5.` defines an undefined RVAL1, reading 0.)."""
     vals: Dict[str, float] = {}
     for line in lines:
         for k in keys:
             if k not in vals and line.startswith(k):
                 vals[k] = _value(line[len(k):])
+                break
     return vals
 
 
@@ -120,6 +132,7 @@ def read_inp(path: str) -> CaseInput:
     flow = _read_keys(secs.get("# FLOWMODEL", []), FLOWMODEL_KEYS)
     spec = _read_keys(secs.get("# SPECIES", []), USED_KEYS)
     picl = _read_keys(secs.get("# PICL", []), USED_KEYS)
+    init = _read_keys(secs.get("# INITFLOW", []), INITFLOW_KEYS)
     n = K.Numerics(
         spaceDiscr=int(round(num.get("DISCR", K.DISCR_UPW_ROE))),
         spaceOrder=int(round(num.get("ORDER", 1))),
@@ -134,7 +147,7 @@ def read_inp(path: str) -> CaseInput:
                    dt_min_limit=ts.get("DTMINLIMIT", 1.0e-10), max_time=ts.get("MAXTIME", 1.0e-4),
                    order_bfaces=int(round(num.get("ORDERBF", 1))),
                    raw={"NUMERICS": num, "TIMESTEP": ts, "REFERENCE": ref, "MIXTURE": mix,
-                        "FLOWMODEL": flow, "SPECIES": spec, "PICL": picl})
+                        "FLOWMODEL": flow, "SPECIES": spec, "PICL": picl, "INITFLOW": init})
     bad = ci.unsupported
     if n.spaceDiscr not in (K.DISCR_UPW_ROE, K.DISCR_UPW_HLLC, K.DISCR_UPW_AUSMPLUS,
                             K.DISCR_UPW_AUSMPLUSUP):

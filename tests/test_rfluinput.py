@@ -164,6 +164,15 @@ def test_reference_airshock_input_read():
     assert not any(b.startswith("RECONST") for b in ci.unsupported)
     assert any(b.startswith("CRECONSTC 1") for b in ci.unsupported)
     assert any(b.startswith("PICL USED") for b in ci.unsupported)
+    # its INITFLOW section: the rectshktb planar shock (hard-coded, FLAG 3)
+    v = ci.raw["INITFLOW"]
+    assert v["FLAG"] == K.INITFLOW_FROMHARDCODE and v["RVAL1"] == -0.005
+    assert (v["RVAL2"], v["RVAL3"], v["RVAL4"]) == (2.0725901075834, 304.1461483936438,
+                                                    252082.2060022760706)
+    assert (v["RVAL5"], v["RVAL6"]) == (0.9721771595969, 82700.0)
+    xyz = np.array([[-0.01, 0.0, 0.0], [0.0, 0.0, 0.0]])
+    r, u, _, _, p = K.hardcoded_prims("rectshktb", xyz, v)
+    assert list(r) == [v["RVAL2"], v["RVAL5"]] and list(p) == [v["RVAL4"], v["RVAL6"]]
 
 
 def test_case_files_round_trip_residual(tmp_path):
@@ -204,3 +213,83 @@ def test_case_files_strict_refuses(tmp_path):
     with pytest.raises(ValueError, match="RECONST 1"):
         K.from_case_files(str(tmp_path / "c.grda"), str(tmp_path / "c.flo"),
                           str(tmp_path / "c.inp"), str(tmp_path / "c.bc"))
+
+
+def test_a_line_defines_one_key(tmp_path):
+    """ReadSection stops at the first undefined key a line matches: with RVAL1
+    undefined, `RVAL10 5.0` defines RVAL1 (reading 0 from `0 5.0`), not RVAL10."""
+    p = tmp_path / "keys.inp"
+    p.write_text("# INITFLOW\nFLAG 3\nRVAL10 5.0\nRVAL1 7.0\nRVAL2 8.0\nRVAL20 9.0\n#\n")
+    v = RI.read_inp(str(p)).raw["INITFLOW"]
+    assert v["FLAG"] == 3 and v["RVAL1"] == 0.0 and "RVAL10" not in v
+    assert v["RVAL2"] == 8.0 and v["RVAL20"] == 9.0
+
+
+def test_initflow_states(tmp_path):
+    """INITFLOW FLAG 1 (RFLU_InitFlowScratch) and FLAG 3 hard-coded states of
+    RFLU_InitFlowHardCode at chosen centroids."""
+    num = K.Numerics()
+    xyz = np.array([[-0.1, 0.2, 0.0], [0.3, -0.4, 0.1], [0.7, 0.0, 0.0]])
+    cv = K.initial_cv("any", xyz, num, {"FLAG": 1, "VELX": 10.0, "VELY": 0.0, "VELZ": -2.0,
+                                         "PRESS": 9.0e4, "DENS": 1.1})
+    assert np.array_equal(cv, K.prim_to_cv(num, *(np.full(3, a) for a in (1.1, 10.0, 0.0, -2.0,
+                                                                          9.0e4))))
+    shk = {"FLAG": 3, "RVAL1": 0.0, "RVAL2": 2.07, "RVAL3": 304.1, "RVAL4": 2.52e5,
+           "RVAL5": 0.972, "RVAL6": 8.27e4}
+    r, u, v, w, p = K.hardcoded_prims("rectshktb", xyz, shk)
+    assert list(r) == [2.07, 0.972, 0.972] and list(u) == [304.1, 0.0, 0.0]
+    assert list(p) == [2.52e5, 8.27e4, 8.27e4] and not v.any() and not w.any()
+    r, u, v, w, p = K.hardcoded_prims("cylds", xyz, shk)     # radius 0.224, 0.5, 0.7
+    assert list(r) == [0.972] * 3
+    r, u, v, w, p = K.hardcoded_prims("cylds", xyz, dict(shk, RVAL1=0.6))
+    assert list(r) == [2.07, 2.07, 0.972]
+    assert np.isclose(u[1], 304.1 * 0.3 / 0.5) and np.isclose(v[1], -304.1 * 0.4 / 0.5)
+    r, _, _, _, p = K.hardcoded_prims("st_sod2", xyz, {})
+    assert list(r) == [1.0, 0.01, 0.01] and list(p) == [1e5, 1e3, 1e3]
+    r, _, _, _, p = K.hardcoded_prims("st_sod1", xyz, {})
+    assert list(r) == [1.0, 1.0, 0.125]
+    stg = {"RVAL1": 0.0, "RVAL2": 1.0, "RVAL3": 1.0, "RVAL4": 1.0, "RVAL5": 2.0, "RVAL6": 2.0,
+           "RVAL7": 2.0, "RVAL11": 0.5, "RVAL12": 3.0, "RVAL13": 3.0, "RVAL14": 3.0}
+    r, u, _, _, p = K.hardcoded_prims("stg1d", xyz, stg)
+    assert list(r) == [1.0, 2.0, 3.0] and list(u) == [1.0, 2.0, 3.0]
+    r, u, v, w, p = K.hardcoded_prims("gtlin", xyz, {})
+    x, y, z = xyz.T
+    assert np.allclose(u, 3 * x + 4 * y + 5 * z) and np.allclose(w, 7 * x + 8 * y + 9 * z)
+    dmin = x.min() + 2 * y.min() + 3 * z.min()
+    assert np.allclose(r, x + 2 * y + 3 * z - 2 * dmin)
+    r, u, _, _, p = K.hardcoded_prims("gttri", xyz, {"RVAL1": 1.0, "RVAL2": 1.0, "RVAL3": 1.0})
+    assert np.allclose(u, np.cos(np.pi * x) * np.sin(np.pi * y) * np.cos(np.pi * z))
+    assert np.allclose(r, u + 2.0) and np.allclose(p, u + 2.0)
+    with pytest.raises(ValueError):
+        K.hardcoded_prims("rectshktb", xyz, {"FLAG": 3})      # RVALs missing
+    with pytest.raises(ValueError):
+        K.initial_cv("wedge", xyz, num, {"FLAG": 3})          # not restated
+    with pytest.raises(ValueError):
+        K.initial_cv("any", xyz, num, {"FLAG": 2})            # from a flow file
+
+
+def test_case_files_without_flow_file(tmp_path):
+    """No flow file: rfluinit's state from the deck's INITFLOW section, named
+    after the .inp file (st_sod1.inp -> the st_sod1 tube), or a uniform state
+    (FLAG 1), on the grid file's centroids."""
+    from rocflupicl_gb300 import rfluio as IO
+    c = K.shock_tube(20, 2, 2, length=(1.0, 0.1, 0.1))
+    IO.write_grid_ascii(str(tmp_path / "g.grda"), IO.grid_of_mesh(c.mesh))
+    deck = ("# NUMERICS\nCFL 0.5\nDISCR 1\nORDER 2\nRECONST 11\n#\n# TIMESTEP\nFLOWTYPE 1\n"
+            "RKSCHEME 2\nMAXTIME 2.0E-4\n#\n# INITFLOW\n{}#\n")
+    (tmp_path / "st_sod1.inp").write_text(deck.format("FLAG 3\n"))
+    (tmp_path / "uniform.inp").write_text(
+        deck.format("FLAG 1\nVELX 5.0\nVELY 0.0\nVELZ 0.0\nPRESS 1.0E5\nDENS 1.2\n"))
+    (tmp_path / "c.bc").write_text("# BC_OUTFLOW\nPATCH 1 2\nTYPE 0\n#\n# BC_SLIPW\nPATCH 3 6\n#\n")
+    args = (str(tmp_path / "g.grda"), None)
+    c1, _, bad = K.from_case_files(*args, str(tmp_path / "st_sod1.inp"), str(tmp_path / "c.bc"))
+    x = c1.mesh.cofg[:c1.mesh.nCells, 0]
+    assert bad == [] and c1.meta["casename"] == "st_sod1"
+    assert np.array_equal(c1.cv[:, 0], np.where(x < 0.5, 1.0, 0.125))
+    assert np.allclose(c1.dv[:, 0], np.where(x < 0.5, 1.0e5, 1.0e4), rtol=1e-14)
+    c2, _, _ = K.from_case_files(*args, str(tmp_path / "uniform.inp"), str(tmp_path / "c.bc"))
+    assert np.array_equal(c2.cv[:, 0], np.full(len(x), 1.2))
+    assert np.allclose(c2.cv[:, 1], 6.0) and np.allclose(c2.dv[:, 0], 1.0e5, rtol=1e-14)
+    with pytest.raises(ValueError, match="not restated"):
+        K.from_case_files(*args, str(tmp_path / "st_sod1.inp"), str(tmp_path / "c.bc"),
+                          casename="wedge")
