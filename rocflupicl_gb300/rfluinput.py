@@ -4,7 +4,8 @@ sections of the `.bc` file, read the way the reference reads them, mapped onto
 the engine's options, with every setting outside the engine's envelope
 reported.
 
-Reading rules (libfloflu/ReadInputUtil.F90, ReadSection / ReadPatchSection):
+Reading rules (libfloflu/ReadInputUtil.F90, ReadSection; the `.bc` sections
+follow ReadPatchSection, where a key given twice takes the later value):
 a section starts at a line whose trimmed text is its header (`# NUMERICS`) and
 ends at the next line starting with `#`; a key matches a line that starts with
 the key's text, in key-list order, and each key takes the first value after it
@@ -87,6 +88,18 @@ def _read_keys(lines: List[str], keys: List[str]) -> Dict[str, float]:
             if k not in vals and line.startswith(k):
                 vals[k] = _value(line[len(k):])
                 break
+    return vals
+
+
+def _read_patch_keys(lines: List[str], keys: List[str]) -> Dict[str, float]:
+    """ReadPatchSection's value keys (libfloflu/ReadInputUtil.F90): every line
+    against every key, with no record of what is defined, so a key given on
+    two lines takes the later value."""
+    vals: Dict[str, float] = {}
+    for line in lines:
+        for k in keys:
+            if line.startswith(k):
+                vals[k] = _value(line[len(k):])
     return vals
 
 
@@ -210,7 +223,7 @@ def read_bc(path: str, n_patches: int, order_bfaces: int = 1):
                 pass
             else:
                 body.append(line)
-        v = _read_keys(body, keys)
+        v = _read_patch_keys(body, keys)
         if distrib:
             bad.append(f"{head[2:]} PATCH {p0} {p1}: distributed values (DISTRIB 1) come from a "
                        "separate file; give them per face through PatchBC.vals")

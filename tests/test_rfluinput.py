@@ -293,3 +293,15 @@ def test_case_files_without_flow_file(tmp_path):
     with pytest.raises(ValueError, match="not restated"):
         K.from_case_files(*args, str(tmp_path / "st_sod1.inp"), str(tmp_path / "c.bc"),
                           casename="wedge")
+
+
+def test_bc_key_given_twice_takes_the_later_value(tmp_path):
+    """ReadPatchSection keeps no record of defined keys: the later line wins
+    (the .inp sections' ReadSection keeps the first)."""
+    b = tmp_path / "twice.bc"
+    b.write_text("# BC_OUTFLOW\nPATCH 1 1\nTYPE 1\nPRESS 9.0E4\nPRESS 8.0E4\n#\n")
+    bcs, _ = RI.read_bc(str(b), 1)
+    assert bcs[0].pout[0] == 8.0e4
+    p = tmp_path / "twice.inp"
+    p.write_text("# NUMERICS\nCFL 0.5\nCFL 0.9\n#\n")
+    assert RI.read_inp(str(p)).numerics.cfl == 0.5
