@@ -728,6 +728,21 @@ __device__ __forceinline__ void state_from_fp64(const RegionDev<float> &g, int c
     state_from_fp64_split(g, c, q, pGiven);
 }
 
+// The double of a float (IEEE widening, always exact) assembled from its bit
+// fields with integer operations: the download join is FP64-pipe bound on
+// GB300, and this keeps the conversion off that pipe.  Zeros are assembled
+// too; subnormals, infinities and NaNs take the conversion instruction.
+__device__ __forceinline__ double widen_f32(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, m = u & 0x7fffffu;
+  if (e == 0xffu || (e == 0u && m != 0u)) return (double)f;
+  const unsigned long long s = (unsigned long long)(u & 0x80000000u) << 32;
+  // exponent bias 127 -> 1023 (+896), 23 -> 52 fraction bits (<< 29)
+  const unsigned long long b =
+      e ? (s | ((unsigned long long)(e + 896u) << 52) | ((unsigned long long)m << 29)) : s;
+  return __longlong_as_double((long long)b);
+}
+
 // Conserved state of a cell as FP64 (the float-float pair joined on the
 // mixed path).
 template <typename R>
@@ -2168,7 +2183,7 @@ __global__ void k_download_list(const RegionDev<R> *__restrict__ regs, const int
   } else {
 #pragma unroll
     for (int j = 0; j < 5; ++j)
-      q[j] = (double)g.cvF[(size_t)j * N + c] + (double)g.cvF[(size_t)(5 + j) * N + c];
+      q[j] = widen_f32(g.cvF[(size_t)j * N + c]) + widen_f32(g.cvF[(size_t)(5 + j) * N + c]);
   }
   if (cvH) {
 #pragma unroll
