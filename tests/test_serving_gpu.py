@@ -37,11 +37,3 @@ def test_admission_respects_hbm_budget():
     assert srv.max_active == 1
     queues = sorted(r.queue for r in res.values())
     assert queues[-1] > queues[0]
-
-
-def test_poisson_stream_is_seeded():
-    a = S.poisson_requests(50, lam=5.0, seed=1)
-    b = S.poisson_requests(50, lam=5.0, seed=1)
-    assert [(x.arrival, x.n, x.Ms, x.scheme) for x in a] == [(x.arrival, x.n, x.Ms, x.scheme) for x in b]
-    cells = np.array([x.cells for x in a])
-    assert cells.min() >= 6 * 11 ** 3 and cells.max() <= 6 * 88 ** 3
